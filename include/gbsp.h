@@ -1,0 +1,264 @@
+/* gbsp.h - C ABI of the GB300 path tracer (libgbsp.so).
+ *
+ * A drop-in for the CPU path-tracing hot path of vk_cinematic: the sp_Scene
+ * build (mesh midphase + scene broadphase BVHs), the sp_MaterialSystem
+ * registries and the tile entry point sp_PathTraceTile with its per-sample
+ * RNG.  Every entry point is plain C: opaque handles, plain pointers and
+ * sizes, an int status.  Each declaration names the reference interface it
+ * replaces as file:line inside the vk_cinematic tree.
+ *
+ * Semantics kept from the reference: camera model, XorShift32 draws, the
+ * Moller-Trumbore back-face-culled triangle test with the per-triangle AABB
+ * slab gate, the two-level (object / mesh) query with its local-space
+ * re-normalisation and world-space t, material evaluation, and the shading
+ * estimator of ComputeRadianceForPath including RADIANCE_CLAMP.
+ *
+ * Differences, all deliberate:
+ *  - the library copies geometry at mesh creation and owns device memory;
+ *  - capacities are runtime sizes, not the reference's compile-time 32
+ *    objects / 32 materials / 16 textures / 3 bounces / 32 and 128 BVH hits;
+ *  - no call aborts: errors come back as a negative status, with a message
+ *    from gbsp_last_error_string();
+ *  - spp, bounces, seeding mode and NaN policy are per-call options.
+ */
+#ifndef GBSP_H
+#define GBSP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBSP_VERSION 1
+
+/* Status codes (0 = success). */
+#define GBSP_OK 0
+#define GBSP_ERR_INVALID_ARGUMENT (-1)
+#define GBSP_ERR_OUT_OF_MEMORY (-2)
+#define GBSP_ERR_CAPACITY (-3)
+#define GBSP_ERR_CUDA (-4)
+#define GBSP_ERR_DEVICE_STATUS (-5) /* a kernel reported a bounded-loop or stack limit */
+#define GBSP_ERR_NOT_READY (-6)     /* scene broadphase not built since the last change */
+#define GBSP_ERR_NO_DEVICE (-7)
+
+/* Texture id meaning "no texture" (the reference uses U32_MAX). */
+#define GBSP_NO_TEXTURE 0xFFFFFFFFu
+/* Emission-texture id selecting the analytic sky (extension). */
+#define GBSP_SKY_TEXTURE 0xFFFFFFFEu
+
+/* Seeding modes. */
+#define GBSP_RNG_HASH_PER_SAMPLE 0u   /* state = hash(seed, x, y, sample) */
+#define GBSP_RNG_TILE_SEQUENTIAL 1u   /* one stream per tile, drawn in the
+                                         reference's pixel/sample/bounce order */
+/* NaN policy for a sample whose radiance has a NaN component. */
+#define GBSP_NAN_ZERO 0u      /* contributes 0, counted in metrics */
+#define GBSP_NAN_PROPAGATE 1u /* summed as is (what the reference does) */
+
+/* Metric slots, same order as the reference's sp_Metrics (src/sp_metrics.h:3-41).
+ * Cycle slots hold nanoseconds of device time on this library. */
+#define GBSP_METRIC_ELAPSED_NS 0
+#define GBSP_METRIC_PATHS_TRACED 1
+#define GBSP_METRIC_RAYS_TRACED 2
+#define GBSP_METRIC_RAY_HIT_COUNT 3
+#define GBSP_METRIC_RAY_MISS_COUNT 4
+#define GBSP_METRIC_INTERSECT_SCENE_NS 5
+#define GBSP_METRIC_BROADPHASE_NODE_VISITS 6   /* top-level node visits */
+#define GBSP_METRIC_SHADE_NS 7
+#define GBSP_METRIC_MIDPHASE_NODE_VISITS 8     /* mesh-level node visits */
+#define GBSP_METRIC_TRIANGLE_TESTS 9
+#define GBSP_METRIC_MIDPHASE_BOX_TESTS 10
+#define GBSP_METRIC_MESH_TESTS_PERFORMED 11
+#define GBSP_METRIC_NAN_SAMPLES 12
+#define GBSP_METRIC_TRACE_LAUNCHES 13          /* closest-hit kernel launches */
+#define GBSP_METRIC_KERNEL_LAUNCHES 14         /* all kernels the call launched */
+#define GBSP_METRIC_COUNT 16
+
+/* gbsp_options.flags */
+#define GBSP_FLAG_STAGE_TIMING 1u  /* fill the *_NS metric slots per stage
+                                      (CUDA events around each launch) */
+
+typedef struct gbsp_runtime gbsp_runtime;
+typedef struct gbsp_scene gbsp_scene;
+typedef struct gbsp_material_system gbsp_material_system;
+
+/* VertexPNT (src/mesh.h:10-15): 32 bytes. */
+typedef struct {
+    float position[3];
+    float normal[3];
+    float uv[2];
+} gbsp_vertex;
+
+/* Tile (src/tile.h:3-9). */
+typedef struct {
+    uint32_t minX, minY, maxX, maxY;
+} gbsp_tile;
+
+/* RandomNumberGenerator (src/math_utils.h:184-187). */
+typedef struct {
+    uint32_t state;
+} gbsp_rng;
+
+/* sp_Metrics (src/sp_metrics.h:44-48), widened to GBSP_METRIC_COUNT slots. */
+typedef struct {
+    uint64_t values[GBSP_METRIC_COUNT];
+} gbsp_metrics;
+
+/* sp_Material (src/sp_material_system.h:3-12): 36 bytes, same layout. */
+typedef struct {
+    float albedo[3];
+    uint32_t albedoTexture;
+    float emission[3];
+    uint32_t emissionTexture;
+    float roughness;
+} gbsp_material;
+
+/* ImagePlane (src/simd_path_tracer.h:3-8).  pixels is host memory holding
+ * width*height RGBA32F values, or NULL to keep the frame on the device. */
+typedef struct {
+    float *pixels;
+    uint32_t width;
+    uint32_t height;
+} gbsp_image_plane;
+
+/* sp_Camera (src/simd_path_tracer.h:17-32). */
+typedef struct {
+    float right[3], up[3], forward[3];
+    float position[3];
+    float filmCenter[3];
+    gbsp_image_plane *imagePlane;
+    float halfPixelWidth, halfPixelHeight;
+    float halfFilmWidth, halfFilmHeight;
+} gbsp_camera;
+
+/* Per-call knobs that the reference fixes at compile time. */
+typedef struct {
+    uint32_t spp;            /* SAMPLES_PER_PIXEL (src/simd_path_tracer.cpp:194) */
+    uint32_t max_bounces;    /* 3 in the reference (src/simd_path_tracer.cpp:195) */
+    uint32_t seed;           /* hash seed for GBSP_RNG_HASH_PER_SAMPLE */
+    uint32_t rng_mode;       /* GBSP_RNG_* */
+    uint32_t nan_policy;     /* GBSP_NAN_* */
+    float radiance_clamp;    /* RADIANCE_CLAMP (src/config.h:37); 0 disables */
+    uint32_t wave_paths;     /* paths in flight per wave (0 = library default) */
+    uint32_t flags;          /* GBSP_FLAG_* */
+} gbsp_options;
+
+/* sp_Context (src/simd_path_tracer.h:34-46) plus the runtime and options. */
+typedef struct {
+    gbsp_camera *camera;
+    gbsp_scene *scene;
+    gbsp_material_system *materialSystem;
+    gbsp_runtime *runtime;
+    const gbsp_options *options;
+} gbsp_context;
+
+/* ---- runtime -------------------------------------------------------------- */
+/* Device, stream and work buffers.  stream may be NULL (the library creates
+ * one) or a cudaStream_t cast to void*. No reference counterpart: the
+ * reference runs on host threads (src/main.cpp:790-817). */
+int gbsp_runtime_create(int device, void *stream, gbsp_runtime **out);
+int gbsp_runtime_destroy(gbsp_runtime *rt);
+int gbsp_runtime_synchronize(gbsp_runtime *rt);
+/* The stream the library launches on (a cudaStream_t). */
+void *gbsp_runtime_stream(gbsp_runtime *rt);
+/* Message for the last failing call on this thread. */
+const char *gbsp_last_error_string(void);
+int gbsp_version(void);
+void gbsp_options_default(gbsp_options *opt);
+
+/* ---- camera (host, same arithmetic as the reference) --------------------- */
+/* replaces sp_ConfigureCamera (src/simd_path_tracer.cpp:1-36) */
+int gbsp_configure_camera(gbsp_camera *camera, gbsp_image_plane *imagePlane,
+    const float position[3], const float rotation[4], float filmDistance);
+/* replaces sp_CalculateFilmPositions (src/simd_path_tracer.cpp:38-63) */
+uint32_t gbsp_calculate_film_positions(const gbsp_camera *camera,
+    float *filmPositions, const float *pixelPositions, uint32_t count);
+
+/* ---- scene ------------------------------------------------------------------ */
+/* replaces sp_InitializeScene (src/sp_scene.cpp:1-5) */
+int gbsp_scene_create(gbsp_runtime *rt, gbsp_scene **out);
+int gbsp_scene_destroy(gbsp_scene *scene);
+/* replaces sp_CreateMesh + sp_BuildMeshMidphase (src/sp_scene.cpp:8-54):
+ * copies the vertices and indices to the device and builds the mesh BVH
+ * there.  *meshOut receives the mesh handle used by add_object. */
+int gbsp_create_mesh(gbsp_scene *scene, const gbsp_vertex *vertices,
+    uint32_t vertexCount, const uint32_t *indices, uint32_t indexCount,
+    int useSmoothShading, uint32_t *meshOut);
+/* replaces sp_AddObjectToScene (src/sp_scene.cpp:77-117) */
+int gbsp_add_object_to_scene(gbsp_scene *scene, uint32_t mesh,
+    uint32_t material, const float position[3], const float orientation[4],
+    const float scale[3]);
+/* Removes every object (meshes stay); lets a caller rebuild the object set
+ * per frame as src/main.cpp:1529-1556 does. */
+int gbsp_clear_objects(gbsp_scene *scene);
+/* replaces sp_BuildSceneBroadphase (src/sp_scene.cpp:119-125): uploads the
+ * objects and builds the object BVH on the device. */
+int gbsp_build_scene_broadphase(gbsp_scene *scene);
+/* Object and triangle counts of the committed scene. */
+int gbsp_scene_info(const gbsp_scene *scene, uint32_t *objects,
+    uint64_t *triangles, uint32_t *meshNodes, uint32_t *maxDepth);
+
+/* ---- queries -------------------------------------------------------------- */
+/* replaces sp_RayIntersectScene (src/sp_scene.cpp:229-339) for a batch of
+ * rays in host memory: rays = count * (origin xyz, direction xyz).
+ * resultOut = count * (t, normal xyz, u, v), t = -1 on a miss;
+ * materialOut = count material ids. */
+int gbsp_ray_intersect_scene(gbsp_scene *scene, uint32_t count,
+    const float *rays, float *resultOut, uint32_t *materialOut,
+    gbsp_metrics *metrics);
+/* Closest hit for rays already in device memory (no reference counterpart as
+ * a batch; the per-ray rules are sp_RayIntersectScene's).  rays: count *
+ * (ox, oy, oz, pad, dx, dy, dz, pad) float; tOut: world t (-1 miss);
+ * triangleOut: the mesh's triangle index (-1 miss); objectOut may be NULL.
+ * Launches on the runtime's stream and returns without synchronising. */
+int gbsp_intersect_closest_device(gbsp_scene *scene, uint32_t count,
+    const float *rays, float *tOut, int32_t *triangleOut, int32_t *objectOut);
+
+/* ---- materials -------------------------------------------------------------- */
+int gbsp_material_system_create(gbsp_runtime *rt, gbsp_material_system **out);
+int gbsp_material_system_destroy(gbsp_material_system *ms);
+/* replaces sp_RegisterMaterial (src/sp_material_system.cpp:1-13) */
+int gbsp_register_material(gbsp_material_system *ms,
+    const gbsp_material *material, uint32_t id);
+/* replaces sp_RegisterTexture (src/sp_material_system.cpp:45-57); rgba is
+ * width*height RGBA32F, copied. */
+int gbsp_register_texture(gbsp_material_system *ms, const float *rgba,
+    uint32_t width, uint32_t height, uint32_t id);
+/* replaces the backgroundMaterialId field (src/sp_material_system.h:45) */
+int gbsp_set_background_material(gbsp_material_system *ms, uint32_t id);
+/* Analytic sky used by materials whose emissionTexture is GBSP_SKY_TEXTURE
+ * (extension): params = bottom rgb, top rgb, sun direction xyz (unit),
+ * cos(sun radius), sun radiance rgb. */
+int gbsp_set_procedural_sky(gbsp_material_system *ms, const float params[13]);
+
+/* ---- path tracing ----------------------------------------------------------- */
+/* replaces sp_PathTraceTile (src/simd_path_tracer.cpp:178-345).  Renders
+ * the tile into ctx->camera->imagePlane->pixels (host) and adds to
+ * *metrics.  With GBSP_RNG_TILE_SEQUENTIAL the tile draws from *rng in the
+ * reference's order and *rng is advanced; with GBSP_RNG_HASH_PER_SAMPLE
+ * every sample is seeded from options->seed and *rng is left unchanged. */
+int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile,
+    gbsp_rng *rng, gbsp_metrics *metrics);
+/* Whole image in one call (the caller's 510-tile loop of src/main.cpp:819-844
+ * in one device pass).  The frame stays on the device (gbsp_frame_device_pointer)
+ * and is also copied to imagePlane->pixels when that is not NULL. */
+int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics);
+/* Device pointer of the runtime's last frame (width*height RGBA32F). */
+const float *gbsp_frame_device_pointer(gbsp_runtime *rt);
+
+/* ---- procedural meshes (src/mesh_generation.cpp) ------------------------------ */
+/* CreateIcosahedronMesh (src/mesh_generation.cpp:220-337) without its 2048
+ * vertex cap.  Pass NULL arrays to get the counts only. */
+int gbsp_icosphere(uint32_t level, gbsp_vertex *vertices, uint32_t *indices,
+    uint32_t *vertexCount, uint32_t *indexCount);
+/* CreatePlaneMesh (src/mesh_generation.cpp:1-21): 4 vertices, 6 indices. */
+int gbsp_plane_mesh(gbsp_vertex vertices[4], uint32_t indices[6]);
+
+/* The per-sample RNG state used by GBSP_RNG_HASH_PER_SAMPLE. */
+uint32_t gbsp_sample_seed(uint32_t seed, uint32_t x, uint32_t y,
+    uint32_t sample);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBSP_H */

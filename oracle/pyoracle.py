@@ -330,6 +330,21 @@ class World:
             raise RuntimeError(f"closest failed {rc}")
         return t, obj, tri
 
+    def set_build_bvh(self, on: bool):
+        assert self.kind == "port"
+        self.L.fn("world_set_build_bvh")(self.h, _i32(int(on)))
+
+    def closest_brute(self, rays, threads=None):
+        assert self.kind == "port"
+        rays = _f32(rays).reshape(-1, 6)
+        t = np.zeros(len(rays), np.float32)
+        obj = np.zeros(len(rays), np.int32)
+        tri = np.zeros(len(rays), np.int32)
+        threads = threads or os.cpu_count() or 1
+        self.L.fn("world_closest_brute")(self.h, _u32(len(rays)), _p(rays), _u32(threads), _p(t),
+                                         _p(obj), _p(tri))
+        return t, obj, tri
+
     def path_trace_tile(self, width, height, cam_pos, cam_rot, film, tile, rng_state, pixels=None):
         if pixels is None:
             pixels = np.zeros((height, width, 4), np.float32)

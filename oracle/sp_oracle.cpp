@@ -599,6 +599,7 @@ struct World
     Sky sky = {};
     bool haveSky = false;
     oracle_options opt = {1, 3, 10.0f, 32, 128};
+    bool buildMeshBvh = true;  // false: meshes are only queried by brute force
 };
 
 const Material *find_material(const World &w, uint32_t id)  // sp_material_system.cpp:15-28
@@ -1111,7 +1112,7 @@ int oracle_world_add_mesh(void *wp, const float *vertices, uint32_t vertexCount,
         lo[i] = vmin3(a, vmin3(b, c));
         hi[i] = vmax3(a, vmax3(b, c));
     }
-    m.tree = bvh_build(lo.data(), hi.data(), triCount);
+    if (w.buildMeshBvh) m.tree = bvh_build(lo.data(), hi.data(), triCount);
     m.aabbMin = m.pos[0];
     m.aabbMax = m.pos[0];
     for (uint32_t i = 1; i < vertexCount; i++)
@@ -1362,6 +1363,71 @@ double oracle_world_render_hashed_mt(void *wp, uint32_t width, uint32_t height,
             for (int i = 0; i < 12; i++) metrics[i] += v[i];
     }
     return allOk ? dt : -dt;
+}
+
+void oracle_world_set_build_bvh(void *wp, int on) { ((World *)wp)->buildMeshBvh = on != 0; }
+
+// Closest hit without BVHs: every object whose world box passes the slab
+// test, every triangle whose own box passes it in object space (the set the
+// reference's BVH queries return), Moller-Trumbore, smallest object-space t
+// per object (ties to the lower triangle index), world t, smallest world t
+// (ties to the lower object index).  Threads split the rays.
+int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
+    uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut)
+{
+    const World &w = *(const World *)wp;
+    std::atomic<uint32_t> next(0);
+    auto worker = [&]() {
+        for (;;)
+        {
+            uint32_t r = next.fetch_add(1);
+            if (r >= rayCount) break;
+            F3 o = ld3(rays + 6 * (size_t)r), d = ld3(rays + 6 * (size_t)r + 3);
+            F3 invd = inverse3(d);
+            float best = INFINITY;
+            int32_t bestObj = -1, bestTri = -1;
+            for (size_t oi = 0; oi < w.objects.size(); oi++)
+            {
+                const Object &obj = w.objects[oi];
+                if (!slab_hit(obj.aabbMin, obj.aabbMax, o, invd)) continue;
+                const Mesh &mesh = w.meshes[obj.mesh];
+                F3 lo = transform_point(o, obj.invModel);
+                F3 ld = normalize3(transform_vector(d, obj.invModel));
+                F3 linvd = inverse3(ld);
+                float lbest = -1.0f;
+                int32_t ltri = -1;
+                uint32_t triCount = (uint32_t)(mesh.idx.size() / 3);
+                for (uint32_t t = 0; t < triCount; t++)
+                {
+                    F3 a = mesh.pos[mesh.idx[3 * t]], b = mesh.pos[mesh.idx[3 * t + 1]],
+                       c = mesh.pos[mesh.idx[3 * t + 2]];
+                    if (!slab_hit(vmin3(a, vmin3(b, c)), vmax3(a, vmax3(b, c)), lo, linvd)) continue;
+                    TriHit h = ray_triangle_mt(lo, ld, a, b, c);
+                    if (h.t > 0.0f && (h.t < lbest || lbest < 0.0f))
+                    {
+                        lbest = h.t;
+                        ltri = (int32_t)t;
+                    }
+                }
+                if (ltri < 0) continue;
+                F3 worldHit = transform_point(lo + ld * lbest, obj.model);
+                float tw = dot3(worldHit - o, d);
+                if (tw < best)
+                {
+                    best = tw;
+                    bestObj = (int32_t)oi;
+                    bestTri = ltri;
+                }
+            }
+            tOut[r] = bestObj >= 0 ? best : -1.0f;
+            objectOut[r] = bestObj;
+            triangleOut[r] = bestTri;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t i = 0; i < (threads ? threads : 1); i++) pool.emplace_back(worker);
+    for (auto &t : pool) t.join();
+    return 0;
 }
 
 }  // extern "C"

@@ -108,6 +108,12 @@ double oracle_world_render_hashed_mt(void *w, uint32_t width, uint32_t height,
 int oracle_world_closest(void *w, uint32_t rayCount, const float *rays,
     float *tOut, int32_t *objectOut, int32_t *triangleOut);
 
+// Meshes added after this call skip the reference's O(n^2 log n) BVH build
+// (they can then only be queried with oracle_world_closest_brute).
+void oracle_world_set_build_bvh(void *w, int on);
+int oracle_world_closest_brute(void *w, uint32_t rayCount, const float *rays,
+    uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,217 @@
+// Host-side objects behind the gbsp C ABI.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "gbsp.h"
+#include "gbsp_common.cuh"
+
+namespace gbsp {
+
+// Sets the thread's last error message and returns the status.
+int set_error(int status, const char *fmt, ...);
+int cuda_error(cudaError_t e, const char *what);
+#define GBSP_CUDA_TRY(call)                                            \
+    do {                                                               \
+        cudaError_t e_ = (call);                                       \
+        if (e_ != cudaSuccess) return ::gbsp::cuda_error(e_, #call);   \
+    } while (0)
+
+// Owning device allocation (stream-ordered).
+template <typename T>
+struct DeviceBuffer {
+    T *ptr = nullptr;
+    size_t count = 0;  // elements allocated
+    cudaStream_t stream = nullptr;
+
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer &) = delete;
+    DeviceBuffer &operator=(const DeviceBuffer &) = delete;
+    ~DeviceBuffer() { release(); }
+
+    void release()
+    {
+        if (ptr) cudaFreeAsync(ptr, stream);
+        ptr = nullptr;
+        count = 0;
+    }
+    // Grows to at least n elements; contents are not kept.
+    int reserve(size_t n, cudaStream_t s)
+    {
+        if (n <= count && ptr) return GBSP_OK;
+        release();
+        stream = s;
+        size_t bytes = (n ? n : 1) * sizeof(T);
+        cudaError_t e = cudaMallocAsync((void **)&ptr, bytes, s);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            return set_error(e == cudaErrorMemoryAllocation ? GBSP_ERR_OUT_OF_MEMORY : GBSP_ERR_CUDA,
+                "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+        }
+        count = n ? n : 1;
+        return GBSP_OK;
+    }
+    int upload(const T *host, size_t n, cudaStream_t s)
+    {
+        int rc = reserve(n, s);
+        if (rc) return rc;
+        if (n) GBSP_CUDA_TRY(cudaMemcpyAsync(ptr, host, n * sizeof(T), cudaMemcpyHostToDevice, s));
+        return GBSP_OK;
+    }
+};
+
+struct Counters;  // device metric block
+
+}  // namespace gbsp
+
+struct gbsp_runtime {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool ownsStream = false;
+    int smCount = 0;
+    uint32_t *dStatus = nullptr;        // kernel status word
+    unsigned long long *dCounters = nullptr;  // GBSP_METRIC_COUNT u64 counters
+    cudaEvent_t ev[8] = {};
+    // wavefront state, grown on demand
+    gbsp::DeviceBuffer<float4> rayO, rayD;         // two queues back to back
+    gbsp::DeviceBuffer<int4> hitA;                 // t, u, v, prim
+    gbsp::DeviceBuffer<int> hitInst;
+    gbsp::DeviceBuffer<uint32_t> pathRng;
+    gbsp::DeviceBuffer<uint32_t> pathLen;
+    gbsp::DeviceBuffer<float4> vertE;              // emission xyz, cosine
+    gbsp::DeviceBuffer<float4> vertA;              // response xyz
+    gbsp::DeviceBuffer<float4> pathRad;            // radiance per path
+    gbsp::DeviceBuffer<unsigned int> queueCounts;  // small control block
+    gbsp::DeviceBuffer<float4> frame;              // last frame, RGBA32F
+    uint32_t frameW = 0, frameH = 0;
+    // launch accounting and optional per-stage timing of the current call
+    uint64_t launches = 0, traceLaunches = 0;
+    std::vector<cudaEvent_t> evPool;
+    size_t evUsed = 0;
+    std::vector<std::pair<int, int>> traceSpans, shadeSpans;  // event index pairs
+    bool stageTiming = false;
+    int stage_event(cudaStream_t s)  // records and returns an event index, -1 on failure
+    {
+        if (evUsed == evPool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            evPool.push_back(e);
+        }
+        if (cudaEventRecord(evPool[evUsed], s) != cudaSuccess) return -1;
+        return (int)evUsed++;
+    }
+    void begin_call(bool timing)
+    {
+        launches = traceLaunches = 0;
+        evUsed = 0;
+        traceSpans.clear();
+        shadeSpans.clear();
+        stageTiming = timing;
+    }
+};
+
+struct gbsp_mesh_info {
+    uint32_t rootNode;     // in the scene's node pool
+    uint32_t triFirst;     // first triangle in the pool
+    uint32_t triCount;
+    uint32_t nodeCount;
+    uint32_t depth;
+    bool smooth;
+    float aabbMin[3], aabbMax[3];  // vertex AABB (src/sp_scene.cpp:57-75)
+};
+
+struct gbsp_object_info {
+    uint32_t mesh;
+    uint32_t material;
+    float position[3], rotation[4], scale[3];
+    gbsp::Instance inst;
+};
+
+struct gbsp_scene {
+    gbsp_runtime *rt = nullptr;
+    std::vector<gbsp_mesh_info> meshes;
+    std::vector<gbsp_object_info> objects;
+    // node pool: mesh BVHs first, then the object BVH (rebuilt per commit)
+    gbsp::DeviceBuffer<gbsp::Node8> nodes;
+    uint32_t meshNodeCount = 0;   // nodes used by meshes
+    uint32_t totalNodeCount = 0;
+    gbsp::DeviceBuffer<gbsp::TriRecord> tris;
+    gbsp::DeviceBuffer<gbsp::TriAttr> attrs;
+    gbsp::DeviceBuffer<uint32_t> triIds;
+    uint64_t triCount = 0;
+    gbsp::DeviceBuffer<gbsp::Instance> instances;
+    uint32_t tlasRoot = gbsp::kEmptyChild;
+    uint32_t tlasDepth = 0;
+    uint32_t maxDepth = 0;
+    bool committed = false;
+    std::vector<uint32_t> leafOrder;  // object-BVH leaf position -> object index
+    // resolved material slots depend on the material system; objects keep ids
+    gbsp::SceneView view() const
+    {
+        gbsp::SceneView v;
+        v.nodes = nodes.ptr;
+        v.tris = tris.ptr;
+        v.attrs = attrs.ptr;
+        v.triIds = triIds.ptr;
+        v.instances = instances.ptr;
+        v.tlasRoot = tlasRoot;
+        v.instanceCount = (uint32_t)objects.size();
+        return v;
+    }
+};
+
+struct gbsp_material_system {
+    gbsp_runtime *rt = nullptr;
+    std::vector<uint32_t> keys;
+    std::vector<gbsp_material> materials;
+    std::vector<uint32_t> textureKeys;
+    std::vector<std::vector<float>> texturePixels;
+    std::vector<uint32_t> textureW, textureH;
+    uint32_t backgroundId = 0;
+    gbsp::SkyParams sky = {};
+    bool haveSky = false;
+    bool dirty = true;
+    gbsp::DeviceBuffer<gbsp::DeviceMaterial> dMaterials;
+    gbsp::DeviceBuffer<float4> dTexels;
+    gbsp::DeviceBuffer<gbsp::TextureDesc> dTextures;
+};
+
+namespace gbsp {
+
+// bvh_build.cu
+// Builds an 8-wide BVH over n primitive boxes on the device.  Appends the
+// nodes to *nodes starting at nodeBase (growing the pool, keeping its
+// contents) and returns the primitive order (sorted position -> primitive).
+int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_t n,
+    uint32_t leafMax, DeviceBuffer<Node8> *nodes, uint32_t nodeBase, uint32_t *nodeCountOut,
+    DeviceBuffer<uint32_t> *orderOut, uint32_t *depthOut, uint32_t *dStatus);
+// Triangle boxes + records for a mesh: positions from VertexPNT, indices.
+int mesh_prepare(cudaStream_t s, const gbsp_vertex *dVerts, const uint32_t *dIdx,
+    uint32_t triCount, float4 *dLo, float4 *dHi);
+int mesh_emit(cudaStream_t s, const gbsp_vertex *dVerts, const uint32_t *dIdx,
+    uint32_t triCount, const uint32_t *dOrder, TriRecord *dTris, TriAttr *dAttrs,
+    uint32_t *dTriIds, uint32_t nodeBase, Node8 *dNodes, uint32_t nodeCount,
+    uint32_t triBase);
+int offset_nodes(cudaStream_t s, Node8 *dNodes, uint32_t nodeCount, uint32_t nodeBase,
+    uint32_t leafBase);
+
+// trace.cu
+int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const float4 *rays,
+    float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut, uint32_t *matOut,
+    const Instance *instHost, int smCount, unsigned long long *counters, uint32_t *dStatus);
+
+// pathtrace.cu
+int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
+    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState);
+
+// api.cu
+int material_view(gbsp_material_system *ms, MaterialView *out);
+int resolve_material(const gbsp_material_system *ms, uint32_t id);
+
+}  // namespace gbsp

@@ -1,0 +1,559 @@
+// Wavefront path tracer: the tile loop of sp_PathTraceTile
+// (src/simd_path_tracer.cpp:178-345) split into stages over a wave of paths.
+//
+//   generate   one thread per (pixel, sample): seed, jitter, camera ray
+//   trace      persistent closest-hit kernel pulling 32 rays per warp from a
+//              global atomic counter
+//   shade      persistent: surface attributes, hemisphere sample, material
+//              and BRDF terms of the path vertex; continuing rays are
+//              compacted into the next queue with one atomic per warp
+//              (ballot + popc); finished paths are evaluated at once
+//   accumulate one thread per pixel: Neumaier sum of sample * (1/spp)
+//
+// A wave holds a run of whole pixels with all their samples, so the
+// accumulation is a deterministic, ordered sum per pixel.  Bounce counts and
+// queue sizes stay on the device: a wave is enqueued with no host round trip.
+//
+// ComputeRadianceForPath (src/simd_path_tracer.cpp:107-175) evaluates each
+// vertex from its own data plus the clamped radiance of the next vertex.
+// The per-vertex part is computed at shade time and stored as
+// E (emission), A (kD*albedo/pi + specular) and the cosine; the reverse pass
+// then is radiance = E + (A * clamp(radiance_next)) * cos, the reference's
+// expression in the reference's order.
+
+#include <algorithm>
+
+#include "gbsp_internal.h"
+#include "traverse.cuh"
+
+namespace gbsp {
+
+// Work/queue control words (u32) behind the metric counters.
+enum Ctl : int {
+    kCtlTraceWork = 0,
+    kCtlShadeWork = 1,
+    kCtlQueue0 = 2,
+    kCtlQueue1 = 3,
+    kCtlCount = 8
+};
+
+struct WaveBuffers {
+    float4 *rayO;      // 2 * cap: (origin, path id bits)
+    float4 *rayD;      // 2 * cap: (direction, 0)
+    int4 *hitA;        // cap: (t, u, v, prim) bits
+    int *hitInst;      // cap
+    uint32_t *pathRng; // cap
+    uint32_t *pathLen; // cap
+    float4 *vertE;     // maxBounces * cap: (emission xyz, cosine)
+    float4 *vertA;     // maxBounces * cap: (A xyz, 0)
+    float4 *pathRad;   // cap
+    uint32_t cap;
+};
+
+struct WaveParams {
+    CameraParams cam;
+    uint32_t x0, y0, regionW;
+    uint64_t pixelBase;   // first pixel (row-major in the region) of this wave
+    uint32_t pixels;      // pixels in this wave
+    uint32_t spp;
+    uint32_t maxBounces;
+    uint32_t seed;
+    float clampValue;
+    uint32_t nanPolicy;
+    float invSpp;
+};
+
+// ---------------------------------------------------------------------------
+// Material evaluation (src/sp_material_system.cpp:59-105, image.h:3-18)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V3 texel_nearest(const MaterialView &mv, int slot, float u, float v)
+{
+    TextureDesc t = mv.textures[slot];
+    float fx = u * (float)t.width;
+    float fy = v * (float)t.height;
+    uint32_t x = (uint32_t)floorf(fx);
+    uint32_t y = (uint32_t)floorf(fy);
+    uint64_t idx = (uint64_t)y * t.width + x;
+    uint64_t maxIdx = (uint64_t)t.width * t.height - 1;  // the reference may read index W*H
+    if (idx > maxIdx) idx = maxIdx;
+    float4 p = __ldg(mv.texels + t.offset + idx);
+    return v3(p.x, p.y, p.z);
+}
+
+__device__ __forceinline__ V3 sky_radiance(const SkyParams &s, V3 dir)
+{
+    float t = rclamp(0.5f * (dir.y + 1.0f), 0.0f, 1.0f);
+    V3 c = add(s.bottom, mul(sub(s.top, s.bottom), t));
+    if (dot(dir, s.sunDir) >= s.cosSunRadius) c = add(c, s.sunRadiance);
+    return c;
+}
+
+// Per-vertex terms of ComputeRadianceForPath for the material in `slot`.
+__device__ __forceinline__ void vertex_terms(const MaterialView &mv, int slot, V3 N, V3 L, V3 V,
+    float uvx, float uvy, float4 &ec, float4 &aa)
+{
+    V3 albedo = v3(0.0f, 0.0f, 0.0f), emission;
+    float roughness = 0.0f;
+    if (slot < 0) {
+        emission = v3(1.0f, 0.0f, 1.0f);  // missing material: magenta
+    } else {
+        const DeviceMaterial &m = mv.materials[slot];
+        albedo = m.albedoTex >= 0 ? texel_nearest(mv, m.albedoTex, uvx, uvy)
+                                  : v3(m.albedo[0], m.albedo[1], m.albedo[2]);
+        if (m.emissionTex == -2) {
+            emission = sky_radiance(mv.sky, neg(V));
+        } else if (m.emissionTex >= 0) {
+            V3 dir = neg(V);  // src/math_lib.h:849-884
+            float inc = atan2f(sqrtf(dir.x * dir.x + dir.z * dir.z), dir.y);
+            float az = atan2f(dir.z, dir.x);
+            if (az < 0.0f) az += 2.0f * kPi;
+            float eu = az / (2.0f * kPi);
+            float ev = cosf(inc) * 0.5f + 0.5f;
+            ev = 1.0f - ev;
+            emission = mul(texel_nearest(mv, m.emissionTex, eu, ev), 1.0f);
+        } else {
+            emission = v3(m.emission[0], m.emission[1], m.emission[2]);
+        }
+        roughness = m.roughness;
+    }
+    float cosine = rmax(0.0f, dot(N, L));
+    V3 H = normalize(add(L, V));
+    // FresnelSchlick(max(H.V, 0), 0.04) (src/simd_path_tracer.cpp:65-70)
+    float p5 = powf(1.0f - rmax(dot(H, V), 0.0f), 5.0f);
+    float F0 = 0.04f;
+    float Fs = F0 + (1.0f - F0) * p5;
+    V3 F = v3(Fs, Fs, Fs);
+    V3 kD = sub(v3(1.0f, 1.0f, 1.0f), F);
+    // DistributionGGX (:72-84)
+    float a = roughness * roughness;
+    float a2 = a * a;
+    float NdotH = rmax(dot(N, H), 0.0f);
+    float NdotH2 = NdotH * NdotH;
+    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
+    denom = kPi * denom * denom;
+    float NDF = a2 / denom;
+    // GeometrySmith (:86-105)
+    float NdotV = rmax(dot(N, V), 0.0f);
+    float NdotL = rmax(dot(N, L), 0.0f);
+    float r1 = roughness + 1.0f;
+    float k = (r1 * r1) / 8.0f;
+    float ggx2 = NdotV / (NdotV * (1.0f - k) + k);
+    float ggx1 = NdotL / (NdotL * (1.0f - k) + k);
+    float G = ggx1 * ggx2;
+    V3 numerator = mul(F, NDF * G);
+    float denominator = 4.0f * rmax(dot(N, V), 0.0f) * rmax(dot(N, L), 0.0f) + 0.0001f;
+    V3 specular = mul(numerator, 1.0f / denominator);
+    float oneOverPi = 1.0f / kPi;
+    V3 A = add(mul(hadamard(kD, albedo), oneOverPi), specular);
+    ec = make_float4(emission.x, emission.y, emission.z, cosine);
+    aa = make_float4(A.x, A.y, A.z, 0.0f);
+}
+
+// Reverse pass over stored vertex terms.
+__device__ __forceinline__ V3 path_radiance(const float4 *vertE, const float4 *vertA,
+    size_t stride, uint32_t p, uint32_t len, float clampValue)
+{
+    V3 radiance = v3(0.0f, 0.0f, 0.0f);
+    for (int i = (int)len - 1; i >= 0; i--) {
+        float4 ec = vertE[(size_t)i * stride + p];
+        float4 aa = vertA[(size_t)i * stride + p];
+        V3 Li = radiance;
+        if (clampValue != 0.0f)
+            Li = v3(rclamp(Li.x, 0.0f, clampValue), rclamp(Li.y, 0.0f, clampValue),
+                rclamp(Li.z, 0.0f, clampValue));
+        radiance = add(v3(ec.x, ec.y, ec.z), mul(hadamard(v3(aa.x, aa.y, aa.z), Li), ec.w));
+    }
+    return radiance;
+}
+
+// ---------------------------------------------------------------------------
+// Stage kernels
+// ---------------------------------------------------------------------------
+__global__ void k_reset_ctl(unsigned int *ctl, uint32_t queue0)
+{
+    if (threadIdx.x < kCtlCount) ctl[threadIdx.x] = 0;
+    __syncthreads();
+    if (threadIdx.x == 0) ctl[kCtlQueue0] = queue0;
+}
+
+__global__ void k_reset_stage(unsigned int *ctl, int outQueue)
+{
+    ctl[kCtlTraceWork] = 0;
+    ctl[kCtlShadeWork] = 0;
+    ctl[outQueue] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuffers wb)
+{
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t paths = wp.pixels * wp.spp;
+    if (p >= paths) return;
+    uint64_t pix = wp.pixelBase + p / wp.spp;
+    uint32_t s = p % wp.spp;
+    uint32_t x = wp.x0 + (uint32_t)(pix % wp.regionW);
+    uint32_t y = wp.y0 + (uint32_t)(pix / wp.regionW);
+    uint32_t rng = sample_seed(wp.seed, x, y, s);
+    V3 o, d;
+    camera_ray(wp.cam, x, y, rng, o, d);
+    wb.rayO[p] = make_float4(o.x, o.y, o.z, __int_as_float((int)p));
+    wb.rayD[p] = make_float4(d.x, d.y, d.z, 0.0f);
+    wb.pathRng[p] = rng;
+    wb.pathLen[p] = 0;
+}
+
+__global__ void __launch_bounds__(128) k_trace(SceneView sv, const float4 *__restrict__ rayO,
+    const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
+    unsigned int *ctl, unsigned long long *counters, uint32_t *status)
+{
+    int lane = threadIdx.x & 31;
+    uint32_t count = *queueCount;
+    TraceCounters cnt = {0, 0, 0, 0, 0};
+    uint32_t done = 0, hits = 0;
+    for (uint32_t guard = 0; guard <= count / 32 + 1; guard++) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&ctl[kCtlTraceWork], 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= count) break;
+        uint32_t i = base + lane;
+        if (i < count) {
+            float4 o4 = rayO[i], d4 = rayD[i];
+            RayHit h = trace_closest<true>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z), status,
+                cnt);
+            hitA[i] = make_int4(__float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v),
+                h.prim);
+            hitInst[i] = h.inst;
+            done++;
+            hits += (h.prim >= 0 && h.t > 0.0f) ? 1u : 0u;
+        }
+    }
+    uint32_t v[7] = {done, hits, cnt.topNodes, cnt.meshNodes, cnt.triTests, cnt.boxTests,
+        cnt.meshTests};
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+        for (int off = 16; off; off >>= 1) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+    if (lane == 0) {
+        atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)v[0]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)v[1]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(v[0] - v[1]));
+        atomicAdd(&counters[GBSP_METRIC_BROADPHASE_NODE_VISITS], (unsigned long long)v[2]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_NODE_VISITS], (unsigned long long)v[3]);
+        atomicAdd(&counters[GBSP_METRIC_TRIANGLE_TESTS], (unsigned long long)v[4]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_BOX_TESTS], (unsigned long long)v[5]);
+        atomicAdd(&counters[GBSP_METRIC_MESH_TESTS_PERFORMED], (unsigned long long)v[6]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_shade(SceneView sv, MaterialView mv, WaveParams wp,
+    WaveBuffers wb, uint32_t bounce, int inQueue, unsigned int *ctl, unsigned long long *counters)
+{
+    int lane = threadIdx.x & 31;
+    uint32_t count = ctl[inQueue];
+    int outQueue = inQueue == kCtlQueue0 ? kCtlQueue1 : kCtlQueue0;
+    const float4 *inO = wb.rayO + (inQueue == kCtlQueue0 ? 0 : wb.cap);
+    const float4 *inD = wb.rayD + (inQueue == kCtlQueue0 ? 0 : wb.cap);
+    float4 *outO = wb.rayO + (inQueue == kCtlQueue0 ? wb.cap : 0);
+    float4 *outD = wb.rayD + (inQueue == kCtlQueue0 ? wb.cap : 0);
+    bool lastBounce = bounce + 1 >= wp.maxBounces;
+    uint32_t finished = 0;
+    for (uint32_t guard = 0; guard <= count / 32 + 1; guard++) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&ctl[kCtlShadeWork], 32u);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= count) break;
+        uint32_t i = base + lane;
+        bool active = i < count;
+        bool cont = false;
+        float4 newO = make_float4(0, 0, 0, 0), newD = make_float4(0, 0, 0, 0);
+        uint32_t p = 0;
+        if (active) {
+            float4 o4 = inO[i], d4 = inD[i];
+            p = (uint32_t)__float_as_int(o4.w);
+            int4 hA = wb.hitA[i];
+            RayHit h;
+            h.t = __int_as_float(hA.x);
+            h.u = __int_as_float(hA.y);
+            h.v = __int_as_float(hA.z);
+            h.prim = hA.w;
+            h.inst = wb.hitInst[i];
+            V3 o = v3(o4.x, o4.y, o4.z), d = v3(d4.x, d4.y, d4.z);
+            uint32_t len = wb.pathLen[p];
+            float4 ec, aa;
+            if (h.prim >= 0 && h.t > 0.0f) {
+                // hit vertex (src/simd_path_tracer.cpp:268-288)
+                V3 n;
+                float ux, uy;
+                hit_surface(sv, h, n, ux, uy);
+                V3 pos = add(o, mul(d, h.t));
+                uint32_t rng = wb.pathRng[p];
+                V3 dir = random_hemisphere(n, rng);
+                wb.pathRng[p] = rng;
+                int slot = mv.instanceSlot[h.inst];
+                vertex_terms(mv, slot, n, dir, neg(d), ux, uy, ec, aa);
+                V3 no = add(pos, mul(n, 0.0001f));
+                newO = make_float4(no.x, no.y, no.z, __int_as_float((int)p));
+                newD = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                cont = !lastBounce;
+            } else {
+                // miss: background vertex, path ends (:302-314)
+                vertex_terms(mv, mv.backgroundSlot, v3(0, 0, 0), v3(0, 0, 0), neg(d), 0.0f, 0.0f,
+                    ec, aa);
+            }
+            wb.vertE[(size_t)len * wb.cap + p] = ec;
+            wb.vertA[(size_t)len * wb.cap + p] = aa;
+            len++;
+            wb.pathLen[p] = len;
+            if (!cont) {
+                V3 r = path_radiance(wb.vertE, wb.vertA, wb.cap, p, len, wp.clampValue);
+                wb.pathRad[p] = make_float4(r.x, r.y, r.z, 0.0f);
+                finished++;
+            }
+        }
+        // compaction: one atomic per warp for the continuing rays
+        uint32_t mask = __ballot_sync(0xFFFFFFFFu, cont);
+        uint32_t outBase = 0;
+        if (lane == 0 && mask) outBase = atomicAdd(&ctl[outQueue], (unsigned)__popc(mask));
+        outBase = __shfl_sync(0xFFFFFFFFu, outBase, 0);
+        if (cont) {
+            uint32_t slot = outBase + __popc(mask & ((1u << lane) - 1u));
+            outO[slot] = newO;
+            outD[slot] = newD;
+        }
+    }
+    for (int off = 16; off; off >>= 1) finished += __shfl_xor_sync(0xFFFFFFFFu, finished, off);
+    if (lane == 0 && finished)
+        atomicAdd(&counters[GBSP_METRIC_PATHS_TRACED], (unsigned long long)finished);
+}
+
+__global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBuffers wb, float4 *image,
+    uint32_t imageWidth, unsigned long long *counters)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nans = 0;
+    if (k < wp.pixels) {
+        uint64_t pix = wp.pixelBase + k;
+        uint32_t x = wp.x0 + (uint32_t)(pix % wp.regionW);
+        uint32_t y = wp.y0 + (uint32_t)(pix / wp.regionW);
+        CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+        for (uint32_t s = 0; s < wp.spp; s++) {
+            float4 r = wb.pathRad[(size_t)k * wp.spp + s];
+            if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
+                nans++;
+                if (wp.nanPolicy == GBSP_NAN_ZERO) continue;
+            }
+            csum_add(acc[0], r.x * wp.invSpp);
+            csum_add(acc[1], r.y * wp.invSpp);
+            csum_add(acc[2], r.z * wp.invSpp);
+        }
+        image[(size_t)y * imageWidth + x] =
+            make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
+    }
+    for (int off = 16; off; off >>= 1) nans += __shfl_xor_sync(0xFFFFFFFFu, nans, off);
+    if ((threadIdx.x & 31) == 0 && nans)
+        atomicAdd(&counters[GBSP_METRIC_NAN_SAMPLES], (unsigned long long)nans);
+}
+
+// ---------------------------------------------------------------------------
+// Reference-order tile mode: one thread walks one tile exactly like
+// sp_PathTraceTile, drawing every random number from one XorShift32 stream.
+// ---------------------------------------------------------------------------
+constexpr int kMaxSeqBounces = 16;
+
+__global__ void __launch_bounds__(64) k_tile_sequential(SceneView sv, MaterialView mv,
+    CameraParams cam, const uint4 *tiles, uint32_t tileCount, uint32_t *rngStates, uint32_t spp,
+    uint32_t maxBounces, float clampValue, float4 *image, uint32_t imageWidth,
+    unsigned long long *counters, uint32_t *status)
+{
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tileCount) return;
+    uint4 tile = tiles[t];
+    uint32_t rng = rngStates[t];
+    uint32_t maxX = tile.z < cam.width ? tile.z : cam.width;
+    uint32_t maxY = tile.w < cam.height ? tile.w : cam.height;
+    float4 vE[kMaxSeqBounces], vA[kMaxSeqBounces];
+    TraceCounters cnt = {0, 0, 0, 0, 0};
+    uint64_t rays = 0, hits = 0, paths = 0;
+    for (uint32_t y = tile.y; y < maxY; y++) {
+        for (uint32_t x = tile.x; x < maxX; x++) {
+            V3 total = v3(0, 0, 0);
+            for (uint32_t s = 0; s < spp; s++) {
+                V3 o, d;
+                camera_ray(cam, x, y, rng, o, d);
+                uint32_t len = 0;
+                for (uint32_t b = 0; b < maxBounces; b++) {
+                    RayHit h = trace_closest<true>(sv, o, d, status, cnt);
+                    rays++;
+                    float4 ec, aa;
+                    if (h.prim >= 0 && h.t > 0.0f) {
+                        hits++;
+                        V3 n;
+                        float ux, uy;
+                        hit_surface(sv, h, n, ux, uy);
+                        V3 pos = add(o, mul(d, h.t));
+                        V3 dir = random_hemisphere(n, rng);
+                        vertex_terms(mv, mv.instanceSlot[h.inst], n, dir, neg(d), ux, uy, ec, aa);
+                        vE[len] = ec;
+                        vA[len] = aa;
+                        len++;
+                        o = add(pos, mul(n, 0.0001f));
+                        d = dir;
+                    } else {
+                        vertex_terms(mv, mv.backgroundSlot, v3(0, 0, 0), v3(0, 0, 0), neg(d), 0.0f,
+                            0.0f, ec, aa);
+                        vE[len] = ec;
+                        vA[len] = aa;
+                        len++;
+                        break;
+                    }
+                }
+                V3 r = path_radiance(vE, vA, 1, 0, len, clampValue);
+                total = add(total, mul(r, 1.0f / (float)spp));
+                paths++;
+            }
+            image[(size_t)y * imageWidth + x] = make_float4(total.x, total.y, total.z, 1.0f);
+        }
+    }
+    rngStates[t] = rng;
+    atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)rays);
+    atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)hits);
+    atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(rays - hits));
+    atomicAdd(&counters[GBSP_METRIC_PATHS_TRACED], (unsigned long long)paths);
+    atomicAdd(&counters[GBSP_METRIC_TRIANGLE_TESTS], (unsigned long long)cnt.triTests);
+    atomicAdd(&counters[GBSP_METRIC_MIDPHASE_BOX_TESTS], (unsigned long long)cnt.boxTests);
+    atomicAdd(&counters[GBSP_METRIC_MESH_TESTS_PERFORMED], (unsigned long long)cnt.meshTests);
+}
+
+// ---------------------------------------------------------------------------
+// Host driver
+// ---------------------------------------------------------------------------
+static int ensure_wave_buffers(gbsp_runtime *rt, uint32_t cap, uint32_t maxBounces)
+{
+    cudaStream_t s = rt->stream;
+    int rc;
+    if ((rc = rt->rayO.reserve(2 * (size_t)cap, s)) || (rc = rt->rayD.reserve(2 * (size_t)cap, s)) ||
+        (rc = rt->hitA.reserve(cap, s)) || (rc = rt->hitInst.reserve(cap, s)) ||
+        (rc = rt->pathRng.reserve(cap, s)) || (rc = rt->pathLen.reserve(cap, s)) ||
+        (rc = rt->vertE.reserve((size_t)maxBounces * cap, s)) ||
+        (rc = rt->vertA.reserve((size_t)maxBounces * cap, s)) ||
+        (rc = rt->pathRad.reserve(cap, s)))
+        return rc;
+    return GBSP_OK;
+}
+
+int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
+    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState)
+{
+    cudaStream_t s = rt->stream;
+    unsigned long long *counters = rt->dCounters;
+    unsigned int *ctl = reinterpret_cast<unsigned int *>(rt->dCounters + GBSP_METRIC_COUNT);
+    if (x1 <= x0 || y1 <= y0) return GBSP_OK;
+    uint32_t spp = opt.spp ? opt.spp : 1;
+    uint32_t maxBounces = opt.max_bounces;
+    if (maxBounces == 0) {
+        // no bounce at all: every path has zero vertices and zero radiance
+        maxBounces = 0;
+    }
+    if (opt.rng_mode == GBSP_RNG_TILE_SEQUENTIAL) {
+        if (maxBounces > (uint32_t)kMaxSeqBounces)
+            return set_error(GBSP_ERR_CAPACITY, "tile-sequential mode supports at most %d bounces",
+                kMaxSeqBounces);
+        // tiles of 64x64 in row-major order (src/tile.h:11-42), each starting
+        // from the caller's RNG state (src/main.cpp:738-739); with one tile
+        // the state is advanced and returned (sp_PathTraceTile semantics)
+        std::vector<uint4> tiles;
+        uint32_t tw = rngState ? (x1 - x0) : 64u, th = rngState ? (y1 - y0) : 64u;
+        for (uint32_t ty = y0; ty < y1; ty += th)
+            for (uint32_t tx = x0; tx < x1; tx += tw)
+                tiles.push_back(make_uint4(tx, ty, std::min(tx + tw, x1), std::min(ty + th, y1)));
+        std::vector<uint32_t> states(tiles.size(), rngState ? *rngState : 0xF51C0E49u);
+        DeviceBuffer<uint4> dTiles;
+        DeviceBuffer<uint32_t> dStates;
+        int rc;
+        if ((rc = dTiles.upload(tiles.data(), tiles.size(), s)) ||
+            (rc = dStates.upload(states.data(), states.size(), s)))
+            return rc;
+        uint32_t n = (uint32_t)tiles.size();
+        k_tile_sequential<<<(n + 63) / 64, 64, 0, s>>>(sv, mv, cam, dTiles.ptr, n, dStates.ptr, spp,
+            maxBounces, opt.radiance_clamp, dImage, imageWidth, counters, rt->dStatus);
+        GBSP_CUDA_TRY(cudaGetLastError());
+        rt->launches += 1;
+        if (rngState) {
+            GBSP_CUDA_TRY(cudaMemcpyAsync(rngState, dStates.ptr, 4, cudaMemcpyDeviceToHost, s));
+            GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+        }
+        return GBSP_OK;
+    }
+
+    uint64_t regionPixels = (uint64_t)(x1 - x0) * (y1 - y0);
+    uint64_t waveTarget = opt.wave_paths ? opt.wave_paths : (1u << 22);
+    uint64_t pixelsPerWave = std::max<uint64_t>(1, waveTarget / spp);
+    pixelsPerWave = std::min<uint64_t>(pixelsPerWave, regionPixels);
+    uint64_t capWide = pixelsPerWave * spp;
+    if (capWide > 0x7FFFFFFFull)
+        return set_error(GBSP_ERR_CAPACITY, "wave of %llu paths is too large",
+            (unsigned long long)capWide);
+    uint32_t cap = (uint32_t)capWide;
+    int rc = ensure_wave_buffers(rt, cap, std::max<uint32_t>(maxBounces, 1));
+    if (rc) return rc;
+    WaveBuffers wb;
+    wb.rayO = rt->rayO.ptr;
+    wb.rayD = rt->rayD.ptr;
+    wb.hitA = rt->hitA.ptr;
+    wb.hitInst = rt->hitInst.ptr;
+    wb.pathRng = rt->pathRng.ptr;
+    wb.pathLen = rt->pathLen.ptr;
+    wb.vertE = rt->vertE.ptr;
+    wb.vertA = rt->vertA.ptr;
+    wb.pathRad = rt->pathRad.ptr;
+    wb.cap = cap;
+    WaveParams wp;
+    wp.cam = cam;
+    wp.x0 = x0;
+    wp.y0 = y0;
+    wp.regionW = x1 - x0;
+    wp.spp = spp;
+    wp.maxBounces = maxBounces;
+    wp.seed = opt.seed;
+    wp.clampValue = opt.radiance_clamp;
+    wp.nanPolicy = opt.nan_policy;
+    wp.invSpp = 1.0f / (float)spp;
+    int persistentGrid = rt->smCount * 8;
+    bool timing = rt->stageTiming;
+    for (uint64_t pb = 0; pb < regionPixels; pb += pixelsPerWave) {
+        wp.pixelBase = pb;
+        wp.pixels = (uint32_t)std::min<uint64_t>(pixelsPerWave, regionPixels - pb);
+        uint32_t paths = wp.pixels * spp;
+        if (maxBounces == 0) {
+            GBSP_CUDA_TRY(cudaMemsetAsync(wb.pathRad, 0, sizeof(float4) * (size_t)paths, s));
+        } else {
+            k_reset_ctl<<<1, 32, 0, s>>>(ctl, paths);
+            k_generate<<<(paths + 255) / 256, 256, 0, s>>>(wp, wb);
+            rt->launches += 2;
+            for (uint32_t b = 0; b < maxBounces; b++) {
+                int inQ = (b & 1) ? kCtlQueue1 : kCtlQueue0;
+                int outQ = (b & 1) ? kCtlQueue0 : kCtlQueue1;
+                const float4 *qO = wb.rayO + ((b & 1) ? cap : 0);
+                const float4 *qD = wb.rayD + ((b & 1) ? cap : 0);
+                k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
+                int e0 = timing ? rt->stage_event(s) : -1;
+                k_trace<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA, wb.hitInst,
+                    ctl, counters, rt->dStatus);
+                int e1 = timing ? rt->stage_event(s) : -1;
+                k_shade<<<persistentGrid, 128, 0, s>>>(sv, mv, wp, wb, b, inQ, ctl, counters);
+                int e2 = timing ? rt->stage_event(s) : -1;
+                if (timing && e0 >= 0 && e1 >= 0 && e2 >= 0) {
+                    rt->traceSpans.emplace_back(e0, e1);
+                    rt->shadeSpans.emplace_back(e1, e2);
+                }
+                rt->launches += 3;
+                rt->traceLaunches += 1;
+            }
+        }
+        k_accumulate<<<(wp.pixels + 255) / 256, 256, 0, s>>>(wp, wb, dImage, imageWidth, counters);
+        rt->launches += 1;
+        GBSP_CUDA_TRY(cudaGetLastError());
+    }
+    return GBSP_OK;
+}
+
+}  // namespace gbsp

@@ -1,0 +1,246 @@
+// Closest-hit traversal of the two-level scene (device code).
+//
+// Semantics follow sp_RayIntersectScene / sp_RayIntersectMesh
+// (src/sp_scene.cpp:127-339):
+//   * an object is a candidate iff its world AABB passes the reference's
+//     slab test (src/simd.h:198-271) for the world ray;
+//   * the ray enters object space through the inverse model matrix and its
+//     direction is re-normalised there (src/sp_scene.cpp:274-276);
+//   * a triangle is a candidate iff its own AABB passes the slab test in
+//     object space (the reference collects exactly those BVH leaves,
+//     src/bvh.cpp:203-311) and the Moller-Trumbore test hits with t > 0;
+//   * per object the smallest object-space t wins, its hit point goes back
+//     to world space and t = dot(worldHit - o, d) (src/sp_scene.cpp:302-308);
+//     the smallest world t over objects wins.
+// Node boxes here are exact unions of the reference's leaf boxes, and the
+// slab test is monotone in the box, so interior tests never drop a leaf the
+// reference would test.  Unlike the reference, the walk is ordered and
+// prunes boxes that start beyond the best hit so far; pruning keeps a
+// relative margin of 2^-10 so that a triangle whose rounded t lands just
+// under its box's rounded entry distance is still tested.  Exact t ties go
+// to the lower triangle (or object) index instead of the reference's
+// BVH-order-dependent first find.
+#pragma once
+
+#include "gbsp_common.cuh"
+
+namespace gbsp {
+
+constexpr int kStackSize = 96;
+constexpr float kInf = __builtin_huge_valf();
+
+struct RayHit {
+    float t;       // world t, +inf = miss
+    float u, v;    // barycentrics of the winning triangle
+    int32_t prim;  // leaf-order triangle index in the pool, -1 = miss
+    int32_t inst;  // instance index (object-BVH leaf order), -1 = miss
+};
+
+struct TraceCounters {
+    uint32_t topNodes, meshNodes, boxTests, triTests, meshTests;
+};
+
+__device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765625f; }
+
+// Tests the 8 children of a node against the ray, pushing hits nearest-last.
+template <bool kCount>
+__device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
+    V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp, uint32_t *status,
+    TraceCounters &cnt)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(nodes + ref);
+    uint32_t nearRef = kEmptyChild;
+    float nearT = kInf;
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        float4 lx = __ldg(p + 0 + half), hx = __ldg(p + 2 + half);
+        float4 ly = __ldg(p + 4 + half), hy = __ldg(p + 6 + half);
+        float4 lz = __ldg(p + 8 + half), hz = __ldg(p + 10 + half);
+        uint4 ch = __ldg(reinterpret_cast<const uint4 *>(p + 12 + half));
+        float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, hxs[4] = {hx.x, hx.y, hx.z, hx.w};
+        float lys[4] = {ly.x, ly.y, ly.z, ly.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
+        float lzs[4] = {lz.x, lz.y, lz.z, lz.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
+        uint32_t chs[4] = {ch.x, ch.y, ch.z, ch.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t c = chs[k];
+            if (c == kEmptyChild) continue;
+            if (kCount) cnt.boxTests++;
+            float te = slab_entry(v3(lxs[k], lys[k], lzs[k]), v3(hxs[k], hys[k], hzs[k]), o, invd);
+            if (te < 0.0f || te > bound) continue;
+            if (te < nearT) {
+                if (nearRef != kEmptyChild) {
+                    if (sp < kStackSize) {
+                        stackRef[sp] = nearRef;
+                        stackT[sp] = nearT;
+                        sp++;
+                    } else {
+                        atomicOr(status, kStatusStackOverflow);
+                    }
+                }
+                nearRef = c;
+                nearT = te;
+            } else {
+                if (sp < kStackSize) {
+                    stackRef[sp] = c;
+                    stackT[sp] = te;
+                    sp++;
+                } else {
+                    atomicOr(status, kStatusStackOverflow);
+                }
+            }
+        }
+    }
+    if (nearRef != kEmptyChild) {
+        if (sp < kStackSize) {
+            stackRef[sp] = nearRef;
+            stackT[sp] = nearT;
+            sp++;
+        } else {
+            atomicOr(status, kStatusStackOverflow);
+        }
+    }
+}
+
+// Triangle candidates of one mesh leaf, in object space.
+template <bool kCount>
+__device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
+    V3 linvd, float &bestT, float &bestU, float &bestV, int32_t &bestPrim, TraceCounters &cnt)
+{
+    uint32_t first = leaf_first(ref), count = leaf_count(ref);
+    for (uint32_t k = 0; k < count; k++) {
+        uint32_t j = first + k;
+        const float4 *tp = reinterpret_cast<const float4 *>(sv.tris + j);
+        float4 A = __ldg(tp + 0), B = __ldg(tp + 1), C = __ldg(tp + 2);
+        V3 a = v3(A.x, A.y, A.z), b = v3(B.x, B.y, B.z), c = v3(C.x, C.y, C.z);
+        if (kCount) cnt.triTests++;
+        // the reference only reaches triangles whose own box passes
+        V3 bl = vmin(a, vmin(b, c)), bh = vmax(a, vmax(b, c));
+        if (slab_entry(bl, bh, lo, linvd) < 0.0f) continue;
+        TriHit h = ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
+        if (!h.hit || !(h.t > 0.0f)) continue;
+        bool take = h.t < bestT;
+        if (!take && h.t == bestT && bestPrim >= 0)
+            take = __ldg(sv.triIds + j) < __ldg(sv.triIds + bestPrim);
+        if (take) {
+            bestT = h.t;
+            bestU = h.u;
+            bestV = h.v;
+            bestPrim = (int32_t)j;
+        }
+    }
+}
+
+template <bool kCount>
+__device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *status,
+    TraceCounters &cnt)
+{
+    RayHit best;
+    best.t = kInf;
+    best.u = best.v = 0.0f;
+    best.prim = -1;
+    best.inst = -1;
+    if (sv.tlasRoot == kEmptyChild) return best;
+    uint32_t stackRef[kStackSize];
+    float stackT[kStackSize];
+    int sp = 0;
+    V3 invd = inverse(d);
+    stackRef[sp] = sv.tlasRoot;
+    stackT[sp] = 0.0f;
+    sp++;
+    const Node8 *__restrict__ nodes = sv.nodes;
+    // trees are validated at build time (children after parents), so the
+    // walk is finite; the guard only bounds it against corrupted memory
+    for (int guard = 0; sp > 0; guard++) {
+        if (guard >= (1 << 20)) {
+            atomicOr(status, kStatusStackOverflow);
+            break;
+        }
+        sp--;
+        uint32_t ref = stackRef[sp];
+        float te = stackT[sp];
+        if (te > prune_bound(best.t)) continue;
+        if (!child_is_leaf(ref)) {
+            if (kCount) cnt.topNodes++;
+            visit_node<kCount>(nodes, ref, o, invd, prune_bound(best.t), stackRef, stackT, sp,
+                status, cnt);
+            continue;
+        }
+        // an object whose world box passed: descend into its mesh
+        uint32_t inst = leaf_first(ref);
+        const Instance &in = sv.instances[inst];
+        Affine inv, model;
+#pragma unroll
+        for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
+        V3 lo = transform_point(inv, o);
+        float len;
+        V3 ld = normalize(transform_vector(inv, d), &len);
+        V3 linvd = inverse(ld);
+        if (kCount) cnt.meshTests++;
+        float lBestT = kInf, lU = 0.0f, lV = 0.0f;
+        int32_t lPrim = -1;
+        float localBound = best.t * len;
+        int base = sp;
+        if (sp >= kStackSize) {
+            atomicOr(status, kStatusStackOverflow);
+            continue;
+        }
+        stackRef[sp] = __ldg(&in.blasRoot);
+        stackT[sp] = 0.0f;
+        sp++;
+        for (int guard = 0; sp > base && guard < (1 << 22); guard++) {
+            sp--;
+            uint32_t r2 = stackRef[sp];
+            float t2 = stackT[sp];
+            float bound = prune_bound(rmin(lBestT, localBound));
+            if (t2 > bound) continue;
+            if (!child_is_leaf(r2)) {
+                if (kCount) cnt.meshNodes++;
+                visit_node<kCount>(nodes, r2, lo, linvd, bound, stackRef, stackT, sp, status, cnt);
+            } else {
+                visit_leaf<kCount>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+            }
+        }
+        sp = base;
+        if (lPrim < 0) continue;
+#pragma unroll
+        for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
+        V3 localHit = add(lo, mul(ld, lBestT));
+        V3 worldHit = transform_point(model, localHit);
+        float tw = dot(sub(worldHit, o), d);
+        if (tw < best.t || (tw == best.t && (int32_t)inst < best.inst)) {
+            best.t = tw;
+            best.u = lU;
+            best.v = lV;
+            best.prim = lPrim;
+            best.inst = (int32_t)inst;
+        }
+    }
+    return best;
+}
+
+// World-space normal and uv of a hit (src/sp_scene.cpp:189-215, 302-312).
+__device__ __forceinline__ void hit_surface(const SceneView &sv, const RayHit &h, V3 &normal,
+    float &uvx, float &uvy)
+{
+    const Instance &in = sv.instances[h.inst];
+    const float4 *tp = reinterpret_cast<const float4 *>(sv.tris + h.prim);
+    float4 A = __ldg(tp + 0), B = __ldg(tp + 1), C = __ldg(tp + 2);
+    const float4 *ap = reinterpret_cast<const float4 *>(sv.attrs + h.prim);
+    float4 a0 = __ldg(ap + 0), a1 = __ldg(ap + 1), a2 = __ldg(ap + 2), a3 = __ldg(ap + 3);
+    float w = 1.0f - h.u - h.v;
+    // uv0 = (a2.y, a2.z), uv1 = (a2.w, a3.x), uv2 = (a3.y, a3.z)
+    uvx = a2.y * w + a2.w * h.u + a3.y * h.v;
+    uvy = a2.z * w + a3.x * h.u + a3.z * h.v;
+    V3 ln = v3(A.w, B.w, C.w);
+    if (__ldg(&in.smooth)) {
+        V3 n0 = v3(a0.x, a0.y, a0.z), n1 = v3(a0.w, a1.x, a1.y), n2 = v3(a1.z, a1.w, a2.x);
+        ln = normalize(add(add(mul(n0, w), mul(n1, h.u)), mul(n2, h.v)));
+    }
+    Affine model;
+#pragma unroll
+    for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
+    normal = normalize(transform_vector(model, ln));
+}
+
+}  // namespace gbsp

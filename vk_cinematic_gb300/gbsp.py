@@ -1,0 +1,379 @@
+"""ctypes binding of libgbsp.so (include/gbsp.h) for tests and the benchmark.
+
+The library is the product; this module only marshals arguments.  It never
+falls back to anything: if the shared library is missing or the device
+call fails, it raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_vp = ctypes.c_void_p
+_u32 = ctypes.c_uint32
+_i32 = ctypes.c_int32
+_f32 = ctypes.c_float
+_u64 = ctypes.c_uint64
+
+GBSP_NO_TEXTURE = 0xFFFFFFFF
+GBSP_SKY_TEXTURE = 0xFFFFFFFE
+RNG_HASH_PER_SAMPLE = 0
+RNG_TILE_SEQUENTIAL = 1
+NAN_ZERO = 0
+NAN_PROPAGATE = 1
+METRIC_COUNT = 16
+METRIC_NAMES = [
+    "elapsed_ns", "paths_traced", "rays_traced", "ray_hit_count", "ray_miss_count",
+    "intersect_scene_ns", "broadphase_node_visits", "shade_ns", "midphase_node_visits",
+    "triangle_tests", "midphase_box_tests", "mesh_tests_performed", "nan_samples",
+    "trace_launches", "kernel_launches",
+]
+
+# Every symbol include/gbsp.h declares.
+EXPORTS = [
+    "gbsp_runtime_create", "gbsp_runtime_destroy", "gbsp_runtime_synchronize",
+    "gbsp_runtime_stream", "gbsp_last_error_string", "gbsp_version", "gbsp_options_default",
+    "gbsp_configure_camera", "gbsp_calculate_film_positions", "gbsp_scene_create",
+    "gbsp_scene_destroy", "gbsp_create_mesh", "gbsp_add_object_to_scene", "gbsp_clear_objects",
+    "gbsp_build_scene_broadphase", "gbsp_scene_info", "gbsp_ray_intersect_scene",
+    "gbsp_intersect_closest_device", "gbsp_material_system_create",
+    "gbsp_material_system_destroy", "gbsp_register_material", "gbsp_register_texture",
+    "gbsp_set_background_material", "gbsp_set_procedural_sky", "gbsp_path_trace_tile",
+    "gbsp_path_trace_frame", "gbsp_frame_device_pointer", "gbsp_icosphere", "gbsp_plane_mesh",
+    "gbsp_sample_seed",
+]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("spp", _u32), ("max_bounces", _u32), ("seed", _u32), ("rng_mode", _u32),
+                ("nan_policy", _u32), ("radiance_clamp", _f32), ("wave_paths", _u32),
+                ("flags", _u32)]
+
+
+FLAG_STAGE_TIMING = 1
+
+
+class ImagePlane(ctypes.Structure):
+    _fields_ = [("pixels", _vp), ("width", _u32), ("height", _u32)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("right", _f32 * 3), ("up", _f32 * 3), ("forward", _f32 * 3),
+                ("position", _f32 * 3), ("filmCenter", _f32 * 3),
+                ("imagePlane", ctypes.POINTER(ImagePlane)), ("halfPixelWidth", _f32),
+                ("halfPixelHeight", _f32), ("halfFilmWidth", _f32), ("halfFilmHeight", _f32)]
+
+
+class Context(ctypes.Structure):
+    _fields_ = [("camera", ctypes.POINTER(Camera)), ("scene", _vp), ("materialSystem", _vp),
+                ("runtime", _vp), ("options", ctypes.POINTER(Options))]
+
+
+class Tile(ctypes.Structure):
+    _fields_ = [("minX", _u32), ("minY", _u32), ("maxX", _u32), ("maxY", _u32)]
+
+
+class Metrics(ctypes.Structure):
+    _fields_ = [("values", _u64 * METRIC_COUNT)]
+
+    def as_dict(self):
+        return {n: int(self.values[i]) for i, n in enumerate(METRIC_NAMES)}
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("albedo", _f32 * 3), ("albedoTexture", _u32), ("emission", _f32 * 3),
+                ("emissionTexture", _u32), ("roughness", _f32)]
+
+
+assert ctypes.sizeof(Material) == 36
+
+
+class GbspError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libgbsp.so (building it in-tree if needed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(path):
+        raise GbspError(f"{path} is missing: run vk_cinematic_gb300.build first")
+    lib = ctypes.CDLL(path)
+    lib.gbsp_last_error_string.restype = ctypes.c_char_p
+    lib.gbsp_runtime_stream.restype = _vp
+    lib.gbsp_frame_device_pointer.restype = _vp
+    lib.gbsp_sample_seed.restype = _u32
+    lib.gbsp_calculate_film_positions.restype = _u32
+    for name in EXPORTS:
+        getattr(lib, name)  # raises if a declared symbol is not exported
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = _LIB.gbsp_last_error_string().decode(errors="replace")
+        raise GbspError(f"gbsp status {rc}: {msg}")
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_vp)
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    load().gbsp_options_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Runtime:
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self.L = load()
+        h = _vp()
+        _check(self.L.gbsp_runtime_create(_i32(device), _vp(stream) if stream else None,
+                                          ctypes.byref(h)))
+        self.h = h
+
+    @property
+    def stream(self) -> int:
+        return self.L.gbsp_runtime_stream(self.h)
+
+    def synchronize(self):
+        _check(self.L.gbsp_runtime_synchronize(self.h))
+
+    def close(self):
+        if self.h:
+            self.L.gbsp_runtime_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MaterialSystem:
+    def __init__(self, rt: Runtime):
+        self.L, self.rt = rt.L, rt
+        h = _vp()
+        _check(self.L.gbsp_material_system_create(rt.h, ctypes.byref(h)))
+        self.h = h
+
+    def register(self, mid: int, albedo=(0, 0, 0), emission=(0, 0, 0), roughness=0.0,
+                 albedo_texture=GBSP_NO_TEXTURE, emission_texture=GBSP_NO_TEXTURE):
+        m = Material()
+        m.albedo[:] = [float(a) for a in albedo]
+        m.emission[:] = [float(e) for e in emission]
+        m.roughness = float(roughness)
+        m.albedoTexture = int(albedo_texture)
+        m.emissionTexture = int(emission_texture)
+        _check(self.L.gbsp_register_material(self.h, ctypes.byref(m), _u32(mid)))
+
+    def register_texture(self, tid: int, rgba: np.ndarray):
+        a = np.ascontiguousarray(rgba, dtype=np.float32)
+        _check(self.L.gbsp_register_texture(self.h, _p(a), _u32(a.shape[1]), _u32(a.shape[0]),
+                                            _u32(tid)))
+
+    def set_background(self, mid: int):
+        _check(self.L.gbsp_set_background_material(self.h, _u32(mid)))
+
+    def set_sky(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == 13
+        _check(self.L.gbsp_set_procedural_sky(self.h, _p(p)))
+
+    def close(self):
+        if self.h:
+            self.L.gbsp_material_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    def __init__(self, rt: Runtime):
+        self.L, self.rt = rt.L, rt
+        h = _vp()
+        _check(self.L.gbsp_scene_create(rt.h, ctypes.byref(h)))
+        self.h = h
+
+    def create_mesh(self, vertices: np.ndarray, indices: np.ndarray, smooth=False) -> int:
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 8)
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1)
+        out = _u32()
+        _check(self.L.gbsp_create_mesh(self.h, _p(v), _u32(len(v)), _p(i), _u32(len(i)),
+                                       _i32(int(smooth)), ctypes.byref(out)))
+        return out.value
+
+    def add_object(self, mesh, material, position, rotation, scale):
+        p = np.ascontiguousarray(position, dtype=np.float32)
+        r = np.ascontiguousarray(rotation, dtype=np.float32)
+        s = np.ascontiguousarray(scale, dtype=np.float32)
+        _check(self.L.gbsp_add_object_to_scene(self.h, _u32(mesh), _u32(material), _p(p), _p(r),
+                                               _p(s)))
+
+    def clear_objects(self):
+        _check(self.L.gbsp_clear_objects(self.h))
+
+    def build_broadphase(self):
+        _check(self.L.gbsp_build_scene_broadphase(self.h))
+
+    def info(self):
+        o, t, n, d = _u32(), _u64(), _u32(), _u32()
+        _check(self.L.gbsp_scene_info(self.h, ctypes.byref(o), ctypes.byref(t), ctypes.byref(n),
+                                      ctypes.byref(d)))
+        return dict(objects=o.value, triangles=t.value, mesh_nodes=n.value, max_depth=d.value)
+
+    def intersect(self, rays: np.ndarray):
+        """sp_RayIntersectScene on a host batch: returns (t,n,u,v) rows, material ids, metrics."""
+        r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        out = np.zeros((len(r), 6), np.float32)
+        mat = np.zeros(len(r), np.uint32)
+        m = Metrics()
+        _check(self.L.gbsp_ray_intersect_scene(self.h, _u32(len(r)), _p(r), _p(out), _p(mat),
+                                               ctypes.byref(m)))
+        return out, mat, m
+
+    def intersect_closest_device(self, count: int, rays_ptr: int, t_ptr: int, tri_ptr: int,
+                                 obj_ptr: int = 0):
+        _check(self.L.gbsp_intersect_closest_device(self.h, _u32(count), _vp(rays_ptr),
+                                                    _vp(t_ptr), _vp(tri_ptr),
+                                                    _vp(obj_ptr) if obj_ptr else None))
+
+    def close(self):
+        if self.h:
+            self.L.gbsp_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Renderer:
+    """Camera + image plane + context for one scene and material system."""
+
+    def __init__(self, rt: Runtime, scene: Scene, ms: MaterialSystem, width: int, height: int,
+                 position, rotation, film_distance: float, options: Options | None = None):
+        self.L, self.rt, self.scene, self.ms = rt.L, rt, scene, ms
+        self.plane = ImagePlane(None, width, height)
+        self.camera = Camera()
+        p = np.ascontiguousarray(position, dtype=np.float32)
+        r = np.ascontiguousarray(rotation, dtype=np.float32)
+        _check(self.L.gbsp_configure_camera(ctypes.byref(self.camera), ctypes.byref(self.plane),
+                                            _p(p), _p(r), _f32(film_distance)))
+        self.options = options or default_options()
+        self.ctx = Context(ctypes.pointer(self.camera), scene.h, ms.h, rt.h,
+                           ctypes.pointer(self.options))
+        self.width, self.height = width, height
+
+    def set_host_pixels(self, array: np.ndarray | None):
+        if array is None:
+            self.plane.pixels = None
+        else:
+            assert array.dtype == np.float32 and array.flags["C_CONTIGUOUS"]
+            assert array.size == self.width * self.height * 4
+            self.plane.pixels = array.ctypes.data
+        self._pixels = array
+
+    def frame(self, metrics: bool = True, pixels: np.ndarray | None = None):
+        out = pixels if pixels is not None else np.zeros((self.height, self.width, 4), np.float32)
+        self.set_host_pixels(out)
+        m = Metrics() if metrics else None
+        _check(self.L.gbsp_path_trace_frame(ctypes.byref(self.ctx),
+                                            ctypes.byref(m) if m is not None else None))
+        self.set_host_pixels(None)
+        return out, m
+
+    def frame_async(self):
+        """Device-only frame (no host copy, no metrics, no synchronisation)."""
+        self.set_host_pixels(None)
+        _check(self.L.gbsp_path_trace_frame(ctypes.byref(self.ctx), None))
+
+    def tile(self, tile, rng_state: int = 0, pixels: np.ndarray | None = None):
+        out = pixels if pixels is not None else np.zeros((self.height, self.width, 4), np.float32)
+        self.set_host_pixels(out)
+        rng = _u32(rng_state)
+        m = Metrics()
+        t = Tile(*[int(v) for v in tile])
+        _check(self.L.gbsp_path_trace_tile(ctypes.byref(self.ctx), t, ctypes.byref(rng),
+                                           ctypes.byref(m)))
+        self.set_host_pixels(None)
+        return out, rng.value, m
+
+    def frame_device_pointer(self) -> int:
+        return self.L.gbsp_frame_device_pointer(self.rt.h)
+
+
+def film_positions(camera: Camera, pixels: np.ndarray) -> np.ndarray:
+    px = np.ascontiguousarray(pixels, dtype=np.float32).reshape(-1, 2)
+    out = np.zeros((len(px), 3), np.float32)
+    load().gbsp_calculate_film_positions(ctypes.byref(camera), _p(out), _p(px), _u32(len(px)))
+    return out
+
+
+def sample_seed(seed, x, y, s) -> int:
+    return int(load().gbsp_sample_seed(_u32(seed), _u32(x), _u32(y), _u32(s)))
+
+
+def icosphere(level: int):
+    L = load()
+    nv, ni = _u32(), _u32()
+    _check(L.gbsp_icosphere(_u32(level), None, None, ctypes.byref(nv), ctypes.byref(ni)))
+    v = np.zeros((nv.value, 8), np.float32)
+    i = np.zeros(ni.value, np.uint32)
+    _check(L.gbsp_icosphere(_u32(level), _p(v), _p(i), ctypes.byref(nv), ctypes.byref(ni)))
+    return v, i
+
+
+def plane_mesh():
+    v = np.zeros((4, 8), np.float32)
+    i = np.zeros(6, np.uint32)
+    _check(load().gbsp_plane_mesh(_p(v), _p(i)))
+    return v, i
+
+
+def upload_scene(rt: Runtime, s, options: Options | None = None):
+    """Builds device objects for a vk_cinematic_gb300.scenes.Scene."""
+    scene = Scene(rt)
+    meshes = [scene.create_mesh(v, i, sm) for (v, i, sm) in s.meshes]
+    for o in s.objects:
+        scene.add_object(meshes[o.mesh], o.material, o.position, o.rotation, o.scale)
+    scene.build_broadphase()
+    ms = MaterialSystem(rt)
+    for tid, tex in s.textures.items():
+        ms.register_texture(tid, tex)
+    for mid, m in s.materials.items():
+        ms.register(mid, **m)
+    ms.set_background(s.background)
+    if s.sky is not None:
+        ms.set_sky(s.sky)
+    opt = options or default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed)
+    rend = Renderer(rt, scene, ms, s.width, s.height, s.camera_position, s.camera_rotation,
+                    s.film_distance, opt) if s.width else None
+    return scene, ms, rend
