@@ -1,0 +1,424 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 path tracer on its headline workload.
+
+Workload (default "config3"): 1920x1080, 64 spp, up to 5 bounces; 256
+icospheres (subdivision 5, 20,480 triangles each, one shared mesh) over a
+ground quad, 85% diffuse / 15% emissive, analytic sky with a sun disc.  One
+step renders one whole frame.
+
+  value   samples/s of frames rendered with the image kept in device memory
+  e2e     the same metric through the C ABI as a caller of sp_PathTraceTile
+          uses it each frame: rebuild the object set and broadphase from host
+          data (src/main.cpp:1529-1556) and read the RGBA32F frame back into
+          pinned host memory
+  roofline  the closest-hit kernel: algorithmic bytes per launch (rays in/out
+          + node and triangle fetches counted by the kernel) over its mean
+          launch time from CUDA events recorded around every launch on the
+          launching stream during the timed frames
+  cpu_baseline  the oracle port (a restatement of the reference's CPU path
+          tracer) in the reference's own tile mode on this host's cores
+
+--impl reference times the reference's CPU path tracer algorithm (the oracle
+port; the x86-only reference build cannot run on this host) on the same
+workload and prints the same metric.
+
+Multi-GPU: replicas.  Each rank renders its own frames of the same scene
+with its own sample seed (weak scaling); there is no data-path exchange.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+TRACE_BYTES_PER_RAY = 32    # ray in (origin + direction, 24 B) and hit out (8 B)
+NODE_BYTES = 224            # one 8-wide node
+TRI_BYTES = 48              # one triangle record
+FLUSH_BYTES = 256 << 20     # > 129 MB L2
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gbsp", "reference"], default="gbsp")
+    ap.add_argument("--workload", choices=["config3", "config1"], default="config3")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU work of the cpu_baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def make_scene(workload, rank=0):
+    from vk_cinematic_gb300 import scenes
+
+    if workload == "config1":
+        s = scenes.config1_scene()
+    else:
+        s = scenes.config3_scene()
+    s.seed = s.seed + 1000 * rank
+    return s
+
+
+def workload_config(s, workload):
+    return {
+        "workload": ("config3: 1920x1080, 64 spp, 5 bounces, 256 icospheres (subdivision 5) + "
+                     "ground, analytic sky" if workload == "config3" else
+                     "config1: 128x128, 8 spp, 3 bounces, icosphere (subdivision 3) + ground"),
+        "width": s.width, "height": s.height, "spp": s.spp, "max_bounces": s.max_bounces,
+        "objects": len(s.objects), "triangles": int(s.triangle_count),
+        "rng": "hash per (seed, x, y, sample)",
+        "l2": "flushed (256 MB device write) before every timed step",
+    }
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the closest-hit kernel from a committed ncu
+    summary (profiles/trace_kernel_dram.json), scaled to this run's rays per
+    launch; None if no capture was committed."""
+    p = os.path.join(ROOT, "profiles", "trace_kernel_dram.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f)
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_baseline_run(s, seconds_target, threads=None):
+    """The oracle port in the reference's tile mode (64x64 tiles, RNG reset to
+    0xF51C0E49 per tile, src/main.cpp:731-759) on a bounded, evenly spread
+    subset of the frame's tiles.  Returns a dict in the bench format."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle as po
+    from golden_scenes import build_world
+
+    po.build_port()
+    threads = threads or os.cpu_count() or 1
+    t0 = time.time()
+    w = build_world("port", s)
+    if s.sky is not None:
+        w.set_sky(s.sky)
+    w.set_options(spp=s.spp, max_bounces=s.max_bounces, max_broadphase=1 << 16,
+                  max_midphase=1 << 20)
+    setup_s = time.time() - t0
+    tiles_x = (s.width + 63) // 64
+    tiles_y = (s.height + 63) // 64
+    total_tiles = tiles_x * tiles_y
+    pixels = np.zeros((s.height, s.width, 4), np.float32)
+    # calibrate on a few tiles in the middle of the frame
+    cal = max(1, min(threads, total_tiles))
+    first = total_tiles // 2
+    dt, _, m = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
+                                 s.film_distance, 64, first, cal, threads, pixels)
+    per_tile = dt / cal
+    n = int(max(cal, min(total_tiles, seconds_target / max(per_tile, 1e-6))))
+    # evenly spread contiguous runs: render n tiles starting at a centred offset
+    start = max(0, (total_tiles - n) // 2)
+    dt, _, m = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
+                                 s.film_distance, 64, start, n, threads, pixels)
+    paths, rays = int(m[1]), int(m[2])
+    return {
+        "value": paths / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+        "mrays_per_s": rays / dt / 1e6,
+        "sample": (f"{n} of {total_tiles} 64x64 tiles (tiles {start}..{start + n - 1}) at "
+                   f"{s.spp} spp, {paths} paths, {rays} rays in {dt:.2f} s; "
+                   f"reference tile-mode RNG; BVH/scene setup {setup_s:.1f} s untimed"),
+        "seconds": dt,
+    }
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    s = make_scene(args.workload)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pyoracle as po
+    from golden_scenes import build_world
+
+    po.build_port()
+    threads = os.cpu_count() or 1
+    w = build_world("port", s)
+    if s.sky is not None:
+        w.set_sky(s.sky)
+    w.set_options(spp=s.spp, max_bounces=s.max_bounces, max_broadphase=1 << 16,
+                  max_midphase=1 << 20)
+    tiles_x = (s.width + 63) // 64
+    total = tiles_x * ((s.height + 63) // 64)
+    pixels = np.zeros((s.height, s.width, 4), np.float32)
+    dt, _, _ = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
+                                 s.film_distance, 64, total // 2, threads, threads, pixels)
+    per_tile = dt / threads
+    # each step renders a fixed run of tiles sized to about 4 s of work
+    n = int(max(threads, min(total, 4.0 / max(per_tile, 1e-6))))
+    start = max(0, (total - n) // 2)
+    for _ in range(args.warmup):
+        w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
+                          s.film_distance, 64, start, n, threads, pixels)
+    paths = rays = 0
+    elapsed = 0.0
+    for _ in range(args.steps):
+        dt, _, m = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
+                                     s.film_distance, 64, start, n, threads, pixels)
+        elapsed += dt
+        paths += int(m[1])
+        rays += int(m[2])
+    value = paths / elapsed / 1e6
+    line = {
+        "impl": "reference", "metric": "spp/s at 1080p (path-traced samples per second)",
+        "value": value, "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded procedural scene", "config": workload_config(s, args.workload),
+        "mrays_per_s": rays / elapsed / 1e6,
+        "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} of {total} 64x64 tiles per step at {s.spp} spp "
+                                   f"(reference tile-mode RNG)"},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    if world > 1:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl", rank=rank, world_size=world)
+    torch.cuda.set_device(local)
+    from vk_cinematic_gb300 import gbsp
+
+    stream = torch.cuda.current_stream()
+    rt = gbsp.Runtime(local, stream=stream.cuda_stream)
+    s = make_scene(args.workload, rank)
+    opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed,
+                               flags=gbsp.FLAG_STAGE_TIMING)
+    scene, ms, rend = gbsp.upload_scene(rt, s, opt)
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        rend.frame_device(metrics=True)
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    totals = np.zeros(gbsp.METRIC_COUNT, np.uint64)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        flush.zero_()
+        m = rend.frame_device(metrics=True)
+        totals += np.array(list(m.values), np.uint64)
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
+    cnt = torch.tensor([float(totals[1]), float(totals[2])], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(cnt, op=dist.ReduceOp.SUM)
+    elapsed_ms = float(t.item())
+    paths_all, rays_all = float(cnt[0].item()), float(cnt[1].item())
+    M = dict(zip(gbsp.METRIC_NAMES, [int(v) for v in totals]))
+    value = paths_all / (elapsed_ms / 1e3) / 1e6
+
+    # ---- roofline of the closest-hit kernel (this rank's launches)
+    peak, peak_kind = measured_peaks()
+    launches = max(1, M["trace_launches"])
+    trace_s = M["intersect_scene_ns"] / 1e9
+    alg_bytes = (M["rays_traced"] * TRACE_BYTES_PER_RAY
+                 + (M["broadphase_node_visits"] + M["midphase_node_visits"]) * NODE_BYTES
+                 + M["triangle_tests"] * TRI_BYTES)
+    achieved = (alg_bytes / launches) / (trace_s / launches) / 1e9 if trace_s > 0 else None
+    traffic = None
+    tp = profiled_traffic()
+    if tp and tp.get("dram_bytes_per_ray"):
+        traffic = tp["dram_bytes_per_ray"] * M["rays_traced"] / launches
+    roofline = {
+        "bound": "hbm", "kernel": "k_trace (closest hit)", "achieved": achieved, "peak": peak,
+        "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+        "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+        "bytes_per_launch": alg_bytes / launches, "mean_launch_ms": 1e3 * trace_s / launches,
+        "trace_share_of_frame": (M["intersect_scene_ns"] / 1e6) / max(elapsed_ms, 1e-9),
+        "per_ray": {"node_visits": (M["broadphase_node_visits"] + M["midphase_node_visits"])
+                    / max(1, M["rays_traced"]),
+                    "triangle_tests": M["triangle_tests"] / max(1, M["rays_traced"])},
+    }
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((s.height, s.width, 4), dtype=torch.float32, pin_memory=True)
+        host_np = host.numpy()
+        objs = s.objects
+        inst_bytes = 176  # per object: world box (32 B) + instance record (144 B)
+        h2d = len(objs) * (inst_bytes + 4)
+        d2h = host_np.nbytes
+        opt.flags = 0
+        for _ in range(1):
+            scene.clear_objects()
+            for o in objs:
+                scene.add_object(o.mesh, o.material, o.position, o.rotation, o.scale)
+            scene.build_broadphase()
+            rend.frame(metrics=False, pixels=host_np)
+        barrier()
+        e_paths = 0
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            scene.clear_objects()
+            for o in objs:
+                scene.add_object(o.mesh, o.material, o.position, o.rotation, o.scale)
+            scene.build_broadphase()
+            rend.frame(metrics=False, pixels=host_np)
+            e_paths += s.width * s.height * s.spp
+        barrier()
+        e_dt = time.perf_counter() - t0
+        et = torch.tensor([e_dt], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(et, op=dist.ReduceOp.MAX)
+        e2e = {"value": e_paths * world / float(et.item()) / 1e6, "unit": "Msamples/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": 1e3 * float(et.item()) / args.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline_run(make_scene(args.workload), args.cpu_seconds)
+        except Exception as ex:  # report, never fail the GPU measurement on it
+            cpu = {"error": str(ex)}
+
+    if rank == 0:
+        line = {
+            "metric": "spp/s at 1080p (path-traced samples per second)",
+            "value": value, "unit": "Msamples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded procedural scene", "config": workload_config(s, args.workload),
+            "mrays_per_s": rays_all / (elapsed_ms / 1e3) / 1e6,
+            "parallelism": f"replicas x{world}",
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(M["kernel_launches"]), "clocks": clk,
+            "metrics": {k: M[k] for k in ("paths_traced", "rays_traced", "ray_hit_count",
+                                          "ray_miss_count", "nan_samples", "trace_launches")},
+        }
+        print(json.dumps(line), flush=True)
+    rt.synchronize()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -106,6 +106,23 @@ def test_tile_entry_point_rng_and_region(rt, port):
     assert m.as_dict()["paths_traced"] == 16 * 12 * 2
 
 
+def test_runtime_outlives_its_scenes(gpu_lib):
+    """Destroying a runtime before its scene and material system is allowed:
+    the runtime stays alive until the last of them is destroyed."""
+    r = gbsp.Runtime()
+    scene = gbsp.Scene(r)
+    ms = gbsp.MaterialSystem(r)
+    v, i = scenes.icosphere(1)
+    mesh = scene.create_mesh(v, i)
+    r.close()
+    scene.add_object(mesh, 1, (0, 0, 0), scenes.IDENTITY_QUAT, (1, 1, 1))
+    scene.build_broadphase()
+    out, _, _ = scene.intersect(np.array([[0, 0, 5, 0, 0, -1]], np.float32))
+    assert abs(out[0, 0] - 4.0) < 0.1
+    scene.close()
+    ms.close()
+
+
 def test_empty_scene_is_magenta(rt):
     """TestPathTraceSingleColor / TestPathTraceTile
     (unit_tests/test_simd_path_tracer.cpp:49-135): no objects and no material

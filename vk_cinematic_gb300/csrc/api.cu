@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "gbsp_internal.h"
@@ -277,9 +278,12 @@ int gbsp_runtime_create(int device, void *stream, gbsp_runtime **out)
     return GBSP_OK;
 }
 
-int gbsp_runtime_destroy(gbsp_runtime *rt)
+}  // extern "C"
+
+static std::mutex g_runtimeMutex;
+
+static void runtime_teardown(gbsp_runtime *rt)
 {
-    if (!rt) return GBSP_OK;
     cudaStreamSynchronize(rt->stream);
     rt->rayO.release();
     rt->rayD.release();
@@ -297,8 +301,41 @@ int gbsp_runtime_destroy(gbsp_runtime *rt)
     if (rt->dCounters) cudaFree(rt->dCounters);
     for (auto &ev : rt->ev)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : rt->evPool) cudaEventDestroy(ev);
     if (rt->ownsStream) cudaStreamDestroy(rt->stream);
     delete rt;
+}
+
+// Drops one reference; the last one tears the runtime down.
+static void runtime_release(gbsp_runtime *rt)
+{
+    bool last;
+    {
+        std::lock_guard<std::mutex> lock(g_runtimeMutex);
+        last = --rt->refs == 0;
+    }
+    if (last) runtime_teardown(rt);
+}
+
+static int runtime_retain(gbsp_runtime *rt)
+{
+    std::lock_guard<std::mutex> lock(g_runtimeMutex);
+    if (rt->closed) return set_error(GBSP_ERR_INVALID_ARGUMENT, "runtime already destroyed");
+    rt->refs++;
+    return GBSP_OK;
+}
+
+extern "C" {
+
+int gbsp_runtime_destroy(gbsp_runtime *rt)
+{
+    if (!rt) return GBSP_OK;
+    {
+        std::lock_guard<std::mutex> lock(g_runtimeMutex);
+        if (rt->closed) return set_error(GBSP_ERR_INVALID_ARGUMENT, "runtime destroyed twice");
+        rt->closed = true;
+    }
+    runtime_release(rt);
     return GBSP_OK;
 }
 
@@ -379,6 +416,8 @@ uint32_t gbsp_sample_seed(uint32_t seed, uint32_t x, uint32_t y, uint32_t sample
 int gbsp_scene_create(gbsp_runtime *rt, gbsp_scene **out)
 {
     if (!rt || !out) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    int rc = runtime_retain(rt);
+    if (rc) return rc;
     gbsp_scene *s = new gbsp_scene();
     s->rt = rt;
     *out = s;
@@ -388,8 +427,10 @@ int gbsp_scene_create(gbsp_runtime *rt, gbsp_scene **out)
 int gbsp_scene_destroy(gbsp_scene *scene)
 {
     if (!scene) return GBSP_OK;
-    cudaStreamSynchronize(scene->rt->stream);
-    delete scene;
+    gbsp_runtime *rt = scene->rt;
+    cudaStreamSynchronize(rt->stream);
+    delete scene;  // device buffers are freed in stream order on rt's stream
+    runtime_release(rt);
     return GBSP_OK;
 }
 
@@ -687,6 +728,8 @@ int gbsp_ray_intersect_scene(gbsp_scene *scene, uint32_t count, const float *ray
 int gbsp_material_system_create(gbsp_runtime *rt, gbsp_material_system **out)
 {
     if (!rt || !out) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    int rc = runtime_retain(rt);
+    if (rc) return rc;
     gbsp_material_system *ms = new gbsp_material_system();
     ms->rt = rt;
     *out = ms;
@@ -696,8 +739,10 @@ int gbsp_material_system_create(gbsp_runtime *rt, gbsp_material_system **out)
 int gbsp_material_system_destroy(gbsp_material_system *ms)
 {
     if (!ms) return GBSP_OK;
-    cudaStreamSynchronize(ms->rt->stream);
+    gbsp_runtime *rt = ms->rt;
+    cudaStreamSynchronize(rt->stream);
     delete ms;
+    runtime_release(rt);
     return GBSP_OK;
 }
 

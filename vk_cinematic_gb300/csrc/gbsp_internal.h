@@ -69,7 +69,11 @@ struct Counters;  // device metric block
 
 }  // namespace gbsp
 
+// A runtime lives until gbsp_runtime_destroy has been called AND every scene
+// and material system created on it has been destroyed (reference count).
 struct gbsp_runtime {
+    int refs = 1;                       // guarded by the API's runtime mutex
+    bool closed = false;
     int device = 0;
     cudaStream_t stream = nullptr;
     bool ownsStream = false;

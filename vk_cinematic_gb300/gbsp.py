@@ -315,6 +315,15 @@ class Renderer:
         self.set_host_pixels(None)
         _check(self.L.gbsp_path_trace_frame(ctypes.byref(self.ctx), None))
 
+    def frame_device(self, metrics: bool = True):
+        """Device-only frame (the image stays in device memory); with metrics
+        the call waits for the frame and returns its counters."""
+        self.set_host_pixels(None)
+        m = Metrics() if metrics else None
+        _check(self.L.gbsp_path_trace_frame(ctypes.byref(self.ctx),
+                                            ctypes.byref(m) if m is not None else None))
+        return m
+
     def tile(self, tile, rng_state: int = 0, pixels: np.ndarray | None = None):
         out = pixels if pixels is not None else np.zeros((self.height, self.width, 4), np.float32)
         self.set_host_pixels(out)
