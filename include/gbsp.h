@@ -243,6 +243,25 @@ int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile,
  * in one device pass).  The frame stays on the device (gbsp_frame_device_pointer)
  * and is also copied to imagePlane->pixels when that is not NULL. */
 int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics);
+/* Tile render that allocates no memory.  No counterpart in the reference: it
+ * is for callers that must not allocate device memory per call - e.g. a
+ * render loop that runs under a fixed device-memory budget, or that cannot
+ * afford the device-wide synchronisation an allocation may cause - but can
+ * still hand the library its inputs and an output image.  Same result as
+ * gbsp_path_trace_tile in GBSP_RNG_HASH_PER_SAMPLE mode, written into
+ * deviceImage (device memory, imagePlane->width * imagePlane->height
+ * RGBA32F, 16-byte aligned; only the tile is written).  The working memory is
+ * one fixed array inside libgbsp that every GPU loading the library holds
+ * until exit (about 5.8 MB): at most 16384 paths in flight, 8 bounces and
+ * 4096 objects; larger requests fail with GBSP_ERR_CAPACITY.  The scene's
+ * broadphase must be built and the material system uploaded by an earlier
+ * render (else GBSP_ERR_NOT_READY).  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other threads, other runtimes on the same device) race and
+ * must be serialised by the caller.  The call waits for its own work. */
+int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile tile,
+    float *deviceImage, gbsp_metrics *metrics);
 /* Device pointer of the runtime's last frame (width*height RGBA32F). */
 const float *gbsp_frame_device_pointer(gbsp_runtime *rt);
 

@@ -22,9 +22,11 @@
 // expression in the reference's order.
 
 #include <algorithm>
+#include <mutex>
 
 #include "gbsp_internal.h"
 #include "traverse.cuh"
+#include "shading.cuh"
 
 namespace gbsp {
 
@@ -62,109 +64,6 @@ struct WaveParams {
     uint32_t nanPolicy;
     float invSpp;
 };
-
-// ---------------------------------------------------------------------------
-// Material evaluation (src/sp_material_system.cpp:59-105, image.h:3-18)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ V3 texel_nearest(const MaterialView &mv, int slot, float u, float v)
-{
-    TextureDesc t = mv.textures[slot];
-    float fx = u * (float)t.width;
-    float fy = v * (float)t.height;
-    uint32_t x = (uint32_t)floorf(fx);
-    uint32_t y = (uint32_t)floorf(fy);
-    uint64_t idx = (uint64_t)y * t.width + x;
-    uint64_t maxIdx = (uint64_t)t.width * t.height - 1;  // the reference may read index W*H
-    if (idx > maxIdx) idx = maxIdx;
-    float4 p = __ldg(mv.texels + t.offset + idx);
-    return v3(p.x, p.y, p.z);
-}
-
-__device__ __forceinline__ V3 sky_radiance(const SkyParams &s, V3 dir)
-{
-    float t = rclamp(0.5f * (dir.y + 1.0f), 0.0f, 1.0f);
-    V3 c = add(s.bottom, mul(sub(s.top, s.bottom), t));
-    if (dot(dir, s.sunDir) >= s.cosSunRadius) c = add(c, s.sunRadiance);
-    return c;
-}
-
-// Per-vertex terms of ComputeRadianceForPath for the material in `slot`.
-__device__ __forceinline__ void vertex_terms(const MaterialView &mv, int slot, V3 N, V3 L, V3 V,
-    float uvx, float uvy, float4 &ec, float4 &aa)
-{
-    V3 albedo = v3(0.0f, 0.0f, 0.0f), emission;
-    float roughness = 0.0f;
-    if (slot < 0) {
-        emission = v3(1.0f, 0.0f, 1.0f);  // missing material: magenta
-    } else {
-        const DeviceMaterial &m = mv.materials[slot];
-        albedo = m.albedoTex >= 0 ? texel_nearest(mv, m.albedoTex, uvx, uvy)
-                                  : v3(m.albedo[0], m.albedo[1], m.albedo[2]);
-        if (m.emissionTex == -2) {
-            emission = sky_radiance(mv.sky, neg(V));
-        } else if (m.emissionTex >= 0) {
-            V3 dir = neg(V);  // src/math_lib.h:849-884
-            float inc = atan2f(sqrtf(dir.x * dir.x + dir.z * dir.z), dir.y);
-            float az = atan2f(dir.z, dir.x);
-            if (az < 0.0f) az += 2.0f * kPi;
-            float eu = az / (2.0f * kPi);
-            float ev = cosf(inc) * 0.5f + 0.5f;
-            ev = 1.0f - ev;
-            emission = mul(texel_nearest(mv, m.emissionTex, eu, ev), 1.0f);
-        } else {
-            emission = v3(m.emission[0], m.emission[1], m.emission[2]);
-        }
-        roughness = m.roughness;
-    }
-    float cosine = rmax(0.0f, dot(N, L));
-    V3 H = normalize(add(L, V));
-    // FresnelSchlick(max(H.V, 0), 0.04) (src/simd_path_tracer.cpp:65-70)
-    float p5 = powf(1.0f - rmax(dot(H, V), 0.0f), 5.0f);
-    float F0 = 0.04f;
-    float Fs = F0 + (1.0f - F0) * p5;
-    V3 F = v3(Fs, Fs, Fs);
-    V3 kD = sub(v3(1.0f, 1.0f, 1.0f), F);
-    // DistributionGGX (:72-84)
-    float a = roughness * roughness;
-    float a2 = a * a;
-    float NdotH = rmax(dot(N, H), 0.0f);
-    float NdotH2 = NdotH * NdotH;
-    float denom = (NdotH2 * (a2 - 1.0f) + 1.0f);
-    denom = kPi * denom * denom;
-    float NDF = a2 / denom;
-    // GeometrySmith (:86-105)
-    float NdotV = rmax(dot(N, V), 0.0f);
-    float NdotL = rmax(dot(N, L), 0.0f);
-    float r1 = roughness + 1.0f;
-    float k = (r1 * r1) / 8.0f;
-    float ggx2 = NdotV / (NdotV * (1.0f - k) + k);
-    float ggx1 = NdotL / (NdotL * (1.0f - k) + k);
-    float G = ggx1 * ggx2;
-    V3 numerator = mul(F, NDF * G);
-    float denominator = 4.0f * rmax(dot(N, V), 0.0f) * rmax(dot(N, L), 0.0f) + 0.0001f;
-    V3 specular = mul(numerator, 1.0f / denominator);
-    float oneOverPi = 1.0f / kPi;
-    V3 A = add(mul(hadamard(kD, albedo), oneOverPi), specular);
-    ec = make_float4(emission.x, emission.y, emission.z, cosine);
-    aa = make_float4(A.x, A.y, A.z, 0.0f);
-}
-
-// Reverse pass over stored vertex terms.
-__device__ __forceinline__ V3 path_radiance(const float4 *vertE, const float4 *vertA,
-    size_t stride, uint32_t p, uint32_t len, float clampValue)
-{
-    V3 radiance = v3(0.0f, 0.0f, 0.0f);
-    for (int i = (int)len - 1; i >= 0; i--) {
-        float4 ec = vertE[(size_t)i * stride + p];
-        float4 aa = vertA[(size_t)i * stride + p];
-        V3 Li = radiance;
-        if (clampValue != 0.0f)
-            Li = v3(rclamp(Li.x, 0.0f, clampValue), rclamp(Li.y, 0.0f, clampValue),
-                rclamp(Li.z, 0.0f, clampValue));
-        radiance = add(v3(ec.x, ec.y, ec.z), mul(hadamard(v3(aa.x, aa.y, aa.z), Li), ec.w));
-    }
-    return radiance;
-}
 
 // ---------------------------------------------------------------------------
 // Stage kernels
@@ -556,4 +455,196 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     return GBSP_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free tile render (gbsp_path_trace_tile_noalloc).
+//
+// Its working memory is this one file-scope device array, laid out below.
+// Host code never uses the symbol as an address: the device address comes
+// from cudaGetSymbolAddress, once per device, with that device current.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kNoAllocMaxPaths = 16384;
+constexpr uint32_t kNoAllocMaxBounces = 8;
+constexpr uint32_t kNoAllocMaxObjects = 4096;
+constexpr size_t kNoAllocAlign = 256;
+
+constexpr size_t na_align(size_t x) { return (x + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign; }
+constexpr size_t kNaCtl = 0;  // metric counters + control words + status
+constexpr size_t kNaCtlBytes = sizeof(unsigned long long) * (GBSP_METRIC_COUNT + 16) + 16;
+constexpr size_t kNaSlots = na_align(kNaCtl + kNaCtlBytes);
+constexpr size_t kNaRayO = na_align(kNaSlots + 4 * (size_t)kNoAllocMaxObjects);
+constexpr size_t kNaRayD = na_align(kNaRayO + 2 * 16 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaHitA = na_align(kNaRayD + 2 * 16 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaHitInst = na_align(kNaHitA + 16 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaRng = na_align(kNaHitInst + 4 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaLen = na_align(kNaRng + 4 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaVertE = na_align(kNaLen + 4 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaVertA = na_align(kNaVertE + 16 * (size_t)kNoAllocMaxBounces * kNoAllocMaxPaths);
+constexpr size_t kNaRad = na_align(kNaVertA + 16 * (size_t)kNoAllocMaxBounces * kNoAllocMaxPaths);
+constexpr size_t kNoAllocBytes = na_align(kNaRad + 16 * (size_t)kNoAllocMaxPaths);
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
+
+static int noalloc_scratch(int device, unsigned char **out)
+{
+    static std::mutex lock;
+    static unsigned char *addr[64] = {};
+    if (device < 0 || device >= 64) return set_error(GBSP_ERR_INVALID_ARGUMENT, "device %d", device);
+    std::lock_guard<std::mutex> g(lock);
+    if (!addr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noallocScratch)");
+        addr[device] = (unsigned char *)p;
+    }
+    *out = addr[device];
+    return GBSP_OK;
+}
+
 }  // namespace gbsp
+
+using namespace gbsp;
+
+extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile tile,
+    float *deviceImage, gbsp_metrics *metrics)
+{
+    if (!ctx || !ctx->camera || !ctx->camera->imagePlane || !ctx->scene || !ctx->materialSystem ||
+        !ctx->runtime || !deviceImage)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "incomplete context or NULL image");
+    if (((uintptr_t)deviceImage & 15u) != 0)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "deviceImage must be 16-byte aligned");
+    gbsp_options opt;
+    if (ctx->options)
+        opt = *ctx->options;
+    else
+        gbsp_options_default(&opt);
+    gbsp_runtime *rt = ctx->runtime;
+    const gbsp_scene *sc = ctx->scene;
+    gbsp_material_system *ms = ctx->materialSystem;
+    if (!sc->committed)
+        return set_error(GBSP_ERR_NOT_READY, "scene changed since gbsp_build_scene_broadphase");
+    if (ms->dirty)
+        return set_error(GBSP_ERR_NOT_READY,
+            "materials not uploaded: render once with gbsp_path_trace_tile or _frame first");
+    if (sc->rt != rt || ms->rt != rt)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "scene, materials and context use different runtimes");
+    if (opt.rng_mode != GBSP_RNG_HASH_PER_SAMPLE)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "the allocation-free entry renders hash-per-sample only");
+    uint32_t spp = opt.spp ? opt.spp : 1;
+    if (spp > kNoAllocMaxPaths || opt.max_bounces > kNoAllocMaxBounces ||
+        sc->objects.size() > kNoAllocMaxObjects)
+        return set_error(GBSP_ERR_CAPACITY,
+            "allocation-free render limits: spp <= %u, bounces <= %u, objects <= %u (got %u, %u, %zu)",
+            kNoAllocMaxPaths, kNoAllocMaxBounces, kNoAllocMaxObjects, spp, opt.max_bounces,
+            sc->objects.size());
+    const gbsp_image_plane *ip = ctx->camera->imagePlane;
+    uint32_t x0 = tile.minX, y0 = tile.minY;
+    uint32_t x1 = tile.maxX < ip->width ? tile.maxX : ip->width;
+    uint32_t y1 = tile.maxY < ip->height ? tile.maxY : ip->height;
+    if (x1 <= x0 || y1 <= y0) return GBSP_OK;
+
+    GBSP_CUDA_TRY(cudaSetDevice(rt->device));
+    unsigned char *base = nullptr;
+    int rc = noalloc_scratch(rt->device, &base);
+    if (rc) return rc;
+    cudaStream_t s = rt->stream;
+    unsigned long long *counters = reinterpret_cast<unsigned long long *>(base + kNaCtl);
+    unsigned int *ctl = reinterpret_cast<unsigned int *>(counters + GBSP_METRIC_COUNT);
+    uint32_t *status = reinterpret_cast<uint32_t *>(base + kNaCtl + kNaCtlBytes - 16);
+    int32_t *slots = reinterpret_cast<int32_t *>(base + kNaSlots);
+    // the array keeps the previous call's contents: zero what must start at zero
+    GBSP_CUDA_TRY(cudaMemsetAsync(base + kNaCtl, 0, kNaCtlBytes, s));
+
+    // material slots per object in leaf order, built on the host stack
+    int32_t hostSlots[kNoAllocMaxObjects];
+    size_t nObj = sc->leafOrder.size();
+    for (size_t j = 0; j < nObj; j++)
+        hostSlots[j] = resolve_material(ms, sc->objects[sc->leafOrder[j]].material);
+    if (nObj) GBSP_CUDA_TRY(cudaMemcpyAsync(slots, hostSlots, 4 * nObj, cudaMemcpyHostToDevice, s));
+
+    MaterialView mv;
+    mv.instanceSlot = slots;
+    mv.materials = ms->dMaterials.ptr;
+    mv.materialCount = (uint32_t)ms->materials.size();
+    mv.texels = ms->dTexels.ptr;
+    mv.textures = ms->dTextures.ptr;
+    mv.textureCount = (uint32_t)ms->texturePixels.size();
+    mv.backgroundSlot = resolve_material(ms, ms->backgroundId);
+    mv.sky = ms->sky;
+    mv.haveSky = ms->haveSky ? 1u : 0u;
+
+    const gbsp_camera *c = ctx->camera;
+    CameraParams cam;
+    cam.right = v3(c->right[0], c->right[1], c->right[2]);
+    cam.up = v3(c->up[0], c->up[1], c->up[2]);
+    cam.forward = v3(c->forward[0], c->forward[1], c->forward[2]);
+    cam.position = v3(c->position[0], c->position[1], c->position[2]);
+    cam.filmCenter = v3(c->filmCenter[0], c->filmCenter[1], c->filmCenter[2]);
+    cam.halfPixelWidth = c->halfPixelWidth;
+    cam.halfPixelHeight = c->halfPixelHeight;
+    cam.halfFilmWidth = c->halfFilmWidth;
+    cam.halfFilmHeight = c->halfFilmHeight;
+    cam.width = ip->width;
+    cam.height = ip->height;
+
+    WaveBuffers wb;
+    wb.rayO = reinterpret_cast<float4 *>(base + kNaRayO);
+    wb.rayD = reinterpret_cast<float4 *>(base + kNaRayD);
+    wb.hitA = reinterpret_cast<int4 *>(base + kNaHitA);
+    wb.hitInst = reinterpret_cast<int *>(base + kNaHitInst);
+    wb.pathRng = reinterpret_cast<uint32_t *>(base + kNaRng);
+    wb.pathLen = reinterpret_cast<uint32_t *>(base + kNaLen);
+    wb.vertE = reinterpret_cast<float4 *>(base + kNaVertE);
+    wb.vertA = reinterpret_cast<float4 *>(base + kNaVertA);
+    wb.pathRad = reinterpret_cast<float4 *>(base + kNaRad);
+    uint32_t pixelsPerWave = kNoAllocMaxPaths / spp;
+    wb.cap = pixelsPerWave * spp;
+
+    WaveParams wp;
+    wp.cam = cam;
+    wp.x0 = x0;
+    wp.y0 = y0;
+    wp.regionW = x1 - x0;
+    wp.spp = spp;
+    wp.maxBounces = opt.max_bounces;
+    wp.seed = opt.seed;
+    wp.clampValue = opt.radiance_clamp;
+    wp.nanPolicy = opt.nan_policy;
+    wp.invSpp = 1.0f / (float)spp;
+    SceneView sv = sc->view();
+    float4 *image = reinterpret_cast<float4 *>(deviceImage);
+    uint64_t regionPixels = (uint64_t)(x1 - x0) * (y1 - y0);
+    int grid = rt->smCount * 8;
+    for (uint64_t pb = 0; pb < regionPixels; pb += pixelsPerWave) {
+        wp.pixelBase = pb;
+        uint64_t left = regionPixels - pb;
+        wp.pixels = (uint32_t)(left < pixelsPerWave ? left : pixelsPerWave);
+        uint32_t paths = wp.pixels * spp;
+        if (opt.max_bounces == 0) {
+            GBSP_CUDA_TRY(cudaMemsetAsync(wb.pathRad, 0, sizeof(float4) * (size_t)paths, s));
+        } else {
+            k_reset_ctl<<<1, 32, 0, s>>>(ctl, paths);
+            k_generate<<<(paths + 255) / 256, 256, 0, s>>>(wp, wb);
+            for (uint32_t b = 0; b < opt.max_bounces; b++) {
+                int inQ = (b & 1) ? kCtlQueue1 : kCtlQueue0;
+                int outQ = (b & 1) ? kCtlQueue0 : kCtlQueue1;
+                k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
+                k_trace<<<grid, 128, 0, s>>>(sv, wb.rayO + ((b & 1) ? wb.cap : 0),
+                    wb.rayD + ((b & 1) ? wb.cap : 0), ctl + inQ, wb.hitA, wb.hitInst, ctl,
+                    counters, status);
+                k_shade<<<grid, 128, 0, s>>>(sv, mv, wp, wb, b, inQ, ctl, counters);
+            }
+        }
+        k_accumulate<<<(wp.pixels + 255) / 256, 256, 0, s>>>(wp, wb, image, ip->width, counters);
+        GBSP_CUDA_TRY(cudaGetLastError());
+    }
+    unsigned long long hostCounters[GBSP_METRIC_COUNT];
+    uint32_t st = 0;
+    GBSP_CUDA_TRY(cudaMemcpyAsync(hostCounters, counters, sizeof(hostCounters), cudaMemcpyDeviceToHost, s));
+    GBSP_CUDA_TRY(cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s));
+    GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st)
+        return set_error(GBSP_ERR_DEVICE_STATUS, "device status 0x%x in the allocation-free render", st);
+    if (metrics)
+        for (int i = 0; i < GBSP_METRIC_COUNT; i++) metrics->values[i] += hostCounters[i];
+    return GBSP_OK;
+}

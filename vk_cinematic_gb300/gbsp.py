@@ -45,7 +45,7 @@ EXPORTS = [
     "gbsp_material_system_destroy", "gbsp_register_material", "gbsp_register_texture",
     "gbsp_set_background_material", "gbsp_set_procedural_sky", "gbsp_path_trace_tile",
     "gbsp_path_trace_frame", "gbsp_frame_device_pointer", "gbsp_icosphere", "gbsp_plane_mesh",
-    "gbsp_sample_seed",
+    "gbsp_sample_seed", "gbsp_path_trace_tile_noalloc",
 ]
 
 
