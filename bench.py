@@ -55,12 +55,19 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gbsp", "reference"], default="gbsp")
-    ap.add_argument("--workload", choices=["config3", "config1"], default="config3")
+    ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4"],
+                    default="config3")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--width", type=int, default=0, help="override (profiling cases only)")
+    ap.add_argument("--height", type=int, default=0, help="override (profiling cases only)")
+    ap.add_argument("--spp", type=int, default=0, help="override (profiling cases only)")
     return ap.parse_args()
+
+
+_OVERRIDES = {}
 
 
 def make_scene(workload, rank=0):
@@ -71,6 +78,9 @@ def make_scene(workload, rank=0):
     else:
         s = scenes.config3_scene()
     s.seed = s.seed + 1000 * rank
+    for k, v in _OVERRIDES.items():
+        if v:
+            setattr(s, k, v)
     return s
 
 
@@ -166,6 +176,20 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
                 "samples": len(rows)}
+
+
+def aggregate_ranks(elapsed_ms, paths, rays, world, device=None):
+    """Whole-job numbers for replicas: the slowest rank's time and the sum of
+    all ranks' paths and rays.  Works on any torch.distributed backend."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=device)
+    c = torch.tensor([float(paths), float(rays)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(c[0].item()), float(c[1].item())
 
 
 def dist_env():
@@ -285,7 +309,9 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     from vk_cinematic_gb300 import gbsp
 
-    stream = torch.cuda.current_stream()
+    # one stream for the library's kernels, the L2 flush and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     rt = gbsp.Runtime(local, stream=stream.cuda_stream)
     s = make_scene(args.workload, rank)
     opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed,
@@ -315,14 +341,8 @@ def run_gpu(args):
     ev1.record(stream)
     barrier()
     clk = clocks.stop()
-    elapsed_ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
-    cnt = torch.tensor([float(totals[1]), float(totals[2])], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dist.all_reduce(cnt, op=dist.ReduceOp.SUM)
-    elapsed_ms = float(t.item())
-    paths_all, rays_all = float(cnt[0].item()), float(cnt[1].item())
+    elapsed_ms, paths_all, rays_all = aggregate_ranks(ev0.elapsed_time(ev1), totals[1], totals[2],
+                                                      world, device="cuda")
     M = dict(zip(gbsp.METRIC_NAMES, [int(v) for v in totals]))
     value = paths_all / (elapsed_ms / 1e3) / 1e6
 
@@ -413,10 +433,140 @@ def run_gpu(args):
     return 0
 
 
+def run_config4(args):
+    """Config 4: 32 scenes of uneven size / spp / bounces rendered by one
+    persistent launch replayed from a CUDA graph (autotuned), against the
+    same 32 renders issued one frame call (wavefront launch sequence) per
+    scene.  Prints its own JSON line."""
+    import torch
+    from vk_cinematic_gb300 import gbsp, scenes
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rt = gbsp.Runtime(0, stream=stream.cuda_stream)
+    ss = scenes.config4_scenes()
+    keep, rends, imgs = [], [], []
+    for s in ss:
+        scene, ms, rend = gbsp.upload_scene(rt, s)
+        keep.append((scene, ms))
+        rends.append(rend)
+        imgs.append(torch.empty((s.height, s.width, 4), dtype=torch.float32, device="cuda"))
+    total = sum(s.width * s.height * s.spp for s in ss)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for r in rends:  # warm-up, wave buffers sized
+        r.frame_device(metrics=False)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        for r in rends:
+            r.frame_device(metrics=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    single_ms = ev0.elapsed_time(ev1) / args.steps
+    batch = gbsp.Batch(rt, rends, [t.data_ptr() for t in imgs])
+    t0 = time.time()
+    tuned = batch.autotune(trials=1)
+    tune_s = time.time() - t0
+    for _ in range(args.warmup):
+        batch.launch(metrics=False)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        batch.launch(metrics=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    batch_ms = ev0.elapsed_time(ev1) / args.steps
+    m = batch.launch(metrics=True).as_dict()
+    line = {
+        "metric": "aggregate spp/s, 32 uneven scenes (config 4)", "value": total / batch_ms / 1e3,
+        "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": batch_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded procedural scenes",
+        "config": {"workload": "config4: 32 scenes, triangles log-uniform 1k-2M, square sides "
+                               "64-1024, spp 1-256, bounces 1-8; one persistent launch replayed "
+                               "from a CUDA graph", "paths_per_step": total,
+                   "triangles": [s.triangle_count for s in ss],
+                   "sides": [s.width for s in ss], "spp": [s.spp for s in ss],
+                   "bounces": [s.max_bounces for s in ss]},
+        "one_launch_sequence_per_scene": {"value": total / single_ms / 1e3, "unit": "Msamples/s",
+                                          "ms_per_step": single_ms},
+        "speedup_vs_per_scene": single_ms / batch_ms,
+        "autotuned": tuned.as_dict(), "autotune_seconds": tune_s,
+        "mrays_per_s": m["rays_traced"] / batch_ms / 1e3, "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    batch.close()
+    return 0
+
+
+def run_config2(args):
+    """Config 2: closest hit of 4,194,304 rays against a 1,048,576-triangle
+    soup (one object, identity transform).  Prints its own JSON line."""
+    import torch
+    from vk_cinematic_gb300 import gbsp, scenes
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rt = gbsp.Runtime(0, stream=stream.cuda_stream)
+    s = scenes.config2_scene(n_tris=1 << 20, seed=2)
+    t0 = time.time()
+    scene, ms, _ = gbsp.upload_scene(rt, s)
+    build_s = time.time() - t0
+    rays = scenes.soup_rays(1 << 22, seed=3)
+    n = len(rays)
+    packed = np.zeros((n, 8), np.float32)
+    packed[:, 0:3] = rays[:, 0:3]
+    packed[:, 4:7] = rays[:, 3:6]
+    dr = torch.from_numpy(packed).cuda()
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    tri = torch.empty(n, dtype=torch.int32, device="cuda")
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        scene.intersect_closest_device(n, dr.data_ptr(), t.data_ptr(), tri.data_ptr())
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        ev0.record(stream)
+        scene.intersect_closest_device(n, dr.data_ptr(), t.data_ptr(), tri.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        total_ms += ev0.elapsed_time(ev1)
+    rt.synchronize()
+    hit_frac = float((tri >= 0).float().mean().item())
+    line = {
+        "metric": "Mrays/s closest hit (config 2)", "value": n * args.steps / total_ms / 1e3,
+        "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded triangle soup and rays",
+        "config": {"workload": "config2: 1,048,576-triangle soup (centres in the unit cube, "
+                               "vertex offsets in [-0.01, 0.01]^3), 4,194,304 rays from a radius-2 "
+                               "sphere towards the cube", "triangles": 1 << 20, "rays": n,
+                   "l2": "flushed (256 MB device write) before every timed step; kernel time "
+                         "only (CUDA events around the launch)",
+                   "trace": "static" if os.environ.get("GBSP_TRACE") == "static" else "dynamic"},
+        "hit_fraction": hit_frac, "device_bvh_build_and_upload_s": build_s,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
+    _OVERRIDES.update(width=args.width, height=args.height, spp=args.spp)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "config4":
+        return run_config4(args)
+    if args.workload == "config2":
+        return run_config2(args)
     return run_gpu(args)
 
 

@@ -265,6 +265,41 @@ int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile tile,
 /* Device pointer of the runtime's last frame (width*height RGBA32F). */
 const float *gbsp_frame_device_pointer(gbsp_runtime *rt);
 
+/* ---- batched rendering ---------------------------------------------------------- */
+/* Many scenes and images of uneven size rendered by one persistent kernel
+ * launch that pulls pixels from a global atomic queue, launched through a
+ * captured CUDA graph.  No reference counterpart: the reference renders one
+ * frame at a time through its tile queue (src/main.cpp:819-844).  Every item
+ * renders exactly what gbsp_path_trace_frame renders for it in
+ * GBSP_RNG_HASH_PER_SAMPLE mode (bit-identical images). */
+typedef struct gbsp_batch gbsp_batch;
+
+typedef struct {
+    gbsp_scene *scene;                     /* broadphase built */
+    gbsp_material_system *materialSystem;
+    const gbsp_camera *camera;             /* camera->imagePlane gives the size */
+    gbsp_options options;                  /* hash-per-sample mode, <= 16 bounces */
+    float *deviceImage;                    /* width*height RGBA32F, device memory */
+} gbsp_batch_item;
+
+typedef struct {
+    uint32_t block;        /* threads per block: 64, 128 or 256 */
+    uint32_t chunk;        /* pixels a thread takes per queue pop: 1..8 */
+    uint32_t blocksPerSm;  /* persistent grid = SM count * blocksPerSm */
+    uint32_t useGraph;     /* 1 = replay a captured CUDA graph */
+} gbsp_batch_config;
+
+int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t count,
+    gbsp_batch **out);
+int gbsp_batch_destroy(gbsp_batch *batch);
+int gbsp_batch_set_config(gbsp_batch *batch, const gbsp_batch_config *config);
+int gbsp_batch_get_config(const gbsp_batch *batch, gbsp_batch_config *config);
+/* Times every candidate configuration (block x chunk x blocks per SM) over
+ * `trials` launches each and keeps the fastest; *best receives it. */
+int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best);
+/* Renders every item.  metrics NULL: asynchronous on the runtime's stream. */
+int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics);
+
 /* ---- procedural meshes (src/mesh_generation.cpp) ------------------------------ */
 /* CreateIcosahedronMesh (src/mesh_generation.cpp:220-337) without its 2048
  * vertex cap.  Pass NULL arrays to get the counts only. */

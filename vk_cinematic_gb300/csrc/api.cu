@@ -254,6 +254,8 @@ int gbsp_runtime_create(int device, void *stream, gbsp_runtime **out)
     GBSP_CUDA_TRY(cudaSetDevice(device));
     gbsp_runtime *rt = new gbsp_runtime();
     rt->device = device;
+    const char *traceMode = getenv("GBSP_TRACE");
+    rt->dynamicTrace = !(traceMode && strcmp(traceMode, "static") == 0);
     if (stream) {
         rt->stream = (cudaStream_t)stream;
     } else {
@@ -684,7 +686,7 @@ int gbsp_intersect_closest_device(gbsp_scene *scene, uint32_t count, const float
     if ((rc = counters_begin(rt))) return rc;
     return launch_intersect(rt->stream, scene->view(), count, reinterpret_cast<const float4 *>(rays),
         tOut, triangleOut, objectOut, nullptr, nullptr, nullptr, rt->smCount, rt->dCounters,
-        rt->dStatus);
+        rt->dStatus, rt->dynamicTrace);
 }
 
 int gbsp_ray_intersect_scene(gbsp_scene *scene, uint32_t count, const float *rays, float *resultOut,
@@ -711,7 +713,7 @@ int gbsp_ray_intersect_scene(gbsp_scene *scene, uint32_t count, const float *ray
     if ((rc = counters_begin(rt))) return rc;
     GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
     if ((rc = launch_intersect(s, scene->view(), count, dr.ptr, nullptr, nullptr, nullptr, dattr.ptr,
-             dmat.ptr, nullptr, rt->smCount, rt->dCounters, rt->dStatus)))
+             dmat.ptr, nullptr, rt->smCount, rt->dCounters, rt->dStatus, rt->dynamicTrace)))
         return rc;
     GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
     GBSP_CUDA_TRY(cudaMemcpyAsync(resultOut, dattr.ptr, 24 * (size_t)count, cudaMemcpyDeviceToHost, s));

@@ -1,0 +1,351 @@
+// Batched rendering of many scenes of uneven size in one persistent launch.
+//
+// Work unit = one pixel of one item (all of its samples, traced one after
+// another in one thread, each seeded from hash(seed, x, y, sample)), so the
+// per-pixel sum is the same ordered Neumaier sum as the wavefront path and
+// every image is bit-identical to a single-scene render.  The items' pixels
+// are numbered back to back; warps pop 32*chunk of them at a time from one
+// global 64-bit atomic counter until the total is exhausted, which balances
+// items of 1 to 256 spp and 1 to 8 bounces without any host involvement.
+// The reset + kernel pair is captured once into a CUDA graph and replayed.
+
+#include <algorithm>
+#include <vector>
+
+#include "gbsp_internal.h"
+#include "shading.cuh"
+
+namespace gbsp {
+
+constexpr int kBatchMaxBounces = 16;
+
+struct BatchItemDev {
+    SceneView sv;
+    MaterialView mv;
+    CameraParams cam;
+    float4 *image;
+    uint64_t pixelBase;
+    uint32_t width, height, spp, maxBounces, seed, nanPolicy;
+    float clampValue, invSpp;
+};
+
+__global__ void k_batch_reset(unsigned long long *work, unsigned long long *counters)
+{
+    if (threadIdx.x == 0) *work = 0;
+    if (threadIdx.x < GBSP_METRIC_COUNT) counters[threadIdx.x] = 0;
+}
+
+__global__ void __launch_bounds__(256) k_batch(const BatchItemDev *__restrict__ items,
+    uint32_t itemCount, uint64_t totalPixels, uint32_t chunk, unsigned long long *work,
+    unsigned long long *counters, uint32_t *status)
+{
+    int lane = threadIdx.x & 31;
+    TraceCounters cnt = {0, 0, 0, 0, 0};
+    uint32_t rays = 0, hits = 0, paths = 0, nans = 0;
+    uint64_t step = 32ull * chunk;
+    for (uint64_t guard = 0; guard <= totalPixels / step + 1; guard++) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(work, (unsigned long long)step);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= totalPixels) break;
+        for (uint32_t c = 0; c < chunk; c++) {
+            uint64_t pix = base + (uint64_t)c * 32 + lane;  // neighbouring lanes, neighbouring pixels
+            if (pix >= totalPixels) continue;
+            uint32_t lo = 0, hi = itemCount - 1;
+            while (lo < hi) {
+                uint32_t mid = (lo + hi + 1) >> 1;
+                if (items[mid].pixelBase <= pix)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const BatchItemDev &it = items[lo];
+            uint64_t local = pix - it.pixelBase;
+            uint32_t x = (uint32_t)(local % it.width), y = (uint32_t)(local / it.width);
+            CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+            for (uint32_t s = 0; s < it.spp; s++) {
+                uint32_t rng = sample_seed(it.seed, x, y, s);
+                V3 r = trace_full_path<kBatchMaxBounces>(it.sv, it.mv, it.cam, x, y, rng,
+                    it.maxBounces, it.clampValue, status, cnt, rays, hits);
+                paths++;
+                if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
+                    nans++;
+                    if (it.nanPolicy == GBSP_NAN_ZERO) continue;
+                }
+                csum_add(acc[0], r.x * it.invSpp);
+                csum_add(acc[1], r.y * it.invSpp);
+                csum_add(acc[2], r.z * it.invSpp);
+            }
+            it.image[(size_t)y * it.width + x] =
+                make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
+        }
+    }
+    uint32_t v[10] = {rays, hits, paths, nans, cnt.topNodes, cnt.meshNodes, cnt.triTests,
+        cnt.boxTests, cnt.meshTests, 0};
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+        for (int off = 16; off; off >>= 1) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+    if (lane == 0) {
+        atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)v[0]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)v[1]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(v[0] - v[1]));
+        atomicAdd(&counters[GBSP_METRIC_PATHS_TRACED], (unsigned long long)v[2]);
+        atomicAdd(&counters[GBSP_METRIC_NAN_SAMPLES], (unsigned long long)v[3]);
+        atomicAdd(&counters[GBSP_METRIC_BROADPHASE_NODE_VISITS], (unsigned long long)v[4]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_NODE_VISITS], (unsigned long long)v[5]);
+        atomicAdd(&counters[GBSP_METRIC_TRIANGLE_TESTS], (unsigned long long)v[6]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_BOX_TESTS], (unsigned long long)v[7]);
+        atomicAdd(&counters[GBSP_METRIC_MESH_TESTS_PERFORMED], (unsigned long long)v[8]);
+    }
+}
+
+}  // namespace gbsp
+
+using namespace gbsp;
+
+struct gbsp_batch {
+    gbsp_runtime *rt = nullptr;
+    std::vector<gbsp_batch_item> items;
+    DeviceBuffer<BatchItemDev> dItems;
+    DeviceBuffer<int32_t> dSlots;
+    DeviceBuffer<unsigned long long> dWork;
+    uint64_t totalPixels = 0, totalPaths = 0;
+    gbsp_batch_config cfg = {128, 1, 8, 1};
+    cudaGraphExec_t exec = nullptr;
+};
+
+static void drop_graph(gbsp_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+}
+
+static int enqueue(gbsp_batch *b)
+{
+    gbsp_runtime *rt = b->rt;
+    cudaStream_t s = rt->stream;
+    k_batch_reset<<<1, 32, 0, s>>>(b->dWork.ptr, rt->dCounters);
+    int grid = rt->smCount * (int)b->cfg.blocksPerSm;
+    k_batch<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(), b->totalPixels,
+        b->cfg.chunk, b->dWork.ptr, rt->dCounters, rt->dStatus);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+static int launch_once(gbsp_batch *b)
+{
+    cudaStream_t s = b->rt->stream;
+    if (!b->cfg.useGraph) return enqueue(b);
+    if (!b->exec) {
+        cudaGraph_t g = nullptr;
+        GBSP_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue(b);
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e != cudaSuccess) return cuda_error(e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->exec = nullptr;
+            return cuda_error(e, "cudaGraphInstantiate");
+        }
+    }
+    GBSP_CUDA_TRY(cudaGraphLaunch(b->exec, s));
+    return GBSP_OK;
+}
+
+static int check_config(const gbsp_batch_config *c)
+{
+    if (c->block != 64 && c->block != 128 && c->block != 256)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "block must be 64, 128 or 256");
+    if (c->chunk < 1 || c->chunk > 8) return set_error(GBSP_ERR_INVALID_ARGUMENT, "chunk must be 1..8");
+    if (c->blocksPerSm < 1 || c->blocksPerSm > 32)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "blocksPerSm must be 1..32");
+    return GBSP_OK;
+}
+
+extern "C" {
+
+int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t count,
+    gbsp_batch **out)
+{
+    if (!rt || !items || !count || !out) return set_error(GBSP_ERR_INVALID_ARGUMENT, "empty batch");
+    *out = nullptr;
+    gbsp_batch *b = new gbsp_batch();
+    b->rt = rt;
+    b->items.assign(items, items + count);
+    std::vector<BatchItemDev> dev(count);
+    std::vector<int32_t> slots;
+    std::vector<size_t> slotOffset(count);
+    uint64_t base = 0;
+    int rc = GBSP_OK;
+    for (uint32_t i = 0; i < count && !rc; i++) {
+        const gbsp_batch_item &it = items[i];
+        if (!it.scene || !it.materialSystem || !it.camera || !it.camera->imagePlane ||
+            !it.deviceImage) {
+            rc = set_error(GBSP_ERR_INVALID_ARGUMENT, "batch item %u is incomplete", i);
+            break;
+        }
+        if (!it.scene->committed || it.scene->rt != rt || it.materialSystem->rt != rt) {
+            rc = set_error(GBSP_ERR_NOT_READY, "batch item %u: scene not built or other runtime", i);
+            break;
+        }
+        if (it.options.rng_mode != GBSP_RNG_HASH_PER_SAMPLE ||
+            it.options.max_bounces > (uint32_t)kBatchMaxBounces) {
+            rc = set_error(GBSP_ERR_INVALID_ARGUMENT,
+                "batch item %u: hash-per-sample seeding and at most %d bounces", i,
+                kBatchMaxBounces);
+            break;
+        }
+        MaterialView mv;
+        if ((rc = material_view(it.materialSystem, &mv))) break;
+        slotOffset[i] = slots.size();
+        const gbsp_scene *sc = it.scene;
+        for (size_t j = 0; j < sc->leafOrder.size(); j++)
+            slots.push_back(resolve_material(it.materialSystem, sc->objects[sc->leafOrder[j]].material));
+        slots.push_back(-1);
+        BatchItemDev &d = dev[i];
+        d.sv = sc->view();
+        d.mv = mv;
+        const gbsp_camera *c = it.camera;
+        d.cam.right = v3(c->right[0], c->right[1], c->right[2]);
+        d.cam.up = v3(c->up[0], c->up[1], c->up[2]);
+        d.cam.forward = v3(c->forward[0], c->forward[1], c->forward[2]);
+        d.cam.position = v3(c->position[0], c->position[1], c->position[2]);
+        d.cam.filmCenter = v3(c->filmCenter[0], c->filmCenter[1], c->filmCenter[2]);
+        d.cam.halfPixelWidth = c->halfPixelWidth;
+        d.cam.halfPixelHeight = c->halfPixelHeight;
+        d.cam.halfFilmWidth = c->halfFilmWidth;
+        d.cam.halfFilmHeight = c->halfFilmHeight;
+        d.cam.width = c->imagePlane->width;
+        d.cam.height = c->imagePlane->height;
+        d.image = reinterpret_cast<float4 *>(it.deviceImage);
+        d.pixelBase = base;
+        d.width = c->imagePlane->width;
+        d.height = c->imagePlane->height;
+        d.spp = it.options.spp ? it.options.spp : 1;
+        d.maxBounces = it.options.max_bounces;
+        d.seed = it.options.seed;
+        d.nanPolicy = it.options.nan_policy;
+        d.clampValue = it.options.radiance_clamp;
+        d.invSpp = 1.0f / (float)d.spp;
+        base += (uint64_t)d.width * d.height;
+        b->totalPaths += (uint64_t)d.width * d.height * d.spp;
+    }
+    if (!rc && base == 0) rc = set_error(GBSP_ERR_INVALID_ARGUMENT, "batch has no pixels");
+    cudaStream_t s = rt->stream;
+    if (!rc) rc = b->dSlots.upload(slots.data(), slots.size(), s);
+    if (!rc) {
+        for (uint32_t i = 0; i < count; i++) dev[i].mv.instanceSlot = b->dSlots.ptr + slotOffset[i];
+        rc = b->dItems.upload(dev.data(), dev.size(), s);
+    }
+    if (!rc) rc = b->dWork.reserve(1, s);
+    if (!rc && cudaStreamSynchronize(s) != cudaSuccess)
+        rc = set_error(GBSP_ERR_CUDA, "batch upload failed");
+    if (rc) {
+        delete b;
+        return rc;
+    }
+    b->totalPixels = base;
+    *out = b;
+    return GBSP_OK;
+}
+
+int gbsp_batch_destroy(gbsp_batch *batch)
+{
+    if (!batch) return GBSP_OK;
+    cudaStreamSynchronize(batch->rt->stream);
+    drop_graph(batch);
+    delete batch;
+    return GBSP_OK;
+}
+
+int gbsp_batch_set_config(gbsp_batch *batch, const gbsp_batch_config *config)
+{
+    if (!batch || !config) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    int rc = check_config(config);
+    if (rc) return rc;
+    batch->cfg = *config;
+    drop_graph(batch);
+    return GBSP_OK;
+}
+
+int gbsp_batch_get_config(const gbsp_batch *batch, gbsp_batch_config *config)
+{
+    if (!batch || !config) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    *config = batch->cfg;
+    return GBSP_OK;
+}
+
+int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics)
+{
+    if (!batch) return set_error(GBSP_ERR_INVALID_ARGUMENT, "batch is NULL");
+    gbsp_runtime *rt = batch->rt;
+    cudaStream_t s = rt->stream;
+    if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
+    int rc = launch_once(batch);
+    if (rc) return rc;
+    if (!metrics) return GBSP_OK;
+    GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
+    unsigned long long c[GBSP_METRIC_COUNT];
+    uint32_t st = 0;
+    GBSP_CUDA_TRY(cudaMemcpyAsync(c, rt->dCounters, sizeof(c), cudaMemcpyDeviceToHost, s));
+    GBSP_CUDA_TRY(cudaMemcpyAsync(&st, rt->dStatus, 4, cudaMemcpyDeviceToHost, s));
+    GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st) {
+        cudaMemsetAsync(rt->dStatus, 0, 4, s);
+        return set_error(GBSP_ERR_DEVICE_STATUS, "device status 0x%x in the batch kernel", st);
+    }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, rt->ev[0], rt->ev[1]);
+    for (int i = 0; i < GBSP_METRIC_COUNT; i++) metrics->values[i] += c[i];
+    metrics->values[GBSP_METRIC_ELAPSED_NS] += (uint64_t)((double)ms * 1.0e6);
+    metrics->values[GBSP_METRIC_KERNEL_LAUNCHES] += 2;
+    return GBSP_OK;
+}
+
+int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best)
+{
+    if (!batch) return set_error(GBSP_ERR_INVALID_ARGUMENT, "batch is NULL");
+    gbsp_runtime *rt = batch->rt;
+    cudaStream_t s = rt->stream;
+    if (trials == 0) trials = 1;
+    const uint32_t blocks[] = {64, 128, 256};
+    const uint32_t chunks[] = {1, 4};
+    const uint32_t perSm[] = {2, 4, 8};
+    gbsp_batch_config keep = batch->cfg, bestCfg = batch->cfg;
+    float bestMs = 3.0e38f;
+    for (uint32_t bl : blocks)
+        for (uint32_t ch : chunks)
+            for (uint32_t ps : perSm) {
+                gbsp_batch_config c = {bl, ch, ps, keep.useGraph};
+                batch->cfg = c;
+                drop_graph(batch);
+                int rc = launch_once(batch);  // warm-up (and graph capture)
+                if (rc) return rc;
+                GBSP_CUDA_TRY(cudaEventRecord(rt->ev[2], s));
+                for (uint32_t t = 0; t < trials; t++)
+                    if ((rc = launch_once(batch))) return rc;
+                GBSP_CUDA_TRY(cudaEventRecord(rt->ev[3], s));
+                GBSP_CUDA_TRY(cudaEventSynchronize(rt->ev[3]));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, rt->ev[2], rt->ev[3]);
+                if (ms < bestMs) {
+                    bestMs = ms;
+                    bestCfg = c;
+                }
+            }
+    batch->cfg = bestCfg;
+    drop_graph(batch);
+    if (best) *best = bestCfg;
+    uint32_t st = 0;
+    GBSP_CUDA_TRY(cudaMemcpyAsync(&st, rt->dStatus, 4, cudaMemcpyDeviceToHost, s));
+    GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+    if (st) return set_error(GBSP_ERR_DEVICE_STATUS, "device status 0x%x while tuning", st);
+    return GBSP_OK;
+}
+
+}  // extern "C"

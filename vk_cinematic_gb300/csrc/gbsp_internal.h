@@ -74,6 +74,9 @@ struct Counters;  // device metric block
 struct gbsp_runtime {
     int refs = 1;                       // guarded by the API's runtime mutex
     bool closed = false;
+    // closest-hit kernel of the wavefront: dynamic per-lane fetch (default)
+    // or one ray per lane until the warp finishes (GBSP_TRACE=static)
+    bool dynamicTrace = true;
     int device = 0;
     cudaStream_t stream = nullptr;
     bool ownsStream = false;
@@ -207,7 +210,8 @@ int offset_nodes(cudaStream_t s, Node8 *dNodes, uint32_t nodeCount, uint32_t nod
 // trace.cu
 int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const float4 *rays,
     float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut, uint32_t *matOut,
-    const Instance *instHost, int smCount, unsigned long long *counters, uint32_t *dStatus);
+    const Instance *instHost, int smCount, unsigned long long *counters, uint32_t *dStatus,
+    bool dynamicTrace);
 
 // pathtrace.cu
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,

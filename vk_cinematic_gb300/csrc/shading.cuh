@@ -117,4 +117,46 @@ __device__ __forceinline__ V3 path_radiance(const float4 *vertE, const float4 *v
     return radiance;
 }
 
+// One whole path in one thread: the body of the reference's per-sample loop
+// (src/simd_path_tracer.cpp:208-324) - jitter and camera ray drawn from
+// `rng`, up to maxBounces closest-hit queries, per-vertex terms, reverse pass.
+template <int kMaxBounces>
+__device__ __forceinline__ V3 trace_full_path(const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, uint32_t x, uint32_t y, uint32_t &rng, uint32_t maxBounces,
+    float clampValue, uint32_t *status, TraceCounters &cnt, uint32_t &rays, uint32_t &hits)
+{
+    float4 vE[kMaxBounces], vA[kMaxBounces];
+    V3 o, d;
+    camera_ray(cam, x, y, rng, o, d);
+    uint32_t len = 0;
+    if (maxBounces > (uint32_t)kMaxBounces) maxBounces = kMaxBounces;
+    for (uint32_t b = 0; b < maxBounces; b++) {
+        RayHit h = trace_closest<true>(sv, o, d, status, cnt);
+        rays++;
+        float4 ec, aa;
+        if (h.prim >= 0 && h.t > 0.0f) {
+            hits++;
+            V3 n;
+            float ux, uy;
+            hit_surface(sv, h, n, ux, uy);
+            V3 pos = add(o, mul(d, h.t));
+            V3 dir = random_hemisphere(n, rng);
+            vertex_terms(mv, mv.instanceSlot[h.inst], n, dir, neg(d), ux, uy, ec, aa);
+            vE[len] = ec;
+            vA[len] = aa;
+            len++;
+            o = add(pos, mul(n, 0.0001f));
+            d = dir;
+        } else {
+            vertex_terms(mv, mv.backgroundSlot, v3(0, 0, 0), v3(0, 0, 0), neg(d), 0.0f, 0.0f, ec,
+                aa);
+            vE[len] = ec;
+            vA[len] = aa;
+            len++;
+            break;
+        }
+    }
+    return path_radiance(vE, vA, 1, 0, len, clampValue);
+}
+
 }  // namespace gbsp

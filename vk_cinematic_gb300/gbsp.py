@@ -45,7 +45,9 @@ EXPORTS = [
     "gbsp_material_system_destroy", "gbsp_register_material", "gbsp_register_texture",
     "gbsp_set_background_material", "gbsp_set_procedural_sky", "gbsp_path_trace_tile",
     "gbsp_path_trace_frame", "gbsp_frame_device_pointer", "gbsp_icosphere", "gbsp_plane_mesh",
-    "gbsp_sample_seed", "gbsp_path_trace_tile_noalloc",
+    "gbsp_sample_seed", "gbsp_path_trace_tile_noalloc", "gbsp_batch_create",
+    "gbsp_batch_destroy", "gbsp_batch_set_config", "gbsp_batch_get_config",
+    "gbsp_batch_autotune", "gbsp_batch_launch",
 ]
 
 
@@ -386,3 +388,66 @@ def upload_scene(rt: Runtime, s, options: Options | None = None):
     rend = Renderer(rt, scene, ms, s.width, s.height, s.camera_position, s.camera_rotation,
                     s.film_distance, opt) if s.width else None
     return scene, ms, rend
+
+
+class BatchItem(ctypes.Structure):
+    _fields_ = [("scene", _vp), ("materialSystem", _vp), ("camera", ctypes.POINTER(Camera)),
+                ("options", Options), ("deviceImage", _vp)]
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [("block", _u32), ("chunk", _u32), ("blocksPerSm", _u32), ("useGraph", _u32)]
+
+    def as_dict(self):
+        return dict(block=self.block, chunk=self.chunk, blocks_per_sm=self.blocksPerSm,
+                    use_graph=self.useGraph)
+
+
+class Batch:
+    """Many renderers' frames in one persistent launch (gbsp_batch_*).  Each
+    item renders into a device image (a torch tensor's storage)."""
+
+    def __init__(self, rt: Runtime, renderers, images):
+        self.L, self.rt = rt.L, rt
+        n = len(renderers)
+        arr = (BatchItem * n)()
+        for k, (r, img) in enumerate(zip(renderers, images)):
+            arr[k].scene = r.scene.h
+            arr[k].materialSystem = r.ms.h
+            arr[k].camera = ctypes.pointer(r.camera)
+            arr[k].options = r.options
+            arr[k].deviceImage = img
+        self._keep = (renderers, arr)
+        h = _vp()
+        _check(self.L.gbsp_batch_create(rt.h, arr, _u32(n), ctypes.byref(h)))
+        self.h = h
+
+    def config(self) -> BatchConfig:
+        c = BatchConfig()
+        _check(self.L.gbsp_batch_get_config(self.h, ctypes.byref(c)))
+        return c
+
+    def set_config(self, block=128, chunk=1, blocks_per_sm=8, use_graph=1):
+        c = BatchConfig(block, chunk, blocks_per_sm, use_graph)
+        _check(self.L.gbsp_batch_set_config(self.h, ctypes.byref(c)))
+
+    def autotune(self, trials=2) -> BatchConfig:
+        c = BatchConfig()
+        _check(self.L.gbsp_batch_autotune(self.h, _u32(trials), ctypes.byref(c)))
+        return c
+
+    def launch(self, metrics: bool = True):
+        m = Metrics() if metrics else None
+        _check(self.L.gbsp_batch_launch(self.h, ctypes.byref(m) if m is not None else None))
+        return m
+
+    def close(self):
+        if self.h:
+            self.L.gbsp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

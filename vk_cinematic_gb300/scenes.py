@@ -281,3 +281,26 @@ def config3_scene(width=1920, height=1080, spp=64, max_bounces=5, n_spheres=256,
     s.camera_rotation = look_rotation_x(s.camera_position, (0, 1, 0))
     s.film_distance = 0.5
     return s
+
+
+def config4_scenes(count=32, seed=4, max_triangles=2_000_000) -> list:
+    """Config 4: `count` scenes generated like config 3 with per-scene triangle
+    counts log-uniform in [1k, 2M] (sphere count and subdivision level vary),
+    square images with side log-uniform in [64, 1024], spp log-uniform in
+    [1, 256] and max bounces uniform in 1..8."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        tris = float(np.exp(rng.uniform(math.log(1000), math.log(max_triangles))))
+        level = 5
+        while level > 1 and 20 * 4 ** level > tris:
+            level -= 1
+        n_spheres = int(max(1, min(4096, round(tris / (20 * 4 ** level)))))
+        side = int(round(math.exp(rng.uniform(math.log(64), math.log(1024)))))
+        spp = int(round(math.exp(rng.uniform(math.log(1), math.log(256)))))
+        bounces = int(rng.integers(1, 9))
+        s = config3_scene(width=side, height=side, spp=spp, max_bounces=bounces,
+                          n_spheres=n_spheres, level=level, seed=seed * 1000 + k)
+        s.name = f"config4[{k}]"
+        out.append(s)
+    return out
