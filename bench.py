@@ -55,8 +55,16 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gbsp", "reference"], default="gbsp")
-    ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4"],
+    ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4", "config5"],
                     default="config3")
+    ap.add_argument("--dn-scenes", type=int, default=125)
+    ap.add_argument("--dn-crops", type=int, default=16)
+    ap.add_argument("--dn-ref-spp", type=int, default=4096)
+    ap.add_argument("--dn-steps", type=int, default=2000)
+    ap.add_argument("--dn-lr", type=float, default=1e-4)
+    ap.add_argument("--dn-eval-seeds", type=int, default=50)
+    ap.add_argument("--dn-eval-crop", type=int, default=256)
+    ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -558,6 +566,124 @@ def run_config2(args):
     return 0
 
 
+def run_config5(args):
+    """Config 5: learned denoiser.  Train on path-traced pairs (4-spp inputs +
+    G-buffers, high-spp targets, 128x128 crops, batch 16, Adam, relMSE), then
+    on held-out scenes compare, at equal render resolution, the wall time for
+    plain path tracing to reach relMSE 0.01 against an FP64-accumulated
+    16,384-spp oracle with the time of 4 spp + denoising.  Prints its own line."""
+    import torch
+    from vk_cinematic_gb300 import denoiser, gbsp
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rt = gbsp.Runtime(0, stream=stream.cuda_stream)
+    log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
+    t0 = time.time()
+    noisy, aov, target = denoiser.make_dataset(
+        rt, n_scenes=args.dn_scenes, crops_per_scene=args.dn_crops, crop=128, spp_in=4,
+        spp_ref=args.dn_ref_spp, seed0=0, log=log)
+    data_s = time.time() - t0
+    net = denoiser.KPCNN(seed=0)
+    feats_all = net.features(noisy, aov)
+    n = noisy.shape[0]
+    g = torch.Generator(device="cpu").manual_seed(0)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    losses = []
+    ev0.record(stream)
+    for step in range(args.dn_steps):
+        idx = torch.randint(0, n, (16,), generator=g).cuda()
+        loss = net.train_step(feats_all[idx].contiguous(), noisy[idx].contiguous(),
+                              target[idx].contiguous(), lr=args.dn_lr)
+        if step % 100 == 0 or step == args.dn_steps - 1:
+            losses.append((step, float(loss.item())))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    train_ms = ev0.elapsed_time(ev1)
+    log("training", losses)
+
+    # ---- timing at 1920x1080: plain spp vs 4 spp + denoise
+    s = denoiser.denoise_scene(10_000)
+    sr = denoiser.SceneRenderer(rt, s)
+    W, H = s.width, s.height
+    sr.render(0, 0, W, H, 4, seed=1, aov=True)  # warm-up
+    ev0.record(stream)
+    rad4, aov4 = sr.render(0, 0, W, H, 4, seed=2, aov=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    t4_ms = ev0.elapsed_time(ev1)
+    x4 = rad4.unsqueeze(0).contiguous()
+    a4 = aov4.unsqueeze(0).contiguous()
+    net.denoise(x4, a4)
+    ev0.record(stream)
+    den_full = net.denoise(x4, a4)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dn_ms = ev0.elapsed_time(ev1)
+    ev0.record(stream)
+    sr.render(0, 0, W, H, 64, seed=3)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_per_spp = ev0.elapsed_time(ev1) / 64.0
+    flops = 2.0 * W * H * sum(9 * ci * co for ci, co, _ in [(10, 48, 0)] + [(48, 48, 0)] * 6 +
+                              [(48, 25, 1)])
+
+    # ---- quality on held-out scenes (crops, FP64-accumulated oracle)
+    crop = args.dn_eval_crop
+    spps = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024]
+    plain = {k: [] for k in spps}
+    den = []
+    rng = np.random.default_rng(99)
+    for e in range(args.dn_eval_seeds):
+        se = denoiser.denoise_scene(20_000 + e)
+        sre = denoiser.SceneRenderer(rt, se)
+        x0 = int(rng.integers(0, se.width - crop))
+        y0 = int(rng.integers(se.height // 3, se.height - crop))
+        ref = sre.reference(x0, y0, crop, crop, args.dn_oracle_spp).float()
+        for k in spps:
+            img, _ = sre.render(x0, y0, crop, crop, k, seed=7 + k)
+            plain[k].append(denoiser.relmse(img, ref))
+        r4, a4c = sre.render(x0, y0, crop, crop, 4, seed=5, aov=True)
+        d = net.denoise(r4.unsqueeze(0).contiguous(), a4c.unsqueeze(0).contiguous())[0]
+        den.append(denoiser.relmse(d, ref))
+    plain_mean = {k: float(np.mean(v)) for k, v in plain.items()}
+    den_mean = float(np.mean(den))
+    # spp plain path tracing needs for relMSE 0.01 (log-log interpolation)
+    need = None
+    for a, b in zip(spps, spps[1:]):
+        ea, eb = plain_mean[a], plain_mean[b]
+        if ea >= 0.01 >= eb:
+            f = (math.log(ea) - math.log(0.01)) / max(math.log(ea) - math.log(eb), 1e-12)
+            need = math.exp(math.log(a) + f * (math.log(b) - math.log(a)))
+            break
+    if need is None and plain_mean[spps[-1]] > 0.01:
+        # extrapolate with the Monte Carlo rate relMSE ~ 1/spp from the last point
+        need = spps[-1] * plain_mean[spps[-1]] / 0.01
+    plain_ms = need * ms_per_spp if need else None
+    den_total_ms = t4_ms + dn_ms
+    line = {
+        "metric": "time-to-relMSE 0.01 at 1080p: plain PT / (4 spp + denoiser) (config 5)",
+        "value": (plain_ms / den_total_ms) if plain_ms else None, "unit": "x (higher is better)",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 (conv) / f32", "vs_baseline": None,
+        "data": "synthetic: path-traced seeded config-3-style scenes",
+        "config": {"workload": "config5: KPCNN 8 x conv3x3 (48 ch) + softmax 5x5 filter",
+                   "train_crops": int(n), "crop": 128, "batch": 16, "steps": args.dn_steps,
+                   "lr": args.dn_lr, "target_spp": args.dn_ref_spp,
+                   "eval_seeds": args.dn_eval_seeds, "eval_crop": crop,
+                   "oracle_spp": args.dn_oracle_spp},
+        "denoised_relmse": den_mean, "denoised_meets_0.01": den_mean <= 0.01,
+        "plain_relmse_by_spp": plain_mean, "plain_spp_for_0.01": need,
+        "ms_plain_per_spp_1080p": ms_per_spp, "ms_4spp_1080p": t4_ms, "ms_denoise_1080p": dn_ms,
+        "denoiser_tflops": flops / (dn_ms * 1e-3) / 1e12,
+        "plain_ms_to_0.01": plain_ms, "denoised_ms": den_total_ms,
+        "train_ms": train_ms, "dataset_s": data_s, "losses": losses,
+        "params": net.parameters_count(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     _OVERRIDES.update(width=args.width, height=args.height, spp=args.spp)
@@ -567,6 +693,8 @@ def main():
         return run_config4(args)
     if args.workload == "config2":
         return run_config2(args)
+    if args.workload == "config5":
+        return run_config5(args)
     return run_gpu(args)
 
 

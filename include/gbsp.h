@@ -77,6 +77,8 @@ extern "C" {
 /* gbsp_options.flags */
 #define GBSP_FLAG_STAGE_TIMING 1u  /* fill the *_NS metric slots per stage
                                       (CUDA events around each launch) */
+#define GBSP_FLAG_AOV 2u           /* also write first-hit G-buffers, averaged over
+                                      the samples (gbsp_frame_aov_device_pointer) */
 
 typedef struct gbsp_runtime gbsp_runtime;
 typedef struct gbsp_scene gbsp_scene;
@@ -264,6 +266,16 @@ int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile tile,
     float *deviceImage, gbsp_metrics *metrics);
 /* Device pointer of the runtime's last frame (width*height RGBA32F). */
 const float *gbsp_frame_device_pointer(gbsp_runtime *rt);
+/* Device pointer of the last frame's G-buffers when GBSP_FLAG_AOV was set:
+ * width*height*8 floats per pixel = albedo rgb, depth (world t of the first
+ * hit), normal xyz, fraction of samples whose first ray hit; means over the
+ * samples (misses contribute zeros).  No reference counterpart: input of the
+ * learned denoiser. */
+const float *gbsp_frame_aov_device_pointer(gbsp_runtime *rt);
+/* Copies a w x h window at (x0, y0) of the last frame (and of its G-buffers
+ * when dstAov is not NULL) into packed device arrays, on the runtime's stream. */
+int gbsp_frame_copy_region(gbsp_runtime *rt, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+    float *dstRadiance, float *dstAov);
 
 /* ---- batched rendering ---------------------------------------------------------- */
 /* Many scenes and images of uneven size rendered by one persistent kernel
@@ -287,18 +299,73 @@ typedef struct {
     uint32_t chunk;        /* pixels a thread takes per queue pop: 1..8 */
     uint32_t blocksPerSm;  /* persistent grid = SM count * blocksPerSm */
     uint32_t useGraph;     /* 1 = replay a captured CUDA graph */
+    uint32_t kernel;       /* GBSP_BATCH_THREAD_PER_PIXEL or GBSP_BATCH_PATH_STATE */
 } gbsp_batch_config;
+
+/* gbsp_batch_config.kernel: one thread traces a whole pixel (all samples,
+ * bounces and traversal) at a time; or every lane runs a state machine whose
+ * steps (one traversal stack pop, one shading event) the warp executes
+ * together for the lanes in the same phase, refilling finished lanes with
+ * new pixels.  Both give identical images. */
+#define GBSP_BATCH_THREAD_PER_PIXEL 0u
+#define GBSP_BATCH_PATH_STATE 1u
 
 int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t count,
     gbsp_batch **out);
 int gbsp_batch_destroy(gbsp_batch *batch);
 int gbsp_batch_set_config(gbsp_batch *batch, const gbsp_batch_config *config);
 int gbsp_batch_get_config(const gbsp_batch *batch, gbsp_batch_config *config);
-/* Times every candidate configuration (block x chunk x blocks per SM) over
+/* Times every candidate configuration (kernel x block x chunk x blocks per SM) over
  * `trials` launches each and keeps the fastest; *best receives it. */
 int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best);
 /* Renders every item.  metrics NULL: asynchronous on the runtime's stream. */
 int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics);
+
+/* ---- display ------------------------------------------------------------------------ */
+/* Tone maps an RGBA32F frame (device memory) into packed 8-bit RGBA (device
+ * memory): replaces PerformToneMapping of src/shaders/post_processing.frag.glsl:19-26
+ * (Reinhard, gamma 1/2.2) and ToColor (src/math_lib.h:523-532). */
+int gbsp_tonemap(void *stream, const float *frame, uint64_t pixels, uint32_t *out);
+
+/* ---- learned denoiser ----------------------------------------------------------- */
+/* Kernels of a kernel-predicting CNN denoiser (8 conv3x3 layers, 48 channels,
+ * softmax 5x5 filter) trained on this path tracer's low/high-spp frames.
+ * No reference counterpart.  All pointers are device memory, tensors are
+ * NHWC, BF16 values travel as uint16_t.  `stream` is a cudaStream_t (NULL =
+ * default stream).  Calls are asynchronous. */
+#define GBSP_DN_EPI_BF16_BIAS_RELU 0  /* BF16 out = relu(conv + bias) */
+#define GBSP_DN_EPI_F32_BIAS 1        /* FP32 out = conv + bias */
+#define GBSP_DN_EPI_F32 2             /* FP32 out = conv */
+/* features[p] = log1p(radiance), albedo, normal, depth/(1+depth), 6 zeros
+ * (16 BF16) from an RGBA32F frame and its G-buffers (8 floats per pixel). */
+int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
+    uint16_t *out);
+/* out[p][co] = sum_tap,ci in[p+off(tap)][ci] * w[tap][co][ci] (zero padded),
+ * with the epilogue above.  Instantiated for (cin, cout) = (16,48), (48,48),
+ * (48,32) and, for data gradients, (48,48)/(32,48) with GBSP_DN_EPI_F32. */
+int gbsp_dn_conv3x3_forward(void *stream, const uint16_t *in, uint32_t B, uint32_t H, uint32_t W,
+    uint32_t cin, const uint16_t *weights, const float *bias, uint32_t cout, int epilogue,
+    uint16_t *outBf16, float *outF32);
+/* wt[8-tap][ci][co] = w[tap][co][ci]: weights of the data-gradient conv. */
+int gbsp_dn_flip_transpose(void *stream, const uint16_t *w, uint32_t cout, uint32_t cin,
+    uint16_t *wt);
+/* out = dAct * (act > 0), as BF16. */
+int gbsp_dn_relu_backward(void *stream, const float *dAct, const uint16_t *act, uint64_t n,
+    uint16_t *out);
+/* dW[tap][co][ci] += sum_p dOut[p][co] * in[p+off(tap)][ci]; dBias[co] += sum_p dOut[p][co]. */
+int gbsp_dn_conv3x3_weight_grad(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
+/* out[p] = sum_k softmax(logits[p][0..24])_k * noisy[p + off5x5(k)] (edge-clamped);
+ * logits have 32 channels per pixel. */
+int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32_t B, uint32_t H,
+    uint32_t W, float *out);
+/* Gradient of relMSE = mean((out - target)^2 / (target^2 + 0.01)) with respect
+ * to the logits (BF16, 32 channels); adds the unnormalised loss to *lossSum. */
+int gbsp_dn_relmse_backward(void *stream, const float *logits, const float *noisy,
+    const float *target, uint32_t B, uint32_t H, uint32_t W, uint16_t *dLogits, float *lossSum);
+/* One Adam step on n parameters (FP32 master copy, optional BF16 mirror). */
+int gbsp_dn_adam(void *stream, float *param, uint16_t *paramBf16, const float *grad, float *m,
+    float *v, uint64_t n, float lr, float beta1, float beta2, float eps, uint32_t step);
 
 /* ---- procedural meshes (src/mesh_generation.cpp) ------------------------------ */
 /* CreateIcosahedronMesh (src/mesh_generation.cpp:220-337) without its 2048

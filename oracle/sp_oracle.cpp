@@ -1367,6 +1367,27 @@ double oracle_world_render_hashed_mt(void *wp, uint32_t width, uint32_t height,
 
 void oracle_world_set_build_bvh(void *wp, int on) { ((World *)wp)->buildMeshBvh = on != 0; }
 
+// PerformToneMapping (src/shaders/post_processing.frag.glsl:19-26) restated
+// in C, then ToColor (src/math_lib.h:523-532).
+void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out)
+{
+    for (uint64_t i = 0; i < pixels; i++)
+    {
+        const float *c = frame + 4 * i;
+        uint32_t v[3];
+        for (int k = 0; k < 3; k++)
+        {
+            float x = c[k] * 1.0f;
+            x = x / (1.0f + x);
+            x = powf(x, 1.0f / 2.2f);
+            float f = floorf(x * 255.0f);
+            f = f < 0.0f ? 0.0f : (f > 255.0f ? 255.0f : f);
+            v[k] = (uint32_t)f;
+        }
+        out[i] = (255u << 24) | (v[2] << 16) | (v[1] << 8) | v[0];
+    }
+}
+
 // Closest hit without BVHs: every object whose world box passes the slab
 // test, every triangle whose own box passes it in object space (the set the
 // reference's BVH queries return), Moller-Trumbore, smallest object-space t

@@ -111,6 +111,8 @@ int oracle_world_closest(void *w, uint32_t rayCount, const float *rays,
 // Meshes added after this call skip the reference's O(n^2 log n) BVH build
 // (they can then only be queried with oracle_world_closest_brute).
 void oracle_world_set_build_bvh(void *w, int on);
+// Display conversion: Reinhard + gamma 1/2.2, then 8-bit packing.
+void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out);
 int oracle_world_closest_brute(void *w, uint32_t rayCount, const float *rays,
     uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut);
 

@@ -20,7 +20,7 @@ def bits(a):
 
 def test_header_declarations_are_exported():
     header = open(os.path.join(ROOT, "include", "gbsp.h")).read()
-    declared = set(re.findall(r"\b(gbsp_[a-z_]+)\s*\(", header))
+    declared = set(re.findall(r"\b(gbsp_[a-z0-9_]+)\s*\(", header))
     assert declared, "no declarations parsed"
     assert declared == set(gbsp.EXPORTS), declared ^ set(gbsp.EXPORTS)
     lib = gbsp.load()

@@ -41,8 +41,9 @@ def test_batch_matches_single_scene_renders(gpu_lib):
     torch.cuda.synchronize()
     batch = gbsp.Batch(rt, rends, [t.data_ptr() for t in imgs])
     total = sum(s.width * s.height * s.spp for s in ss)
-    for use_graph in (0, 1):
-        batch.set_config(block=128, chunk=1, blocks_per_sm=4, use_graph=use_graph)
+    for kernel, use_graph in ((gbsp.BATCH_THREAD_PER_PIXEL, 0), (gbsp.BATCH_THREAD_PER_PIXEL, 1),
+                              (gbsp.BATCH_PATH_STATE, 0), (gbsp.BATCH_PATH_STATE, 1)):
+        batch.set_config(block=128, chunk=1, blocks_per_sm=4, use_graph=use_graph, kernel=kernel)
         for _ in range(2):  # a replayed graph must reset its queue each time
             for t in imgs:
                 t.fill_(-1.0)
@@ -52,9 +53,10 @@ def test_batch_matches_single_scene_renders(gpu_lib):
             for k, (t, ref) in enumerate(zip(imgs, refs)):
                 got = t.cpu().numpy()
                 assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), \
-                    f"item {k} differs (graph={use_graph})"
+                    f"item {k} differs (kernel={kernel}, graph={use_graph})"
     best = batch.autotune(trials=1)
     assert best.block in (64, 128, 256)
+    assert best.kernel in (gbsp.BATCH_THREAD_PER_PIXEL, gbsp.BATCH_PATH_STATE)
     for t in imgs:
         t.fill_(-1.0)
     torch.cuda.synchronize()

@@ -1,0 +1,181 @@
+"""Denoiser kernels against PyTorch FP32 references of the same ops, on the
+same BF16-rounded tensors (tolerances: relative 2e-2 for BF16 outputs,
+accumulation order differs), plus a short training run on path-traced data."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from vk_cinematic_gb300 import gbsp, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def torch_conv(x, w, b=None):
+    """x (B,H,W,Cin), w (9,Cout,Cin) -> (B,H,W,Cout), FP32."""
+    import torch
+
+    B, H, W, cin = x.shape
+    cout = w.shape[1]
+    wt = w.float().reshape(3, 3, cout, cin).permute(2, 3, 0, 1).contiguous()
+    y = torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), wt, b, padding=1)
+    return y.permute(0, 2, 3, 1).contiguous()
+
+
+def close(a, b, rtol=2e-2):
+    a = a.float().cpu()
+    b = b.float().cpu()
+    scale = b.abs().max().item() + 1e-6
+    err = (a - b).abs().max().item() / scale
+    return err, err <= rtol
+
+
+@pytest.mark.parametrize("cin,cout,epi", [(16, 48, 0), (48, 48, 0), (48, 32, 1), (48, 48, 2),
+                                          (32, 48, 2)])
+def test_conv3x3_forward_matches_torch(gpu_lib, cin, cout, epi):
+    import torch
+
+    from vk_cinematic_gb300.denoiser import _ptr, _stream
+
+    torch.manual_seed(cin * 100 + cout + epi)
+    B, H, W = 2, 9, 70
+    x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+    w = (torch.randn((9, cout, cin), device="cuda") * 0.2).to(torch.bfloat16)
+    bias = torch.randn(cout, device="cuda")
+    L = gbsp.load()
+    if epi == 0:
+        out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device="cuda")
+        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), B, H, W, cin, _ptr(w), _ptr(bias), cout,
+                                       epi, _ptr(out), None)
+        ref = torch.relu(torch_conv(x, w, bias))
+    else:
+        out = torch.empty((B, H, W, cout), dtype=torch.float32, device="cuda")
+        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), B, H, W, cin, _ptr(w),
+                                       _ptr(bias) if epi == 1 else None, cout, epi, None, _ptr(out))
+        ref = torch_conv(x, w, bias if epi == 1 else None)
+    assert rc == 0, L.gbsp_last_error_string()
+    torch.cuda.synchronize()
+    err, ok = close(out, ref)
+    print(f"conv {cin}->{cout} epi {epi}: max rel err {err:.2e}")
+    assert ok
+
+
+def test_conv_gradients_match_autograd(gpu_lib):
+    import torch
+
+    from vk_cinematic_gb300.denoiser import KPCNN, _ptr, _stream
+
+    torch.manual_seed(3)
+    net = KPCNN(seed=1)
+    B, H, W = 2, 12, 67
+    for li in (0, 1, 7):
+        cin, cout, _ = [(16, 48, 0), (48, 48, 0)] [min(li, 1)] if li < 7 else (48, 32, 1)
+        x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+        d = (torch.randn((B, H, W, cout), device="cuda") * 0.1).to(torch.bfloat16)
+        dw = torch.zeros((9, cout, cin), device="cuda")
+        db = torch.zeros(cout, device="cuda")
+        net.weight_grad(li, x, d, dw, db)
+        xr = x.float().clone().requires_grad_(True)
+        wr = net.wb[li].float().clone().requires_grad_(True)
+        br = torch.zeros(cout, device="cuda", requires_grad=True)
+        y = torch_conv(xr, wr, br)
+        (y * d.float()).sum().backward()
+        torch.cuda.synchronize()
+        err_w, ok_w = close(dw, wr.grad)
+        err_b, ok_b = close(db, br.grad)
+        print(f"layer {li}: dW rel err {err_w:.2e}, dB rel err {err_b:.2e}")
+        assert ok_w and ok_b
+        if li > 0:
+            dx = net.data_grad(li, d)
+            torch.cuda.synchronize()
+            err_x, ok_x = close(dx, xr.grad)
+            print(f"layer {li}: dX rel err {err_x:.2e}")
+            assert ok_x
+
+
+def test_filter_and_relmse_gradient_match_autograd(gpu_lib):
+    import torch
+
+    from vk_cinematic_gb300.denoiser import KPCNN, _ptr, _stream
+
+    torch.manual_seed(5)
+    B, H, W = 2, 7, 9
+    logits = torch.randn((B, H, W, 32), device="cuda")
+    noisy = torch.rand((B, H, W, 4), device="cuda") * 3
+    target = torch.rand((B, H, W, 4), device="cuda") * 2
+    net = KPCNN(seed=0)
+    out = net.filter(logits, noisy)
+    dlog = torch.empty((B, H, W, 32), dtype=torch.bfloat16, device="cuda")
+    loss = torch.zeros(1, device="cuda")
+    L = gbsp.load()
+    assert L.gbsp_dn_relmse_backward(_stream(), _ptr(logits), _ptr(noisy), _ptr(target), B, H, W,
+                                     _ptr(dlog), _ptr(loss)) == 0
+    # reference
+    lr = logits[..., :25].clone().requires_grad_(True)
+    wts = torch.softmax(lr, dim=-1)
+    pad = torch.nn.functional.pad(noisy[..., :3].permute(0, 3, 1, 2), (2, 2, 2, 2),
+                                  mode="replicate")
+    acc = torch.zeros((B, 3, H, W), device="cuda")
+    for k in range(25):
+        ky, kx = k // 5, k % 5
+        acc = acc + wts[..., k].unsqueeze(1) * pad[:, :, ky:ky + H, kx:kx + W]
+    ref_out = acc.permute(0, 2, 3, 1)
+    t3 = target[..., :3]
+    ref_loss = ((ref_out - t3) ** 2 / (t3 * t3 + 0.01)).mean()
+    ref_loss.backward()
+    torch.cuda.synchronize()
+    err_o, ok_o = close(out[..., :3], ref_out.detach(), rtol=1e-4)
+    assert ok_o, err_o
+    assert abs(loss.item() / (3 * B * H * W) - ref_loss.item()) <= 1e-4 * ref_loss.item()
+    err_g, ok_g = close(dlog[..., :25], lr.grad)
+    print(f"filter rel err {err_o:.2e}, dLogits rel err {err_g:.2e}")
+    assert ok_g
+    assert torch.all(dlog[..., 25:] == 0)
+
+
+def test_adam_matches_torch(gpu_lib):
+    import torch
+
+    from vk_cinematic_gb300.denoiser import _ptr, _stream
+
+    torch.manual_seed(0)
+    p = torch.randn(1000, device="cuda")
+    p_ref = p.clone().requires_grad_(True)
+    opt = torch.optim.Adam([p_ref], lr=1e-3)
+    m = torch.zeros_like(p)
+    v = torch.zeros_like(p)
+    pb = torch.empty(1000, dtype=torch.bfloat16, device="cuda")
+    L = gbsp.load()
+    for step in range(1, 4):
+        g = torch.randn(1000, device="cuda")
+        p_ref.grad = g.clone()
+        opt.step()
+        assert L.gbsp_dn_adam(_stream(), _ptr(p), _ptr(pb), _ptr(g), _ptr(m), _ptr(v),
+                              ctypes.c_uint64(1000), ctypes.c_float(1e-3), ctypes.c_float(0.9),
+                              ctypes.c_float(0.999), ctypes.c_float(1e-8),
+                              ctypes.c_uint32(step)) == 0
+    torch.cuda.synchronize()
+    assert torch.allclose(p, p_ref.detach(), rtol=1e-5, atol=1e-6)
+    assert torch.allclose(pb.float(), p, rtol=1e-2, atol=1e-2)
+
+
+def test_short_training_reduces_loss(gpu_lib):
+    import torch
+
+    from vk_cinematic_gb300 import denoiser
+
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rt = gbsp.Runtime(0, stream=stream.cuda_stream)
+    noisy, aov, target = denoiser.make_dataset(rt, n_scenes=2, crops_per_scene=2, crop=64,
+                                               spp_in=4, spp_ref=256, n_spheres=64, level=3)
+    net = denoiser.KPCNN(seed=0)
+    feats = net.features(noisy, aov)
+    losses = [float(net.train_step(feats, noisy, target, lr=1e-3).item()) for _ in range(60)]
+    print("loss", losses[0], "->", losses[-1])
+    assert np.isfinite(losses).all()
+    assert losses[-1] < 0.8 * losses[0]
+    den = net.denoise(noisy, aov)
+    assert torch.isfinite(den).all()
+    torch.cuda.set_stream(torch.cuda.default_stream())

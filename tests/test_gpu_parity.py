@@ -264,3 +264,34 @@ def test_config3_style_scene_matches_oracle(rt):
     print(f"config3-style mean rel err {err:.3e}")
     assert err <= IMAGE_TOL
     assert m["paths_traced"] == s.width * s.height * s.spp
+
+
+def test_tonemap_matches_oracle(rt, port):
+    """Display conversion (post_processing.frag.glsl:19-26 + ToColor) of a
+    path-traced frame against the C restatement; powf differs in the last
+    bits between CUDA and glibc, so a channel may differ by one level."""
+    import ctypes
+
+    import torch
+
+    import pyoracle as po
+
+    s = scenes.config1_scene(width=64, height=48, spp=4)
+    img, _, _ = render(rt, s)
+    img = np.ascontiguousarray(img * np.float32(3.0))  # spread over the curve
+    dev = torch.from_numpy(img).cuda()
+    out = torch.zeros(img.shape[0] * img.shape[1], dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    L = gbsp.load()
+    assert L.gbsp_tonemap(None, ctypes.c_void_p(dev.data_ptr()),
+                          ctypes.c_uint64(out.numel()), ctypes.c_void_p(out.data_ptr())) == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(np.uint32)
+    lib = ctypes.CDLL(po.PORT_LIB)
+    ref = np.zeros_like(got)
+    lib.oracle_tonemap(img.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint64(ref.size),
+                       ref.ctypes.data_as(ctypes.c_void_p))
+    gb = got.view(np.uint8).astype(int)
+    rb = ref.view(np.uint8).astype(int)
+    assert np.abs(gb - rb).max() <= 1
+    assert (gb == rb).mean() > 0.99

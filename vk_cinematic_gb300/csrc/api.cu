@@ -298,6 +298,8 @@ static void runtime_teardown(gbsp_runtime *rt)
     rt->pathRad.release();
     rt->queueCounts.release();
     rt->frame.release();
+    rt->aov.release();
+    rt->pathAov.release();
     cudaStreamSynchronize(rt->stream);
     if (rt->dStatus) cudaFree(rt->dStatus);
     if (rt->dCounters) cudaFree(rt->dCounters);
@@ -817,13 +819,19 @@ static int prepare_render(const gbsp_context *ctx, gbsp_options &opt, MaterialVi
     return GBSP_OK;
 }
 
-static int ensure_frame(gbsp_runtime *rt, uint32_t w, uint32_t h)
+static int ensure_frame(gbsp_runtime *rt, uint32_t w, uint32_t h, bool aov = false)
 {
     int rc = rt->frame.reserve((size_t)w * h, rt->stream);
     if (rc) return rc;
+    if (aov && (rc = rt->aov.reserve(2 * (size_t)w * h, rt->stream))) return rc;
     rt->frameW = w;
     rt->frameH = h;
     return GBSP_OK;
+}
+
+static float4 *aov_target(gbsp_runtime *rt, const gbsp_options &opt)
+{
+    return (opt.flags & GBSP_FLAG_AOV) ? rt->aov.ptr : nullptr;
 }
 
 int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile, gbsp_rng *rng,
@@ -839,14 +847,15 @@ int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile, gbsp_rng *rng,
     gbsp_image_plane *ip = ctx->camera->imagePlane;
     uint32_t x0 = tile.minX, y0 = tile.minY;
     uint32_t x1 = std::min(tile.maxX, ip->width), y1 = std::min(tile.maxY, ip->height);
-    if ((rc = ensure_frame(rt, ip->width, ip->height))) return rc;
+    if ((rc = ensure_frame(rt, ip->width, ip->height, (opt.flags & GBSP_FLAG_AOV) != 0))) return rc;
     if ((rc = counters_begin(rt, (opt.flags & GBSP_FLAG_STAGE_TIMING) != 0))) return rc;
     GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
     bool seq = opt.rng_mode == GBSP_RNG_TILE_SEQUENTIAL;
     if (seq && !rng) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile-sequential mode needs an RNG");
     if (x1 > x0 && y1 > y0) {
         if ((rc = render_frame(rt, ctx->scene->view(), mv, camera_params(ctx->camera), opt, x0, y0,
-                 x1, y1, rt->frame.ptr, ip->width, seq ? &rng->state : nullptr)))
+                 x1, y1, rt->frame.ptr, ip->width, seq ? &rng->state : nullptr,
+                 seq ? nullptr : aov_target(rt, opt))))
             return rc;
     }
     GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
@@ -873,12 +882,14 @@ int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics)
     gbsp_runtime *rt = ctx->runtime;
     cudaStream_t s = rt->stream;
     gbsp_image_plane *ip = ctx->camera->imagePlane;
-    if ((rc = ensure_frame(rt, ip->width, ip->height))) return rc;
+    if ((rc = ensure_frame(rt, ip->width, ip->height, (opt.flags & GBSP_FLAG_AOV) != 0))) return rc;
     rt->begin_call(false);
     if (metrics && (rc = counters_begin(rt, (opt.flags & GBSP_FLAG_STAGE_TIMING) != 0))) return rc;
     if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
+    bool seq = opt.rng_mode == GBSP_RNG_TILE_SEQUENTIAL;
     if ((rc = render_frame(rt, ctx->scene->view(), mv, camera_params(ctx->camera), opt, 0, 0,
-             ip->width, ip->height, rt->frame.ptr, ip->width, nullptr)))
+             ip->width, ip->height, rt->frame.ptr, ip->width, nullptr,
+             seq ? nullptr : aov_target(rt, opt))))
         return rc;
     if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
     if (ip->pixels)
@@ -894,6 +905,31 @@ int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics)
     if (metrics) cudaEventElapsedTime(&ms, rt->ev[0], rt->ev[1]);
     if ((rc = counters_end(rt, metrics, ms))) return rc;
     return check_stream_status(rt);
+}
+
+const float *gbsp_frame_aov_device_pointer(gbsp_runtime *rt)
+{
+    return rt ? reinterpret_cast<const float *>(rt->aov.ptr) : nullptr;
+}
+
+int gbsp_frame_copy_region(gbsp_runtime *rt, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+    float *dstRadiance, float *dstAov)
+{
+    if (!rt || !dstRadiance) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (x0 + w > rt->frameW || y0 + h > rt->frameH || !rt->frame.ptr)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "region outside the last frame");
+    size_t srcPitch = (size_t)rt->frameW * sizeof(float4);
+    GBSP_CUDA_TRY(cudaMemcpy2DAsync(dstRadiance, (size_t)w * sizeof(float4),
+        rt->frame.ptr + (size_t)y0 * rt->frameW + x0, srcPitch, (size_t)w * sizeof(float4), h,
+        cudaMemcpyDeviceToDevice, rt->stream));
+    if (dstAov) {
+        if (!rt->aov.ptr || rt->aov.count < 2 * (size_t)rt->frameW * rt->frameH)
+            return set_error(GBSP_ERR_NOT_READY, "no G-buffers: render with GBSP_FLAG_AOV");
+        GBSP_CUDA_TRY(cudaMemcpy2DAsync(dstAov, (size_t)w * 2 * sizeof(float4),
+            rt->aov.ptr + 2 * ((size_t)y0 * rt->frameW + x0), 2 * srcPitch,
+            (size_t)w * 2 * sizeof(float4), h, cudaMemcpyDeviceToDevice, rt->stream));
+    }
+    return GBSP_OK;
 }
 
 const float *gbsp_frame_device_pointer(gbsp_runtime *rt)

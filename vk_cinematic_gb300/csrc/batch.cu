@@ -99,6 +99,260 @@ __global__ void __launch_bounds__(256) k_batch(const BatchItemDev *__restrict__ 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Path state machine variant.  Every lane owns one pixel at a time and walks
+// its samples, paths, bounces and traversal as a sequence of small steps:
+// one stack pop of the closest-hit traversal (object or mesh level), or one
+// shading event.  The warp executes either a traversal step for the lanes
+// that are tracing or a shading step for the lanes whose query finished
+// (once at least half of the warp waits for it, or nobody traces), so the
+// instructions of a step are shared by most lanes; lanes that finish a pixel
+// take the next ones from the global queue (one atomicAdd per refill).
+// Per lane the sequence of operations - and so every result bit - is the
+// one of trace_full_path.
+// ---------------------------------------------------------------------------
+constexpr int kSmRefill = 8;
+constexpr int kSmShade = 16;
+
+__global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict__ items,
+    uint32_t itemCount, uint64_t totalPixels, unsigned long long *work,
+    unsigned long long *counters, uint32_t *status)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t laneMaskLt = (1u << lane) - 1u;
+    TraceCounters cnt = {0, 0, 0, 0, 0};
+    uint32_t rays = 0, hitsCnt = 0, paths = 0, nans = 0;
+    // lane state
+    int phase = 0;  // 0 idle, 1 tracing, 2 query done
+    uint32_t it = 0, x = 0, y = 0, s = 0, rng = 0, b = 0, len = 0;
+    CSum acc[3];
+    float4 vE[kBatchMaxBounces], vA[kBatchMaxBounces];
+    V3 o = v3(0, 0, 0), d = v3(0, 0, 0), invd = v3(0, 0, 0);
+    // traversal state
+    uint32_t stackRef[kStackSize];
+    float stackT[kStackSize];
+    int sp = 0, tmode = 1, base = 0;
+    float bestT = kInf, bestU = 0, bestV = 0;
+    int32_t bestPrim = -1, bestInst = -1;
+    uint32_t inst = 0;
+    V3 lo = v3(0, 0, 0), ld = v3(0, 0, 0), linvd = v3(0, 0, 0);
+    float llen = 0, lBestT = kInf, lU = 0, lV = 0;
+    int32_t lPrim = -1;
+    bool exhausted = false;
+
+    auto trace_begin = [&](const SceneView &sv) {
+        invd = inverse(d);
+        bestT = kInf;
+        bestU = bestV = 0.0f;
+        bestPrim = bestInst = -1;
+        sp = 0;
+        if (sv.tlasRoot != kEmptyChild) {
+            stackRef[0] = sv.tlasRoot;
+            stackT[0] = 0.0f;
+            sp = 1;
+        }
+        tmode = 1;
+        phase = 1;
+    };
+    bool emptyPath = false;  // max_bounces 0: the sample has no query at all
+    auto start_sample = [&](const BatchItemDev &itd) {
+        rng = sample_seed(itd.seed, x, y, s);
+        camera_ray(itd.cam, x, y, rng, o, d);
+        b = 0;
+        len = 0;
+        emptyPath = itd.maxBounces == 0;
+        if (emptyPath)
+            phase = 2;
+        else
+            trace_begin(itd.sv);
+    };
+
+    for (uint64_t guard = 0; guard < (1ull << 40); guard++) {
+        // ---- refill idle lanes with pixels
+        uint32_t idle = __ballot_sync(0xFFFFFFFFu, phase == 0);
+        if (idle && !exhausted && (__popc(idle) >= kSmRefill || idle == 0xFFFFFFFFu)) {
+            uint32_t n = __popc(idle);
+            int leader = __ffs(idle) - 1;
+            unsigned long long first = 0;
+            if (lane == leader) first = atomicAdd(work, (unsigned long long)n);
+            first = __shfl_sync(0xFFFFFFFFu, first, leader);
+            if (first + n >= totalPixels) exhausted = true;
+            if (phase == 0) {
+                uint64_t pix = first + __popc(idle & laneMaskLt);
+                if (pix < totalPixels) {
+                    uint32_t lo_ = 0, hi_ = itemCount - 1;
+                    while (lo_ < hi_) {
+                        uint32_t mid = (lo_ + hi_ + 1) >> 1;
+                        if (items[mid].pixelBase <= pix)
+                            lo_ = mid;
+                        else
+                            hi_ = mid - 1;
+                    }
+                    it = lo_;
+                    const BatchItemDev &itd = items[it];
+                    uint64_t local = pix - itd.pixelBase;
+                    x = (uint32_t)(local % itd.width);
+                    y = (uint32_t)(local / itd.width);
+                    s = 0;
+                    acc[0] = acc[1] = acc[2] = CSum{0.0f, 0.0f};
+                    start_sample(itd);
+                }
+            }
+        }
+        uint32_t tmask = __ballot_sync(0xFFFFFFFFu, phase == 1);
+        uint32_t smask = __ballot_sync(0xFFFFFFFFu, phase == 2);
+        if (!tmask && !smask) {
+            if (exhausted) break;
+            continue;
+        }
+        bool doShade = smask && (__popc(smask) >= kSmShade || !tmask);
+        const BatchItemDev &itd = items[it];
+        if (doShade) {
+            if (phase != 2) continue;
+            float4 ec, aa;
+            bool more = false;
+            bool hit = false;
+            if (!emptyPath) {
+                rays++;
+                hit = bestPrim >= 0 && bestT > 0.0f;
+            }
+            if (hit) {
+                hitsCnt++;
+                RayHit h;
+                h.t = bestT;
+                h.u = bestU;
+                h.v = bestV;
+                h.prim = bestPrim;
+                h.inst = bestInst;
+                V3 n;
+                float ux, uy;
+                hit_surface(itd.sv, h, n, ux, uy);
+                V3 pos = add(o, mul(d, h.t));
+                V3 dir = random_hemisphere(n, rng);
+                vertex_terms(itd.mv, itd.mv.instanceSlot[h.inst], n, dir, neg(d), ux, uy, ec, aa);
+                vE[len] = ec;
+                vA[len] = aa;
+                len++;
+                if (b + 1 < itd.maxBounces && b + 1 < (uint32_t)kBatchMaxBounces) {
+                    o = add(pos, mul(n, 0.0001f));
+                    d = dir;
+                    b++;
+                    more = true;
+                    trace_begin(itd.sv);
+                }
+            } else if (!emptyPath) {
+                vertex_terms(itd.mv, itd.mv.backgroundSlot, v3(0, 0, 0), v3(0, 0, 0), neg(d), 0.0f,
+                    0.0f, ec, aa);
+                vE[len] = ec;
+                vA[len] = aa;
+                len++;
+            }
+            if (more) continue;
+            V3 r = path_radiance(vE, vA, 1, 0, len, itd.clampValue);
+            paths++;
+            bool isNan = isnan(r.x) || isnan(r.y) || isnan(r.z);
+            if (isNan) nans++;
+            if (!isNan || itd.nanPolicy != GBSP_NAN_ZERO) {
+                csum_add(acc[0], r.x * itd.invSpp);
+                csum_add(acc[1], r.y * itd.invSpp);
+                csum_add(acc[2], r.z * itd.invSpp);
+            }
+            s++;
+            if (s < itd.spp) {
+                start_sample(itd);
+            } else {
+                itd.image[(size_t)y * itd.width + x] =
+                    make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
+                phase = 0;
+            }
+            continue;
+        }
+        if (phase != 1) continue;
+        // ---- one traversal step (dyn_trace_loop's step, per-lane scene)
+        const SceneView &sv = itd.sv;
+        if (tmode == 2 && sp == base) {
+            if (lPrim >= 0) {
+                const Instance &in = sv.instances[inst];
+                Affine model;
+#pragma unroll
+                for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
+                V3 worldHit = transform_point(model, add(lo, mul(ld, lBestT)));
+                float tw = dot(sub(worldHit, o), d);
+                if (tw < bestT || (tw == bestT && (int32_t)inst < bestInst)) {
+                    bestT = tw;
+                    bestU = lU;
+                    bestV = lV;
+                    bestPrim = lPrim;
+                    bestInst = (int32_t)inst;
+                }
+            }
+            tmode = 1;
+            continue;
+        }
+        if (tmode == 1 && sp == 0) {
+            phase = 2;
+            continue;
+        }
+        sp--;
+        uint32_t ref = stackRef[sp];
+        float te = stackT[sp];
+        float bound = tmode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * llen));
+        if (te > bound) continue;
+        if (!child_is_leaf(ref)) {
+            if (tmode == 1)
+                cnt.topNodes++;
+            else
+                cnt.meshNodes++;
+            V3 ro = tmode == 1 ? o : lo;
+            V3 ri = tmode == 1 ? invd : linvd;
+            visit_node<true>(sv.nodes, ref, ro, ri, bound, stackRef, stackT, sp, status, cnt);
+            continue;
+        }
+        if (tmode == 1) {
+            inst = leaf_first(ref);
+            const Instance &in = sv.instances[inst];
+            Affine inv;
+#pragma unroll
+            for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
+            lo = transform_point(inv, o);
+            ld = normalize(transform_vector(inv, d), &llen);
+            linvd = inverse(ld);
+            cnt.meshTests++;
+            lBestT = kInf;
+            lU = lV = 0.0f;
+            lPrim = -1;
+            base = sp;
+            if (sp >= kStackSize) {
+                atomicOr(status, kStatusStackOverflow);
+                continue;
+            }
+            stackRef[sp] = __ldg(&in.blasRoot);
+            stackT[sp] = 0.0f;
+            sp++;
+            tmode = 2;
+            continue;
+        }
+        visit_leaf<true>(sv, ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+    }
+    uint32_t v[9] = {rays, hitsCnt, paths, nans, cnt.topNodes, cnt.meshNodes, cnt.triTests,
+        cnt.boxTests, cnt.meshTests};
+#pragma unroll
+    for (int k = 0; k < 9; k++)
+        for (int off = 16; off; off >>= 1) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+    if (lane == 0) {
+        atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)v[0]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)v[1]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(v[0] - v[1]));
+        atomicAdd(&counters[GBSP_METRIC_PATHS_TRACED], (unsigned long long)v[2]);
+        atomicAdd(&counters[GBSP_METRIC_NAN_SAMPLES], (unsigned long long)v[3]);
+        atomicAdd(&counters[GBSP_METRIC_BROADPHASE_NODE_VISITS], (unsigned long long)v[4]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_NODE_VISITS], (unsigned long long)v[5]);
+        atomicAdd(&counters[GBSP_METRIC_TRIANGLE_TESTS], (unsigned long long)v[6]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_BOX_TESTS], (unsigned long long)v[7]);
+        atomicAdd(&counters[GBSP_METRIC_MESH_TESTS_PERFORMED], (unsigned long long)v[8]);
+    }
+}
+
 }  // namespace gbsp
 
 using namespace gbsp;
@@ -110,7 +364,7 @@ struct gbsp_batch {
     DeviceBuffer<int32_t> dSlots;
     DeviceBuffer<unsigned long long> dWork;
     uint64_t totalPixels = 0, totalPaths = 0;
-    gbsp_batch_config cfg = {128, 1, 8, 1};
+    gbsp_batch_config cfg = {128, 1, 8, 1, GBSP_BATCH_PATH_STATE};
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -126,8 +380,12 @@ static int enqueue(gbsp_batch *b)
     cudaStream_t s = rt->stream;
     k_batch_reset<<<1, 32, 0, s>>>(b->dWork.ptr, rt->dCounters);
     int grid = rt->smCount * (int)b->cfg.blocksPerSm;
-    k_batch<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(), b->totalPixels,
-        b->cfg.chunk, b->dWork.ptr, rt->dCounters, rt->dStatus);
+    if (b->cfg.kernel == GBSP_BATCH_PATH_STATE)
+        k_batch_sm<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(),
+            b->totalPixels, b->dWork.ptr, rt->dCounters, rt->dStatus);
+    else
+        k_batch<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(),
+            b->totalPixels, b->cfg.chunk, b->dWork.ptr, rt->dCounters, rt->dStatus);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }
@@ -159,8 +417,12 @@ static int launch_once(gbsp_batch *b)
 
 static int check_config(const gbsp_batch_config *c)
 {
+    if (c->kernel != GBSP_BATCH_THREAD_PER_PIXEL && c->kernel != GBSP_BATCH_PATH_STATE)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "unknown batch kernel %u", c->kernel);
     if (c->block != 64 && c->block != 128 && c->block != 256)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "block must be 64, 128 or 256");
+    if (c->kernel == GBSP_BATCH_PATH_STATE && c->block > 128)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "the path-state kernel takes 64 or 128 threads");
     if (c->chunk < 1 || c->chunk > 8) return set_error(GBSP_ERR_INVALID_ARGUMENT, "chunk must be 1..8");
     if (c->blocksPerSm < 1 || c->blocksPerSm > 32)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "blocksPerSm must be 1..32");
@@ -318,10 +580,13 @@ int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *b
     const uint32_t perSm[] = {2, 4, 8};
     gbsp_batch_config keep = batch->cfg, bestCfg = batch->cfg;
     float bestMs = 3.0e38f;
+    for (uint32_t kern : {GBSP_BATCH_THREAD_PER_PIXEL, GBSP_BATCH_PATH_STATE})
     for (uint32_t bl : blocks)
         for (uint32_t ch : chunks)
             for (uint32_t ps : perSm) {
-                gbsp_batch_config c = {bl, ch, ps, keep.useGraph};
+                // the state machine ignores chunk and takes at most 128 threads
+                if (kern == GBSP_BATCH_PATH_STATE && (bl > 128 || ch != 1)) continue;
+                gbsp_batch_config c = {bl, ch, ps, keep.useGraph, kern};
                 batch->cfg = c;
                 drop_graph(batch);
                 int rc = launch_once(batch);  // warm-up (and graph capture)

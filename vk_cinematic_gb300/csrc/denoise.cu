@@ -1,0 +1,485 @@
+// Learned denoiser kernels: a kernel-predicting CNN (8 conv3x3 layers of 48
+// channels, ReLU, a 5x5 per-pixel filter from a softmax over 25 logits),
+// trained on pairs of low-spp frames (radiance + albedo, normal, depth
+// G-buffers) and high-spp targets rendered by this path tracer.  No
+// reference counterpart: vk_cinematic has no denoiser.
+//
+// Tensors are NHWC.  Activations and weights are BF16, accumulation FP32.
+//  * conv3x3 forward / data gradient: implicit GEMM on the tensor cores,
+//    M = pixels, N = output channels, K = 9 taps x input channels, with
+//    mma.sync m16n8k16 BF16.  CTAs are persistent: each loads the layer's
+//    weights into shared memory once (padded rows, conflict-free fragment
+//    loads) and then walks 64-pixel row segments.
+//  * weight gradient: FP32 outer products over pixel chunks, one tap per
+//    CTA, reduced with atomics.
+//  * filter, loss and Adam: elementwise FP32.
+
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+#include "gbsp_internal.h"
+
+namespace gbsp {
+namespace dn {
+
+constexpr int kTileP = 64;   // pixels per row segment
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ void mma_bf16_16816(float *c, uint32_t a0, uint32_t a1, uint32_t a2,
+    uint32_t a3, uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+
+enum Epilogue : int { kEpiBf16BiasRelu = 0, kEpiF32Bias = 1, kEpiF32 = 2 };
+
+// out[p][co] = sum_{tap, ci} in[p + off(tap)][ci] * w[tap][co][ci] (+ bias, ReLU)
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(kThreads) k_conv3x3(const __nv_bfloat16 *__restrict__ in, int B,
+    int H, int W, const __nv_bfloat16 *__restrict__ w, const float *__restrict__ bias,
+    __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
+{
+    static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel padding");
+    constexpr int SIN = CIN + 8;  // padded element stride per pixel (bank-conflict free)
+    constexpr int SPX = kTileP + 2;
+    extern __shared__ __align__(16) unsigned char smemRaw[];
+    __nv_bfloat16 *sW = reinterpret_cast<__nv_bfloat16 *>(smemRaw);   // [9][COUT][SIN]
+    __nv_bfloat16 *sIn = sW + 9 * COUT * SIN;                          // [3][SPX][SIN]
+    const int tid = threadIdx.x;
+    for (int i = tid; i < 9 * COUT * (CIN / 2); i += kThreads) {
+        int row = i / (CIN / 2), c2 = i % (CIN / 2);
+        reinterpret_cast<uint32_t *>(sW + row * SIN)[c2] =
+            reinterpret_cast<const uint32_t *>(w)[(size_t)row * (CIN / 2) + c2];
+    }
+    const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int tilesPerRow = (W + kTileP - 1) / kTileP;
+    const int numTiles = tilesPerRow * B * H;
+    for (int tile = blockIdx.x; tile < numTiles; tile += gridDim.x) {
+        const int row = tile / tilesPerRow;  // b * H + y
+        const int x0 = (tile % tilesPerRow) * kTileP;
+        const int b = row / H, y = row % H;
+        __syncthreads();  // previous tile's reads of sIn are done (and sW is loaded)
+        for (int i = tid; i < 3 * SPX * (CIN / 2); i += kThreads) {
+            int c2 = i % (CIN / 2);
+            int px = (i / (CIN / 2)) % SPX;
+            int ry = i / ((CIN / 2) * SPX);
+            int gy = y + ry - 1, gx = x0 + px - 1;
+            uint32_t v = 0;
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+                v = reinterpret_cast<const uint32_t *>(in)[((size_t)(b * H + gy) * W + gx) * (CIN / 2) + c2];
+            reinterpret_cast<uint32_t *>(sIn + (ry * SPX + px) * SIN)[c2] = v;
+        }
+        __syncthreads();
+        float acc[COUT / 8][4];
+#pragma unroll
+        for (int n = 0; n < COUT / 8; n++) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
+        const int m0 = warp * 16;
+#pragma unroll 1
+        for (int tap = 0; tap < 9; tap++) {
+            const int ty = tap / 3, tx = tap % 3;
+            const __nv_bfloat16 *aBase = sIn + (ty * SPX + m0 + tx) * SIN;
+            const __nv_bfloat16 *bBase = sW + tap * COUT * SIN;
+#pragma unroll
+            for (int kc = 0; kc < CIN; kc += 16) {
+                uint32_t a0 = *reinterpret_cast<const uint32_t *>(aBase + g * SIN + kc + 2 * t);
+                uint32_t a1 = *reinterpret_cast<const uint32_t *>(aBase + (g + 8) * SIN + kc + 2 * t);
+                uint32_t a2 = *reinterpret_cast<const uint32_t *>(aBase + g * SIN + kc + 2 * t + 8);
+                uint32_t a3 = *reinterpret_cast<const uint32_t *>(aBase + (g + 8) * SIN + kc + 2 * t + 8);
+#pragma unroll
+                for (int n = 0; n < COUT / 8; n++) {
+                    const __nv_bfloat16 *bp = bBase + (n * 8 + g) * SIN + kc + 2 * t;
+                    uint32_t b0 = *reinterpret_cast<const uint32_t *>(bp);
+                    uint32_t b1 = *reinterpret_cast<const uint32_t *>(bp + 8);
+                    mma_bf16_16816(acc[n], a0, a1, a2, a3, b0, b1);
+                }
+            }
+        }
+        // epilogue: rows g and g+8 of the warp's slab, columns 2t, 2t+1 of each n tile
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            int x = x0 + m0 + g + 8 * half;
+            if (x >= W) continue;
+            size_t p = (size_t)row * W + x;
+#pragma unroll
+            for (int n = 0; n < COUT / 8; n++) {
+                int co = n * 8 + 2 * t;
+                float v0 = acc[n][2 * half], v1 = acc[n][2 * half + 1];
+                if (EPI != kEpiF32) {
+                    v0 += bias[co];
+                    v1 += bias[co + 1];
+                }
+                if (EPI == kEpiBf16BiasRelu) {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                    reinterpret_cast<uint32_t *>(outB + p * COUT)[co / 2] = pack_bf16(v0, v1);
+                } else {
+                    *reinterpret_cast<float2 *>(outF + p * COUT + co) = make_float2(v0, v1);
+                }
+            }
+        }
+    }
+}
+
+template <int CIN, int COUT, int EPI>
+int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W, const void *w,
+    const float *bias, void *outB, float *outF)
+{
+    constexpr int SIN = CIN + 8;
+    size_t smem = (size_t)(9 * COUT + 3 * (kTileP + 2)) * SIN * 2;
+    auto kern = k_conv3x3<CIN, COUT, EPI>;
+    GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int tiles = ((W + kTileP - 1) / kTileP) * B * H;
+    int grid = smCount * 3;
+    if (grid > tiles) grid = tiles;
+    kern<<<grid, kThreads, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W,
+        reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
+        outF);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+// Input features: log(1 + radiance), albedo, normal, depth/(1 + depth),
+// zero-padded to 16 channels.
+__global__ void k_features(const float4 *__restrict__ rad, const float4 *__restrict__ aov,
+    uint64_t n, __nv_bfloat16 *__restrict__ out)
+{
+    uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    float4 r = rad[p];
+    float4 a = aov[2 * p], nn = aov[2 * p + 1];
+    float d = fmaxf(a.w, 0.0f);
+    float f[16] = {log1pf(fmaxf(r.x, 0.0f)), log1pf(fmaxf(r.y, 0.0f)), log1pf(fmaxf(r.z, 0.0f)),
+        a.x, a.y, a.z, nn.x, nn.y, nn.z, d / (1.0f + d), 0, 0, 0, 0, 0, 0};
+    uint32_t *o = reinterpret_cast<uint32_t *>(out + p * 16);
+#pragma unroll
+    for (int i = 0; i < 8; i++) o[i] = pack_bf16(f[2 * i], f[2 * i + 1]);
+}
+
+// w'[8 - tap][ci][co] = w[tap][co][ci]: weights of the data-gradient conv.
+__global__ void k_flip_transpose(const __nv_bfloat16 *w, int cout, int cin, __nv_bfloat16 *wt)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 9 * cout * cin) return;
+    int tap = i / (cout * cin), r = i % (cout * cin), co = r / cin, ci = r % cin;
+    wt[((8 - tap) * cin + ci) * cout + co] = w[i];
+}
+
+// d = dAct * (act > 0) as BF16 (ReLU backward).
+__global__ void k_relu_bwd(const float *__restrict__ dAct, const __nv_bfloat16 *__restrict__ act,
+    uint64_t n, __nv_bfloat16 *__restrict__ out)
+{
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a = __bfloat162float(act[i]);
+    out[i] = __float2bfloat16_rn(a > 0.0f ? dAct[i] : 0.0f);
+}
+
+// dW[tap][co][ci] += sum_p d[p][co] * in[p + off(tap)][ci]; dBias[co] += sum_p d[p][co].
+// CTA = (pixel chunk, tap); 128 threads, each owns a (COUT/8 x CIN/16) block.
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(128) k_conv3x3_wgrad(const __nv_bfloat16 *__restrict__ in,
+    const __nv_bfloat16 *__restrict__ d, int B, int H, int W, int chunk, float *dW, float *dBias)
+{
+    constexpr int TC = COUT / 8, TI = CIN / 16;  // 8 x 16 thread grid
+    constexpr int STAGE = 32;                    // pixels staged per iteration
+    __shared__ float sD[STAGE][COUT];
+    __shared__ float sI[STAGE][CIN];
+    const int tap = blockIdx.y, dy = tap / 3 - 1, dx = tap % 3 - 1;
+    const uint64_t N = (uint64_t)B * H * W;
+    const uint64_t p0 = (uint64_t)blockIdx.x * chunk;
+    const int tco = threadIdx.x / 16, tci = threadIdx.x % 16;
+    float acc[TC][TI];
+#pragma unroll
+    for (int a = 0; a < TC; a++)
+#pragma unroll
+        for (int c = 0; c < TI; c++) acc[a][c] = 0.0f;
+    float bacc = 0.0f;
+    for (int base = 0; base < chunk; base += STAGE) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < STAGE * COUT; i += 128) {
+            int k = i / COUT, co = i % COUT;
+            uint64_t p = p0 + base + k;
+            sD[k][co] = p < N ? __bfloat162float(d[p * COUT + co]) : 0.0f;
+        }
+        for (int i = threadIdx.x; i < STAGE * CIN; i += 128) {
+            int k = i / CIN, ci = i % CIN;
+            uint64_t p = p0 + base + k;
+            float v = 0.0f;
+            if (p < N) {
+                int x = (int)(p % W), y = (int)((p / W) % H);
+                int gx = x + dx, gy = y + dy;
+                if (gx >= 0 && gx < W && gy >= 0 && gy < H)
+                    v = __bfloat162float(in[(p + (int64_t)dy * W + dx) * CIN + ci]);
+            }
+            sI[k][ci] = v;
+        }
+        __syncthreads();
+        for (int k = 0; k < STAGE; k++) {
+            float dv[TC], iv[TI];
+#pragma unroll
+            for (int a = 0; a < TC; a++) dv[a] = sD[k][tco * TC + a];
+#pragma unroll
+            for (int c = 0; c < TI; c++) iv[c] = sI[k][tci * TI + c];
+#pragma unroll
+            for (int a = 0; a < TC; a++)
+#pragma unroll
+                for (int c = 0; c < TI; c++) acc[a][c] += dv[a] * iv[c];
+            if (tap == 4 && threadIdx.x < COUT) bacc += sD[k][threadIdx.x];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < TC; a++)
+#pragma unroll
+        for (int c = 0; c < TI; c++)
+            atomicAdd(&dW[((size_t)tap * COUT + tco * TC + a) * CIN + tci * TI + c], acc[a][c]);
+    if (tap == 4 && threadIdx.x < COUT) atomicAdd(&dBias[threadIdx.x], bacc);
+}
+
+// Per-pixel 5x5 filter from softmax(logits[0..24]) applied to the noisy
+// radiance (clamped to the image edge).
+__device__ __forceinline__ void softmax25(const float *l, float *w)
+{
+    float m = l[0];
+#pragma unroll
+    for (int k = 1; k < 25; k++) m = fmaxf(m, l[k]);
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 25; k++) {
+        w[k] = __expf(l[k] - m);
+        s += w[k];
+    }
+    float inv = 1.0f / s;
+#pragma unroll
+    for (int k = 0; k < 25; k++) w[k] *= inv;
+}
+
+__device__ __forceinline__ uint64_t tap_pixel(uint64_t p, int x, int y, int W, int H, int k)
+{
+    int gx = min(max(x + k % 5 - 2, 0), W - 1), gy = min(max(y + k / 5 - 2, 0), H - 1);
+    return p - (uint64_t)x - (uint64_t)y * W + (uint64_t)gy * W + gx;
+}
+
+__global__ void k_filter(const float *__restrict__ logits, const float4 *__restrict__ noisy, int B,
+    int H, int W, float4 *__restrict__ out)
+{
+    uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p >= (uint64_t)B * H * W) return;
+    int x = (int)(p % W), y = (int)((p / W) % H);
+    float l[25], w[25];
+#pragma unroll
+    for (int k = 0; k < 25; k++) l[k] = logits[p * 32 + k];
+    softmax25(l, w);
+    float3 o = make_float3(0, 0, 0);
+#pragma unroll
+    for (int k = 0; k < 25; k++) {
+        float4 c = noisy[tap_pixel(p, x, y, W, H, k)];
+        o.x += w[k] * c.x;
+        o.y += w[k] * c.y;
+        o.z += w[k] * c.z;
+    }
+    out[p] = make_float4(o.x, o.y, o.z, 1.0f);
+}
+
+// relMSE = mean over pixels and channels of (out - ref)^2 / (ref^2 + 0.01);
+// writes dLogits (BF16, 32 channels, zeros beyond 25) and adds the loss sum.
+__global__ void k_relmse_bwd(const float *__restrict__ logits, const float4 *__restrict__ noisy,
+    const float4 *__restrict__ target, int B, int H, int W, float invCount,
+    __nv_bfloat16 *__restrict__ dLogits, float *lossSum)
+{
+    uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    float loss = 0.0f;
+    if (p < (uint64_t)B * H * W) {
+        int x = (int)(p % W), y = (int)((p / W) % H);
+        float l[25], w[25];
+#pragma unroll
+        for (int k = 0; k < 25; k++) l[k] = logits[p * 32 + k];
+        softmax25(l, w);
+        float3 o = make_float3(0, 0, 0);
+        uint64_t tp[25];
+#pragma unroll
+        for (int k = 0; k < 25; k++) {
+            tp[k] = tap_pixel(p, x, y, W, H, k);
+            float4 c = noisy[tp[k]];
+            o.x += w[k] * c.x;
+            o.y += w[k] * c.y;
+            o.z += w[k] * c.z;
+        }
+        float4 r = target[p];
+        float ex = o.x - r.x, ey = o.y - r.y, ez = o.z - r.z;
+        float nx = 1.0f / (r.x * r.x + 0.01f), ny = 1.0f / (r.y * r.y + 0.01f),
+              nz = 1.0f / (r.z * r.z + 0.01f);
+        loss = ex * ex * nx + ey * ey * ny + ez * ez * nz;
+        float gx = 2.0f * ex * nx * invCount, gy = 2.0f * ey * ny * invCount,
+              gz = 2.0f * ez * nz * invCount;
+        float gk[25], dot = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 25; k++) {
+            float4 c = noisy[tp[k]];
+            gk[k] = gx * c.x + gy * c.y + gz * c.z;
+            dot += w[k] * gk[k];
+        }
+        uint32_t *o32 = reinterpret_cast<uint32_t *>(dLogits + p * 32);
+#pragma unroll
+        for (int k = 0; k < 32; k += 2) {
+            float v0 = k < 25 ? w[k] * (gk[k] - dot) : 0.0f;
+            float v1 = k + 1 < 25 ? w[k + 1] * (gk[k + 1] - dot) : 0.0f;
+            o32[k / 2] = pack_bf16(v0, v1);
+        }
+    }
+    for (int off = 16; off; off >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(lossSum, loss);
+}
+
+__global__ void k_adam(float *param, __nv_bfloat16 *paramBf16, const float *grad, float *m,
+    float *v, uint64_t n, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float g = grad[i];
+    float mi = b1 * m[i] + (1.0f - b1) * g;
+    float vi = b2 * v[i] + (1.0f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    float p = param[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    param[i] = p;
+    if (paramBf16) paramBf16[i] = __float2bfloat16_rn(p);
+}
+
+inline unsigned blocks(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace dn
+}  // namespace gbsp
+
+using namespace gbsp;
+using namespace gbsp::dn;
+
+extern "C" {
+
+int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
+    uint16_t *out)
+{
+    if (!radiance || !aov || !out) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!pixels) return GBSP_OK;
+    k_features<<<blocks(pixels, 256), 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(radiance), reinterpret_cast<const float4 *>(aov), pixels,
+        reinterpret_cast<__nv_bfloat16 *>(out));
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_conv3x3_forward(void *stream, const uint16_t *in, uint32_t B, uint32_t H, uint32_t W,
+    uint32_t cin, const uint16_t *weights, const float *bias, uint32_t cout, int epilogue,
+    uint16_t *outBf16, float *outF32)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!in || !weights || !B || !H || !W) return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad conv args");
+    int sm = sm_count();
+    if (epilogue == kEpiBf16BiasRelu && !outBf16) return set_error(GBSP_ERR_INVALID_ARGUMENT, "outBf16");
+    if (epilogue != kEpiBf16BiasRelu && !outF32) return set_error(GBSP_ERR_INVALID_ARGUMENT, "outF32");
+    if (epilogue != kEpiF32 && !bias) return set_error(GBSP_ERR_INVALID_ARGUMENT, "bias");
+#define GBSP_CONV_CASE(CI, CO, EP)                                                               \
+    if (cin == CI && cout == CO && epilogue == EP)                                               \
+        return launch_conv<CI, CO, EP>(s, sm, in, B, H, W, weights, bias, outBf16, outF32);
+    GBSP_CONV_CASE(16, 48, kEpiBf16BiasRelu)
+    GBSP_CONV_CASE(48, 48, kEpiBf16BiasRelu)
+    GBSP_CONV_CASE(48, 32, kEpiF32Bias)
+    GBSP_CONV_CASE(48, 48, kEpiF32)
+    GBSP_CONV_CASE(32, 48, kEpiF32)
+#undef GBSP_CONV_CASE
+    return set_error(GBSP_ERR_INVALID_ARGUMENT, "conv3x3 %u->%u epilogue %d not instantiated", cin,
+        cout, epilogue);
+}
+
+int gbsp_dn_flip_transpose(void *stream, const uint16_t *w, uint32_t cout, uint32_t cin,
+    uint16_t *wt)
+{
+    uint32_t n = 9 * cout * cin;
+    k_flip_transpose<<<blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const __nv_bfloat16 *>(w), (int)cout, (int)cin,
+        reinterpret_cast<__nv_bfloat16 *>(wt));
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_relu_backward(void *stream, const float *dAct, const uint16_t *act, uint64_t n,
+    uint16_t *out)
+{
+    if (!n) return GBSP_OK;
+    k_relu_bwd<<<blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(dAct,
+        reinterpret_cast<const __nv_bfloat16 *>(act), n, reinterpret_cast<__nv_bfloat16 *>(out));
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_conv3x3_weight_grad(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    uint64_t n = (uint64_t)B * H * W;
+    int chunk = 2048;
+    dim3 grid(blocks(n, chunk), 9);
+    const __nv_bfloat16 *i16 = reinterpret_cast<const __nv_bfloat16 *>(in);
+    const __nv_bfloat16 *d16 = reinterpret_cast<const __nv_bfloat16 *>(dOut);
+    if (cin == 16 && cout == 48)
+        k_conv3x3_wgrad<16, 48><<<grid, 128, 0, s>>>(i16, d16, B, H, W, chunk, dW, dBias);
+    else if (cin == 48 && cout == 48)
+        k_conv3x3_wgrad<48, 48><<<grid, 128, 0, s>>>(i16, d16, B, H, W, chunk, dW, dBias);
+    else if (cin == 48 && cout == 32)
+        k_conv3x3_wgrad<48, 32><<<grid, 128, 0, s>>>(i16, d16, B, H, W, chunk, dW, dBias);
+    else
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32_t B, uint32_t H,
+    uint32_t W, float *out)
+{
+    uint64_t n = (uint64_t)B * H * W;
+    k_filter<<<blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(logits,
+        reinterpret_cast<const float4 *>(noisy), B, H, W, reinterpret_cast<float4 *>(out));
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_relmse_backward(void *stream, const float *logits, const float *noisy,
+    const float *target, uint32_t B, uint32_t H, uint32_t W, uint16_t *dLogits, float *lossSum)
+{
+    uint64_t n = (uint64_t)B * H * W;
+    k_relmse_bwd<<<blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(logits,
+        reinterpret_cast<const float4 *>(noisy), reinterpret_cast<const float4 *>(target), B, H, W,
+        1.0f / (3.0f * (float)n), reinterpret_cast<__nv_bfloat16 *>(dLogits), lossSum);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_adam(void *stream, float *param, uint16_t *paramBf16, const float *grad, float *m,
+    float *v, uint64_t n, float lr, float beta1, float beta2, float eps, uint32_t step)
+{
+    float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+    k_adam<<<blocks(n, 256), 256, 0, (cudaStream_t)stream>>>(param,
+        reinterpret_cast<__nv_bfloat16 *>(paramBf16), grad, m, v, n, lr, beta1, beta2, eps, c1, c2);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+}  // extern "C"

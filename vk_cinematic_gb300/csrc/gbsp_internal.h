@@ -95,6 +95,8 @@ struct gbsp_runtime {
     gbsp::DeviceBuffer<float4> pathRad;            // radiance per path
     gbsp::DeviceBuffer<unsigned int> queueCounts;  // small control block
     gbsp::DeviceBuffer<float4> frame;              // last frame, RGBA32F
+    gbsp::DeviceBuffer<float4> aov;                // 2 per pixel when GBSP_FLAG_AOV
+    gbsp::DeviceBuffer<float4> pathAov;            // 2 per path of a wave
     uint32_t frameW = 0, frameH = 0;
     // launch accounting and optional per-stage timing of the current call
     uint64_t launches = 0, traceLaunches = 0;
@@ -216,7 +218,8 @@ int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const 
 // pathtrace.cu
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
-    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState);
+    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState,
+    float4 *dAov = nullptr);
 
 // api.cu
 int material_view(gbsp_material_system *ms, MaterialView *out);

@@ -50,6 +50,7 @@ struct WaveBuffers {
     float4 *vertE;     // maxBounces * cap: (emission xyz, cosine)
     float4 *vertA;     // maxBounces * cap: (A xyz, 0)
     float4 *pathRad;   // cap
+    float4 *pathAov;   // 2 * cap first-hit G-buffer per path, or null
     uint32_t cap;
 };
 
@@ -64,6 +65,7 @@ struct WaveParams {
     float clampValue;
     uint32_t nanPolicy;
     float invSpp;
+    float4 *aovImage;     // 2 float4 per image pixel, or null
 };
 
 // ---------------------------------------------------------------------------
@@ -237,10 +239,19 @@ __global__ void __launch_bounds__(128) k_shade(SceneView sv, MaterialView mv, Wa
                 newO = make_float4(no.x, no.y, no.z, __int_as_float((int)p));
                 newD = make_float4(dir.x, dir.y, dir.z, 0.0f);
                 cont = !lastBounce;
+                if (wb.pathAov && bounce == 0) {
+                    V3 al = material_albedo(mv, slot, ux, uy);
+                    wb.pathAov[2 * (size_t)p] = make_float4(al.x, al.y, al.z, h.t);
+                    wb.pathAov[2 * (size_t)p + 1] = make_float4(n.x, n.y, n.z, 1.0f);
+                }
             } else {
                 // miss: background vertex, path ends (:302-314)
                 vertex_terms(mv, mv.backgroundSlot, v3(0, 0, 0), v3(0, 0, 0), neg(d), 0.0f, 0.0f,
                     ec, aa);
+                if (wb.pathAov && bounce == 0) {
+                    wb.pathAov[2 * (size_t)p] = make_float4(0, 0, 0, 0);
+                    wb.pathAov[2 * (size_t)p + 1] = make_float4(0, 0, 0, 0);
+                }
             }
             wb.vertE[(size_t)len * wb.cap + p] = ec;
             wb.vertA[(size_t)len * wb.cap + p] = aa;
@@ -290,6 +301,19 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBuffers w
         }
         image[(size_t)y * imageWidth + x] =
             make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
+        if (wp.aovImage) {
+            float4 a = make_float4(0, 0, 0, 0), b = make_float4(0, 0, 0, 0);
+            for (uint32_t s = 0; s < wp.spp; s++) {
+                float4 u = wb.pathAov[2 * ((size_t)k * wp.spp + s)];
+                float4 v = wb.pathAov[2 * ((size_t)k * wp.spp + s) + 1];
+                a = make_float4(a.x + u.x, a.y + u.y, a.z + u.z, a.w + u.w);
+                b = make_float4(b.x + v.x, b.y + v.y, b.z + v.z, b.w + v.w);
+            }
+            float is = wp.invSpp;
+            size_t o = 2 * ((size_t)y * imageWidth + x);
+            wp.aovImage[o] = make_float4(a.x * is, a.y * is, a.z * is, a.w * is);
+            wp.aovImage[o + 1] = make_float4(b.x * is, b.y * is, b.z * is, b.w * is);
+        }
     }
     for (int off = 16; off; off >>= 1) nans += __shfl_xor_sync(0xFFFFFFFFu, nans, off);
     if ((threadIdx.x & 31) == 0 && nans)
@@ -385,7 +409,7 @@ static int ensure_wave_buffers(gbsp_runtime *rt, uint32_t cap, uint32_t maxBounc
 
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
-    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState)
+    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState, float4 *dAov)
 {
     cudaStream_t s = rt->stream;
     unsigned long long *counters = rt->dCounters;
@@ -449,6 +473,11 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     wb.vertE = rt->vertE.ptr;
     wb.vertA = rt->vertA.ptr;
     wb.pathRad = rt->pathRad.ptr;
+    wb.pathAov = nullptr;
+    if (dAov) {
+        if ((rc = rt->pathAov.reserve(2 * (size_t)cap, s))) return rc;
+        wb.pathAov = rt->pathAov.ptr;
+    }
     wb.cap = cap;
     WaveParams wp;
     wp.cam = cam;
@@ -461,6 +490,7 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     wp.clampValue = opt.radiance_clamp;
     wp.nanPolicy = opt.nan_policy;
     wp.invSpp = 1.0f / (float)spp;
+    wp.aovImage = dAov;
     int persistentGrid = rt->smCount * 8;
     bool timing = rt->stageTiming;
     for (uint64_t pb = 0; pb < regionPixels; pb += pixelsPerWave) {
@@ -645,6 +675,7 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     wb.vertE = reinterpret_cast<float4 *>(base + kNaVertE);
     wb.vertA = reinterpret_cast<float4 *>(base + kNaVertA);
     wb.pathRad = reinterpret_cast<float4 *>(base + kNaRad);
+    wb.pathAov = nullptr;
     uint32_t pixelsPerWave = kNoAllocMaxPaths / spp;
     wb.cap = pixelsPerWave * spp;
 
@@ -659,6 +690,7 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     wp.clampValue = opt.radiance_clamp;
     wp.nanPolicy = opt.nan_policy;
     wp.invSpp = 1.0f / (float)spp;
+    wp.aovImage = nullptr;
     SceneView sv = sc->view();
     float4 *image = reinterpret_cast<float4 *>(deviceImage);
     uint64_t regionPixels = (uint64_t)(x1 - x0) * (y1 - y0);

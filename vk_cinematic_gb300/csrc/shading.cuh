@@ -39,6 +39,15 @@ __device__ __forceinline__ V3 sky_radiance(const SkyParams &s, V3 dir)
     return c;
 }
 
+// Albedo of the material in `slot` at uv (sp_EvaluateMaterial's albedo).
+__device__ __forceinline__ V3 material_albedo(const MaterialView &mv, int slot, float uvx, float uvy)
+{
+    if (slot < 0) return v3(0.0f, 0.0f, 0.0f);
+    const DeviceMaterial &m = mv.materials[slot];
+    return m.albedoTex >= 0 ? texel_nearest(mv, m.albedoTex, uvx, uvy)
+                            : v3(m.albedo[0], m.albedo[1], m.albedo[2]);
+}
+
 // Per-vertex terms of ComputeRadianceForPath for the material in `slot`.
 __device__ __forceinline__ void vertex_terms(const MaterialView &mv, int slot, V3 N, V3 L, V3 V,
     float uvx, float uvy, float4 &ec, float4 &aa)

@@ -1,0 +1,256 @@
+"""Kernel-predicting CNN denoiser on libgbsp's denoiser kernels.
+
+Network (the config-5 description): 8 conv3x3 layers, 10 -> 48, six 48 -> 48,
+48 -> 25, ReLU between layers; the 25 outputs of a pixel are softmax weights
+of a 5x5 filter applied to the noisy radiance around it.  Inputs: log(1 +
+radiance), albedo, normal and depth/(1 + depth) of a low-spp frame, BF16.
+Training minimises relMSE = mean((out - ref)^2 / (ref^2 + 0.01)) with Adam.
+
+Every arithmetic step runs in libgbsp kernels (include/gbsp.h,
+"learned denoiser"); torch only provides device memory and the stream.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+
+import numpy as np
+
+from . import gbsp, scenes
+
+N_FEATURES = 10
+FEATURE_CHANNELS = 16
+# (cin, cout, epilogue): epilogue 0 = BF16 ReLU, 1 = FP32 logits
+LAYERS = [(16, 48, 0)] + [(48, 48, 0)] * 6 + [(48, 32, 1)]
+
+_c = ctypes
+_u32, _u64, _f32, _int, _vp = _c.c_uint32, _c.c_uint64, _c.c_float, _c.c_int, _c.c_void_p
+
+
+def _stream():
+    import torch
+
+    return _vp(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t) -> _vp:
+    return _vp(t.data_ptr())
+
+
+def _check(rc):
+    gbsp._check(rc)
+
+
+def relmse(x, ref):
+    """mean over pixels and RGB of (x - ref)^2 / (ref^2 + 0.01)."""
+    import torch
+
+    x = x[..., :3].double()
+    r = ref[..., :3].double()
+    return float(torch.mean((x - r) ** 2 / (r * r + 0.01)).item())
+
+
+class KPCNN:
+    def __init__(self, seed: int = 0):
+        import torch
+
+        self.L = gbsp.load()
+        g = torch.Generator().manual_seed(seed)
+        self.w, self.b, self.wb, self.state = [], [], [], []
+        for li, (cin, cout, epi) in enumerate(LAYERS):
+            fan_in = 9 * (N_FEATURES if cin == FEATURE_CHANNELS else cin)
+            std = math.sqrt(2.0 / fan_in) * (0.1 if epi == 1 else 1.0)
+            w = torch.randn((9, cout, cin), generator=g) * std
+            if cin == FEATURE_CHANNELS:
+                w[:, :, N_FEATURES:] = 0
+            if epi == 1:
+                w[:, 25:, :] = 0
+            w = w.cuda().contiguous()
+            b = torch.zeros(cout, device="cuda")
+            self.w.append(w)
+            self.b.append(b)
+            self.wb.append(w.to(torch.bfloat16).contiguous())
+            self.state.append([torch.zeros_like(w), torch.zeros_like(w), torch.zeros_like(b),
+                               torch.zeros_like(b)])
+        self.step = 0
+
+    def parameters_count(self) -> int:
+        return sum(w.numel() + b.numel() for w, b in zip(self.w, self.b))
+
+    # ---- forward -----------------------------------------------------------------
+    def features(self, radiance, aov):
+        import torch
+
+        B, H, W, _ = radiance.shape
+        f = torch.empty((B, H, W, FEATURE_CHANNELS), dtype=torch.bfloat16, device="cuda")
+        _check(self.L.gbsp_dn_features(_stream(), _ptr(radiance), _ptr(aov), _u64(B * H * W),
+                                       _ptr(f)))
+        return f
+
+    def conv(self, li, x, keep_f32=False):
+        import torch
+
+        B, H, W, cin = x.shape
+        _, cout, _ = self.wb[li].shape
+        epi = LAYERS[li][2]
+        if epi == 0:
+            out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device="cuda")
+            _check(self.L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W),
+                                                  _u32(cin), _ptr(self.wb[li]), _ptr(self.b[li]),
+                                                  _u32(cout), _int(0), _ptr(out), None))
+        else:
+            out = torch.empty((B, H, W, cout), dtype=torch.float32, device="cuda")
+            _check(self.L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W),
+                                                  _u32(cin), _ptr(self.wb[li]), _ptr(self.b[li]),
+                                                  _u32(cout), _int(1), None, _ptr(out)))
+        return out
+
+    def forward(self, feats, keep=False):
+        acts = []
+        x = feats
+        for li in range(len(LAYERS)):
+            x = self.conv(li, x)
+            if keep and li < len(LAYERS) - 1:
+                acts.append(x)
+        return x, acts
+
+    def filter(self, logits, noisy):
+        import torch
+
+        B, H, W, _ = noisy.shape
+        out = torch.empty_like(noisy)
+        _check(self.L.gbsp_dn_filter(_stream(), _ptr(logits), _ptr(noisy), _u32(B), _u32(H),
+                                     _u32(W), _ptr(out)))
+        return out
+
+    def denoise(self, radiance, aov):
+        logits, _ = self.forward(self.features(radiance, aov))
+        return self.filter(logits, radiance)
+
+    # ---- training ------------------------------------------------------------------
+    def data_grad(self, li, d):
+        """dIn of layer li from its output gradient d (BF16), FP32."""
+        import torch
+
+        B, H, W, cout = d.shape
+        _, _, cin = self.wb[li].shape
+        wt = torch.empty((9, cin, cout), dtype=torch.bfloat16, device="cuda")
+        _check(self.L.gbsp_dn_flip_transpose(_stream(), _ptr(self.wb[li]), _u32(cout), _u32(cin),
+                                             _ptr(wt)))
+        out = torch.empty((B, H, W, cin), dtype=torch.float32, device="cuda")
+        _check(self.L.gbsp_dn_conv3x3_forward(_stream(), _ptr(d), _u32(B), _u32(H), _u32(W),
+                                              _u32(cout), _ptr(wt), None, _u32(cin), _int(2), None,
+                                              _ptr(out)))
+        return out
+
+    def weight_grad(self, li, x, d, dw, db):
+        B, H, W, cin = x.shape
+        cout = d.shape[-1]
+        _check(self.L.gbsp_dn_conv3x3_weight_grad(_stream(), _ptr(x), _ptr(d), _u32(B), _u32(H),
+                                                  _u32(W), _u32(cin), _u32(cout), _ptr(dw),
+                                                  _ptr(db)))
+
+    def gradients(self, feats, noisy, target):
+        """Loss and parameter gradients for one batch."""
+        import torch
+
+        B, H, W, _ = noisy.shape
+        logits, acts = self.forward(feats, keep=True)
+        dlog = torch.empty((B, H, W, 32), dtype=torch.bfloat16, device="cuda")
+        loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+        _check(self.L.gbsp_dn_relmse_backward(_stream(), _ptr(logits), _ptr(noisy), _ptr(target),
+                                              _u32(B), _u32(H), _u32(W), _ptr(dlog), _ptr(loss)))
+        dws = [torch.zeros_like(w) for w in self.w]
+        dbs = [torch.zeros_like(b) for b in self.b]
+        last = len(LAYERS) - 1
+        inputs = [feats] + acts
+        self.weight_grad(last, inputs[last], dlog, dws[last], dbs[last])
+        dact = self.data_grad(last, dlog)
+        for li in range(last - 1, -1, -1):
+            dm = torch.empty(acts[li].shape, dtype=torch.bfloat16, device="cuda")
+            _check(self.L.gbsp_dn_relu_backward(_stream(), _ptr(dact), _ptr(acts[li]),
+                                                _u64(dact.numel()), _ptr(dm)))
+            self.weight_grad(li, inputs[li], dm, dws[li], dbs[li])
+            if li > 0:
+                dact = self.data_grad(li, dm)
+        return loss, dws, dbs
+
+    def train_step(self, feats, noisy, target, lr=1e-4):
+        loss, dws, dbs = self.gradients(feats, noisy, target)
+        self.step += 1
+        for li in range(len(LAYERS)):
+            m, v, mb, vb = self.state[li]
+            _check(self.L.gbsp_dn_adam(_stream(), _ptr(self.w[li]), _ptr(self.wb[li]),
+                                       _ptr(dws[li]), _ptr(m), _ptr(v), _u64(self.w[li].numel()),
+                                       _f32(lr), _f32(0.9), _f32(0.999), _f32(1e-8),
+                                       _u32(self.step)))
+            _check(self.L.gbsp_dn_adam(_stream(), _ptr(self.b[li]), None, _ptr(dbs[li]),
+                                       _ptr(mb), _ptr(vb), _u64(self.b[li].numel()), _f32(lr),
+                                       _f32(0.9), _f32(0.999), _f32(1e-8), _u32(self.step)))
+        B, H, W, _ = noisy.shape
+        return loss / (3.0 * B * H * W)
+
+
+# ---- data from the path tracer --------------------------------------------------------
+def denoise_scene(seed, width=1920, height=1080, n_spheres=256, level=5):
+    """A config-3-style scene (the config-5 scene family)."""
+    return scenes.config3_scene(width=width, height=height, spp=4, max_bounces=5,
+                                n_spheres=n_spheres, level=level, seed=seed)
+
+
+class SceneRenderer:
+    """One uploaded scene that renders windows at any spp and seed."""
+
+    def __init__(self, rt, s):
+        self.s = s
+        self.scene, self.ms, self.rend = gbsp.upload_scene(rt, s)
+
+    def render(self, x0, y0, w, h, spp, seed, aov=False):
+        import torch
+
+        o = self.rend.options
+        o.spp, o.seed = spp, seed
+        o.flags = gbsp.FLAG_AOV if aov else 0
+        self.rend.tile_device((x0, y0, x0 + w, y0 + h))
+        rad = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+        av = torch.empty((h, w, 8), dtype=torch.float32, device="cuda") if aov else None
+        self.rend.copy_region(x0, y0, w, h, rad.data_ptr(), av.data_ptr() if aov else 0)
+        return rad, av
+
+    def reference(self, x0, y0, w, h, spp_total, per_pass=1024, seed=1 << 20):
+        """FP64-accumulated high-spp image: the mean of FP32 passes, summed in FP64."""
+        import torch
+
+        passes = max(1, spp_total // per_pass)
+        acc = torch.zeros((h, w, 4), dtype=torch.float64, device="cuda")
+        for k in range(passes):
+            rad, _ = self.render(x0, y0, w, h, min(per_pass, spp_total), seed + k)
+            acc += rad.double()
+        return (acc / passes)
+
+
+def make_dataset(rt, n_scenes, crops_per_scene, crop=128, spp_in=4, spp_ref=4096, seed0=0,
+                 n_spheres=256, level=5, log=print):
+    """Training pairs: random crops of config-3-style frames, low-spp inputs
+    (+ G-buffers) and independent high-spp targets."""
+    import torch
+
+    rng = np.random.default_rng(seed0)
+    feats_l, noisy_l, tgt_l = [], [], []
+    t0 = time.time()
+    for k in range(n_scenes):
+        s = denoise_scene(seed0 + k, n_spheres=n_spheres, level=level)
+        sr = SceneRenderer(rt, s)
+        for c in range(crops_per_scene):
+            x0 = int(rng.integers(0, s.width - crop))
+            y0 = int(rng.integers(0, s.height - crop))
+            noisy, aov = sr.render(x0, y0, crop, crop, spp_in, seed=1000 * k + 2 * c, aov=True)
+            target, _ = sr.render(x0, y0, crop, crop, spp_ref, seed=1000 * k + 2 * c + 1)
+            noisy_l.append(noisy)
+            tgt_l.append(target)
+            feats_l.append(aov)
+    torch.cuda.synchronize()
+    log(f"dataset: {len(noisy_l)} crops in {time.time() - t0:.1f} s")
+    return torch.stack(noisy_l), torch.stack(feats_l), torch.stack(tgt_l)

@@ -47,7 +47,10 @@ EXPORTS = [
     "gbsp_path_trace_frame", "gbsp_frame_device_pointer", "gbsp_icosphere", "gbsp_plane_mesh",
     "gbsp_sample_seed", "gbsp_path_trace_tile_noalloc", "gbsp_batch_create",
     "gbsp_batch_destroy", "gbsp_batch_set_config", "gbsp_batch_get_config",
-    "gbsp_batch_autotune", "gbsp_batch_launch",
+    "gbsp_batch_autotune", "gbsp_batch_launch", "gbsp_frame_aov_device_pointer",
+    "gbsp_frame_copy_region", "gbsp_dn_features", "gbsp_dn_conv3x3_forward",
+    "gbsp_dn_flip_transpose", "gbsp_dn_relu_backward", "gbsp_dn_conv3x3_weight_grad",
+    "gbsp_dn_filter", "gbsp_dn_relmse_backward", "gbsp_dn_adam", "gbsp_tonemap",
 ]
 
 
@@ -58,6 +61,7 @@ class Options(ctypes.Structure):
 
 
 FLAG_STAGE_TIMING = 1
+FLAG_AOV = 2
 
 
 class ImagePlane(ctypes.Structure):
@@ -120,6 +124,7 @@ def load(build_if_missing: bool = True):
     lib.gbsp_last_error_string.restype = ctypes.c_char_p
     lib.gbsp_runtime_stream.restype = _vp
     lib.gbsp_frame_device_pointer.restype = _vp
+    lib.gbsp_frame_aov_device_pointer.restype = _vp
     lib.gbsp_sample_seed.restype = _u32
     lib.gbsp_calculate_film_positions.restype = _u32
     for name in EXPORTS:
@@ -326,6 +331,16 @@ class Renderer:
                                             ctypes.byref(m) if m is not None else None))
         return m
 
+    def tile_device(self, tile, rng_state: int = 0):
+        """Tile render kept in device memory (frame buffer of the runtime)."""
+        self.set_host_pixels(None)
+        rng = _u32(rng_state)
+        m = Metrics()
+        t = Tile(*[int(v) for v in tile])
+        _check(self.L.gbsp_path_trace_tile(ctypes.byref(self.ctx), t, ctypes.byref(rng),
+                                           ctypes.byref(m)))
+        return m
+
     def tile(self, tile, rng_state: int = 0, pixels: np.ndarray | None = None):
         out = pixels if pixels is not None else np.zeros((self.height, self.width, 4), np.float32)
         self.set_host_pixels(out)
@@ -339,6 +354,14 @@ class Renderer:
 
     def frame_device_pointer(self) -> int:
         return self.L.gbsp_frame_device_pointer(self.rt.h)
+
+    def aov_device_pointer(self) -> int:
+        return self.L.gbsp_frame_aov_device_pointer(self.rt.h)
+
+    def copy_region(self, x0, y0, w, h, dst_radiance_ptr: int, dst_aov_ptr: int = 0):
+        _check(self.L.gbsp_frame_copy_region(self.rt.h, _u32(x0), _u32(y0), _u32(w), _u32(h),
+                                             _vp(dst_radiance_ptr),
+                                             _vp(dst_aov_ptr) if dst_aov_ptr else None))
 
 
 def film_positions(camera: Camera, pixels: np.ndarray) -> np.ndarray:
@@ -395,12 +418,18 @@ class BatchItem(ctypes.Structure):
                 ("options", Options), ("deviceImage", _vp)]
 
 
+BATCH_THREAD_PER_PIXEL = 0
+BATCH_PATH_STATE = 1
+BATCH_KERNEL_NAMES = {BATCH_THREAD_PER_PIXEL: "thread_per_pixel", BATCH_PATH_STATE: "path_state"}
+
+
 class BatchConfig(ctypes.Structure):
-    _fields_ = [("block", _u32), ("chunk", _u32), ("blocksPerSm", _u32), ("useGraph", _u32)]
+    _fields_ = [("block", _u32), ("chunk", _u32), ("blocksPerSm", _u32), ("useGraph", _u32),
+                ("kernel", _u32)]
 
     def as_dict(self):
-        return dict(block=self.block, chunk=self.chunk, blocks_per_sm=self.blocksPerSm,
-                    use_graph=self.useGraph)
+        return dict(kernel=BATCH_KERNEL_NAMES[self.kernel], block=self.block, chunk=self.chunk,
+                    blocks_per_sm=self.blocksPerSm, use_graph=self.useGraph)
 
 
 class Batch:
@@ -427,8 +456,9 @@ class Batch:
         _check(self.L.gbsp_batch_get_config(self.h, ctypes.byref(c)))
         return c
 
-    def set_config(self, block=128, chunk=1, blocks_per_sm=8, use_graph=1):
-        c = BatchConfig(block, chunk, blocks_per_sm, use_graph)
+    def set_config(self, block=128, chunk=1, blocks_per_sm=8, use_graph=1,
+                   kernel=BATCH_PATH_STATE):
+        c = BatchConfig(block, chunk, blocks_per_sm, use_graph, kernel)
         _check(self.L.gbsp_batch_set_config(self.h, ctypes.byref(c)))
 
     def autotune(self, trials=2) -> BatchConfig:
