@@ -55,7 +55,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gbsp", "reference"], default="gbsp")
-    ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4", "config5"],
+    ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4", "config5",
+                                           "compute_pt"],
                     default="config3")
     ap.add_argument("--dn-scenes", type=int, default=125)
     ap.add_argument("--dn-crops", type=int, default=16)
@@ -684,6 +685,67 @@ def run_config5(args):
     return 0
 
 
+def run_compute_pt(args):
+    """The reference's compute-shader path tracer (test_compute.comp.glsl)
+    on its own image: every 16x16 tile of the frame per step, one warp per
+    tile.  Prints its own JSON line with the oracle timed on a tile sample."""
+    import torch
+    from vk_cinematic_gb300 import gbsp, scenes
+
+    w = args.width or 1024
+    h = args.height or 768
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rt = gbsp.Runtime(0, stream=stream.cuda_stream)
+    s = scenes.compute_pt_scene(n_spheres=16, level=3)
+    sc = gbsp.ComputePTScene(rt, s["vertices"], s["indices"], s["meshes"], s["model"],
+                             s["inv_model"], s["entities"], s["texture"])
+    view = gbsp.cpt_view(w, h, 16, 0.8, s["camera_transform"])
+    tiles = np.arange((w // 16) * (h // 16), dtype=np.uint32)
+    img = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    tris = sum(int(s["meshes"][m][0]) // 3 for m in s["entities"][:, 0])
+    for _ in range(args.warmup):
+        sc.render_tiles(view, tiles, img.data_ptr(), metrics=False)
+    m = sc.render_tiles(view, tiles, img.data_ptr(), metrics=True).as_dict()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sc.render_tiles(view, tiles, img.data_ptr(), metrics=False)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    rays = m["rays_traced"]
+    line = {
+        "metric": "Mrays/s, compute-shader path tracer (brute force)",
+        "value": rays / ms / 1e3, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded procedural scene",
+        "config": {"workload": f"compute_pt: {w}x{h}, 16x16 tiles, 1 spp, 3 bounces, "
+                               f"{len(s['entities'])} entities, {tris} triangles per ray",
+                   "l2": "scene (<2 MB) stays L2-resident by design"},
+        "triangle_tests_per_s": m["triangle_tests"] / ms * 1e3,
+        "rays_per_step": rays, "gpu_launches": args.steps, "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle
+
+        pyoracle.build_port()
+        sample = tiles[:: max(1, len(tiles) // 24)][:24]
+        t0 = time.perf_counter()
+        _, c = pyoracle.compute_pt_tiles(s, w, h, 16, 0.8, sample)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": float(c[0]) / dt / 1e6, "unit": "Mrays/s", "cores": 1,
+                                "kind": "port", "sample": f"{len(sample)} of {len(tiles)} tiles"}
+    print(json.dumps(line), flush=True)
+    sc.close()
+    return 0
+
+
 def main():
     args = parse_args()
     _OVERRIDES.update(width=args.width, height=args.height, spp=args.spp)
@@ -695,6 +757,8 @@ def main():
         return run_config2(args)
     if args.workload == "config5":
         return run_config5(args)
+    if args.workload == "compute_pt":
+        return run_compute_pt(args)
     return run_gpu(args)
 
 

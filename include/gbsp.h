@@ -321,6 +321,52 @@ int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *b
 /* Renders every item.  metrics NULL: asynchronous on the runtime's stream. */
 int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics);
 
+/* ---- compute-shader path tracer ------------------------------------------------- */
+/* The reference's GPU compute path tracer, src/shaders/test_compute.comp.glsl,
+ * as CUDA: replaces its Vulkan dispatch (src/vulkan_renderer.cpp:1340-1368:
+ * up to 64 tile indices in push constants, one invocation per tile) and the
+ * descriptor bindings of its scene buffers (test_compute.comp.glsl:60-100).
+ * Brute-force closest hit over every entity's triangles, RNG chained through
+ * each tile, three bounces, hard-coded material ids (0 red, 2 checkerboard,
+ * 5 white light, others black). */
+typedef struct gbsp_cpt_scene gbsp_cpt_scene;
+
+typedef struct {                 /* Mesh, test_compute.comp.glsl:46-51 */
+    uint32_t indexCount;
+    uint32_t indicesOffset;      /* in indices */
+    uint32_t vertexDataOffset;   /* in vertices */
+} gbsp_cpt_mesh;
+
+typedef struct {                 /* Entity, test_compute.comp.glsl:53-58 */
+    uint32_t meshIndex;
+    uint32_t materialId;
+    uint32_t modelMatrixIndex;
+} gbsp_cpt_entity;
+
+typedef struct {
+    uint32_t width, height;          /* IMAGE_WIDTH / IMAGE_HEIGHT (256 x 192 in the shader) */
+    uint32_t tileWidth, tileHeight;  /* TILE_WIDTH / TILE_HEIGHT (16) */
+    float filmDistance;              /* 0.8 in the shader */
+    float cameraTransform[16];       /* column-major: right, up, forward, position
+                                        (ComputeShaderUniformBuffer, src/main.cpp:686-693) */
+} gbsp_cpt_view;
+
+/* Copies the scene buffers to the device.  Matrices are column-major 4x4,
+ * 16 floats each; checkerBoard is an RGBA32F texture sampled with the
+ * reference's linear/REPEAT sampler (NULL with size 0: albedo 0). */
+int gbsp_cpt_scene_create(gbsp_runtime *rt, const gbsp_vertex *vertices, uint32_t vertexCount,
+    const uint32_t *indices, uint32_t indexCount, const gbsp_cpt_mesh *meshes, uint32_t meshCount,
+    const float *modelMatrices, const float *invModelMatrices, uint32_t matrixCount,
+    const gbsp_cpt_entity *entities, uint32_t entityCount, const float *checkerBoard,
+    uint32_t texWidth, uint32_t texHeight, gbsp_cpt_scene **out);
+int gbsp_cpt_scene_destroy(gbsp_cpt_scene *scene);
+/* Renders the tiles tileIndices[0..tileCount) (host array; tile i covers
+ * (i % (width / tileWidth), i / (width / tileWidth)), clipped to the image)
+ * into deviceImage (width * height RGBA32F, device memory).  Pixels outside
+ * the listed tiles are left as they are.  metrics NULL: asynchronous. */
+int gbsp_cpt_render_tiles(gbsp_cpt_scene *scene, const gbsp_cpt_view *view,
+    const uint32_t *tileIndices, uint32_t tileCount, float *deviceImage, gbsp_metrics *metrics);
+
 /* ---- display ------------------------------------------------------------------------ */
 /* Tone maps an RGBA32F frame (device memory) into packed 8-bit RGBA (device
  * memory): replaces PerformToneMapping of src/shaders/post_processing.frag.glsl:19-26

@@ -417,3 +417,31 @@ class World:
         if dt < 0:
             raise RuntimeError("render_hashed_mt: a capacity of the reference overflowed")
         return dt, out, metrics
+
+
+def compute_pt_tiles(scene: dict, width: int, height: int, tile: int, film_distance: float,
+                     tiles, image=None):
+    """The compute-shader path tracer's restatement (oracle_compute_pt_tiles)
+    over the listed tiles.  `scene` holds the arrays of
+    vk_cinematic_gb300.scenes.compute_pt_scene.  Returns (image, counters)
+    with counters = [rays, hits, triangle tests]."""
+    L = _Lib.get("port").lib
+    if image is None:
+        image = np.zeros((height, width, 4), np.float32)
+    v = np.ascontiguousarray(scene["vertices"], np.float32)
+    i = np.ascontiguousarray(scene["indices"], np.uint32)
+    m = np.ascontiguousarray(scene["meshes"], np.uint32)
+    mm = np.ascontiguousarray(scene["model"], np.float32)
+    im = np.ascontiguousarray(scene["inv_model"], np.float32)
+    e = np.ascontiguousarray(scene["entities"], np.uint32)
+    tex = scene.get("texture")
+    tex = None if tex is None else np.ascontiguousarray(tex, np.float32)
+    ct = np.ascontiguousarray(scene["camera_transform"], np.float32)
+    tl = np.ascontiguousarray(tiles, np.uint32).reshape(-1)
+    counters = np.zeros(3, np.uint64)
+    L.oracle_compute_pt_tiles(
+        _p(v), _p(i), _p(m), _p(mm), _p(im), _p(e), _u32(len(e)),
+        _p(tex) if tex is not None else None, _u32(0 if tex is None else tex.shape[1]),
+        _u32(0 if tex is None else tex.shape[0]), _p(ct), _u32(width), _u32(height), _u32(tile),
+        _u32(tile), _f(film_distance), _p(tl), _u32(len(tl)), _p(image), _p(counters))
+    return image, counters

@@ -24,7 +24,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libgbsp.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["api.cu", "bvh_build.cu", "trace.cu", "pathtrace.cu", "batch.cu", "denoise.cu", "post.cu"]
+SOURCES = ["api.cu", "bvh_build.cu", "trace.cu", "pathtrace.cu", "batch.cu", "denoise.cu", "post.cu",
+           "compute_pt.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

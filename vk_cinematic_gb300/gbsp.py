@@ -51,6 +51,7 @@ EXPORTS = [
     "gbsp_frame_copy_region", "gbsp_dn_features", "gbsp_dn_conv3x3_forward",
     "gbsp_dn_flip_transpose", "gbsp_dn_relu_backward", "gbsp_dn_conv3x3_weight_grad",
     "gbsp_dn_filter", "gbsp_dn_relmse_backward", "gbsp_dn_adam", "gbsp_tonemap",
+    "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
 ]
 
 
@@ -481,3 +482,78 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+# ---- compute-shader path tracer (gbsp_cpt_*) ------------------------------------------
+
+class CptMesh(ctypes.Structure):
+    _fields_ = [("indexCount", _u32), ("indicesOffset", _u32), ("vertexDataOffset", _u32)]
+
+
+class CptEntity(ctypes.Structure):
+    _fields_ = [("meshIndex", _u32), ("materialId", _u32), ("modelMatrixIndex", _u32)]
+
+
+class CptView(ctypes.Structure):
+    _fields_ = [("width", _u32), ("height", _u32), ("tileWidth", _u32), ("tileHeight", _u32),
+                ("filmDistance", _f32), ("cameraTransform", _f32 * 16)]
+
+
+class ComputePTScene:
+    """Scene buffers of the compute-shader path tracer on the device.
+
+    vertices: (V, 8) float32 VertexPNT rows; indices: (I,) uint32; meshes:
+    (M, 3) uint32 (indexCount, indicesOffset, vertexDataOffset); model /
+    inv_model: (K, 16) float32 column-major; entities: (E, 3) uint32 (mesh,
+    material, matrix); texture: (H, W, 4) float32 or None."""
+
+    def __init__(self, rt: Runtime, vertices, indices, meshes, model, inv_model, entities,
+                 texture=None):
+        self.L, self.rt = rt.L, rt
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 8)
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1)
+        m = np.ascontiguousarray(meshes, dtype=np.uint32).reshape(-1, 3)
+        mm = np.ascontiguousarray(model, dtype=np.float32).reshape(-1, 16)
+        im = np.ascontiguousarray(inv_model, dtype=np.float32).reshape(-1, 16)
+        e = np.ascontiguousarray(entities, dtype=np.uint32).reshape(-1, 3)
+        if texture is not None:
+            t = np.ascontiguousarray(texture, dtype=np.float32)
+            th, tw = t.shape[:2]
+        else:
+            t, th, tw = None, 0, 0
+        h = _vp()
+        _check(self.L.gbsp_cpt_scene_create(
+            rt.h, _p(v), _u32(len(v)), _p(i), _u32(len(i)), _p(m), _u32(len(m)), _p(mm), _p(im),
+            _u32(len(mm)), _p(e), _u32(len(e)), _p(t) if t is not None else None, _u32(tw),
+            _u32(th), ctypes.byref(h)))
+        self.h = h
+
+    def render_tiles(self, view: CptView, tiles, device_image: int, metrics: bool = True):
+        tl = np.ascontiguousarray(tiles, dtype=np.uint32).reshape(-1)
+        m = Metrics() if metrics else None
+        _check(self.L.gbsp_cpt_render_tiles(self.h, ctypes.byref(view), _p(tl), _u32(len(tl)),
+                                            _vp(device_image),
+                                            ctypes.byref(m) if m is not None else None))
+        return m
+
+    def close(self):
+        if self.h:
+            self.L.gbsp_cpt_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cpt_view(width=256, height=192, tile=16, film_distance=0.8, camera_transform=None) -> CptView:
+    v = CptView()
+    v.width, v.height, v.tileWidth, v.tileHeight = width, height, tile, tile
+    v.filmDistance = film_distance
+    ct = np.eye(4, dtype=np.float32).reshape(-1) if camera_transform is None else \
+        np.asarray(camera_transform, dtype=np.float32).reshape(-1)
+    for k in range(16):
+        v.cameraTransform[k] = float(ct[k])
+    return v

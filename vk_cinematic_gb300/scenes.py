@@ -304,3 +304,86 @@ def config4_scenes(count=32, seed=4, max_triangles=2_000_000) -> list:
         s.name = f"config4[{k}]"
         out.append(s)
     return out
+
+
+# ---- compute-shader path tracer inputs ---------------------------------------------------
+
+CPT_MATERIAL_RED, CPT_MATERIAL_BLUE, CPT_MATERIAL_CHECKERBOARD = 0, 1, 2
+CPT_MATERIAL_WHITE_LIGHT = 5
+
+
+def checkerboard_image(size: int = 256, grid: int = 16) -> np.ndarray:
+    """CreateCheckerBoardImage (src/image.cpp:134-160): 0.18 grey with 0.04
+    squares of 16 texels, RGBA32F."""
+    y, x = np.mgrid[0:size, 0:size]
+    odd = ((x // grid) + (y // grid)) % 2 == 1
+    img = np.empty((size, size, 4), np.float32)
+    img[...] = np.array([0.18, 0.18, 0.18, 1.0], np.float32)
+    img[odd] = np.array([0.04, 0.04, 0.04, 1.0], np.float32)
+    return img
+
+
+def _trs(position, rotation_x: float, scale) -> tuple[np.ndarray, np.ndarray]:
+    """Column-major model matrix T * Rx * S and its inverse, each computed in
+    double and rounded once (16 floats each)."""
+    c, s = math.cos(rotation_x), math.sin(rotation_x)
+    t = np.eye(4)
+    t[:3, 3] = position
+    r = np.eye(4)
+    r[1, 1], r[1, 2], r[2, 1], r[2, 2] = c, -s, s, c
+    sc = np.diag([scale[0], scale[1], scale[2], 1.0])
+    m = t @ r @ sc
+    inv = np.linalg.inv(m)
+    return (m.T.reshape(-1).astype(np.float32), inv.T.reshape(-1).astype(np.float32))
+
+
+def compute_pt_scene(n_spheres: int = 16, level: int = 3, seed: int = 5,
+                     light: bool = True) -> dict:
+    """A scene for the compute-shader path tracer, laid out like the
+    reference's disabled test geometry in src/shaders/test_compute.comp.glsl:
+    a 50 x 50 checkerboard ground quad, unit red spheres on a 5-unit grid
+    from (-8, 1, -8) (4 x 4 for 16 spheres; further spheres at seeded spots),
+    a radius-5 white light sphere at (0, 10, 0) and one blue sphere (a
+    material the shader treats as black).  Returns the buffers of
+    ComputePTScene plus the camera transform."""
+    rng = np.random.default_rng(seed)
+    pv, pi = plane()
+    sv, si = icosphere(level)
+    sv8 = np.zeros((len(sv), 8), np.float32)
+    sv8[:, 0:3] = sv[:, 0:3]
+    sv8[:, 3:6] = sv[:, 0:3]
+    sv8[:, 6:8] = sv[:, 6:8] if sv.shape[1] >= 8 else 0.0
+    vertices = np.concatenate([pv, sv8]).astype(np.float32)
+    indices = np.concatenate([pi, si]).astype(np.uint32)
+    meshes = np.array([[len(pi), 0, 0], [len(si), len(pi), len(pv)]], np.uint32)
+    models, invs, ents = [], [], []
+
+    def add(mesh, material, position, rot_x=0.0, scale=(1.0, 1.0, 1.0)):
+        m, inv = _trs(position, rot_x, scale)
+        models.append(m)
+        invs.append(inv)
+        ents.append((mesh, material, len(models) - 1))
+
+    add(0, CPT_MATERIAL_CHECKERBOARD, (0.0, 0.0, 0.0), -math.pi / 2, (50.0, 50.0, 50.0))
+    for k in range(n_spheres):
+        if k < 16:
+            pos = (-8.0 + 5.0 * (k % 4), 1.0, -8.0 + 5.0 * (k // 4))
+        else:
+            pos = (float(rng.uniform(-20, 20)), float(rng.uniform(0.5, 4)),
+                   float(rng.uniform(-20, 10)))
+        add(1, CPT_MATERIAL_RED, pos)
+    add(1, CPT_MATERIAL_BLUE, (6.0, 1.5, 6.0), 0.0, (1.5, 1.5, 1.5))
+    if light:
+        add(1, CPT_MATERIAL_WHITE_LIGHT, (0.0, 10.0, 0.0), 0.0, (5.0, 5.0, 5.0))
+    # camera: position (0, 6, 22), pitched down 12 degrees; forward = R * (0, 0, -1)
+    a = math.radians(-12.0)
+    ca, sa = math.cos(a), math.sin(a)
+    cam = np.zeros((4, 4))
+    cam[0] = (1.0, 0.0, 0.0, 0.0)        # right
+    cam[1] = (0.0, ca, sa, 0.0)          # up
+    cam[2] = (0.0, sa, -ca, 0.0)         # forward
+    cam[3] = (0.0, 6.0, 22.0, 0.0)       # position
+    return dict(vertices=vertices, indices=indices, meshes=meshes,
+                model=np.stack(models), inv_model=np.stack(invs),
+                entities=np.array(ents, np.uint32), texture=checkerboard_image(),
+                camera_transform=cam.reshape(-1).astype(np.float32))
