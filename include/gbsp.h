@@ -367,6 +367,30 @@ int gbsp_cpt_scene_destroy(gbsp_cpt_scene *scene);
 int gbsp_cpt_render_tiles(gbsp_cpt_scene *scene, const gbsp_cpt_view *view,
     const uint32_t *tileIndices, uint32_t tileCount, float *deviceImage, gbsp_metrics *metrics);
 
+/* ---- cube maps ------------------------------------------------------------------- */
+/* Equirectangular RGBA32F image (eqWidth x eqHeight, row 0 = top) -> six
+ * faces (face-major: 6 x height x width RGBA32F, faces +X -X +Y -Y +Z -Z).
+ * Device pointers, 16-byte aligned; asynchronous on `stream` (a
+ * cudaStream_t, NULL = default stream). */
+/* replaces CreateCubeMap (src/cubemap.cpp:235-291) */
+int gbsp_create_cube_map(void *stream, const float *equirect, uint32_t eqWidth, uint32_t eqHeight,
+    uint32_t width, uint32_t height, float *faces);
+/* replaces CreateIrradianceCubeMap (src/cubemap.cpp:106-233).  mode
+ * GBSP_IRRADIANCE_UNIFORM integrates the (phi, theta) grid of step 0.1 (the
+ * application's IRRADIANCE_CUBEMAP_USE_UNIFORM_SAMPLING 1, src/config.h:43;
+ * samplesPerPixel unused); GBSP_IRRADIANCE_RANDOM draws samplesPerPixel
+ * offsets per texel from one XorShift32 stream seeded 0x45BA12F3 in face,
+ * row, column order, as the reference does. */
+#define GBSP_IRRADIANCE_UNIFORM 0u
+#define GBSP_IRRADIANCE_RANDOM 1u
+int gbsp_create_irradiance_cube_map(void *stream, const float *equirect, uint32_t eqWidth,
+    uint32_t eqHeight, uint32_t width, uint32_t height, uint32_t samplesPerPixel, uint32_t mode,
+    float *faces);
+/* XorShift32 (src/math_utils.h:184-192) advanced `steps` times in
+ * O(log steps) GF(2) matrix products.  Host function, no device needed; no
+ * reference counterpart. */
+uint32_t gbsp_xorshift32_jump(uint32_t state, uint64_t steps);
+
 /* ---- display ------------------------------------------------------------------------ */
 /* Tone maps an RGBA32F frame (device memory) into packed 8-bit RGBA (device
  * memory): replaces PerformToneMapping of src/shaders/post_processing.frag.glsl:19-26

@@ -445,3 +445,35 @@ def compute_pt_tiles(scene: dict, width: int, height: int, tile: int, film_dista
         _u32(0 if tex is None else tex.shape[0]), _p(ct), _u32(width), _u32(height), _u32(tile),
         _u32(tile), _f(film_distance), _p(tl), _u32(len(tl)), _p(image), _p(counters))
     return image, counters
+
+
+def create_cube_map(equirect: np.ndarray, width: int, height: int, kind: str = "port"):
+    """CreateCubeMap (src/cubemap.cpp:235-291): (6, height, width, 4) float32."""
+    lib = _Lib.get(kind).lib
+    eq = np.ascontiguousarray(equirect, np.float32)
+    out = np.zeros((6, height, width, 4), np.float32)
+    fn = lib.oracle_create_cube_map if kind == "port" else lib.ref_create_cube_map
+    rc = fn(_p(eq), _u32(eq.shape[1]), _u32(eq.shape[0]), _u32(width), _u32(height), _p(out))
+    if kind == "ref" and rc != 0:
+        raise RuntimeError("the reference asserted in CreateCubeMap")
+    return out
+
+
+def create_irradiance_cube_map(equirect: np.ndarray, width: int, height: int, spp: int = 32,
+                               mode: int = 0, kind: str = "port"):
+    """CreateIrradianceCubeMap (src/cubemap.cpp:106-233); mode 0 = uniform
+    (phi, theta) grid, 1 = random offsets."""
+    lib = _Lib.get(kind).lib
+    eq = np.ascontiguousarray(equirect, np.float32)
+    out = np.zeros((6, height, width, 4), np.float32)
+    if kind == "port":
+        lib.oracle_create_irradiance_cube_map(_p(eq), _u32(eq.shape[1]), _u32(eq.shape[0]),
+                                              _u32(width), _u32(height), _u32(spp), _u32(mode),
+                                              _p(out))
+    else:
+        rc = lib.ref_create_irradiance_cube_map(_p(eq), _u32(eq.shape[1]), _u32(eq.shape[0]),
+                                                _u32(width), _u32(height), _u32(spp),
+                                                _u32(mode), _p(out))
+        if rc != 0:
+            raise RuntimeError("the reference asserted in CreateIrradianceCubeMap")
+    return out

@@ -61,6 +61,20 @@ static unsigned int g_harness_spp = 1;
 #include "simd_path_tracer.cpp"
 #include "mesh_generation.cpp"
 
+// src/cubemap.cpp twice: the application's uniform (phi, theta) irradiance
+// integration (src/config.h:43) and the random-sampling variant behind the
+// same switch.
+#define IRRADIANCE_CUBEMAP_USE_UNIFORM_SAMPLING 1
+namespace ref_cube_uniform {
+#include "cubemap.cpp"
+}
+#undef IRRADIANCE_CUBEMAP_USE_UNIFORM_SAMPLING
+#define IRRADIANCE_CUBEMAP_USE_UNIFORM_SAMPLING 0
+namespace ref_cube_random {
+#include "cubemap.cpp"
+}
+#undef IRRADIANCE_CUBEMAP_USE_UNIFORM_SAMPLING
+
 // ---------------------------------------------------------------------------
 // Abort capture
 // ---------------------------------------------------------------------------
@@ -625,3 +639,56 @@ int ref_sizeof(int which)
 }
 
 } // extern "C"
+
+// --- Cube maps (src/cubemap.cpp:108-291) ------------------------------------
+// equirect: RGBA32F eqWidth x eqHeight; out: 6 faces of width x height RGBA32F.
+extern "C" {
+
+static int ref_cube_common(int which, const float *equirect, uint32_t eqWidth,
+    uint32_t eqHeight, uint32_t width, uint32_t height, uint32_t spp, float *out)
+{
+    GUARDED_BEGIN
+    HdrImage eq = {};
+    eq.width = eqWidth;
+    eq.height = eqHeight;
+    eq.pixels = (f32 *)equirect;
+    uint64_t bytes = (uint64_t)width * height * 16 * 6 + 4096;
+    void *mem = calloc(1, bytes);
+    MemoryArena arena = {};
+    InitializeMemoryArena(&arena, mem, bytes);
+    HdrImage faces[6];
+    if (which == 0) {
+        ref_cube_uniform::HdrCubeMap c = ref_cube_uniform::CreateCubeMap(eq, &arena, width, height);
+        for (int i = 0; i < 6; i++) faces[i] = c.images[i];
+    } else if (which == 1) {
+        ref_cube_uniform::HdrCubeMap c =
+            ref_cube_uniform::CreateIrradianceCubeMap(eq, &arena, width, height, spp);
+        for (int i = 0; i < 6; i++) faces[i] = c.images[i];
+    } else {
+        ref_cube_random::HdrCubeMap c =
+            ref_cube_random::CreateIrradianceCubeMap(eq, &arena, width, height, spp);
+        for (int i = 0; i < 6; i++) faces[i] = c.images[i];
+    }
+    for (int i = 0; i < 6; i++)
+        memcpy(out + (size_t)i * width * height * 4, faces[i].pixels,
+            (size_t)width * height * 16);
+    free(mem);
+    GUARDED_END
+    return 0;
+}
+
+int ref_create_cube_map(const float *equirect, uint32_t eqWidth, uint32_t eqHeight,
+    uint32_t width, uint32_t height, float *out)
+{
+    return ref_cube_common(0, equirect, eqWidth, eqHeight, width, height, 0, out);
+}
+
+// mode 0: uniform (phi, theta) grid (the application's setting); 1: random
+int ref_create_irradiance_cube_map(const float *equirect, uint32_t eqWidth,
+    uint32_t eqHeight, uint32_t width, uint32_t height, uint32_t spp, uint32_t mode, float *out)
+{
+    return ref_cube_common(mode == 0 ? 1 : 2, equirect, eqWidth, eqHeight, width, height, spp,
+        out);
+}
+
+}  // extern "C"

@@ -25,7 +25,7 @@ LIB = os.path.join(BUILD, "libgbsp.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["api.cu", "bvh_build.cu", "trace.cu", "pathtrace.cu", "batch.cu", "denoise.cu", "post.cu",
-           "compute_pt.cu"]
+           "compute_pt.cu", "cubemap.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -147,7 +147,7 @@ int check_stream_status(gbsp_runtime *rt)
         GBSP_CUDA_TRY(cudaMemsetAsync(rt->dStatus, 0, 4, rt->stream));
         return set_error(GBSP_ERR_DEVICE_STATUS,
             "device status 0x%x (1 = traversal stack overflow, 2 = queue overflow, 4 = bad index, "
-            "8 = build capacity)",
+            "8 = build capacity, 16 = per-ray step cap)",
             st);
     }
     return GBSP_OK;

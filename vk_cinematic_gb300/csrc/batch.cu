@@ -14,6 +14,7 @@
 
 #include "gbsp_internal.h"
 #include "shading.cuh"
+#include "traverse_dyn.cuh"
 
 namespace gbsp {
 
@@ -140,7 +141,9 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
     int32_t lPrim = -1;
     bool exhausted = false;
 
+    uint32_t steps = 0;
     auto trace_begin = [&](const SceneView &sv) {
+        steps = 0;
         invd = inverse(d);
         bestT = kInf;
         bestU = bestV = 0.0f;
@@ -270,6 +273,12 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
         if (phase != 1) continue;
         // ---- one traversal step (dyn_trace_loop's step, per-lane scene)
         const SceneView &sv = itd.sv;
+        if (++steps > kMaxRaySteps) {
+            atomicOr(status, kStatusRayStepLimit);
+            tmode = 1;
+            sp = 0;
+            steps = 0;
+        }
         if (tmode == 2 && sp == base) {
             if (lPrim >= 0) {
                 const Instance &in = sv.instances[inst];

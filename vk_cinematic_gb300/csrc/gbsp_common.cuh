@@ -329,5 +329,6 @@ constexpr uint32_t kStatusStackOverflow = 1u;
 constexpr uint32_t kStatusQueueOverflow = 2u;
 constexpr uint32_t kStatusBadIndex = 4u;
 constexpr uint32_t kStatusBuildLoop = 8u;
+constexpr uint32_t kStatusRayStepLimit = 16u;  // a ray exceeded the per-ray step cap
 
 }  // namespace gbsp

@@ -19,6 +19,10 @@
 namespace gbsp {
 
 constexpr int kRefillIdleLanes = 8;
+// A ray of a validated tree needs far fewer steps (every node is popped at
+// most once per object entry); past this cap the ray is ended with the best
+// hit so far and the status word records it.
+constexpr uint32_t kMaxRaySteps = 1u << 22;
 
 template <class Policy>
 __device__ __forceinline__ void dyn_trace_loop(Policy &pol, const SceneView &sv, uint32_t count,
@@ -40,6 +44,7 @@ __device__ __forceinline__ void dyn_trace_loop(Policy &pol, const SceneView &sv,
     float len = 0.0f, lBestT = kInf, lU = 0.0f, lV = 0.0f;
     int32_t lPrim = -1;
     int base = 0;
+    uint32_t steps = 0;
     bool exhausted = false;
     for (uint32_t guard = 0; guard < (1u << 30); guard++) {
         // ---- refill idle lanes (warp-uniform control flow)
@@ -55,6 +60,7 @@ __device__ __forceinline__ void dyn_trace_loop(Policy &pol, const SceneView &sv,
                 uint32_t idx = first + __popc(idle & laneMaskLt);
                 if (idx < count) {
                     slot = idx;
+                    steps = 0;
                     pol.load(idx, o, d);
                     invd = inverse(d);
                     bestT = kInf;
@@ -76,6 +82,12 @@ __device__ __forceinline__ void dyn_trace_loop(Policy &pol, const SceneView &sv,
             continue;
         }
         if (mode == 0) continue;
+        if (++steps > kMaxRaySteps) {
+            atomicOr(status, kStatusRayStepLimit);
+            mode = 1;
+            sp = 0;  // the next step stores the best hit found so far
+            steps = 0;
+        }
 
         // ---- one step for this lane
         if (mode == 2 && sp == base) {

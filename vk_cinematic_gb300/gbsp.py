@@ -52,6 +52,7 @@ EXPORTS = [
     "gbsp_dn_flip_transpose", "gbsp_dn_relu_backward", "gbsp_dn_conv3x3_weight_grad",
     "gbsp_dn_filter", "gbsp_dn_relmse_backward", "gbsp_dn_adam", "gbsp_tonemap",
     "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
+    "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
 ]
 
 
@@ -128,6 +129,8 @@ def load(build_if_missing: bool = True):
     lib.gbsp_frame_aov_device_pointer.restype = _vp
     lib.gbsp_sample_seed.restype = _u32
     lib.gbsp_calculate_film_positions.restype = _u32
+    lib.gbsp_xorshift32_jump.restype = _u32
+    lib.gbsp_xorshift32_jump.argtypes = [_u32, ctypes.c_uint64]
     for name in EXPORTS:
         getattr(lib, name)  # raises if a declared symbol is not exported
     _LIB = lib
@@ -557,3 +560,40 @@ def cpt_view(width=256, height=192, tile=16, film_distance=0.8, camera_transform
     for k in range(16):
         v.cameraTransform[k] = float(ct[k])
     return v
+
+
+# ---- cube maps ----------------------------------------------------------------------------
+
+IRRADIANCE_UNIFORM = 0
+IRRADIANCE_RANDOM = 1
+
+
+def create_cube_map(equirect, width: int, height: int, faces=None, stream: int = 0):
+    """CreateCubeMap on the device: equirect is a (H, W, 4) float32 CUDA
+    tensor; returns (6, height, width, 4)."""
+    import torch
+
+    L = load()
+    if faces is None:
+        faces = torch.empty((6, height, width, 4), dtype=torch.float32, device=equirect.device)
+    _check(L.gbsp_create_cube_map(_vp(stream), _vp(equirect.data_ptr()),
+                                  _u32(equirect.shape[1]), _u32(equirect.shape[0]), _u32(width),
+                                  _u32(height), _vp(faces.data_ptr())))
+    return faces
+
+
+def create_irradiance_cube_map(equirect, width: int, height: int, spp: int = 32,
+                               mode: int = IRRADIANCE_UNIFORM, faces=None, stream: int = 0):
+    import torch
+
+    L = load()
+    if faces is None:
+        faces = torch.empty((6, height, width, 4), dtype=torch.float32, device=equirect.device)
+    _check(L.gbsp_create_irradiance_cube_map(
+        _vp(stream), _vp(equirect.data_ptr()), _u32(equirect.shape[1]), _u32(equirect.shape[0]),
+        _u32(width), _u32(height), _u32(spp), _u32(mode), _vp(faces.data_ptr())))
+    return faces
+
+
+def xorshift32_jump(state: int, steps: int) -> int:
+    return int(load().gbsp_xorshift32_jump(_u32(state), ctypes.c_uint64(steps)))

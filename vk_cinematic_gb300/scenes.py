@@ -387,3 +387,34 @@ def compute_pt_scene(n_spheres: int = 16, level: int = 3, seed: int = 5,
                 model=np.stack(models), inv_model=np.stack(invs),
                 entities=np.array(ents, np.uint32), texture=checkerboard_image(),
                 camera_transform=cam.reshape(-1).astype(np.float32))
+
+
+def equirect_hdri(width: int = 2048, height: int = 1024, seed: int = 6) -> np.ndarray:
+    """A seeded synthetic equirectangular HDR environment (RGBA32F, row 0 =
+    top): sky gradient over a darker ground, a sun of radiance 50 (above the
+    radiance clamp of 10), four bright panels and per-texel noise.  Stands in
+    for the EXR HDRI the reference loads from disk (src/main.cpp:1298-1313)."""
+    rng = np.random.default_rng(seed)
+    v = (np.arange(height, dtype=np.float64) + 0.5) / height
+    u = (np.arange(width, dtype=np.float64) + 0.5) / width
+    uu, vv = np.meshgrid(u, v)
+    elev = (0.5 - vv) * np.pi                      # +pi/2 at the top row
+    img = np.zeros((height, width, 4), np.float64)
+    sky = np.clip(elev / (np.pi / 2), 0, 1)[..., None]
+    img[..., :3] = (np.array([0.9, 0.95, 1.0]) * (1 - sky) + np.array([0.25, 0.45, 0.9]) * sky)
+    ground = (elev < 0)[..., None]
+    img[..., :3] = np.where(ground, np.array([0.12, 0.1, 0.08]) * (1 + 0.5 * np.cos(8 * uu))[..., None],
+                            img[..., :3])
+    # sun at azimuth 0.3 turns, elevation 35 degrees, radius 2 degrees
+    az0, el0 = 0.3 * 2 * np.pi, np.radians(35)
+    az = uu * 2 * np.pi
+    cosd = np.sin(elev) * np.sin(el0) + np.cos(elev) * np.cos(el0) * np.cos(az - az0)
+    img[..., :3] += np.where((cosd > np.cos(np.radians(2.0)))[..., None], 50.0, 0.0)
+    for k in range(4):
+        u0, v0 = rng.uniform(0, 0.9), rng.uniform(0.2, 0.45)
+        du, dv = rng.uniform(0.02, 0.08), rng.uniform(0.02, 0.06)
+        m = (uu > u0) & (uu < u0 + du) & (vv > v0) & (vv < v0 + dv)
+        img[m, :3] += rng.uniform(3, 15, 3)
+    img[..., :3] *= 1.0 + 0.05 * rng.standard_normal((height, width, 1))
+    img[..., 3] = 1.0
+    return np.ascontiguousarray(img.astype(np.float32))
