@@ -56,7 +56,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gbsp", "reference"], default="gbsp")
     ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4", "config5",
-                                           "compute_pt"],
+                                           "compute_pt", "cubemap"],
                     default="config3")
     ap.add_argument("--dn-scenes", type=int, default=125)
     ap.add_argument("--dn-crops", type=int, default=16)
@@ -559,8 +559,7 @@ def run_config2(args):
                                "vertex offsets in [-0.01, 0.01]^3), 4,194,304 rays from a radius-2 "
                                "sphere towards the cube", "triangles": 1 << 20, "rays": n,
                    "l2": "flushed (256 MB device write) before every timed step; kernel time "
-                         "only (CUDA events around the launch)",
-                   "trace": "static" if os.environ.get("GBSP_TRACE") == "static" else "dynamic"},
+                         "only (CUDA events around the launch)"},
         "hit_fraction": hit_frac, "device_bvh_build_and_upload_s": build_s,
     }
     print(json.dumps(line), flush=True)
@@ -746,6 +745,82 @@ def run_compute_pt(args):
     return 0
 
 
+def run_cubemap(args):
+    """The application's image-based-lighting bake (src/main.cpp:1308-1313):
+    CreateCubeMap at 1024 x 1024 per face and CreateIrradianceCubeMap at
+    32 x 32 (uniform grid) from a 2048 x 1024 equirectangular HDR image.  A
+    step is both kernels; the oracle port (the reference's algorithm, bit
+    exact with it) is timed on the host for the CPU baseline."""
+    import torch
+    from vk_cinematic_gb300 import gbsp, scenes
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    eq_np = scenes.equirect_hdri(2048, 1024)
+    eq = torch.from_numpy(eq_np).cuda()
+    cube = torch.empty((6, 1024, 1024, 4), dtype=torch.float32, device="cuda")
+    irr = torch.empty((6, 32, 32, 4), dtype=torch.float32, device="cuda")
+    sid = stream.cuda_stream
+    flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        gbsp.create_cube_map(eq, 1024, 1024, cube, sid)
+        gbsp.create_irradiance_cube_map(eq, 32, 32, 32, gbsp.IRRADIANCE_UNIFORM, irr, sid)
+    torch.cuda.synchronize()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    cube_ms = irr_ms = 0.0
+    clocks = ClockSampler(0)
+    clocks.start()
+    for _ in range(args.steps):
+        flush.zero_()
+        evs[0].record(stream)
+        gbsp.create_cube_map(eq, 1024, 1024, cube, sid)
+        evs[1].record(stream)
+        gbsp.create_irradiance_cube_map(eq, 32, 32, 32, gbsp.IRRADIANCE_UNIFORM, irr, sid)
+        evs[2].record(stream)
+        torch.cuda.synchronize()
+        cube_ms += evs[0].elapsed_time(evs[1])
+        irr_ms += evs[1].elapsed_time(evs[2])
+    clk = clocks.stop()
+    cube_ms /= args.steps
+    irr_ms /= args.steps
+    step_ms = cube_ms + irr_ms
+    peak, peak_kind = measured_peaks()
+    # cube map: 16 B written per texel plus one pass over the source image
+    cube_bytes = 6 * 1024 * 1024 * 16 + eq_np.nbytes
+    line = {
+        "metric": "IBL bake time (cube map 1024^2 + irradiance 32^2 from a 2048x1024 HDRI)",
+        "value": step_ms, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded equirectangular HDR image",
+        "config": {"workload": "cubemap: CreateCubeMap 6 x 1024 x 1024 + CreateIrradianceCubeMap "
+                               "6 x 32 x 32, uniform (phi, theta) grid of 1,008 samples",
+                   "l2": "flushed (256 MB device write) before every timed step"},
+        "cube_map_ms": cube_ms, "irradiance_ms": irr_ms,
+        "irradiance_samples_per_s": 6 * 32 * 32 * 1008 / (irr_ms * 1e-3),
+        "roofline": {"bound": "hbm", "kernel": "k_cube_map", "achieved": cube_bytes / (cube_ms * 1e-3) / 1e9,
+                     "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": cube_bytes / (cube_ms * 1e-3) / 1e9 / peak, "traffic": None},
+        "gpu_launches": 2 * args.steps, "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle
+
+        pyoracle.build_port()
+        t0 = time.perf_counter()
+        pyoracle.create_cube_map(eq_np, 256, 256)  # 1/16 of the texels
+        t_cube = (time.perf_counter() - t0) * 16
+        t0 = time.perf_counter()
+        pyoracle.create_irradiance_cube_map(eq_np, 32, 32, 32, 0)
+        t_irr = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": (t_cube + t_irr) * 1e3, "unit": "ms", "cores": 1,
+                                "kind": "port",
+                                "sample": "irradiance 6x32x32 in full; cube map at 6x256x256 "
+                                          "scaled by 16 to 6x1024x1024"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     _OVERRIDES.update(width=args.width, height=args.height, spp=args.spp)
@@ -759,6 +834,8 @@ def main():
         return run_config5(args)
     if args.workload == "compute_pt":
         return run_compute_pt(args)
+    if args.workload == "cubemap":
+        return run_cubemap(args)
     return run_gpu(args)
 
 

@@ -254,8 +254,6 @@ int gbsp_runtime_create(int device, void *stream, gbsp_runtime **out)
     GBSP_CUDA_TRY(cudaSetDevice(device));
     gbsp_runtime *rt = new gbsp_runtime();
     rt->device = device;
-    const char *traceMode = getenv("GBSP_TRACE");
-    rt->dynamicTrace = !(traceMode && strcmp(traceMode, "static") == 0);
     if (stream) {
         rt->stream = (cudaStream_t)stream;
     } else {
@@ -311,7 +309,7 @@ static void runtime_teardown(gbsp_runtime *rt)
 }
 
 // Drops one reference; the last one tears the runtime down.
-static void runtime_release(gbsp_runtime *rt)
+void gbsp::runtime_release(gbsp_runtime *rt)
 {
     bool last;
     {
@@ -321,7 +319,7 @@ static void runtime_release(gbsp_runtime *rt)
     if (last) runtime_teardown(rt);
 }
 
-static int runtime_retain(gbsp_runtime *rt)
+int gbsp::runtime_retain(gbsp_runtime *rt)
 {
     std::lock_guard<std::mutex> lock(g_runtimeMutex);
     if (rt->closed) return set_error(GBSP_ERR_INVALID_ARGUMENT, "runtime already destroyed");
@@ -688,7 +686,7 @@ int gbsp_intersect_closest_device(gbsp_scene *scene, uint32_t count, const float
     if ((rc = counters_begin(rt))) return rc;
     return launch_intersect(rt->stream, scene->view(), count, reinterpret_cast<const float4 *>(rays),
         tOut, triangleOut, objectOut, nullptr, nullptr, nullptr, rt->smCount, rt->dCounters,
-        rt->dStatus, rt->dynamicTrace);
+        rt->dStatus);
 }
 
 int gbsp_ray_intersect_scene(gbsp_scene *scene, uint32_t count, const float *rays, float *resultOut,
@@ -715,7 +713,7 @@ int gbsp_ray_intersect_scene(gbsp_scene *scene, uint32_t count, const float *ray
     if ((rc = counters_begin(rt))) return rc;
     GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
     if ((rc = launch_intersect(s, scene->view(), count, dr.ptr, nullptr, nullptr, nullptr, dattr.ptr,
-             dmat.ptr, nullptr, rt->smCount, rt->dCounters, rt->dStatus, rt->dynamicTrace)))
+             dmat.ptr, nullptr, rt->smCount, rt->dCounters, rt->dStatus)))
         return rc;
     GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
     GBSP_CUDA_TRY(cudaMemcpyAsync(resultOut, dattr.ptr, 24 * (size_t)count, cudaMemcpyDeviceToHost, s));

@@ -14,7 +14,6 @@
 
 #include "gbsp_internal.h"
 #include "shading.cuh"
-#include "traverse_dyn.cuh"
 
 namespace gbsp {
 
@@ -113,6 +112,11 @@ __global__ void __launch_bounds__(256) k_batch(const BatchItemDev *__restrict__ 
 // one of trace_full_path.
 // ---------------------------------------------------------------------------
 constexpr int kSmRefill = 8;
+// A ray of a validated tree needs far fewer steps (every node is popped at
+// most once per object entry); past this cap the ray is ended with the best
+// hit so far and the status word records it.
+constexpr uint32_t kMaxRaySteps = 1u << 22;
+constexpr uint64_t kMaxBatchIterations = 1ull << 34;
 constexpr int kSmShade = 16;
 
 __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict__ items,
@@ -170,7 +174,13 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
             trace_begin(itd.sv);
     };
 
-    for (uint64_t guard = 0; guard < (1ull << 40); guard++) {
+    bool finished = false;
+    for (uint64_t guard = 0; guard < kMaxBatchIterations; guard++) {
+        // One iteration = one convergence point: every lane passes the
+        // __syncwarp and the three ballots exactly once, and each lane's step
+        // is a function call without early exits from the loop, so votes
+        // and shuffles always see the whole warp at the same instruction.
+        __syncwarp();
         // ---- refill idle lanes with pixels
         uint32_t idle = __ballot_sync(0xFFFFFFFFu, phase == 0);
         if (idle && !exhausted && (__popc(idle) >= kSmRefill || idle == 0xFFFFFFFFu)) {
@@ -204,14 +214,14 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
         }
         uint32_t tmask = __ballot_sync(0xFFFFFFFFu, phase == 1);
         uint32_t smask = __ballot_sync(0xFFFFFFFFu, phase == 2);
-        if (!tmask && !smask) {
-            if (exhausted) break;
-            continue;
+        if (!tmask && !smask && exhausted) {
+            finished = true;
+            break;
         }
         bool doShade = smask && (__popc(smask) >= kSmShade || !tmask);
         const BatchItemDev &itd = items[it];
-        if (doShade) {
-            if (phase != 2) continue;
+        // ---- one shading event
+        auto shade_step = [&]() {
             float4 ec, aa;
             bool more = false;
             bool hit = false;
@@ -250,7 +260,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                 vA[len] = aa;
                 len++;
             }
-            if (more) continue;
+            if (more) return;
             V3 r = path_radiance(vE, vA, 1, 0, len, itd.clampValue);
             paths++;
             bool isNan = isnan(r.x) || isnan(r.y) || isnan(r.z);
@@ -268,81 +278,87 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                     make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
                 phase = 0;
             }
-            continue;
-        }
-        if (phase != 1) continue;
-        // ---- one traversal step (dyn_trace_loop's step, per-lane scene)
-        const SceneView &sv = itd.sv;
-        if (++steps > kMaxRaySteps) {
-            atomicOr(status, kStatusRayStepLimit);
-            tmode = 1;
-            sp = 0;
-            steps = 0;
-        }
-        if (tmode == 2 && sp == base) {
-            if (lPrim >= 0) {
-                const Instance &in = sv.instances[inst];
-                Affine model;
+        };
+        // ---- one traversal step (trace_closest's stack walk, one pop per call)
+        auto trace_step = [&]() {
+            const SceneView &sv = itd.sv;
+            if (++steps > kMaxRaySteps) {
+                atomicOr(status, kStatusRayStepLimit);
+                tmode = 1;
+                sp = 0;
+                steps = 0;
+            }
+            if (tmode == 2 && sp == base) {
+                if (lPrim >= 0) {
+                    const Instance &in = sv.instances[inst];
+                    Affine model;
 #pragma unroll
-                for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
-                V3 worldHit = transform_point(model, add(lo, mul(ld, lBestT)));
-                float tw = dot(sub(worldHit, o), d);
-                if (tw < bestT || (tw == bestT && (int32_t)inst < bestInst)) {
-                    bestT = tw;
-                    bestU = lU;
-                    bestV = lV;
-                    bestPrim = lPrim;
-                    bestInst = (int32_t)inst;
+                    for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
+                    V3 worldHit = transform_point(model, add(lo, mul(ld, lBestT)));
+                    float tw = dot(sub(worldHit, o), d);
+                    if (tw < bestT || (tw == bestT && (int32_t)inst < bestInst)) {
+                        bestT = tw;
+                        bestU = lU;
+                        bestV = lV;
+                        bestPrim = lPrim;
+                        bestInst = (int32_t)inst;
+                    }
                 }
+                tmode = 1;
+                return;
             }
-            tmode = 1;
-            continue;
-        }
-        if (tmode == 1 && sp == 0) {
-            phase = 2;
-            continue;
-        }
-        sp--;
-        uint32_t ref = stackRef[sp];
-        float te = stackT[sp];
-        float bound = tmode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * llen));
-        if (te > bound) continue;
-        if (!child_is_leaf(ref)) {
-            if (tmode == 1)
-                cnt.topNodes++;
-            else
-                cnt.meshNodes++;
-            V3 ro = tmode == 1 ? o : lo;
-            V3 ri = tmode == 1 ? invd : linvd;
-            visit_node<true>(sv.nodes, ref, ro, ri, bound, stackRef, stackT, sp, status, cnt);
-            continue;
-        }
-        if (tmode == 1) {
-            inst = leaf_first(ref);
-            const Instance &in = sv.instances[inst];
-            Affine inv;
+            if (tmode == 1 && sp == 0) {
+                phase = 2;
+                return;
+            }
+            sp--;
+            uint32_t ref = stackRef[sp];
+            float te = stackT[sp];
+            float bound = tmode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * llen));
+            if (te > bound) return;
+            if (!child_is_leaf(ref)) {
+                if (tmode == 1)
+                    cnt.topNodes++;
+                else
+                    cnt.meshNodes++;
+                V3 ro = tmode == 1 ? o : lo;
+                V3 ri = tmode == 1 ? invd : linvd;
+                visit_node<true>(sv.nodes, ref, ro, ri, bound, stackRef, stackT, sp, status, cnt);
+                return;
+            }
+            if (tmode == 1) {
+                inst = leaf_first(ref);
+                const Instance &in = sv.instances[inst];
+                Affine inv;
 #pragma unroll
-            for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
-            lo = transform_point(inv, o);
-            ld = normalize(transform_vector(inv, d), &llen);
-            linvd = inverse(ld);
-            cnt.meshTests++;
-            lBestT = kInf;
-            lU = lV = 0.0f;
-            lPrim = -1;
-            base = sp;
-            if (sp >= kStackSize) {
-                atomicOr(status, kStatusStackOverflow);
-                continue;
+                for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
+                lo = transform_point(inv, o);
+                ld = normalize(transform_vector(inv, d), &llen);
+                linvd = inverse(ld);
+                cnt.meshTests++;
+                lBestT = kInf;
+                lU = lV = 0.0f;
+                lPrim = -1;
+                base = sp;
+                if (sp >= kStackSize) {
+                    atomicOr(status, kStatusStackOverflow);
+                    return;
+                }
+                stackRef[sp] = __ldg(&in.blasRoot);
+                stackT[sp] = 0.0f;
+                sp++;
+                tmode = 2;
+                return;
             }
-            stackRef[sp] = __ldg(&in.blasRoot);
-            stackT[sp] = 0.0f;
-            sp++;
-            tmode = 2;
-            continue;
-        }
-        visit_leaf<true>(sv, ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+            visit_leaf<true>(sv, ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+        };
+        if (doShade && phase == 2)
+            shade_step();
+        else if (!doShade && phase == 1)
+            trace_step();
     }
+    if (!finished && lane == 0) atomicOr(status, kStatusQueueOverflow);
+    __syncwarp();
     uint32_t v[9] = {rays, hitsCnt, paths, nans, cnt.topNodes, cnt.meshNodes, cnt.triTests,
         cnt.boxTests, cnt.meshTests};
 #pragma unroll
@@ -373,7 +389,7 @@ struct gbsp_batch {
     DeviceBuffer<int32_t> dSlots;
     DeviceBuffer<unsigned long long> dWork;
     uint64_t totalPixels = 0, totalPaths = 0;
-    gbsp_batch_config cfg = {128, 1, 8, 1, GBSP_BATCH_PATH_STATE};
+    gbsp_batch_config cfg = {128, 1, 8, 1, GBSP_BATCH_THREAD_PER_PIXEL};
     cudaGraphExec_t exec = nullptr;
 };
 
@@ -445,6 +461,8 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
 {
     if (!rt || !items || !count || !out) return set_error(GBSP_ERR_INVALID_ARGUMENT, "empty batch");
     *out = nullptr;
+    int rrc = runtime_retain(rt);
+    if (rrc) return rrc;
     gbsp_batch *b = new gbsp_batch();
     b->rt = rt;
     b->items.assign(items, items + count);
@@ -518,6 +536,7 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
         rc = set_error(GBSP_ERR_CUDA, "batch upload failed");
     if (rc) {
         delete b;
+        runtime_release(rt);
         return rc;
     }
     b->totalPixels = base;
@@ -528,9 +547,11 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
 int gbsp_batch_destroy(gbsp_batch *batch)
 {
     if (!batch) return GBSP_OK;
-    cudaStreamSynchronize(batch->rt->stream);
+    gbsp_runtime *rt = batch->rt;
+    cudaStreamSynchronize(rt->stream);
     drop_graph(batch);
     delete batch;
+    runtime_release(rt);
     return GBSP_OK;
 }
 

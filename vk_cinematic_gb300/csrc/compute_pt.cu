@@ -397,6 +397,8 @@ int gbsp_cpt_scene_create(gbsp_runtime *rt, const gbsp_vertex *vertices, uint32_
             for (int j = 0; j < 3; j++) uv[g * 3 + j] = make_float2(v[j]->uv[0], v[j]->uv[1]);
         }
     }
+    int rrc = runtime_retain(rt);
+    if (rrc) return rrc;
     gbsp_cpt_scene *s = new gbsp_cpt_scene();
     s->rt = rt;
     s->entityCount = entityCount;
@@ -415,6 +417,7 @@ int gbsp_cpt_scene_create(gbsp_runtime *rt, const gbsp_vertex *vertices, uint32_
         rc = set_error(GBSP_ERR_CUDA, "compute path tracer scene upload failed");
     if (rc) {
         delete s;
+        runtime_release(rt);
         return rc;
     }
     *out = s;
@@ -424,8 +427,10 @@ int gbsp_cpt_scene_create(gbsp_runtime *rt, const gbsp_vertex *vertices, uint32_
 int gbsp_cpt_scene_destroy(gbsp_cpt_scene *scene)
 {
     if (!scene) return GBSP_OK;
-    cudaStreamSynchronize(scene->rt->stream);
+    gbsp_runtime *rt = scene->rt;
+    cudaStreamSynchronize(rt->stream);
     delete scene;
+    runtime_release(rt);
     return GBSP_OK;
 }
 

@@ -271,8 +271,8 @@ using namespace gbsp;
 static int check_image(const float *equirect, uint32_t eqW, uint32_t eqH, uint32_t w, uint32_t h,
     const float *faces)
 {
-    if (!equirect || !faces) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL image");
     if (!eqW || !eqH || !w || !h) return set_error(GBSP_ERR_INVALID_ARGUMENT, "empty image");
+    if (!equirect || !faces) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL image");
     if (((uintptr_t)equirect | (uintptr_t)faces) & 15u)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "images must be 16-byte aligned");
     return GBSP_OK;

@@ -74,9 +74,6 @@ struct Counters;  // device metric block
 struct gbsp_runtime {
     int refs = 1;                       // guarded by the API's runtime mutex
     bool closed = false;
-    // closest-hit kernel of the wavefront: dynamic per-lane fetch (default)
-    // or one ray per lane until the warp finishes (GBSP_TRACE=static)
-    bool dynamicTrace = true;
     int device = 0;
     cudaStream_t stream = nullptr;
     bool ownsStream = false;
@@ -210,10 +207,15 @@ int offset_nodes(cudaStream_t s, Node8 *dNodes, uint32_t nodeCount, uint32_t nod
     uint32_t leafBase);
 
 // trace.cu
+// Reference counting of runtimes: scenes, material systems, batches and
+// compute-path-tracer scenes hold a reference so that a runtime destroyed
+// first stays alive (stream and buffers) until its last dependent goes.
+int runtime_retain(gbsp_runtime *rt);
+void runtime_release(gbsp_runtime *rt);
+
 int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const float4 *rays,
     float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut, uint32_t *matOut,
-    const Instance *instHost, int smCount, unsigned long long *counters, uint32_t *dStatus,
-    bool dynamicTrace);
+    const Instance *instHost, int smCount, unsigned long long *counters, uint32_t *dStatus);
 
 // pathtrace.cu
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,

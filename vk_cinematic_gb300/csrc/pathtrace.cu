@@ -26,7 +26,6 @@
 
 #include "gbsp_internal.h"
 #include "traverse.cuh"
-#include "traverse_dyn.cuh"
 #include "shading.cuh"
 
 namespace gbsp {
@@ -134,50 +133,6 @@ __global__ void __launch_bounds__(128) k_trace(SceneView sv, const float4 *__res
     for (int k = 0; k < 7; k++)
         for (int off = 16; off; off >>= 1) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
     if (lane == 0) {
-        atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)v[0]);
-        atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)v[1]);
-        atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(v[0] - v[1]));
-        atomicAdd(&counters[GBSP_METRIC_BROADPHASE_NODE_VISITS], (unsigned long long)v[2]);
-        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_NODE_VISITS], (unsigned long long)v[3]);
-        atomicAdd(&counters[GBSP_METRIC_TRIANGLE_TESTS], (unsigned long long)v[4]);
-        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_BOX_TESTS], (unsigned long long)v[5]);
-        atomicAdd(&counters[GBSP_METRIC_MESH_TESTS_PERFORMED], (unsigned long long)v[6]);
-    }
-}
-
-// Path queues through the dynamic-fetch traversal.
-struct PathRayPolicy {
-    const float4 *rayO, *rayD;
-    int4 *hitA;
-    int *hitInst;
-    __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d) const
-    {
-        float4 o4 = rayO[i], d4 = rayD[i];
-        o = v3(o4.x, o4.y, o4.z);
-        d = v3(d4.x, d4.y, d4.z);
-    }
-    __device__ __forceinline__ void store(uint32_t i, const RayHit &h, const SceneView &) const
-    {
-        hitA[i] = make_int4(__float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v), h.prim);
-        hitInst[i] = h.inst;
-    }
-};
-
-__global__ void __launch_bounds__(128) k_trace_dyn(SceneView sv, const float4 *__restrict__ rayO,
-    const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
-    unsigned int *ctl, unsigned long long *counters, uint32_t *status)
-{
-    uint32_t count = *queueCount;
-    TraceCounters cnt = {0, 0, 0, 0, 0};
-    uint32_t done = 0, hits = 0;
-    PathRayPolicy pol = {rayO, rayD, hitA, hitInst};
-    dyn_trace_loop(pol, sv, count, &ctl[kCtlTraceWork], status, cnt, done, hits);
-    uint32_t v[7] = {done, hits, cnt.topNodes, cnt.meshNodes, cnt.triTests, cnt.boxTests,
-        cnt.meshTests};
-#pragma unroll
-    for (int k = 0; k < 7; k++)
-        for (int off = 16; off; off >>= 1) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
-    if ((threadIdx.x & 31) == 0) {
         atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)v[0]);
         atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)v[1]);
         atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(v[0] - v[1]));
@@ -510,12 +465,8 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
                 const float4 *qD = wb.rayD + ((b & 1) ? cap : 0);
                 k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
                 int e0 = timing ? rt->stage_event(s) : -1;
-                if (rt->dynamicTrace)
-                    k_trace_dyn<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA,
-                        wb.hitInst, ctl, counters, rt->dStatus);
-                else
-                    k_trace<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA,
-                        wb.hitInst, ctl, counters, rt->dStatus);
+                k_trace<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA, wb.hitInst,
+                    ctl, counters, rt->dStatus);
                 int e1 = timing ? rt->stage_event(s) : -1;
                 k_shade<<<persistentGrid, 128, 0, s>>>(sv, mv, wp, wb, b, inQ, ctl, counters);
                 int e2 = timing ? rt->stage_event(s) : -1;

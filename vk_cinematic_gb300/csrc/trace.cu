@@ -7,7 +7,6 @@
 
 #include "gbsp_internal.h"
 #include "traverse.cuh"
-#include "traverse_dyn.cuh"
 
 namespace gbsp {
 
@@ -77,62 +76,9 @@ __global__ void __launch_bounds__(128) k_intersect(SceneView sv, const float4 *_
     warp_add_counters(counters, cnt, rays_done, hits);
 }
 
-// Ray batches through the dynamic-fetch traversal.
-struct BatchRayPolicy {
-    const float4 *rays;
-    float *tOut;
-    int32_t *triOut, *objOut;
-    float *attrOut;
-    uint32_t *matOut;
-    __device__ __forceinline__ void load(uint32_t i, V3 &o, V3 &d) const
-    {
-        float4 o4 = __ldg(rays + 2 * (size_t)i), d4 = __ldg(rays + 2 * (size_t)i + 1);
-        o = v3(o4.x, o4.y, o4.z);
-        d = v3(d4.x, d4.y, d4.z);
-    }
-    __device__ __forceinline__ void store(uint32_t i, const RayHit &h, const SceneView &sv) const
-    {
-        bool hit = h.prim >= 0;
-        if (tOut) tOut[i] = hit ? h.t : -1.0f;
-        if (triOut) triOut[i] = hit ? (int32_t)__ldg(sv.triIds + h.prim) : -1;
-        const Instance *in = hit ? sv.instances + h.inst : nullptr;
-        if (objOut) objOut[i] = hit ? (int32_t)__ldg(&in->objectIndex) : -1;
-        if (attrOut) {
-            float *a = attrOut + 6 * (size_t)i;
-            if (hit) {
-                V3 n;
-                float ux, uy;
-                hit_surface(sv, h, n, ux, uy);
-                a[0] = h.t;
-                a[1] = n.x;
-                a[2] = n.y;
-                a[3] = n.z;
-                a[4] = ux;
-                a[5] = uy;
-            } else {
-                a[0] = -1.0f;
-                a[1] = a[2] = a[3] = a[4] = a[5] = 0.0f;
-            }
-        }
-        if (matOut) matOut[i] = hit ? __ldg(&in->materialId) : 0u;
-    }
-};
-
-__global__ void __launch_bounds__(128) k_intersect_dyn(SceneView sv, const float4 *__restrict__ rays,
-    uint32_t count, float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut,
-    uint32_t *matOut, unsigned int *work, unsigned long long *counters, uint32_t *status)
-{
-    TraceCounters cnt = {0, 0, 0, 0, 0};
-    uint32_t done = 0, hits = 0;
-    BatchRayPolicy pol = {rays, tOut, triOut, objOut, attrOut, matOut};
-    dyn_trace_loop(pol, sv, count, work, status, cnt, done, hits);
-    warp_add_counters(counters, cnt, done, hits);
-}
-
 int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const float4 *rays,
     float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut, uint32_t *matOut,
-    const Instance *, int smCount, unsigned long long *counters, uint32_t *dStatus,
-    bool dynamicTrace)
+    const Instance *, int smCount, unsigned long long *counters, uint32_t *dStatus)
 {
     if (!count) return GBSP_OK;
     // the work counter lives in the last counter slot's neighbour block
@@ -141,12 +87,8 @@ int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const 
     int grid = smCount * 8;
     uint64_t needed = ((uint64_t)count + 127) / 128;
     if ((uint64_t)grid > needed) grid = (int)needed;
-    if (dynamicTrace)
-        k_intersect_dyn<<<grid, 128, 0, s>>>(sv, rays, count, tOut, triOut, objOut, attrOut,
-            matOut, work, counters, dStatus);
-    else
-        k_intersect<<<grid, 128, 0, s>>>(sv, rays, count, tOut, triOut, objOut, attrOut, matOut,
-            work, counters, dStatus);
+    k_intersect<<<grid, 128, 0, s>>>(sv, rays, count, tOut, triOut, objOut, attrOut, matOut, work,
+        counters, dStatus);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }

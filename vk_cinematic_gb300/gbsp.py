@@ -461,7 +461,7 @@ class Batch:
         return c
 
     def set_config(self, block=128, chunk=1, blocks_per_sm=8, use_graph=1,
-                   kernel=BATCH_PATH_STATE):
+                   kernel=BATCH_THREAD_PER_PIXEL):
         c = BatchConfig(block, chunk, blocks_per_sm, use_graph, kernel)
         _check(self.L.gbsp_batch_set_config(self.h, ctypes.byref(c)))
 
@@ -597,3 +597,16 @@ def create_irradiance_cube_map(equirect, width: int, height: int, spp: int = 32,
 
 def xorshift32_jump(state: int, steps: int) -> int:
     return int(load().gbsp_xorshift32_jump(_u32(state), ctypes.c_uint64(steps)))
+
+
+def tonemap(frame, out=None, stream: int = 0):
+    """gbsp_tonemap: (H, W, 4) float32 CUDA tensor -> (H, W) uint32 packed 8-bit RGBA."""
+    import torch
+
+    L = load()
+    n = frame.shape[0] * frame.shape[1]
+    if out is None:
+        out = torch.empty(frame.shape[:2], dtype=torch.int32, device=frame.device)
+    _check(L.gbsp_tonemap(_vp(stream), _vp(frame.data_ptr()), ctypes.c_uint64(n),
+                          _vp(out.data_ptr())))
+    return out
