@@ -79,6 +79,9 @@ extern "C" {
                                       (CUDA events around each launch) */
 #define GBSP_FLAG_AOV 2u           /* also write first-hit G-buffers, averaged over
                                       the samples (gbsp_frame_aov_device_pointer) */
+#define GBSP_FLAG_TRACE_PER_LANE 4u /* closest-hit kernel in which every lane fetches
+                                      its next ray as soon as its current one is done
+                                      (same results; a scheduling choice) */
 
 typedef struct gbsp_runtime gbsp_runtime;
 typedef struct gbsp_scene gbsp_scene;

@@ -144,6 +144,161 @@ __global__ void __launch_bounds__(128) k_trace(SceneView sv, const float4 *__res
     }
 }
 
+// Per-lane variant of k_trace (GBSP_FLAG_TRACE_PER_LANE).  Every lane keeps
+// its own ray and stack and advances by single steps (one stack pop: an
+// object- or mesh-level node visit, entering an object, one triangle leaf,
+// leaving an object); a lane whose ray is done takes the next queue index
+// straight away, so short rays no longer wait for the warp's longest one.
+// The fetch is a warp-aggregated atomic over the lanes that are idle at that
+// moment (__activemask), and a lane leaves the loop as soon as the queue is
+// exhausted: there is no whole-warp vote or shuffle inside the loop.  Same
+// candidate sets, arithmetic and tie rules as trace_closest, hence the same
+// hit records.
+constexpr uint32_t kMaxLaneRaySteps = 1u << 22;
+constexpr uint32_t kMaxLaneIterations = 1u << 28;
+
+__global__ void __launch_bounds__(128) k_trace_lane(SceneView sv, const float4 *__restrict__ rayO,
+    const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
+    unsigned int *ctl, unsigned long long *counters, uint32_t *status)
+{
+    const int lane = threadIdx.x & 31;
+    const uint32_t laneMaskLt = (1u << lane) - 1u;
+    const uint32_t count = *queueCount;
+    unsigned int *work = &ctl[kCtlTraceWork];
+    TraceCounters cnt = {0, 0, 0, 0, 0};
+    uint32_t done = 0, hits = 0;
+    uint32_t stackRef[kStackSize];
+    float stackT[kStackSize];
+    int sp = 0, base = 0;
+    int mode = 0;  // 0 needs a ray, 1 object level, 2 mesh level
+    uint32_t slot = 0, steps = 0, inst = 0;
+    V3 o = v3(0, 0, 0), d = v3(0, 0, 0), invd = v3(0, 0, 0);
+    float bestT = kInf, bestU = 0.0f, bestV = 0.0f;
+    int32_t bestPrim = -1, bestInst = -1;
+    V3 lo = v3(0, 0, 0), ld = v3(0, 0, 0), linvd = v3(0, 0, 0);
+    float len = 0.0f, lBestT = kInf, lU = 0.0f, lV = 0.0f;
+    int32_t lPrim = -1;
+    bool drained = false;
+    for (uint32_t it = 0; it < kMaxLaneIterations; it++) {
+        if (mode == 0) {
+            unsigned int m = __activemask();
+            int leader = __ffs(m) - 1;
+            uint32_t first = 0;
+            if (lane == leader) first = atomicAdd(work, (unsigned int)__popc(m));
+            first = __shfl_sync(m, first, leader);
+            uint32_t idx = first + __popc(m & laneMaskLt);
+            if (idx >= count) {
+                drained = true;
+                break;
+            }
+            slot = idx;
+            steps = 0;
+            float4 o4 = rayO[idx], d4 = rayD[idx];
+            o = v3(o4.x, o4.y, o4.z);
+            d = v3(d4.x, d4.y, d4.z);
+            invd = inverse(d);
+            bestT = kInf;
+            bestU = bestV = 0.0f;
+            bestPrim = bestInst = -1;
+            sp = 0;
+            if (sv.tlasRoot != kEmptyChild) {
+                stackRef[0] = sv.tlasRoot;
+                stackT[0] = 0.0f;
+                sp = 1;
+            }
+            mode = 1;
+        }
+        if (++steps > kMaxLaneRaySteps) {
+            atomicOr(status, kStatusRayStepLimit);
+            mode = 1;
+            sp = 0;  // store the best hit found so far
+        }
+        if (mode == 2 && sp == base) {
+            // leaving an object: its closest triangle goes back to world space
+            if (lPrim >= 0) {
+                const Instance &in = sv.instances[inst];
+                Affine model;
+#pragma unroll
+                for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
+                V3 worldHit = transform_point(model, add(lo, mul(ld, lBestT)));
+                float tw = dot(sub(worldHit, o), d);
+                if (tw < bestT || (tw == bestT && (int32_t)inst < bestInst)) {
+                    bestT = tw;
+                    bestU = lU;
+                    bestV = lV;
+                    bestPrim = lPrim;
+                    bestInst = (int32_t)inst;
+                }
+            }
+            mode = 1;
+        } else if (mode == 1 && sp == 0) {
+            hitA[slot] = make_int4(__float_as_int(bestT), __float_as_int(bestU),
+                __float_as_int(bestV), bestPrim);
+            hitInst[slot] = bestInst;
+            done++;
+            hits += (bestPrim >= 0 && bestT > 0.0f) ? 1u : 0u;
+            mode = 0;
+        } else {
+            sp--;
+            uint32_t ref = stackRef[sp];
+            float te = stackT[sp];
+            float bound = mode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * len));
+            if (te > bound) {
+                // pruned
+            } else if (!child_is_leaf(ref)) {
+                if (mode == 1)
+                    cnt.topNodes++;
+                else
+                    cnt.meshNodes++;
+                visit_node<true>(sv.nodes, ref, mode == 1 ? o : lo, mode == 1 ? invd : linvd,
+                    bound, stackRef, stackT, sp, status, cnt);
+            } else if (mode == 1) {
+                // an object whose world box passed: enter its mesh
+                inst = leaf_first(ref);
+                const Instance &in = sv.instances[inst];
+                Affine inv;
+#pragma unroll
+                for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
+                lo = transform_point(inv, o);
+                ld = normalize(transform_vector(inv, d), &len);
+                linvd = inverse(ld);
+                cnt.meshTests++;
+                lBestT = kInf;
+                lU = lV = 0.0f;
+                lPrim = -1;
+                base = sp;
+                if (sp >= kStackSize) {
+                    atomicOr(status, kStatusStackOverflow);
+                } else {
+                    stackRef[sp] = __ldg(&in.blasRoot);
+                    stackT[sp] = 0.0f;
+                    sp++;
+                    mode = 2;
+                }
+            } else {
+                visit_leaf<true>(sv, ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+            }
+        }
+    }
+    if (!drained) atomicOr(status, kStatusQueueOverflow);
+    __syncwarp();
+    uint32_t v[7] = {done, hits, cnt.topNodes, cnt.meshNodes, cnt.triTests, cnt.boxTests,
+        cnt.meshTests};
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+        for (int off = 16; off; off >>= 1) v[k] += __shfl_xor_sync(0xFFFFFFFFu, v[k], off);
+    if (lane == 0) {
+        atomicAdd(&counters[GBSP_METRIC_RAYS_TRACED], (unsigned long long)v[0]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_HIT_COUNT], (unsigned long long)v[1]);
+        atomicAdd(&counters[GBSP_METRIC_RAY_MISS_COUNT], (unsigned long long)(v[0] - v[1]));
+        atomicAdd(&counters[GBSP_METRIC_BROADPHASE_NODE_VISITS], (unsigned long long)v[2]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_NODE_VISITS], (unsigned long long)v[3]);
+        atomicAdd(&counters[GBSP_METRIC_TRIANGLE_TESTS], (unsigned long long)v[4]);
+        atomicAdd(&counters[GBSP_METRIC_MIDPHASE_BOX_TESTS], (unsigned long long)v[5]);
+        atomicAdd(&counters[GBSP_METRIC_MESH_TESTS_PERFORMED], (unsigned long long)v[6]);
+    }
+}
+
 __global__ void __launch_bounds__(128) k_shade(SceneView sv, MaterialView mv, WaveParams wp,
     WaveBuffers wb, uint32_t bounce, int inQueue, unsigned int *ctl, unsigned long long *counters)
 {
@@ -465,8 +620,12 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
                 const float4 *qD = wb.rayD + ((b & 1) ? cap : 0);
                 k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
                 int e0 = timing ? rt->stage_event(s) : -1;
-                k_trace<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA, wb.hitInst,
-                    ctl, counters, rt->dStatus);
+                if (opt.flags & GBSP_FLAG_TRACE_PER_LANE)
+                    k_trace_lane<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA,
+                        wb.hitInst, ctl, counters, rt->dStatus);
+                else
+                    k_trace<<<persistentGrid, 128, 0, s>>>(sv, qO, qD, ctl + inQ, wb.hitA,
+                        wb.hitInst, ctl, counters, rt->dStatus);
                 int e1 = timing ? rt->stage_event(s) : -1;
                 k_shade<<<persistentGrid, 128, 0, s>>>(sv, mv, wp, wb, b, inQ, ctl, counters);
                 int e2 = timing ? rt->stage_event(s) : -1;
