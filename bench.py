@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
+    ap.add_argument("--trace", choices=["warp", "lane"], default="warp",
+                    help="closest-hit scheduling: 32 rays per warp until all finish, or per-lane fetch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override (profiling cases only)")
@@ -323,8 +325,8 @@ def run_gpu(args):
     torch.cuda.set_stream(stream)
     rt = gbsp.Runtime(local, stream=stream.cuda_stream)
     s = make_scene(args.workload, rank)
-    opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed,
-                               flags=gbsp.FLAG_STAGE_TIMING)
+    flags = gbsp.FLAG_STAGE_TIMING | (gbsp.FLAG_TRACE_PER_LANE if args.trace == "lane" else 0)
+    opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed, flags=flags)
     scene, ms, rend = gbsp.upload_scene(rt, s, opt)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -429,7 +431,7 @@ def run_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded procedural scene", "config": workload_config(s, args.workload),
             "mrays_per_s": rays_all / (elapsed_ms / 1e3) / 1e6,
-            "parallelism": f"replicas x{world}",
+            "parallelism": f"replicas x{world}", "trace_scheduling": args.trace,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(M["kernel_launches"]), "clocks": clk,
             "metrics": {k: M[k] for k in ("paths_traced", "rays_traced", "ray_hit_count",

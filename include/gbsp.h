@@ -302,7 +302,9 @@ typedef struct {
     uint32_t chunk;        /* pixels a thread takes per queue pop: 1..8 */
     uint32_t blocksPerSm;  /* persistent grid = SM count * blocksPerSm */
     uint32_t useGraph;     /* 1 = replay a captured CUDA graph */
-    uint32_t kernel;       /* GBSP_BATCH_THREAD_PER_PIXEL or GBSP_BATCH_PATH_STATE */
+    uint32_t kernel;       /* GBSP_BATCH_WAVEFRONT, GBSP_BATCH_PATH_STATE or
+                              GBSP_BATCH_THREAD_PER_PIXEL */
+    uint32_t wavePaths;    /* wavefront: paths per wave (0 = 2^22) */
 } gbsp_batch_config;
 
 /* gbsp_batch_config.kernel: one thread traces a whole pixel (all samples,
@@ -312,6 +314,10 @@ typedef struct {
  * new pixels.  Both give identical images. */
 #define GBSP_BATCH_THREAD_PER_PIXEL 0u
 #define GBSP_BATCH_PATH_STATE 1u
+/* the frame renderer's stages (generate, per-bounce closest hit and shading
+ * over compacted queues, accumulate) over waves that pack the paths of
+ * several items; the whole sequence is one CUDA graph (default) */
+#define GBSP_BATCH_WAVEFRONT 2u
 
 int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t count,
     gbsp_batch **out);

@@ -41,9 +41,14 @@ def test_batch_matches_single_scene_renders(gpu_lib):
     torch.cuda.synchronize()
     batch = gbsp.Batch(rt, rends, [t.data_ptr() for t in imgs])
     total = sum(s.width * s.height * s.spp for s in ss)
-    for kernel, use_graph in ((gbsp.BATCH_THREAD_PER_PIXEL, 0), (gbsp.BATCH_THREAD_PER_PIXEL, 1),
-                              (gbsp.BATCH_PATH_STATE, 0), (gbsp.BATCH_PATH_STATE, 1)):
-        batch.set_config(block=128, chunk=1, blocks_per_sm=4, use_graph=use_graph, kernel=kernel)
+    # wavefront: one wave, then waves of 1,000 paths (items split across waves)
+    for kernel, use_graph, wave in ((gbsp.BATCH_THREAD_PER_PIXEL, 0, 0),
+                                    (gbsp.BATCH_THREAD_PER_PIXEL, 1, 0),
+                                    (gbsp.BATCH_PATH_STATE, 0, 0), (gbsp.BATCH_PATH_STATE, 1, 0),
+                                    (gbsp.BATCH_WAVEFRONT, 0, 0), (gbsp.BATCH_WAVEFRONT, 1, 0),
+                                    (gbsp.BATCH_WAVEFRONT, 1, 1000)):
+        batch.set_config(block=128, chunk=1, blocks_per_sm=4, use_graph=use_graph, kernel=kernel,
+                         wave_paths=wave)
         for _ in range(2):  # a replayed graph must reset its queue each time
             for t in imgs:
                 t.fill_(-1.0)
@@ -53,10 +58,11 @@ def test_batch_matches_single_scene_renders(gpu_lib):
             for k, (t, ref) in enumerate(zip(imgs, refs)):
                 got = t.cpu().numpy()
                 assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), \
-                    f"item {k} differs (kernel={kernel}, graph={use_graph})"
+                    f"item {k} differs (kernel={kernel}, graph={use_graph}, wave={wave})"
     best = batch.autotune(trials=1)
     assert best.block in (64, 128, 256)
-    assert best.kernel in (gbsp.BATCH_THREAD_PER_PIXEL, gbsp.BATCH_PATH_STATE)
+    assert best.kernel in (gbsp.BATCH_THREAD_PER_PIXEL, gbsp.BATCH_PATH_STATE,
+                           gbsp.BATCH_WAVEFRONT)
     for t in imgs:
         t.fill_(-1.0)
     torch.cuda.synchronize()

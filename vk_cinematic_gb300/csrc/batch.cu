@@ -12,8 +12,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "gbsp_internal.h"
-#include "shading.cuh"
+#include "wavefront.cuh"
 
 namespace gbsp {
 
@@ -25,9 +24,135 @@ struct BatchItemDev {
     CameraParams cam;
     float4 *image;
     uint64_t pixelBase;
+    uint64_t pathBase;  // first path of this item in the batch's path numbering
     uint32_t width, height, spp, maxBounces, seed, nanPolicy;
     float clampValue, invSpp;
 };
+
+// ---------------------------------------------------------------------------
+// Batched wavefront.  The items' paths are numbered back to back (item,
+// pixel, sample) and cut into waves of whole pixels; a wave may hold the
+// tail of one item and the heads of the next ones.  Every wave runs the
+// frame renderer's stages - generate, then per bounce the closest-hit and
+// shading kernels over one compacted queue, then accumulate - with each path
+// finding its scene, materials, bounce count and clamp through its item
+// (ManyScenes), so small scenes share waves instead of each running its own
+// short launches, and the whole sequence replays as one CUDA graph.  Per
+// pixel the same ordered Neumaier sum over the same per-sample seeds as a
+// single-scene render: images are bit-identical.
+// ---------------------------------------------------------------------------
+struct ManyScenes {
+    const BatchItemDev *items;
+    const uint32_t *pathItem;
+    __device__ __forceinline__ const SceneView &scene(uint32_t p) const
+    {
+        return items[__ldg(pathItem + p)].sv;
+    }
+    __device__ __forceinline__ const MaterialView &materials(uint32_t p) const
+    {
+        return items[__ldg(pathItem + p)].mv;
+    }
+    __device__ __forceinline__ uint32_t bounces(uint32_t p) const
+    {
+        return items[__ldg(pathItem + p)].maxBounces;
+    }
+    __device__ __forceinline__ float clamp(uint32_t p) const
+    {
+        return items[__ldg(pathItem + p)].clampValue;
+    }
+};
+
+struct BatchWave {
+    uint64_t pathBase, pixBase;
+    uint32_t paths, pixels, maxBounces;
+};
+
+__device__ __forceinline__ uint32_t find_item_by_path(const BatchItemDev *items, uint32_t n,
+    uint64_t gp)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (items[mid].pathBase <= gp)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t find_item_by_pixel(const BatchItemDev *items, uint32_t n,
+    uint64_t gq)
+{
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (items[mid].pixelBase <= gq)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_bgenerate(const BatchItemDev *__restrict__ items,
+    uint32_t itemCount, BatchWave wave, WaveBuffers wb, uint32_t *pathItem)
+{
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= wave.paths) return;
+    uint64_t gp = wave.pathBase + p;
+    uint32_t k = find_item_by_path(items, itemCount, gp);
+    const BatchItemDev &it = items[k];
+    uint64_t lp = gp - it.pathBase;
+    uint64_t pix = lp / it.spp;
+    uint32_t s = (uint32_t)(lp % it.spp);
+    uint32_t x = (uint32_t)(pix % it.width), y = (uint32_t)(pix / it.width);
+    uint32_t rng = sample_seed(it.seed, x, y, s);
+    V3 o, d;
+    camera_ray(it.cam, x, y, rng, o, d);
+    wb.rayO[p] = make_float4(o.x, o.y, o.z, __int_as_float((int)p));
+    wb.rayD[p] = make_float4(d.x, d.y, d.z, 0.0f);
+    wb.pathRng[p] = rng;
+    wb.pathLen[p] = 0;
+    pathItem[p] = k;
+}
+
+__global__ void __launch_bounds__(256) k_baccumulate(const BatchItemDev *__restrict__ items,
+    uint32_t itemCount, BatchWave wave, WaveBuffers wb, unsigned long long *counters)
+{
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t nans = 0;
+    if (k < wave.pixels) {
+        uint64_t gq = wave.pixBase + k;
+        const BatchItemDev &it = items[find_item_by_pixel(items, itemCount, gq)];
+        uint64_t lq = gq - it.pixelBase;
+        uint32_t x = (uint32_t)(lq % it.width), y = (uint32_t)(lq / it.width);
+        size_t first = (size_t)(it.pathBase + lq * it.spp - wave.pathBase);
+        CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+        for (uint32_t s = 0; s < it.spp; s++) {
+            float4 r = wb.pathRad[first + s];
+            if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
+                nans++;
+                if (it.nanPolicy == GBSP_NAN_ZERO) continue;
+            }
+            csum_add(acc[0], r.x * it.invSpp);
+            csum_add(acc[1], r.y * it.invSpp);
+            csum_add(acc[2], r.z * it.invSpp);
+        }
+        it.image[(size_t)y * it.width + x] =
+            make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
+    }
+    for (int off = 16; off; off >>= 1) nans += __shfl_xor_sync(0xFFFFFFFFu, nans, off);
+    if ((threadIdx.x & 31) == 0 && nans)
+        atomicAdd(&counters[GBSP_METRIC_NAN_SAMPLES], (unsigned long long)nans);
+}
+
+// zero-bounce items: every path of the wave has radiance 0
+__global__ void k_bzero(WaveBuffers wb, uint32_t paths)
+{
+    uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < paths) wb.pathRad[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
 
 __global__ void k_batch_reset(unsigned long long *work, unsigned long long *counters)
 {
@@ -389,9 +514,105 @@ struct gbsp_batch {
     DeviceBuffer<int32_t> dSlots;
     DeviceBuffer<unsigned long long> dWork;
     uint64_t totalPixels = 0, totalPaths = 0;
-    gbsp_batch_config cfg = {128, 1, 8, 1, GBSP_BATCH_THREAD_PER_PIXEL};
+    gbsp_batch_config cfg = {128, 1, 8, 1, GBSP_BATCH_WAVEFRONT, 0};
     cudaGraphExec_t exec = nullptr;
+    // batched wavefront
+    std::vector<BatchItemDev> hostItems;
+    std::vector<BatchWave> waves;
+    uint32_t waveCap = 0, waveBounces = 0;
+    DeviceBuffer<float4> rayO, rayD, vertE, vertA, pathRad;
+    DeviceBuffer<int4> hitA;
+    DeviceBuffer<int> hitInst;
+    DeviceBuffer<uint32_t> pathRng, pathLen, pathItem;
 };
+
+// Cuts the items' paths into waves of whole pixels of at most `cap` paths
+// and reserves the wave buffers (once).
+static int plan_waves(gbsp_batch *b)
+{
+    const std::vector<BatchItemDev> &dev = b->hostItems;
+    uint64_t want = b->cfg.wavePaths ? b->cfg.wavePaths : (1ull << 22);
+    uint64_t cap = std::min<uint64_t>(want, std::max<uint64_t>(b->totalPaths, 1));
+    uint32_t maxSpp = 1, maxB = 1;
+    for (const BatchItemDev &d : dev) {
+        maxSpp = std::max(maxSpp, d.spp);
+        maxB = std::max(maxB, d.maxBounces);
+    }
+    cap = std::max<uint64_t>(cap, maxSpp);
+    b->waves.clear();
+    BatchWave w = {0, 0, 0, 0, 0};
+    for (const BatchItemDev &d : dev) {
+        uint64_t pixels = (uint64_t)d.width * d.height;
+        for (uint64_t q = 0; q < pixels;) {
+            if (w.paths + (uint64_t)d.spp > cap) {
+                b->waves.push_back(w);
+                w = {w.pathBase + w.paths, w.pixBase + w.pixels, 0, 0, 0};
+            }
+            // as many whole pixels of this item as still fit
+            uint64_t fit = std::min<uint64_t>(pixels - q, (cap - w.paths) / d.spp);
+            w.paths += (uint32_t)(fit * d.spp);
+            w.pixels += (uint32_t)fit;
+            w.maxBounces = std::max(w.maxBounces, d.maxBounces);
+            q += fit;
+        }
+    }
+    if (w.paths) b->waves.push_back(w);
+    b->waveCap = (uint32_t)cap;
+    b->waveBounces = maxB;
+    cudaStream_t s = b->rt->stream;
+    size_t c = cap;
+    int rc;
+    if ((rc = b->rayO.reserve(2 * c, s)) || (rc = b->rayD.reserve(2 * c, s)) ||
+        (rc = b->hitA.reserve(c, s)) || (rc = b->hitInst.reserve(c, s)) ||
+        (rc = b->pathRng.reserve(c, s)) || (rc = b->pathLen.reserve(c, s)) ||
+        (rc = b->pathItem.reserve(c, s)) || (rc = b->vertE.reserve((size_t)maxB * c, s)) ||
+        (rc = b->vertA.reserve((size_t)maxB * c, s)) || (rc = b->pathRad.reserve(c, s)))
+        return rc;
+    return GBSP_OK;
+}
+
+static void enqueue_wavefront(gbsp_batch *b)
+{
+    gbsp_runtime *rt = b->rt;
+    cudaStream_t s = rt->stream;
+    unsigned long long *counters = rt->dCounters;
+    unsigned int *ctl = reinterpret_cast<unsigned int *>(rt->dCounters + GBSP_METRIC_COUNT);
+    WaveBuffers wb;
+    wb.rayO = b->rayO.ptr;
+    wb.rayD = b->rayD.ptr;
+    wb.hitA = b->hitA.ptr;
+    wb.hitInst = b->hitInst.ptr;
+    wb.pathRng = b->pathRng.ptr;
+    wb.pathLen = b->pathLen.ptr;
+    wb.vertE = b->vertE.ptr;
+    wb.vertA = b->vertA.ptr;
+    wb.pathRad = b->pathRad.ptr;
+    wb.pathAov = nullptr;
+    wb.cap = b->waveCap;
+    ManyScenes src = {b->dItems.ptr, b->pathItem.ptr};
+    uint32_t n = (uint32_t)b->items.size();
+    int grid = rt->smCount * (int)b->cfg.blocksPerSm;
+    for (const BatchWave &w : b->waves) {
+        k_reset_ctl<<<1, 32, 0, s>>>(ctl, w.paths);
+        if (w.maxBounces == 0) {
+            k_bzero<<<(w.paths + 255) / 256, 256, 0, s>>>(wb, w.paths);
+        } else {
+            k_bgenerate<<<(w.paths + 255) / 256, 256, 0, s>>>(b->dItems.ptr, n, w, wb,
+                b->pathItem.ptr);
+        }
+        for (uint32_t bn = 0; bn < w.maxBounces; bn++) {
+            int inQ = (bn & 1) ? kCtlQueue1 : kCtlQueue0;
+            int outQ = (bn & 1) ? kCtlQueue0 : kCtlQueue1;
+            const float4 *qO = wb.rayO + ((bn & 1) ? wb.cap : 0);
+            const float4 *qD = wb.rayD + ((bn & 1) ? wb.cap : 0);
+            k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
+            k_trace<<<grid, 128, 0, s>>>(src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl,
+                counters, rt->dStatus);
+            k_shade<<<grid, 128, 0, s>>>(src, wb, bn, inQ, ctl, counters);
+        }
+        k_baccumulate<<<(w.pixels + 255) / 256, 256, 0, s>>>(b->dItems.ptr, n, w, wb, counters);
+    }
+}
 
 static void drop_graph(gbsp_batch *b)
 {
@@ -405,7 +626,9 @@ static int enqueue(gbsp_batch *b)
     cudaStream_t s = rt->stream;
     k_batch_reset<<<1, 32, 0, s>>>(b->dWork.ptr, rt->dCounters);
     int grid = rt->smCount * (int)b->cfg.blocksPerSm;
-    if (b->cfg.kernel == GBSP_BATCH_PATH_STATE)
+    if (b->cfg.kernel == GBSP_BATCH_WAVEFRONT)
+        enqueue_wavefront(b);
+    else if (b->cfg.kernel == GBSP_BATCH_PATH_STATE)
         k_batch_sm<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(),
             b->totalPixels, b->dWork.ptr, rt->dCounters, rt->dStatus);
     else
@@ -442,7 +665,8 @@ static int launch_once(gbsp_batch *b)
 
 static int check_config(const gbsp_batch_config *c)
 {
-    if (c->kernel != GBSP_BATCH_THREAD_PER_PIXEL && c->kernel != GBSP_BATCH_PATH_STATE)
+    if (c->kernel != GBSP_BATCH_THREAD_PER_PIXEL && c->kernel != GBSP_BATCH_PATH_STATE &&
+        c->kernel != GBSP_BATCH_WAVEFRONT)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "unknown batch kernel %u", c->kernel);
     if (c->block != 64 && c->block != 128 && c->block != 256)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "block must be 64, 128 or 256");
@@ -513,6 +737,7 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
         d.cam.height = c->imagePlane->height;
         d.image = reinterpret_cast<float4 *>(it.deviceImage);
         d.pixelBase = base;
+        d.pathBase = b->totalPaths;
         d.width = c->imagePlane->width;
         d.height = c->imagePlane->height;
         d.spp = it.options.spp ? it.options.spp : 1;
@@ -532,6 +757,11 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
         rc = b->dItems.upload(dev.data(), dev.size(), s);
     }
     if (!rc) rc = b->dWork.reserve(1, s);
+    if (!rc) {
+        b->hostItems = dev;
+        b->totalPixels = base;
+        rc = plan_waves(b);
+    }
     if (!rc && cudaStreamSynchronize(s) != cudaSuccess)
         rc = set_error(GBSP_ERR_CUDA, "batch upload failed");
     if (rc) {
@@ -560,8 +790,10 @@ int gbsp_batch_set_config(gbsp_batch *batch, const gbsp_batch_config *config)
     if (!batch || !config) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
     int rc = check_config(config);
     if (rc) return rc;
+    bool replan = config->wavePaths != batch->cfg.wavePaths;
     batch->cfg = *config;
     drop_graph(batch);
+    if (replan) return plan_waves(batch);
     return GBSP_OK;
 }
 
@@ -610,13 +842,15 @@ int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *b
     const uint32_t perSm[] = {2, 4, 8};
     gbsp_batch_config keep = batch->cfg, bestCfg = batch->cfg;
     float bestMs = 3.0e38f;
-    for (uint32_t kern : {GBSP_BATCH_THREAD_PER_PIXEL, GBSP_BATCH_PATH_STATE})
+    for (uint32_t kern : {GBSP_BATCH_THREAD_PER_PIXEL, GBSP_BATCH_PATH_STATE, GBSP_BATCH_WAVEFRONT})
     for (uint32_t bl : blocks)
         for (uint32_t ch : chunks)
             for (uint32_t ps : perSm) {
-                // the state machine ignores chunk and takes at most 128 threads
+                // the state machine ignores chunk and takes at most 128 threads; the
+                // wavefront's stage kernels have fixed block sizes (persistent grid = ps per SM)
                 if (kern == GBSP_BATCH_PATH_STATE && (bl > 128 || ch != 1)) continue;
-                gbsp_batch_config c = {bl, ch, ps, keep.useGraph, kern};
+                if (kern == GBSP_BATCH_WAVEFRONT && (bl != 128 || ch != 1)) continue;
+                gbsp_batch_config c = {bl, ch, ps, keep.useGraph, kern, keep.wavePaths};
                 batch->cfg = c;
                 drop_graph(batch);
                 int rc = launch_once(batch);  // warm-up (and graph capture)

@@ -425,16 +425,19 @@ class BatchItem(ctypes.Structure):
 
 BATCH_THREAD_PER_PIXEL = 0
 BATCH_PATH_STATE = 1
-BATCH_KERNEL_NAMES = {BATCH_THREAD_PER_PIXEL: "thread_per_pixel", BATCH_PATH_STATE: "path_state"}
+BATCH_WAVEFRONT = 2
+BATCH_KERNEL_NAMES = {BATCH_THREAD_PER_PIXEL: "thread_per_pixel", BATCH_PATH_STATE: "path_state",
+                      BATCH_WAVEFRONT: "wavefront"}
 
 
 class BatchConfig(ctypes.Structure):
     _fields_ = [("block", _u32), ("chunk", _u32), ("blocksPerSm", _u32), ("useGraph", _u32),
-                ("kernel", _u32)]
+                ("kernel", _u32), ("wavePaths", _u32)]
 
     def as_dict(self):
         return dict(kernel=BATCH_KERNEL_NAMES[self.kernel], block=self.block, chunk=self.chunk,
-                    blocks_per_sm=self.blocksPerSm, use_graph=self.useGraph)
+                    blocks_per_sm=self.blocksPerSm, use_graph=self.useGraph,
+                    wave_paths=self.wavePaths)
 
 
 class Batch:
@@ -462,8 +465,8 @@ class Batch:
         return c
 
     def set_config(self, block=128, chunk=1, blocks_per_sm=8, use_graph=1,
-                   kernel=BATCH_THREAD_PER_PIXEL):
-        c = BatchConfig(block, chunk, blocks_per_sm, use_graph, kernel)
+                   kernel=BATCH_WAVEFRONT, wave_paths=0):
+        c = BatchConfig(block, chunk, blocks_per_sm, use_graph, kernel, wave_paths)
         _check(self.L.gbsp_batch_set_config(self.h, ctypes.byref(c)))
 
     def autotune(self, trials=2) -> BatchConfig:
