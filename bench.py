@@ -68,8 +68,9 @@ def parse_args():
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
-    ap.add_argument("--trace", choices=["warp", "lane"], default="warp",
-                    help="closest-hit scheduling: 32 rays per warp until all finish, or per-lane fetch")
+    ap.add_argument("--trace", choices=["hybrid", "warp", "lane"], default="hybrid",
+                    help="closest-hit scheduling: per-warp for primary and per-lane for bounce "
+                         "rays (library default), or one of the two for every bounce")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override (profiling cases only)")
@@ -325,7 +326,8 @@ def run_gpu(args):
     torch.cuda.set_stream(stream)
     rt = gbsp.Runtime(local, stream=stream.cuda_stream)
     s = make_scene(args.workload, rank)
-    flags = gbsp.FLAG_STAGE_TIMING | (gbsp.FLAG_TRACE_PER_LANE if args.trace == "lane" else 0)
+    flags = gbsp.FLAG_STAGE_TIMING | {"hybrid": 0, "lane": gbsp.FLAG_TRACE_PER_LANE,
+                                      "warp": gbsp.FLAG_TRACE_PER_WARP}[args.trace]
     opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed, flags=flags)
     scene, ms, rend = gbsp.upload_scene(rt, s, opt)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")

@@ -79,9 +79,12 @@ extern "C" {
                                       (CUDA events around each launch) */
 #define GBSP_FLAG_AOV 2u           /* also write first-hit G-buffers, averaged over
                                       the samples (gbsp_frame_aov_device_pointer) */
-#define GBSP_FLAG_TRACE_PER_LANE 4u /* closest-hit kernel in which every lane fetches
-                                      its next ray as soon as its current one is done
-                                      (same results; a scheduling choice) */
+/* Closest-hit scheduling (same results, different speed).  By default primary
+ * rays (coherent) run one ray per lane until the warp's 32 rays are done, and
+ * bounce rays (incoherent) run per-lane: a lane fetches its next ray as soon as
+ * its current one is done.  The flags force one scheduling for every bounce. */
+#define GBSP_FLAG_TRACE_PER_LANE 4u
+#define GBSP_FLAG_TRACE_PER_WARP 8u
 
 typedef struct gbsp_runtime gbsp_runtime;
 typedef struct gbsp_scene gbsp_scene;

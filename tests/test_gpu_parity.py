@@ -299,8 +299,8 @@ def test_tonemap_matches_oracle(rt, port):
 
 @pytest.mark.parametrize("kind", ["config1", "config3_small", "crop_spp64"])
 def test_per_lane_trace_matches_static(rt, kind):
-    """GBSP_FLAG_TRACE_PER_LANE changes only the scheduling of the closest-hit
-    kernel: images and every counter must match the default kernel bit for bit."""
+    """The closest-hit scheduling flags (per warp, per lane, the default mix)
+    change only scheduling: images and every counter match bit for bit."""
     from vk_cinematic_gb300 import scenes
 
     if kind == "config1":
@@ -313,14 +313,15 @@ def test_per_lane_trace_matches_static(rt, kind):
         s = scenes.config3_scene(width=1920, height=1080, spp=64, n_spheres=64, level=3, seed=0)
         region = (1578, 647, 1578 + 64, 647 + 64)
     out = []
-    for flags in (0, gbsp.FLAG_TRACE_PER_LANE):
+    for flags in (gbsp.FLAG_TRACE_PER_WARP, gbsp.FLAG_TRACE_PER_LANE, 0):
         scene, ms, rend = gbsp.upload_scene(rt, s)
         rend.options.flags = flags
         img, _, m = rend.tile(region)
         out.append((img, m.as_dict()))
-    (a, ma), (b, mb) = out
-    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
-    for k in ("paths_traced", "rays_traced", "ray_hit_count", "midphase_node_visits",
-              "triangle_tests", "midphase_box_tests", "mesh_tests_performed",
-              "broadphase_node_visits"):
-        assert ma[k] == mb[k], (k, ma[k], mb[k])
+    a, ma = out[0]
+    for b, mb in out[1:]:
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        for k in ("paths_traced", "rays_traced", "ray_hit_count", "midphase_node_visits",
+                  "triangle_tests", "midphase_box_tests", "mesh_tests_performed",
+                  "broadphase_node_visits"):
+            assert ma[k] == mb[k], (k, ma[k], mb[k])

@@ -606,8 +606,13 @@ static void enqueue_wavefront(gbsp_batch *b)
             const float4 *qO = wb.rayO + ((bn & 1) ? wb.cap : 0);
             const float4 *qD = wb.rayD + ((bn & 1) ? wb.cap : 0);
             k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
-            k_trace<<<grid, 128, 0, s>>>(src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl,
-                counters, rt->dStatus);
+            // primary rays per warp, bounce rays per lane (the frame renderer's default)
+            if (bn == 0)
+                k_trace<<<grid, 128, 0, s>>>(src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl,
+                    counters, rt->dStatus);
+            else
+                k_trace_lane<<<grid, 128, 0, s>>>(src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl,
+                    counters, rt->dStatus);
             k_shade<<<grid, 128, 0, s>>>(src, wb, bn, inQ, ctl, counters);
         }
         k_baccumulate<<<(w.pixels + 255) / 256, 256, 0, s>>>(b->dItems.ptr, n, w, wb, counters);

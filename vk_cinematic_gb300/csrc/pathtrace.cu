@@ -219,7 +219,9 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
                 const float4 *qD = wb.rayD + ((b & 1) ? cap : 0);
                 k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
                 int e0 = timing ? rt->stage_event(s) : -1;
-                if (opt.flags & GBSP_FLAG_TRACE_PER_LANE)
+                bool perLane = (opt.flags & GBSP_FLAG_TRACE_PER_LANE) ||
+                    (!(opt.flags & GBSP_FLAG_TRACE_PER_WARP) && b > 0);
+                if (perLane)
                     k_trace_lane<<<persistentGrid, 128, 0, s>>>(one, qO, qD, ctl + inQ, wb.hitA,
                         wb.hitInst, ctl, counters, rt->dStatus);
                 else

@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict
     }
 }
 
-// Per-lane variant of k_trace (GBSP_FLAG_TRACE_PER_LANE).  Every lane keeps
+// Per-lane variant of k_trace (bounce rays by default).  Every lane keeps
 // its own ray and stack and advances by single steps (one stack pop: an
 // object- or mesh-level node visit, entering an object, one triangle leaf,
 // leaving an object); a lane whose ray is done takes the next queue index

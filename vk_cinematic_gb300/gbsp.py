@@ -65,6 +65,7 @@ class Options(ctypes.Structure):
 FLAG_STAGE_TIMING = 1
 FLAG_AOV = 2
 FLAG_TRACE_PER_LANE = 4
+FLAG_TRACE_PER_WARP = 8
 
 
 class ImagePlane(ctypes.Structure):
