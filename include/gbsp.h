@@ -327,8 +327,10 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
 int gbsp_batch_destroy(gbsp_batch *batch);
 int gbsp_batch_set_config(gbsp_batch *batch, const gbsp_batch_config *config);
 int gbsp_batch_get_config(const gbsp_batch *batch, gbsp_batch_config *config);
-/* Times every candidate configuration (kernel x block x chunk x blocks per SM) over
- * `trials` launches each and keeps the fastest; *best receives it. */
+/* Times every candidate configuration (36: thread-per-pixel block x chunk x
+ * blocks per SM, path-state block x blocks per SM, wavefront blocks per SM x
+ * wave size 2^22..2^24) over `trials` launches each and keeps the fastest;
+ * *best receives it. */
 int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best);
 /* Renders every item.  metrics NULL: asynchronous on the runtime's stream. */
 int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics);

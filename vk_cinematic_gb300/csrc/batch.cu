@@ -842,38 +842,47 @@ int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *b
     gbsp_runtime *rt = batch->rt;
     cudaStream_t s = rt->stream;
     if (trials == 0) trials = 1;
-    const uint32_t blocks[] = {64, 128, 256};
-    const uint32_t chunks[] = {1, 4};
-    const uint32_t perSm[] = {2, 4, 8};
-    gbsp_batch_config keep = batch->cfg, bestCfg = batch->cfg;
+    gbsp_batch_config keep = batch->cfg;
+    // candidates: thread-per-pixel (block x chunk x blocks per SM), path state
+    // (block <= 128 x blocks per SM), wavefront (blocks per SM x wave size)
+    std::vector<gbsp_batch_config> cands;
+    for (uint32_t ps : {2u, 4u, 8u}) {
+        for (uint32_t bl : {64u, 128u, 256u})
+            for (uint32_t ch : {1u, 4u})
+                cands.push_back({bl, ch, ps, keep.useGraph, GBSP_BATCH_THREAD_PER_PIXEL, keep.wavePaths});
+        for (uint32_t bl : {64u, 128u})
+            cands.push_back({bl, 1, ps, keep.useGraph, GBSP_BATCH_PATH_STATE, keep.wavePaths});
+        for (uint32_t wave : {1u << 22, 1u << 23, 1u << 24})
+            cands.push_back({128, 1, ps, keep.useGraph, GBSP_BATCH_WAVEFRONT, wave});
+    }
+    gbsp_batch_config bestCfg = keep;
     float bestMs = 3.0e38f;
-    for (uint32_t kern : {GBSP_BATCH_THREAD_PER_PIXEL, GBSP_BATCH_PATH_STATE, GBSP_BATCH_WAVEFRONT})
-    for (uint32_t bl : blocks)
-        for (uint32_t ch : chunks)
-            for (uint32_t ps : perSm) {
-                // the state machine ignores chunk and takes at most 128 threads; the
-                // wavefront's stage kernels have fixed block sizes (persistent grid = ps per SM)
-                if (kern == GBSP_BATCH_PATH_STATE && (bl > 128 || ch != 1)) continue;
-                if (kern == GBSP_BATCH_WAVEFRONT && (bl != 128 || ch != 1)) continue;
-                gbsp_batch_config c = {bl, ch, ps, keep.useGraph, kern, keep.wavePaths};
-                batch->cfg = c;
-                drop_graph(batch);
-                int rc = launch_once(batch);  // warm-up (and graph capture)
-                if (rc) return rc;
-                GBSP_CUDA_TRY(cudaEventRecord(rt->ev[2], s));
-                for (uint32_t t = 0; t < trials; t++)
-                    if ((rc = launch_once(batch))) return rc;
-                GBSP_CUDA_TRY(cudaEventRecord(rt->ev[3], s));
-                GBSP_CUDA_TRY(cudaEventSynchronize(rt->ev[3]));
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, rt->ev[2], rt->ev[3]);
-                if (ms < bestMs) {
-                    bestMs = ms;
-                    bestCfg = c;
-                }
-            }
+    for (const gbsp_batch_config &c : cands) {
+        bool replan = c.wavePaths != batch->cfg.wavePaths;
+        batch->cfg = c;
+        drop_graph(batch);
+        int rc = replan ? plan_waves(batch) : GBSP_OK;
+        if (!rc) rc = launch_once(batch);  // warm-up (and graph capture)
+        if (rc) return rc;
+        GBSP_CUDA_TRY(cudaEventRecord(rt->ev[2], s));
+        for (uint32_t t = 0; t < trials; t++)
+            if ((rc = launch_once(batch))) return rc;
+        GBSP_CUDA_TRY(cudaEventRecord(rt->ev[3], s));
+        GBSP_CUDA_TRY(cudaEventSynchronize(rt->ev[3]));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, rt->ev[2], rt->ev[3]);
+        if (ms < bestMs) {
+            bestMs = ms;
+            bestCfg = c;
+        }
+    }
+    bool replan = bestCfg.wavePaths != batch->cfg.wavePaths;
     batch->cfg = bestCfg;
     drop_graph(batch);
+    if (replan) {
+        int rc = plan_waves(batch);
+        if (rc) return rc;
+    }
     if (best) *best = bestCfg;
     uint32_t st = 0;
     GBSP_CUDA_TRY(cudaMemcpyAsync(&st, rt->dStatus, 4, cudaMemcpyDeviceToHost, s));
