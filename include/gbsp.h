@@ -430,6 +430,15 @@ int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint
 int gbsp_dn_conv3x3_forward(void *stream, const uint16_t *in, uint32_t B, uint32_t H, uint32_t W,
     uint32_t cin, const uint16_t *weights, const float *bias, uint32_t cout, int epilogue,
     uint16_t *outBf16, float *outF32);
+/* The same convolution on the 5th-generation tensor cores (tcgen05.mma,
+ * accumulator in tensor memory), 128-pixel tiles; tensors 16-byte aligned.
+ * Same instantiations and epilogues. */
+int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uint32_t H,
+    uint32_t W, uint32_t cin, const uint16_t *weights, const float *bias, uint32_t cout,
+    int epilogue, uint16_t *outBf16, float *outF32);
+/* Reads and clears the denoiser kernels' device status word (1 = a tensor-core
+ * completion wait ran out); GBSP_ERR_DEVICE_STATUS when it was set. */
+int gbsp_dn_status(uint32_t *status);
 /* wt[8-tap][ci][co] = w[tap][co][ci]: weights of the data-gradient conv. */
 int gbsp_dn_flip_transpose(void *stream, const uint16_t *w, uint32_t cout, uint32_t cin,
     uint16_t *wt);

@@ -61,6 +61,46 @@ def test_conv3x3_forward_matches_torch(gpu_lib, cin, cout, epi):
     assert ok
 
 
+@pytest.mark.parametrize("cin,cout,epi", [(16, 48, 0), (48, 48, 0), (48, 32, 1), (48, 48, 2),
+                                          (32, 48, 2)])
+@pytest.mark.parametrize("W", [128, 200])
+def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, W):
+    """The tcgen05 convolution (accumulator in tensor memory) against torch and
+    against the mma.sync kernel; W = 200 leaves a partial 128-pixel tile."""
+    import torch
+
+    from vk_cinematic_gb300.denoiser import _ptr, _stream
+
+    torch.manual_seed(cin * 100 + cout + epi + W)
+    B, H = 2, 5
+    x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+    w = (torch.randn((9, cout, cin), device="cuda") * 0.2).to(torch.bfloat16)
+    bias = torch.randn(cout, device="cuda")
+    L = gbsp.load()
+    outs = []
+    for fn in (L.gbsp_dn_conv3x3_forward_tc, L.gbsp_dn_conv3x3_forward):
+        if epi == 0:
+            out = torch.full((B, H, W, cout), 7.0, dtype=torch.bfloat16, device="cuda")
+            rc = fn(_stream(), _ptr(x), B, H, W, cin, _ptr(w), _ptr(bias), cout, epi, _ptr(out),
+                    None)
+        else:
+            out = torch.full((B, H, W, cout), 7.0, dtype=torch.float32, device="cuda")
+            rc = fn(_stream(), _ptr(x), B, H, W, cin, _ptr(w), _ptr(bias) if epi == 1 else None,
+                    cout, epi, None, _ptr(out))
+        assert rc == 0, L.gbsp_last_error_string()
+        outs.append(out)
+    torch.cuda.synchronize()
+    st = ctypes.c_uint32(0)
+    assert L.gbsp_dn_status(ctypes.byref(st)) == 0, st.value
+    ref = torch_conv(x, w, bias if epi != 2 else None)
+    if epi == 0:
+        ref = torch.relu(ref)
+    err, ok = close(outs[0], ref)
+    err2, ok2 = close(outs[0], outs[1], rtol=1e-2 if epi == 0 else 1e-4)
+    print(f"tcgen05 conv {cin}->{cout} epi {epi} W {W}: vs torch {err:.2e}, vs mma.sync {err2:.2e}")
+    assert ok and ok2
+
+
 def test_conv_gradients_match_autograd(gpu_lib):
     import torch
 

@@ -149,6 +149,225 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
     return GBSP_OK;
 }
 
+// ---------------------------------------------------------------------------
+// conv3x3 on the 5th-generation tensor cores (tcgen05).
+//
+// Same GEMM as k_conv3x3 with a 128-pixel tile: M = 128 pixels of one image
+// row, N = COUT, K = 9 taps x CIN.  One elected thread issues
+// tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 -> FP32) for every
+// (tap, 16-channel slice): 9 * CIN / 16 instructions of 128 x COUT x 16 per
+// tile, accumulating in tensor memory; both operands are read straight from
+// shared memory through matrix descriptors, so the 3x3 neighbourhood is never
+// expanded: a tap is just a 16-byte-granular offset of the A descriptor into
+// the staged input rows.
+//
+// Shared memory holds the operands in the canonical no-swizzle K-major
+// layout: 8 x 16-byte core matrices (8 rows of 8 BF16 channels), rows
+// contiguous.  Input tile: [3 rows][CIN/8 channel groups][130 pixels][16 B]
+// (a core matrix = 8 consecutive pixels of one channel group, so a tap's
+// pixel shift moves the start address by 16 B); weights:
+// [9 taps][CIN/8 groups][COUT][16 B].  Descriptor strides: leading (K) =
+// next channel group, stride (M or N) = next 8 rows = 128 B.
+//
+// The accumulator (128 lanes x COUT FP32 columns) is read back by the four
+// warps with tcgen05.ld (warp w owns lanes 32w..32w+31, i.e. pixels
+// 32w..32w+31 of the tile) for the bias / ReLU / store epilogue.  The MMA
+// completion is signalled by tcgen05.commit on an mbarrier; every wait is
+// bounded and a timeout sets g_dnStatus instead of spinning.
+// ---------------------------------------------------------------------------
+constexpr int kTcTileP = 128;
+constexpr int kTcSpx = kTcTileP + 2;
+constexpr uint32_t kTcWaitLimit = 1u << 26;
+constexpr size_t kTcGuardBytes = 36 * 1024;
+
+__device__ uint32_t g_dnStatus;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start >> 4 (bits 0-13), leading-dimension
+// byte offset >> 4 (16-29), stride-dimension byte offset >> 4 (32-45),
+// descriptor version 1 (bits 46-47), base offset 0, no swizzle (bits 61-63 = 0).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+        ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
+template <int M, int N>
+__device__ __forceinline__ uint32_t instr_desc_bf16()
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+        ((uint32_t)(M >> 4) << 24);
+}
+
+template <int CIN, int COUT, int EPI>
+__global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, int B,
+    int H, int W, const __nv_bfloat16 *__restrict__ w, const float *__restrict__ bias,
+    __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
+{
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tcgen05 tile shape");
+    constexpr int KG = CIN / 8;                    // 16-byte channel groups
+    constexpr int TMEM_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+    extern __shared__ __align__(128) unsigned char smemRaw[];
+    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);          // [9][KG][COUT]
+    uint4 *sIn = sW + 9 * KG * COUT;                         // [3][KG][kTcSpx]
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmemBase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // weights -> canonical layout: (tap, kg, co) holds w[tap][co][8 kg .. 8 kg + 7]
+    for (int i = tid; i < 9 * KG * COUT; i += 128) {
+        int co = i % COUT, kg = (i / COUT) % KG, tap = i / (COUT * KG);
+        sW[i] = reinterpret_cast<const uint4 *>(w)[((size_t)tap * COUT + co) * KG + kg];
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmemBase)), "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmemBase;
+    const uint32_t idesc = instr_desc_bf16<kTcTileP, COUT>();
+    const uint32_t sInAddr = smem_u32(sIn), sWAddr = smem_u32(sW);
+
+    const int tilesPerRow = (W + kTcTileP - 1) / kTcTileP;
+    const int numTiles = tilesPerRow * B * H;
+    uint32_t phase = 0;
+    bool failed = false;
+    for (int tile = blockIdx.x; tile < numTiles && !failed; tile += gridDim.x) {
+        const int row = tile / tilesPerRow;  // b * H + y
+        const int x0 = (tile % tilesPerRow) * kTcTileP;
+        const int b = row / H, y = row % H;
+        // stage the three input rows (zero outside the image)
+        for (int i = tid; i < 3 * KG * kTcSpx; i += 128) {
+            int px = i % kTcSpx, kg = (i / kTcSpx) % KG, ry = i / (kTcSpx * KG);
+            int gy = y + ry - 1, gx = x0 + px - 1;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+                v = reinterpret_cast<const uint4 *>(in)[((size_t)(b * H + gy) * W + gx) * KG + kg];
+            sIn[i] = v;
+        }
+        // make the generic-proxy stores visible to the tensor core (async proxy)
+        asm volatile("fence.proxy.async.shared::cta;");
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (tid == 0) {
+#pragma unroll 1
+            for (int tap = 0; tap < 9; tap++) {
+                const int ty = tap / 3, tx = tap % 3;
+#pragma unroll
+                for (int kc = 0; kc < CIN / 16; kc++) {
+                    uint32_t aAddr = sInAddr + (uint32_t)(((ty * KG + 2 * kc) * kTcSpx + tx) * 16);
+                    uint32_t bAddr = sWAddr + (uint32_t)(((tap * KG + 2 * kc) * COUT) * 16);
+                    uint64_t aDesc = smem_desc(aAddr, kTcSpx * 16, 128);
+                    uint64_t bDesc = smem_desc(bAddr, COUT * 16, 128);
+                    uint32_t accumulate = (tap | kc) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\t"
+                        "setp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                        :: "r"(tmem), "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate));
+                }
+            }
+            asm volatile(
+                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                :: "r"(smem_u32(&mbar)));
+        }
+        // wait for the accumulator (bounded)
+        uint32_t done = 0;
+        for (uint32_t it = 0; it < kTcWaitLimit && !done; it++) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done) : "r"(smem_u32(&mbar)), "r"(phase));
+        }
+        // one decision for the whole CTA (a thread that gave up must not skip a barrier)
+        failed = __syncthreads_or(!done) != 0;
+        if (failed && tid == 0) atomicOr(&g_dnStatus, 1u);
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (!failed) {
+            // epilogue: this thread's pixel = lane 32 * warp + lane of the accumulator
+            const int x = x0 + warp * 32 + lane;
+            const size_t p = (size_t)row * W + x;
+#pragma unroll
+            for (int c0 = 0; c0 < COUT; c0 += 16) {
+                uint32_t r[16];
+                uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+                      "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+                      "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;");
+                if (x < W) {
+                    float v[16];
+#pragma unroll
+                    for (int k = 0; k < 16; k++) {
+                        v[k] = __uint_as_float(r[k]);
+                        if (EPI != kEpiF32) v[k] += bias[c0 + k];
+                        if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
+                    }
+                    if (EPI == kEpiBf16BiasRelu) {
+                        uint4 *o = reinterpret_cast<uint4 *>(outB + p * COUT + c0);
+                        o[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
+                            pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+                        o[1] = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
+                            pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
+                    } else {
+                        float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + c0);
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                    }
+                }
+            }
+        }
+        // the next tile overwrites the staged rows and the accumulator
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+    }
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     :: "r"(tmem), "r"(TMEM_COLS));
+}
+
+template <int CIN, int COUT, int EPI>
+int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, int W, const void *w,
+    const float *bias, void *outB, float *outF)
+{
+    // + a guard band: the descriptors' largest reach stays inside the allocation
+    // even if the leading and stride offsets were read the other way round
+    size_t smem = (size_t)(9 * (CIN / 8) * COUT + 3 * (CIN / 8) * kTcSpx) * 16 + kTcGuardBytes;
+    auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
+    GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int tiles = ((W + kTcTileP - 1) / kTcTileP) * B * H;
+    int grid = smCount * 2;
+    if (grid > tiles) grid = tiles;
+    kern<<<grid, 128, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W,
+        reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
+        outF);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
 // Input features: log(1 + radiance), albedo, normal, depth/(1 + depth),
 // zero-padded to 16 channels.
 __global__ void k_features(const float4 *__restrict__ rad, const float4 *__restrict__ aov,
@@ -407,6 +626,41 @@ int gbsp_dn_conv3x3_forward(void *stream, const uint16_t *in, uint32_t B, uint32
 #undef GBSP_CONV_CASE
     return set_error(GBSP_ERR_INVALID_ARGUMENT, "conv3x3 %u->%u epilogue %d not instantiated", cin,
         cout, epilogue);
+}
+
+int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uint32_t H,
+    uint32_t W, uint32_t cin, const uint16_t *weights, const float *bias, uint32_t cout,
+    int epilogue, uint16_t *outBf16, float *outF32)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!in || !weights || !B || !H || !W) return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad conv args");
+    int sm = sm_count();
+    if (epilogue == kEpiBf16BiasRelu && !outBf16) return set_error(GBSP_ERR_INVALID_ARGUMENT, "outBf16");
+    if (epilogue != kEpiBf16BiasRelu && !outF32) return set_error(GBSP_ERR_INVALID_ARGUMENT, "outF32");
+    if (epilogue != kEpiF32 && !bias) return set_error(GBSP_ERR_INVALID_ARGUMENT, "bias");
+    if (((uintptr_t)in | (uintptr_t)weights | (uintptr_t)outBf16 | (uintptr_t)outF32) & 15u)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "conv tensors must be 16-byte aligned");
+#define GBSP_CONV_CASE(CI, CO, EP)                                                               \
+    if (cin == CI && cout == CO && epilogue == EP)                                               \
+        return launch_conv_tc<CI, CO, EP>(s, sm, in, B, H, W, weights, bias, outBf16, outF32);
+    GBSP_CONV_CASE(16, 48, kEpiBf16BiasRelu)
+    GBSP_CONV_CASE(48, 48, kEpiBf16BiasRelu)
+    GBSP_CONV_CASE(48, 32, kEpiF32Bias)
+    GBSP_CONV_CASE(48, 48, kEpiF32)
+    GBSP_CONV_CASE(32, 48, kEpiF32)
+#undef GBSP_CONV_CASE
+    return set_error(GBSP_ERR_INVALID_ARGUMENT, "conv3x3 %u->%u epilogue %d not instantiated", cin,
+        cout, epilogue);
+}
+
+int gbsp_dn_status(uint32_t *status)
+{
+    if (!status) return set_error(GBSP_ERR_INVALID_ARGUMENT, "status is NULL");
+    GBSP_CUDA_TRY(cudaMemcpyFromSymbol(status, g_dnStatus, sizeof(uint32_t)));
+    uint32_t zero = 0;
+    GBSP_CUDA_TRY(cudaMemcpyToSymbol(g_dnStatus, &zero, sizeof(uint32_t)));
+    return *status ? set_error(GBSP_ERR_DEVICE_STATUS, "denoiser device status 0x%x", *status)
+                   : GBSP_OK;
 }
 
 int gbsp_dn_flip_transpose(void *stream, const uint16_t *w, uint32_t cout, uint32_t cin,

@@ -53,6 +53,7 @@ EXPORTS = [
     "gbsp_dn_filter", "gbsp_dn_relmse_backward", "gbsp_dn_adam", "gbsp_tonemap",
     "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
     "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
+    "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status",
 ]
 
 
