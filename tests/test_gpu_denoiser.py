@@ -63,16 +63,16 @@ def test_conv3x3_forward_matches_torch(gpu_lib, cin, cout, epi):
 
 @pytest.mark.parametrize("cin,cout,epi", [(16, 48, 0), (48, 48, 0), (48, 32, 1), (48, 48, 2),
                                           (32, 48, 2)])
-@pytest.mark.parametrize("W", [128, 200])
-def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, W):
+@pytest.mark.parametrize("B,H,W", [(2, 5, 128), (2, 5, 200), (1, 300, 1000)])
+def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, B, H, W):
     """The tcgen05 convolution (accumulator in tensor memory) against torch and
-    against the mma.sync kernel; W = 200 leaves a partial 128-pixel tile."""
+    against the mma.sync kernel; W = 200 leaves a partial 128-pixel tile, the
+    300-row image gives every CTA strips of 8 rows (the row ring wraps)."""
     import torch
 
     from vk_cinematic_gb300.denoiser import _ptr, _stream
 
     torch.manual_seed(cin * 100 + cout + epi + W)
-    B, H = 2, 5
     x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
     w = (torch.randn((9, cout, cin), device="cuda") * 0.2).to(torch.bfloat16)
     bias = torch.randn(cout, device="cuda")
@@ -97,7 +97,8 @@ def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, W):
         ref = torch.relu(ref)
     err, ok = close(outs[0], ref)
     err2, ok2 = close(outs[0], outs[1], rtol=1e-2 if epi == 0 else 1e-4)
-    print(f"tcgen05 conv {cin}->{cout} epi {epi} W {W}: vs torch {err:.2e}, vs mma.sync {err2:.2e}")
+    print(f"tcgen05 conv {cin}->{cout} epi {epi} {B}x{H}x{W}: vs torch {err:.2e}, "
+          f"vs mma.sync {err2:.2e}")
     assert ok and ok2
 
 

@@ -152,33 +152,35 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // ---------------------------------------------------------------------------
 // conv3x3 on the 5th-generation tensor cores (tcgen05).
 //
-// Same GEMM as k_conv3x3 with a 128-pixel tile: M = 128 pixels of one image
-// row, N = COUT, K = 9 taps x CIN.  One elected thread issues
-// tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 -> FP32) for every
-// (tap, 16-channel slice): 9 * CIN / 16 instructions of 128 x COUT x 16 per
-// tile, accumulating in tensor memory; both operands are read straight from
-// shared memory through matrix descriptors, so the 3x3 neighbourhood is never
-// expanded: a tap is just a 16-byte-granular offset of the A descriptor into
-// the staged input rows.
+// GEMM: M = 128 pixels of one image row, N = COUT, K = 9 taps x CIN.  One
+// elected thread issues tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 ->
+// FP32) for every (tap, 16-channel slice): 9 * CIN / 16 instructions of
+// 128 x COUT x 16 per output row, accumulating in tensor memory.  Both
+// operands are read straight from shared memory through matrix descriptors,
+// so the 3x3 neighbourhood is never expanded: a tap is a 16-byte-granular
+// offset of the A descriptor into the staged input rows.
 //
 // Shared memory holds the operands in the canonical no-swizzle K-major
 // layout: 8 x 16-byte core matrices (8 rows of 8 BF16 channels), rows
-// contiguous.  Input tile: [3 rows][CIN/8 channel groups][130 pixels][16 B]
-// (a core matrix = 8 consecutive pixels of one channel group, so a tap's
-// pixel shift moves the start address by 16 B); weights:
-// [9 taps][CIN/8 groups][COUT][16 B].  Descriptor strides: leading (K) =
-// next channel group, stride (M or N) = next 8 rows = 128 B.
+// contiguous.  Input rows: a ring of 4 slots of [CIN/8 channel groups][130
+// pixels][16 B] (a core matrix = 8 consecutive pixels of one channel group,
+// so a pixel shift moves the start by 16 B); weights: [9 taps][CIN/8 groups]
+// [COUT][16 B].  Descriptor strides: leading (K) = next channel group,
+// stride (M or N) = next 8 rows = 128 B.
 //
-// The accumulator (128 lanes x COUT FP32 columns) is read back by the four
-// warps with tcgen05.ld (warp w owns lanes 32w..32w+31, i.e. pixels
-// 32w..32w+31 of the tile) for the bias / ReLU / store epilogue.  The MMA
-// completion is signalled by tcgen05.commit on an mbarrier; every wait is
-// bounded and a timeout sets g_dnStatus instead of spinning.
+// A CTA walks a vertical strip (one 128-pixel column segment, a run of
+// rows).  Per output row y: issue the MMAs of row y into accumulator slot
+// y & 1 (rows y-1..y+1 are in the ring), then - while they run - wait for
+// row y-1's accumulator, read it back with tcgen05.ld (warp w owns lanes
+// 32w..32w+31 = pixels 32w..32w+31) for the bias / ReLU / store epilogue,
+// and prefetch input row y+2 with cp.async into the ring slot row y-2 left.
+// MMA completion is signalled by tcgen05.commit on one mbarrier per
+// accumulator slot; every wait is bounded and a timeout sets g_dnStatus.
 // ---------------------------------------------------------------------------
 constexpr int kTcTileP = 128;
 constexpr int kTcSpx = kTcTileP + 2;
+constexpr int kTcRing = 4;
 constexpr uint32_t kTcWaitLimit = 1u << 26;
-constexpr size_t kTcGuardBytes = 36 * 1024;
 
 __device__ uint32_t g_dnStatus;
 
@@ -205,20 +207,96 @@ __device__ __forceinline__ uint32_t instr_desc_bf16()
         ((uint32_t)(M >> 4) << 24);
 }
 
+// Bounded wait on an mbarrier phase; returns 1 when the phase completed.
+__device__ __forceinline__ uint32_t mbar_wait(uint32_t bar, uint32_t phase)
+{
+    uint32_t done = 0;
+    for (uint32_t it = 0; it < kTcWaitLimit && !done; it++) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done) : "r"(bar), "r"(phase) : "memory");
+    }
+    return done;
+}
+
+// Stages input row gy (zero outside the image) into ring slot `slot` with
+// cp.async (16 B per copy, zero-filled when the source size is 0).
+template <int KG>
+__device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 *in, int b, int gy,
+    int H, int W, int x0, int tid)
+{
+    const bool rowIn = gy >= 0 && gy < H;
+    for (int i = tid; i < KG * kTcSpx; i += 128) {
+        int px = i % kTcSpx, kg = i / kTcSpx;
+        int gx = x0 + px - 1;
+        bool ok = rowIn && gx >= 0 && gx < W;
+        const uint4 *src = ok ? in + ((size_t)(b * H + gy) * W + gx) * KG + kg : in;
+        uint32_t dst = sRing + (uint32_t)(((slot * KG + kg) * kTcSpx + px) * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                     :: "r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int CIN, int COUT, int EPI>
+__device__ __forceinline__ void conv_epilogue(uint32_t tmem, int warp, int lane, int x, int W,
+    size_t p, const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB,
+    float *__restrict__ outF)
+{
+#pragma unroll
+    for (int c0 = 0; c0 < COUT; c0 += 16) {
+        uint32_t r[16];
+        uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
+              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
+              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (x < W) {
+            float v[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                v[k] = __uint_as_float(r[k]);
+                if (EPI != kEpiF32) v[k] += bias[c0 + k];
+                if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
+            }
+            if (EPI == kEpiBf16BiasRelu) {
+                uint4 *o = reinterpret_cast<uint4 *>(outB + p * COUT + c0);
+                o[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
+                    pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+                o[1] = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
+                    pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
+            } else {
+                float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + c0);
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            }
+        }
+    }
+}
+
 template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, int B,
-    int H, int W, const __nv_bfloat16 *__restrict__ w, const float *__restrict__ bias,
-    __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
+    int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
+    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
 {
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tcgen05 tile shape");
-    constexpr int KG = CIN / 8;                    // 16-byte channel groups
-    constexpr int TMEM_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+    constexpr int KG = CIN / 8;  // 16-byte channel groups
+    constexpr int ACC_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+    constexpr int TMEM_COLS = 2 * ACC_COLS;  // two accumulator slots
     extern __shared__ __align__(128) unsigned char smemRaw[];
-    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);          // [9][KG][COUT]
-    uint4 *sIn = sW + 9 * KG * COUT;                         // [3][KG][kTcSpx]
-    __shared__ __align__(8) uint64_t mbar;
+    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [9][KG][COUT]
+    uint4 *sRing = sW + 9 * KG * COUT;               // [4][KG][kTcSpx]
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmemBase;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
 
     // weights -> canonical layout: (tap, kg, co) holds w[tap][co][8 kg .. 8 kg + 7]
     for (int i = tid; i < 9 * KG * COUT; i += 128) {
@@ -231,118 +309,93 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restr
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmemBase;
     const uint32_t idesc = instr_desc_bf16<kTcTileP, COUT>();
-    const uint32_t sInAddr = smem_u32(sIn), sWAddr = smem_u32(sW);
+    const uint32_t ringAddr = smem_u32(sRing), wAddr = smem_u32(sW);
+    const uint32_t bar[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
+    uint32_t phase[2] = {0, 0};
 
-    const int tilesPerRow = (W + kTcTileP - 1) / kTcTileP;
-    const int numTiles = tilesPerRow * B * H;
-    uint32_t phase = 0;
+    const int segs = (W + kTcTileP - 1) / kTcTileP;
+    const int stripsPerCol = (H + rowsPerStrip - 1) / rowsPerStrip;
+    const int numStrips = B * segs * stripsPerCol;
     bool failed = false;
-    for (int tile = blockIdx.x; tile < numTiles && !failed; tile += gridDim.x) {
-        const int row = tile / tilesPerRow;  // b * H + y
-        const int x0 = (tile % tilesPerRow) * kTcTileP;
-        const int b = row / H, y = row % H;
-        // stage the three input rows (zero outside the image)
-        for (int i = tid; i < 3 * KG * kTcSpx; i += 128) {
-            int px = i % kTcSpx, kg = (i / kTcSpx) % KG, ry = i / (kTcSpx * KG);
-            int gy = y + ry - 1, gx = x0 + px - 1;
-            uint4 v = make_uint4(0, 0, 0, 0);
-            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                v = reinterpret_cast<const uint4 *>(in)[((size_t)(b * H + gy) * W + gx) * KG + kg];
-            sIn[i] = v;
-        }
-        // make the generic-proxy stores visible to the tensor core (async proxy)
-        asm volatile("fence.proxy.async.shared::cta;");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (tid == 0) {
+    for (int strip = blockIdx.x; strip < numStrips && !failed; strip += gridDim.x) {
+        const int sy = strip % stripsPerCol, seg = (strip / stripsPerCol) % segs;
+        const int b = strip / (stripsPerCol * segs);
+        const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;
+        const int y1 = min(H, y0 + rowsPerStrip);
+        // prologue: rows y0-1, y0, y0+1 into ring slots (row + 4) % 4
+        for (int gy = y0 - 1; gy <= y0 + 1; gy++)
+            stage_row<KG>(ringAddr, (gy + kTcRing) % kTcRing, in4, b, gy, H, W, x0, tid);
+        for (int y = y0; y <= y1 && !failed; y++) {
+            const int acc = y & 1;
+            if (y < y1) {
+                // rows y-1..y+1 are staged: make them visible to the tensor core
+                asm volatile("cp.async.wait_group 0;" ::: "memory");
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                __syncthreads();
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                if (tid == 0) {
+                    const uint32_t dAcc = tmem + (uint32_t)(acc * ACC_COLS);
 #pragma unroll 1
-            for (int tap = 0; tap < 9; tap++) {
-                const int ty = tap / 3, tx = tap % 3;
+                    for (int tap = 0; tap < 9; tap++) {
+                        const int ty = tap / 3, tx = tap % 3;
+                        const int slot = (y + ty - 1 + kTcRing) % kTcRing;
 #pragma unroll
-                for (int kc = 0; kc < CIN / 16; kc++) {
-                    uint32_t aAddr = sInAddr + (uint32_t)(((ty * KG + 2 * kc) * kTcSpx + tx) * 16);
-                    uint32_t bAddr = sWAddr + (uint32_t)(((tap * KG + 2 * kc) * COUT) * 16);
-                    uint64_t aDesc = smem_desc(aAddr, kTcSpx * 16, 128);
-                    uint64_t bDesc = smem_desc(bAddr, COUT * 16, 128);
-                    uint32_t accumulate = (tap | kc) ? 1u : 0u;
+                        for (int kc = 0; kc < CIN / 16; kc++) {
+                            uint32_t aAddr = ringAddr +
+                                (uint32_t)(((slot * KG + 2 * kc) * kTcSpx + tx) * 16);
+                            uint32_t bAddr = wAddr + (uint32_t)(((tap * KG + 2 * kc) * COUT) * 16);
+                            uint64_t aDesc = smem_desc(aAddr, kTcSpx * 16, 128);
+                            uint64_t bDesc = smem_desc(bAddr, COUT * 16, 128);
+                            uint32_t accumulate = (tap | kc) ? 1u : 0u;
+                            asm volatile(
+                                "{\n\t.reg .pred p;\n\t"
+                                "setp.ne.b32 p, %4, 0;\n\t"
+                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                                :: "r"(dAcc), "l"(aDesc), "l"(bDesc), "r"(idesc),
+                                   "r"(accumulate));
+                        }
+                    }
                     asm volatile(
-                        "{\n\t.reg .pred p;\n\t"
-                        "setp.ne.b32 p, %4, 0;\n\t"
-                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                        :: "r"(tmem), "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate));
+                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                        :: "r"(bar[acc]) : "memory");
                 }
             }
-            asm volatile(
-                "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                :: "r"(smem_u32(&mbar)));
-        }
-        // wait for the accumulator (bounded)
-        uint32_t done = 0;
-        for (uint32_t it = 0; it < kTcWaitLimit && !done; it++) {
-            asm volatile(
-                "{\n\t.reg .pred p;\n\t"
-                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                "selp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(done) : "r"(smem_u32(&mbar)), "r"(phase));
-        }
-        // one decision for the whole CTA (a thread that gave up must not skip a barrier)
-        failed = __syncthreads_or(!done) != 0;
-        if (failed && tid == 0) atomicOr(&g_dnStatus, 1u);
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (!failed) {
-            // epilogue: this thread's pixel = lane 32 * warp + lane of the accumulator
-            const int x = x0 + warp * 32 + lane;
-            const size_t p = (size_t)row * W + x;
-#pragma unroll
-            for (int c0 = 0; c0 < COUT; c0 += 16) {
-                uint32_t r[16];
-                uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                    "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-                      "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-                      "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;");
-                if (x < W) {
-                    float v[16];
-#pragma unroll
-                    for (int k = 0; k < 16; k++) {
-                        v[k] = __uint_as_float(r[k]);
-                        if (EPI != kEpiF32) v[k] += bias[c0 + k];
-                        if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
-                    }
-                    if (EPI == kEpiBf16BiasRelu) {
-                        uint4 *o = reinterpret_cast<uint4 *>(outB + p * COUT + c0);
-                        o[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
-                            pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
-                        o[1] = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
-                            pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
-                    } else {
-                        float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + c0);
-#pragma unroll
-                        for (int k = 0; k < 4; k++)
-                            o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-                    }
-                }
+            if (y > y0) {
+                // row y-1: its MMAs are done -> epilogue, and its oldest input row is free
+                const int pa = acc ^ 1;
+                uint32_t done = mbar_wait(bar[pa], phase[pa]);
+                failed = __syncthreads_or(!done) != 0;
+                if (failed) break;
+                phase[pa] ^= 1u;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const int x = x0 + warp * 32 + lane;
+                conv_epilogue<CIN, COUT, EPI>(tmem + (uint32_t)(pa * ACC_COLS), warp, lane, x, W,
+                    ((size_t)(b * H + (y - 1)) * W + x), bias, outB, outF);
+                asm volatile("tcgen05.fence::before_thread_sync;");
             }
+            // prefetch row y+2 into the slot of row y-2 (its last reader, row y-1, is done)
+            if (y < y1 - 1)
+                stage_row<KG>(ringAddr, (y + 2) % kTcRing, in4, b, y + 2, H, W, x0, tid);
         }
-        // the next tile overwrites the staged rows and the accumulator
+        // the next strip's prologue overwrites the ring
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;");
     }
+    if (failed && tid == 0) atomicOr(&g_dnStatus, 1u);
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
@@ -353,15 +406,17 @@ template <int CIN, int COUT, int EPI>
 int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, int W, const void *w,
     const float *bias, void *outB, float *outF)
 {
-    // + a guard band: the descriptors' largest reach stays inside the allocation
-    // even if the leading and stride offsets were read the other way round
-    size_t smem = (size_t)(9 * (CIN / 8) * COUT + 3 * (CIN / 8) * kTcSpx) * 16 + kTcGuardBytes;
+    size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int tiles = ((W + kTcTileP - 1) / kTcTileP) * B * H;
-    int grid = smCount * 2;
-    if (grid > tiles) grid = tiles;
-    kern<<<grid, 128, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W,
+    const int ctas = smCount * 2;
+    const int cols = B * ((W + kTcTileP - 1) / kTcTileP);
+    // rows per strip: enough strips to fill every CTA slot, at least 4 rows
+    int rows = (int)(((int64_t)cols * H + ctas - 1) / ctas);
+    rows = rows < 4 ? 4 : (rows > H ? H : rows);
+    int strips = cols * ((H + rows - 1) / rows);
+    int grid = strips < ctas ? strips : ctas;
+    kern<<<grid, 128, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
         reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
         outF);
     GBSP_CUDA_TRY(cudaGetLastError());

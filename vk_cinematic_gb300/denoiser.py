@@ -53,10 +53,17 @@ def relmse(x, ref):
 
 
 class KPCNN:
-    def __init__(self, seed: int = 0):
+    """conv: "tcgen05" (5th-generation tensor cores, accumulator in tensor
+    memory) or "mma" (mma.sync BF16 fragments) for the forward and
+    data-gradient convolutions."""
+
+    def __init__(self, seed: int = 0, conv: str = "tcgen05"):
         import torch
 
         self.L = gbsp.load()
+        self._conv = {"tcgen05": self.L.gbsp_dn_conv3x3_forward_tc,
+                      "mma": self.L.gbsp_dn_conv3x3_forward}[conv]
+        self.conv_impl = conv
         g = torch.Generator().manual_seed(seed)
         self.w, self.b, self.wb, self.state = [], [], [], []
         for li, (cin, cout, epi) in enumerate(LAYERS):
@@ -97,14 +104,14 @@ class KPCNN:
         epi = LAYERS[li][2]
         if epi == 0:
             out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device="cuda")
-            _check(self.L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W),
-                                                  _u32(cin), _ptr(self.wb[li]), _ptr(self.b[li]),
-                                                  _u32(cout), _int(0), _ptr(out), None))
+            _check(self._conv(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W), _u32(cin),
+                              _ptr(self.wb[li]), _ptr(self.b[li]), _u32(cout), _int(0), _ptr(out),
+                              None))
         else:
             out = torch.empty((B, H, W, cout), dtype=torch.float32, device="cuda")
-            _check(self.L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W),
-                                                  _u32(cin), _ptr(self.wb[li]), _ptr(self.b[li]),
-                                                  _u32(cout), _int(1), None, _ptr(out)))
+            _check(self._conv(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W), _u32(cin),
+                              _ptr(self.wb[li]), _ptr(self.b[li]), _u32(cout), _int(1), None,
+                              _ptr(out)))
         return out
 
     def forward(self, feats, keep=False):
@@ -140,9 +147,8 @@ class KPCNN:
         _check(self.L.gbsp_dn_flip_transpose(_stream(), _ptr(self.wb[li]), _u32(cout), _u32(cin),
                                              _ptr(wt)))
         out = torch.empty((B, H, W, cin), dtype=torch.float32, device="cuda")
-        _check(self.L.gbsp_dn_conv3x3_forward(_stream(), _ptr(d), _u32(B), _u32(H), _u32(W),
-                                              _u32(cout), _ptr(wt), None, _u32(cin), _int(2), None,
-                                              _ptr(out)))
+        _check(self._conv(_stream(), _ptr(d), _u32(B), _u32(H), _u32(W), _u32(cout), _ptr(wt),
+                          None, _u32(cin), _int(2), None, _ptr(out)))
         return out
 
     def weight_grad(self, li, x, d, dw, db):
