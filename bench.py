@@ -119,14 +119,17 @@ def measured_peaks():
 
 
 def profiled_traffic():
-    """Per-launch DRAM bytes of the closest-hit kernel from a committed ncu
-    summary (profiles/trace_kernel_dram.json), scaled to this run's rays per
-    launch; None if no capture was committed."""
-    p = os.path.join(ROOT, "profiles", "trace_kernel_dram.json")
+    """DRAM bytes per ray of the closest-hit kernels from the committed ncu
+    summary profiles/trace_kernel_dram.md (its `dram_bytes_per_ray:` line);
+    the bench scales it to this run's rays per launch.  None if absent."""
+    p = os.path.join(ROOT, "profiles", "trace_kernel_dram.md")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        return json.load(f)
+        for line in f:
+            if line.strip().startswith("dram_bytes_per_ray:"):
+                return {"dram_bytes_per_ray": float(line.split(":", 1)[1])}
+    return None
 
 
 class ClockSampler:

@@ -13,11 +13,13 @@
 // warp works on one tile and splits each ray's triangle loop across its
 // lanes: lane l tests triangles l, l+32, ... (its own strict-< minimum), then
 // a warp reduction on (t, triangle index) gives the sequential loop's answer
-// (smallest t, lowest index among equal t).  Triangles are pre-expanded per
-// mesh into structure-of-arrays a, e1 = b - a, e2 = c - a (the same IEEE
-// subtractions the shader performs), so each component load of the warp is
-// one coalesced 128-byte line; texture coordinates are read only for the
-// winner.  All other per-ray work is warp-uniform.
+// (smallest t, lowest index among equal t).  The eight warps of a block trace
+// their rays in step so that every chunk of 256 triangles is staged into
+// shared memory once for eight rays.  Triangles are pre-expanded per mesh
+// into structure-of-arrays a, e1 = b - a, e2 = c - a (the same IEEE
+// subtractions the shader performs), so staging is coalesced; texture
+// coordinates are read only for the winner.  All other per-ray work is
+// warp-uniform.
 //
 // Built-ins are fixed to one IEEE definition shared with the oracle (dot in
 // x, y, z order; normalize = v * (1 / sqrt(dot)); mat4 * vec4 summed over
@@ -35,7 +37,8 @@ constexpr float kF32Max = 3.402823466e+38f;
 constexpr uint32_t kMaterialRed = 0, kMaterialCheckerBoard = 2, kMaterialWhiteLight = 5,
                    kMaterialBlack = 6;
 constexpr int kMaxBounces = 3;
-constexpr int kWarpsPerBlock = 4;
+constexpr int kWarpsPerBlock = 8;
+constexpr int kChunk = 32 * kWarpsPerBlock;  // triangles staged per step (one per thread)
 
 struct EntityDev {
     float model[16];
@@ -135,179 +138,261 @@ struct SceneHit {
     float u, v;
 };
 
-// test_compute.comp.glsl:320-430 for one ray, executed by a whole warp.
-__device__ SceneHit intersect_scene(const EntityDev *__restrict__ ents, uint32_t entityCount,
-    const TriSoA &tri, V3 o, V3 d, int lane, uint64_t &tests)
-{
-    SceneHit res;
-    res.t = kF32Max;
-    res.material = kMaterialBlack;
-    res.normal = v3(0.0f, 0.0f, 0.0f);
-    res.u = res.v = 0.0f;
-    for (uint32_t e = 0; e < entityCount; e++) {
-        const EntityDev &ent = ents[e];
-        V3 lo = mat_mul(ent.inv, o, 1.0f);
-        V3 ld = cnormalize(mat_mul(ent.inv, d, 0.0f));
-        uint32_t begin = __ldg(&ent.triBegin), count = __ldg(&ent.triCount);
-        tests += count;
-        // this lane's strict-< minimum over triangles lane, lane + 32, ...
-        float bestT = kF32Max, bestU = 0.0f, bestV = 0.0f;
-        uint32_t bestK = 0xFFFFFFFFu;
-        for (uint32_t k = lane; k < count; k += 32) {
-            uint32_t g = begin + k;
-            V3 a = v3(__ldg(tri.ax + g), __ldg(tri.ay + g), __ldg(tri.az + g));
-            V3 e1 = v3(__ldg(tri.e1x + g), __ldg(tri.e1y + g), __ldg(tri.e1z + g));
-            V3 e2 = v3(__ldg(tri.e2x + g), __ldg(tri.e2y + g), __ldg(tri.e2z + g));
-            V3 T = v3(lo.x - a.x, lo.y - a.y, lo.z - a.z);
-            V3 p = ccross(ld, e2);
-            V3 q = ccross(T, e1);
-            float mx = cdot(q, e2), my = cdot(p, T), mz = cdot(q, ld);
-            float det = 1.0f / cdot(p, e1);
-            float t = det * mx, u = det * my, v = det * mz;
-            float w = 1.0f - u - v;
-            if (u >= 0.0f && u <= 1.0f && v >= 0.0f && v <= 1.0f && w >= 0.0f && w <= 1.0f &&
-                t >= 0.0f && t < kF32Max && t < bestT) {
-                bestT = t;
-                bestU = u;
-                bestV = v;
-                bestK = k;
-            }
-        }
-        // the sequential loop keeps the smallest t and, among equal t, the first index
-#pragma unroll
-        for (int off = 16; off; off >>= 1) {
-            float ot = __shfl_xor_sync(0xFFFFFFFFu, bestT, off);
-            uint32_t ok = __shfl_xor_sync(0xFFFFFFFFu, bestK, off);
-            if (ot < bestT || (ot == bestT && ok < bestK)) {
-                bestT = ot;
-                bestK = ok;
-            }
-        }
-        float meshT = kF32Max, meshU = 0.0f, meshV = 0.0f;
-        V3 localNormal = v3(0.0f, 0.0f, 0.0f);
-        if (bestK != 0xFFFFFFFFu) {
-            int src = (int)(bestK & 31u);
-            float u = __shfl_sync(0xFFFFFFFFu, bestU, src);
-            float v = __shfl_sync(0xFFFFFFFFu, bestV, src);
-            uint32_t g = begin + bestK;
-            V3 e1 = v3(__ldg(tri.e1x + g), __ldg(tri.e1y + g), __ldg(tri.e1z + g));
-            V3 e2 = v3(__ldg(tri.e2x + g), __ldg(tri.e2y + g), __ldg(tri.e2z + g));
-            localNormal = cnormalize(ccross(e1, e2));
-            float w = 1.0f - u - v;
-            float2 t0 = __ldg(&tri.uv[(size_t)g * 3 + 0]);
-            float2 t1 = __ldg(&tri.uv[(size_t)g * 3 + 1]);
-            float2 t2 = __ldg(&tri.uv[(size_t)g * 3 + 2]);
-            meshT = bestT;
-            meshU = (t0.x * w + t1.x * u) + t2.x * v;
-            meshV = (t0.y * w + t1.y * u) + t2.y * v;
-        }
-        V3 localHit = v3(lo.x + ld.x * meshT, lo.y + ld.y * meshT, lo.z + ld.z * meshT);
-        V3 worldHit = mat_mul(ent.model, localHit, 1.0f);
-        float t = cdot(v3(worldHit.x - o.x, worldHit.y - o.y, worldHit.z - o.z), d);
-        V3 worldNormal = cnormalize(mat_mul(ent.model, localNormal, 0.0f));
-        if (t >= 0.0f && t < res.t) {
-            res.t = t;
-            res.material = __ldg(&ent.material);
-            res.normal = worldNormal;
-            res.u = meshU;
-            res.v = meshV;
-        }
-    }
-    return res;
-}
-
 struct PathVertex {
     uint32_t material;
     V3 incoming, normal;
     float u, v;
 };
 
+// Radiance of a finished path (test_compute.comp.glsl:441-481).
+__device__ __forceinline__ V3 path_radiance_cpt(const PathVertex *path, int len,
+    const float4 *__restrict__ tex, uint32_t texW, uint32_t texH)
+{
+    V3 radiance = v3(0.0f, 0.0f, 0.0f);
+    for (int i = len - 1; i >= 0; i--) {
+        V3 emission = v3(0.0f, 0.0f, 0.0f), albedo = v3(0.0f, 0.0f, 0.0f);
+        uint32_t m = path[i].material;
+        if (m == kMaterialRed)
+            albedo = v3(0.18f, 0.1f, 0.1f);
+        else if (m == kMaterialCheckerBoard)
+            albedo = sample_bilinear(tex, texW, texH, path[i].u, path[i].v);
+        else if (m == kMaterialWhiteLight)
+            emission = v3(1.0f, 1.0f, 1.0f);
+        float cosine = glsl_max(0.0f, cdot(path[i].normal, path[i].incoming));
+        radiance = v3(emission.x + (albedo.x * radiance.x) * cosine,
+            emission.y + (albedo.y * radiance.y) * cosine,
+            emission.z + (albedo.z * radiance.z) * cosine);
+    }
+    return radiance;
+}
+
+// Block-lockstep kernel: the kWarpsPerBlock warps of a block own one tile
+// each and trace their current rays together.  The brute-force triangle
+// loop is the same sequence for every ray (entity by entity, triangle by
+// triangle), so the block stages each chunk of kChunk triangles (9 floats
+// each: a, e1, e2) into shared memory once - double-buffered, the next chunk
+// loading while this one is tested - and every warp tests its own ray
+// against it, lane l taking triangles l, l + 32, ...  Per warp the order of
+// triangles, the strict-< minimum and every RNG draw are those of the
+// shader's sequential loops, so results are unchanged; a warp whose tile is
+// done keeps staging chunks for the others until the whole block is done.
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_compute_pt(const EntityDev *__restrict__ ents,
     uint32_t entityCount, TriSoA tri, const float4 *__restrict__ tex, uint32_t texW, uint32_t texH,
     View view, const uint32_t *__restrict__ tiles, uint32_t tileCount, float4 *__restrict__ image,
     Counters counters)
 {
-    const int lane = threadIdx.x & 31;
-    const uint32_t item = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
-    if (item >= tileCount) return;  // warp-uniform
-    uint32_t tileIndex = __ldg(&tiles[item]);
-    uint32_t tx = tileIndex % view.tileCountX, ty = tileIndex / view.tileCountX;
-    uint32_t minX = tx * view.tileW, minY = ty * view.tileH;
-    uint32_t maxX = min(view.width, (tx + 1) * view.tileW);
-    uint32_t maxY = min(view.height, (ty + 1) * view.tileH);
+    __shared__ float sTri[2][9][kChunk];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t item = blockIdx.x * kWarpsPerBlock + (tid >> 5);
+    bool active = item < tileCount;
+    uint32_t minX = 0, minY = 0, maxX = 0, maxY = 0, tileIndex = 0;
+    if (active) {
+        tileIndex = __ldg(&tiles[item]);
+        uint32_t tx = tileIndex % view.tileCountX, ty = tileIndex / view.tileCountX;
+        minX = tx * view.tileW;
+        minY = ty * view.tileH;
+        maxX = min(view.width, (tx + 1) * view.tileW);
+        maxY = min(view.height, (ty + 1) * view.tileH);
+        active = minX < maxX && minY < maxY;
+    }
     Rng rng{(tileIndex + 1u) * 0xF51C0E49u};
     uint64_t rays = 0, hits = 0, tests = 0, paths = 0;
-    for (uint32_t y = minY; y < maxY; y++) {
-        for (uint32_t x = minX; x < maxX; x++) {
-            // test_compute.comp.glsl:510-606, every lane computes the same values
-            float px = (float)x + 0.5f, py = (float)y + 0.5f;
-            float jx = view.halfPixelWidth * rng.bilateral();
-            float jy = view.halfPixelHeight * rng.bilateral();
-            px = px + jx;
-            py = py + jy;
-            float fx = px * view.invW, fy = py * view.invH;
-            fy = 1.0f - fy;
-            fx = fx * 2.0f - 1.0f;
-            fy = fy * 2.0f - 1.0f;
-            V3 filmP = view.center;
-            float sx = view.halfWidth * fx, sy = view.halfHeight * fy;
-            filmP = v3(filmP.x + view.right.x * sx, filmP.y + view.right.y * sx,
-                filmP.z + view.right.z * sx);
-            filmP = v3(filmP.x + view.up.x * sy, filmP.y + view.up.y * sy, filmP.z + view.up.z * sy);
-            V3 o = view.position;
-            V3 d = cnormalize(v3(filmP.x - o.x, filmP.y - o.y, filmP.z - o.z));
-            PathVertex path[kMaxBounces];
-            int len = 0;
-            for (int b = 0; b < kMaxBounces; b++) {
-                SceneHit h = intersect_scene(ents, entityCount, tri, o, d, lane, tests);
-                rays++;
-                if (h.t > 0.0f && h.t < kF32Max) {
-                    hits++;
-                    float r0 = rng.bilateral();
-                    float r1 = rng.bilateral();
-                    float r2 = rng.bilateral();
-                    V3 dir = cnormalize(v3(h.normal.x + r0, h.normal.y + r1, h.normal.z + r2));
-                    if (cdot(dir, h.normal) < 0.0f) dir = v3(-dir.x, -dir.y, -dir.z);
-                    path[len].material = h.material;
-                    path[len].normal = h.normal;
-                    path[len].incoming = dir;
-                    path[len].u = h.u;
-                    path[len].v = h.v;
-                    len++;
-                    V3 wp = v3(o.x + d.x * h.t, o.y + d.y * h.t, o.z + d.z * h.t);
-                    o = v3(wp.x + h.normal.x * 0.001f, wp.y + h.normal.y * 0.001f,
-                        wp.z + h.normal.z * 0.001f);
-                    d = dir;
-                } else {
-                    path[len].material = kMaterialBlack;
-                    path[len].normal = v3(0.0f, 0.0f, 0.0f);
-                    path[len].incoming = v3(0.0f, 0.0f, 0.0f);
-                    path[len].u = path[len].v = 0.0f;
-                    len++;
-                    break;
-                }
-            }
-            // test_compute.comp.glsl:441-481
-            V3 radiance = v3(0.0f, 0.0f, 0.0f);
-            for (int i = len - 1; i >= 0; i--) {
-                V3 emission = v3(0.0f, 0.0f, 0.0f), albedo = v3(0.0f, 0.0f, 0.0f);
-                uint32_t m = path[i].material;
-                if (m == kMaterialRed)
-                    albedo = v3(0.18f, 0.1f, 0.1f);
-                else if (m == kMaterialCheckerBoard)
-                    albedo = sample_bilinear(tex, texW, texH, path[i].u, path[i].v);
-                else if (m == kMaterialWhiteLight)
-                    emission = v3(1.0f, 1.0f, 1.0f);
-                float cosine = glsl_max(0.0f, cdot(path[i].normal, path[i].incoming));
-                radiance = v3(emission.x + (albedo.x * radiance.x) * cosine,
-                    emission.y + (albedo.y * radiance.y) * cosine,
-                    emission.z + (albedo.z * radiance.z) * cosine);
-            }
-            paths++;
-            if (lane == 0)
-                image[(size_t)y * view.width + x] = make_float4(0.0f + radiance.x * 1.0f,
-                    0.0f + radiance.y * 1.0f, 0.0f + radiance.z * 1.0f, 1.0f);
+    uint32_t x = minX, y = minY;
+    int len = 0, bounce = 0;
+    PathVertex path[kMaxBounces];
+    V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 0.0f);
+    // camera ray of pixel (x, y): test_compute.comp.glsl:510-540
+    auto start_pixel = [&]() {
+        float px = (float)x + 0.5f, py = (float)y + 0.5f;
+        float jx = view.halfPixelWidth * rng.bilateral();
+        float jy = view.halfPixelHeight * rng.bilateral();
+        px = px + jx;
+        py = py + jy;
+        float fx = px * view.invW, fy = py * view.invH;
+        fy = 1.0f - fy;
+        fx = fx * 2.0f - 1.0f;
+        fy = fy * 2.0f - 1.0f;
+        V3 filmP = view.center;
+        float sx = view.halfWidth * fx, sy = view.halfHeight * fy;
+        filmP = v3(filmP.x + view.right.x * sx, filmP.y + view.right.y * sx,
+            filmP.z + view.right.z * sx);
+        filmP = v3(filmP.x + view.up.x * sy, filmP.y + view.up.y * sy, filmP.z + view.up.z * sy);
+        o = view.position;
+        d = cnormalize(v3(filmP.x - o.x, filmP.y - o.y, filmP.z - o.z));
+        len = 0;
+        bounce = 0;
+    };
+    if (active) start_pixel();
+    // stage the triangles [c, c + n) of entity e into buffer buf
+    auto stage = [&](uint32_t e, uint32_t c, int buf) {
+        const EntityDev &ent = ents[e];
+        uint32_t count = __ldg(&ent.triCount);
+        uint32_t n = count - c < (uint32_t)kChunk ? count - c : (uint32_t)kChunk;
+        if ((uint32_t)tid < n) {
+            uint32_t g = __ldg(&ent.triBegin) + c + tid;
+            sTri[buf][0][tid] = __ldg(tri.ax + g);
+            sTri[buf][1][tid] = __ldg(tri.ay + g);
+            sTri[buf][2][tid] = __ldg(tri.az + g);
+            sTri[buf][3][tid] = __ldg(tri.e1x + g);
+            sTri[buf][4][tid] = __ldg(tri.e1y + g);
+            sTri[buf][5][tid] = __ldg(tri.e1z + g);
+            sTri[buf][6][tid] = __ldg(tri.e2x + g);
+            sTri[buf][7][tid] = __ldg(tri.e2y + g);
+            sTri[buf][8][tid] = __ldg(tri.e2z + g);
         }
+    };
+
+    for (uint32_t guard = 0; guard < (1u << 30); guard++) {
+        if (!__syncthreads_or(active)) break;
+        // ---- trace: test_compute.comp.glsl:320-430, all warps in step
+        SceneHit res;
+        res.t = kF32Max;
+        res.material = kMaterialBlack;
+        res.normal = v3(0.0f, 0.0f, 0.0f);
+        res.u = res.v = 0.0f;
+        if (entityCount) {
+            uint32_t e = 0, c = 0;
+            int buf = 0;
+            V3 lo = mat_mul(ents[0].inv, o, 1.0f);
+            V3 ld = cnormalize(mat_mul(ents[0].inv, d, 0.0f));
+            float bestT = kF32Max, bestU = 0.0f, bestV = 0.0f;
+            uint32_t bestK = 0xFFFFFFFFu;
+            stage(0, 0, 0);
+            __syncthreads();
+            while (e < entityCount) {
+                const EntityDev &ent = ents[e];
+                const uint32_t count = __ldg(&ent.triCount);
+                // next chunk: the rest of this entity, else the next entity (an
+                // entity without triangles is one empty chunk)
+                uint32_t ne = e, nc = c + kChunk;
+                if (nc >= count) {
+                    ne = e + 1;
+                    nc = 0;
+                }
+                if (ne < entityCount) stage(ne, nc, buf ^ 1);
+                if (active) {
+                    uint32_t n = count - c < (uint32_t)kChunk ? count - c : (uint32_t)kChunk;
+                    if (c == 0) tests += count;
+                    for (uint32_t j = lane; j < n; j += 32) {
+                        V3 a = v3(sTri[buf][0][j], sTri[buf][1][j], sTri[buf][2][j]);
+                        V3 e1 = v3(sTri[buf][3][j], sTri[buf][4][j], sTri[buf][5][j]);
+                        V3 e2 = v3(sTri[buf][6][j], sTri[buf][7][j], sTri[buf][8][j]);
+                        V3 T = v3(lo.x - a.x, lo.y - a.y, lo.z - a.z);
+                        V3 p = ccross(ld, e2);
+                        V3 q = ccross(T, e1);
+                        float mx = cdot(q, e2), my = cdot(p, T), mz = cdot(q, ld);
+                        float det = 1.0f / cdot(p, e1);
+                        float t = det * mx, u = det * my, v = det * mz;
+                        float w = 1.0f - u - v;
+                        if (u >= 0.0f && u <= 1.0f && v >= 0.0f && v <= 1.0f && w >= 0.0f &&
+                            w <= 1.0f && t >= 0.0f && t < kF32Max && t < bestT) {
+                            bestT = t;
+                            bestU = u;
+                            bestV = v;
+                            bestK = c + j;
+                        }
+                    }
+                    if (ne != e) {
+                        // entity e done: the sequential loop's answer, then world space
+#pragma unroll
+                        for (int off = 16; off; off >>= 1) {
+                            float ot = __shfl_xor_sync(0xFFFFFFFFu, bestT, off);
+                            uint32_t ok = __shfl_xor_sync(0xFFFFFFFFu, bestK, off);
+                            if (ot < bestT || (ot == bestT && ok < bestK)) {
+                                bestT = ot;
+                                bestK = ok;
+                            }
+                        }
+                        float meshT = kF32Max, meshU = 0.0f, meshV = 0.0f;
+                        V3 localNormal = v3(0.0f, 0.0f, 0.0f);
+                        if (bestK != 0xFFFFFFFFu) {
+                            int src = (int)(bestK & 31u);
+                            float u = __shfl_sync(0xFFFFFFFFu, bestU, src);
+                            float v = __shfl_sync(0xFFFFFFFFu, bestV, src);
+                            uint32_t g = __ldg(&ent.triBegin) + bestK;
+                            V3 e1 = v3(__ldg(tri.e1x + g), __ldg(tri.e1y + g), __ldg(tri.e1z + g));
+                            V3 e2 = v3(__ldg(tri.e2x + g), __ldg(tri.e2y + g), __ldg(tri.e2z + g));
+                            localNormal = cnormalize(ccross(e1, e2));
+                            float w = 1.0f - u - v;
+                            float2 t0 = __ldg(&tri.uv[(size_t)g * 3 + 0]);
+                            float2 t1 = __ldg(&tri.uv[(size_t)g * 3 + 1]);
+                            float2 t2 = __ldg(&tri.uv[(size_t)g * 3 + 2]);
+                            meshT = bestT;
+                            meshU = (t0.x * w + t1.x * u) + t2.x * v;
+                            meshV = (t0.y * w + t1.y * u) + t2.y * v;
+                        }
+                        V3 localHit = v3(lo.x + ld.x * meshT, lo.y + ld.y * meshT,
+                            lo.z + ld.z * meshT);
+                        V3 worldHit = mat_mul(ent.model, localHit, 1.0f);
+                        float t = cdot(v3(worldHit.x - o.x, worldHit.y - o.y, worldHit.z - o.z), d);
+                        V3 worldNormal = cnormalize(mat_mul(ent.model, localNormal, 0.0f));
+                        if (t >= 0.0f && t < res.t) {
+                            res.t = t;
+                            res.material = __ldg(&ent.material);
+                            res.normal = worldNormal;
+                            res.u = meshU;
+                            res.v = meshV;
+                        }
+                        if (ne < entityCount) {
+                            lo = mat_mul(ents[ne].inv, o, 1.0f);
+                            ld = cnormalize(mat_mul(ents[ne].inv, d, 0.0f));
+                            bestT = kF32Max;
+                            bestU = bestV = 0.0f;
+                            bestK = 0xFFFFFFFFu;
+                        }
+                    }
+                }
+                __syncthreads();  // chunk consumed, next chunk staged
+                e = ne;
+                c = nc;
+                buf ^= 1;
+            }
+        }
+        if (!active) continue;
+        // ---- shade: test_compute.comp.glsl:558-600 (warp-uniform)
+        rays++;
+        bool more = false;
+        if (res.t > 0.0f && res.t < kF32Max) {
+            hits++;
+            float r0 = rng.bilateral();
+            float r1 = rng.bilateral();
+            float r2 = rng.bilateral();
+            V3 dir = cnormalize(v3(res.normal.x + r0, res.normal.y + r1, res.normal.z + r2));
+            if (cdot(dir, res.normal) < 0.0f) dir = v3(-dir.x, -dir.y, -dir.z);
+            path[len].material = res.material;
+            path[len].normal = res.normal;
+            path[len].incoming = dir;
+            path[len].u = res.u;
+            path[len].v = res.v;
+            len++;
+            V3 wp = v3(o.x + d.x * res.t, o.y + d.y * res.t, o.z + d.z * res.t);
+            o = v3(wp.x + res.normal.x * 0.001f, wp.y + res.normal.y * 0.001f,
+                wp.z + res.normal.z * 0.001f);
+            d = dir;
+            bounce++;
+            more = bounce < kMaxBounces;
+        } else {
+            path[len].material = kMaterialBlack;
+            path[len].normal = v3(0.0f, 0.0f, 0.0f);
+            path[len].incoming = v3(0.0f, 0.0f, 0.0f);
+            path[len].u = path[len].v = 0.0f;
+            len++;
+        }
+        if (more) continue;
+        V3 radiance = path_radiance_cpt(path, len, tex, texW, texH);
+        paths++;
+        if (lane == 0)
+            image[(size_t)y * view.width + x] = make_float4(0.0f + radiance.x * 1.0f,
+                0.0f + radiance.y * 1.0f, 0.0f + radiance.z * 1.0f, 1.0f);
+        // next pixel of the tile in scanline order
+        if (++x >= maxX) {
+            x = minX;
+            y++;
+        }
+        if (y >= maxY)
+            active = false;
+        else
+            start_pixel();
     }
     if (lane == 0) {
         atomicAdd(counters.rays, (unsigned long long)rays);
