@@ -61,7 +61,7 @@ def parse_args():
     ap.add_argument("--dn-scenes", type=int, default=125)
     ap.add_argument("--dn-crops", type=int, default=16)
     ap.add_argument("--dn-ref-spp", type=int, default=4096)
-    ap.add_argument("--dn-steps", type=int, default=2000)
+    ap.add_argument("--dn-steps", type=int, default=4000)
     ap.add_argument("--dn-lr", type=float, default=1e-4)
     ap.add_argument("--dn-eval-seeds", type=int, default=50)
     ap.add_argument("--dn-eval-crop", type=int, default=256)
