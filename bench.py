@@ -118,6 +118,18 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_bf16_peak():
+    """Dense BF16 tensor throughput (TFLOP/s) measured on this machine (burst:
+    the denoiser kernels are timed on their own), else the documented fallback."""
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured bf16_tflops (burst)"
+    return 1900.0, "fallback"
+
+
 def profiled_traffic():
     """DRAM bytes per ray of the closest-hit kernels from the committed ncu
     summary profiles/trace_kernel_dram.md (its `dram_bytes_per_ray:` line);
@@ -675,6 +687,7 @@ def run_config5(args):
                               [(48, 25, 1)])
     plain_ms = need * ms_per_spp if need else None
     den_total_ms = tin_ms + dn_ms
+    bf16_peak = measured_bf16_peak()
     value = (plain_ms / den_total_ms) if (plain_ms and in_spp) else None
     line = {
         "metric": "time-to-relMSE 0.01 at 1080p: plain PT / (low spp + denoiser) (config 5)",
@@ -690,6 +703,10 @@ def run_config5(args):
         "plain_relmse_by_spp": plain_mean, "plain_spp_for_0.01": need,
         "ms_plain_per_spp_1080p": ms_per_spp, "ms_input_render_1080p": tin_ms,
         "ms_denoise_1080p": dn_ms, "denoiser_tflops": flops / (dn_ms * 1e-3) / 1e12,
+        "roofline": {"bound": "tensor", "kernel": "denoiser inference (8 x k_conv3x3_tc + filter)",
+                     "achieved": flops / (dn_ms * 1e-3) / 1e12, "peak": bf16_peak[0],
+                     "peak_source": bf16_peak[1], "unit": "TFLOP/s",
+                     "frac": flops / (dn_ms * 1e-3) / 1e12 / bf16_peak[0], "traffic": None},
         "plain_ms_to_0.01": plain_ms, "denoised_ms_to_0.01": den_total_ms if in_spp else None,
         "train_ms": train_ms, "dataset_s": data_s, "losses": losses,
         "params": net.parameters_count(),

@@ -186,6 +186,14 @@ uint32_t gbsp_calculate_film_positions(const gbsp_camera *camera,
 /* replaces sp_InitializeScene (src/sp_scene.cpp:1-5) */
 int gbsp_scene_create(gbsp_runtime *rt, gbsp_scene **out);
 int gbsp_scene_destroy(gbsp_scene *scene);
+/* Triangle test of every query and render of this scene.  REFERENCE_MT
+ * (default) is RayIntersectTriangleMT (src/ray_intersection.cpp:156-190), the
+ * test the bit-exact parity gate runs; WATERTIGHT is the watertight test of
+ * Woop, Benthin and Wald (JCGT 2013), which cannot let a ray slip between
+ * triangles sharing an edge (same face culling).  No reference counterpart. */
+#define GBSP_ISECT_REFERENCE_MT 0u
+#define GBSP_ISECT_WATERTIGHT 1u
+int gbsp_scene_set_intersection(gbsp_scene *scene, uint32_t mode);
 /* replaces sp_CreateMesh + sp_BuildMeshMidphase (src/sp_scene.cpp:8-54):
  * copies the vertices and indices to the device and builds the mesh BVH
  * there.  *meshOut receives the mesh handle used by add_object. */

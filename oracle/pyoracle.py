@@ -334,6 +334,11 @@ class World:
         assert self.kind == "port"
         self.L.fn("world_set_build_bvh")(self.h, _i32(int(on)))
 
+    def set_watertight(self, on: bool):
+        """Brute-force queries (closest_brute) use the watertight triangle test."""
+        assert self.kind == "port"
+        self.L.fn("world_set_watertight")(self.h, _i32(int(on)))
+
     def closest_brute(self, rays, threads=None):
         assert self.kind == "port"
         rays = _f32(rays).reshape(-1, 6)
@@ -476,4 +481,12 @@ def create_irradiance_cube_map(equirect: np.ndarray, width: int, height: int, sp
                                                 _u32(mode), _p(out))
         if rc != 0:
             raise RuntimeError("the reference asserted in CreateIrradianceCubeMap")
+    return out
+
+
+def ray_triangle_watertight(o, d, a, b, c):
+    """Watertight test of the port: (t, u, v); t = -1 on a miss."""
+    out = np.zeros(3, np.float32)
+    _Lib.get("port").lib.oracle_ray_triangle_watertight(
+        _p(_f32(o, 3)), _p(_f32(d, 3)), _p(_f32(a, 3)), _p(_f32(b, 3)), _p(_f32(c, 3)), _p(out))
     return out

@@ -292,6 +292,48 @@ TriHit ray_triangle_mt(F3 o, F3 d, F3 a, F3 b, F3 c)
     return r;
 }
 
+// Watertight test of Woop, Benthin and Wald (JCGT 2013), restated for the
+// optional intersection mode (no reference counterpart): translate to the ray
+// origin, shear so the ray runs along +z (kz = largest |d| component, x / y
+// swapped when d[kz] < 0 to keep the winding), 2D edge functions U, V, W with
+// a double-precision recompute when one rounds to exactly zero, two-sided
+// edge test, then the same face culling as ray_triangle_mt; uv = weights of
+// b and c.
+TriHit ray_triangle_watertight(F3 o, F3 d, F3 a, F3 b, F3 c)
+{
+    TriHit r = {};
+    r.t = -1.0f;
+    const float dv[3] = {d.x, d.y, d.z};
+    float mx_ = std::fabs(d.x), my_ = std::fabs(d.y), mz_ = std::fabs(d.z);
+    int kz = mx_ > my_ ? (mx_ > mz_ ? 0 : 2) : (my_ > mz_ ? 1 : 2);
+    int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+    if (dv[kz] < 0.0f) std::swap(kx, ky);
+    float sx = dv[kx] / dv[kz], sy = dv[ky] / dv[kz], sz = 1.0f / dv[kz];
+    F3 A3 = a - o, B3 = b - o, C3 = c - o;
+    const float A[3] = {A3.x, A3.y, A3.z}, B[3] = {B3.x, B3.y, B3.z}, C[3] = {C3.x, C3.y, C3.z};
+    float ax = A[kx] - sx * A[kz], ay = A[ky] - sy * A[kz];
+    float bx = B[kx] - sx * B[kz], by = B[ky] - sy * B[kz];
+    float cx = C[kx] - sx * C[kz], cy = C[ky] - sy * C[kz];
+    float U = cx * by - cy * bx, V = ax * cy - ay * cx, W = bx * ay - by * ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f)
+    {
+        U = (float)((double)cx * (double)by - (double)cy * (double)bx);
+        V = (float)((double)ax * (double)cy - (double)ay * (double)cx);
+        W = (float)((double)bx * (double)ay - (double)by * (double)ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return r;
+    float det = U + V + W;
+    if (det == 0.0f) return r;
+    float T = (U * (sz * A[kz]) + V * (sz * B[kz])) + W * (sz * C[kz]);
+    float inv = 1.0f / det;
+    F3 n = cross3(b - a, c - a);
+    if (!(dot3(d, n) < 0.0f)) return r;
+    r.t = T * inv;
+    r.uv = F2{V * inv, W * inv};
+    r.normal = n;
+    return r;
+}
+
 // simd.h:198-271: 4-box slab test; hit iff max(0, max(tmin)) <= min(tmax)
 inline bool slab_hit(F3 bmin, F3 bmax, F3 o, F3 invd)
 {
@@ -600,6 +642,7 @@ struct World
     bool haveSky = false;
     oracle_options opt = {1, 3, 10.0f, 32, 128};
     bool buildMeshBvh = true;  // false: meshes are only queried by brute force
+    bool watertight = false;   // brute-force queries use ray_triangle_watertight
 };
 
 const Material *find_material(const World &w, uint32_t id)  // sp_material_system.cpp:15-28
@@ -1366,6 +1409,16 @@ double oracle_world_render_hashed_mt(void *wp, uint32_t width, uint32_t height,
 }
 
 void oracle_world_set_build_bvh(void *wp, int on) { ((World *)wp)->buildMeshBvh = on != 0; }
+void oracle_world_set_watertight(void *wp, int on) { ((World *)wp)->watertight = on != 0; }
+
+void oracle_ray_triangle_watertight(const float *o, const float *d, const float *a,
+    const float *b, const float *c, float *out)
+{
+    TriHit h = ray_triangle_watertight(ld3(o), ld3(d), ld3(a), ld3(b), ld3(c));
+    out[0] = h.t;
+    out[1] = h.uv.x;
+    out[2] = h.uv.y;
+}
 
 // PerformToneMapping (src/shaders/post_processing.frag.glsl:19-26) restated
 // in C, then ToColor (src/math_lib.h:523-532).
@@ -1423,7 +1476,8 @@ int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
                     F3 a = mesh.pos[mesh.idx[3 * t]], b = mesh.pos[mesh.idx[3 * t + 1]],
                        c = mesh.pos[mesh.idx[3 * t + 2]];
                     if (!slab_hit(vmin3(a, vmin3(b, c)), vmax3(a, vmax3(b, c)), lo, linvd)) continue;
-                    TriHit h = ray_triangle_mt(lo, ld, a, b, c);
+                    TriHit h = w.watertight ? ray_triangle_watertight(lo, ld, a, b, c)
+                                            : ray_triangle_mt(lo, ld, a, b, c);
                     if (h.t > 0.0f && (h.t < lbest || lbest < 0.0f))
                     {
                         lbest = h.t;

@@ -111,6 +111,11 @@ int oracle_world_closest(void *w, uint32_t rayCount, const float *rays,
 // Meshes added after this call skip the reference's O(n^2 log n) BVH build
 // (they can then only be queried with oracle_world_closest_brute).
 void oracle_world_set_build_bvh(void *w, int on);
+// Brute-force queries use the watertight triangle test (Woop et al. 2013).
+void oracle_world_set_watertight(void *w, int on);
+// out = t (-1 miss), u, v of the watertight test with the reference's culling.
+void oracle_ray_triangle_watertight(const float *o, const float *d, const float *a,
+    const float *b, const float *c, float *out);
 // Display conversion: Reinhard + gamma 1/2.2, then 8-bit packing.
 void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out);
 int oracle_world_closest_brute(void *w, uint32_t rayCount, const float *rays,

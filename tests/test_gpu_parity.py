@@ -178,10 +178,11 @@ def soup_world(n_tris, seed, bvh=True):
     return s, w
 
 
-def gpu_closest(rt, s, rays):
+def gpu_closest(rt, s, rays, isect=gbsp.ISECT_REFERENCE_MT):
     import torch
 
     scene, ms, _ = gbsp.upload_scene(rt, s)
+    scene.set_intersection(isect)
     n = len(rays)
     packed = np.zeros((n, 8), np.float32)
     packed[:, 0:3] = rays[:, 0:3]
@@ -327,3 +328,33 @@ def test_per_lane_trace_matches_static(rt, kind):
                   "triangle_tests", "midphase_box_tests", "mesh_tests_performed",
                   "broadphase_node_visits"):
             assert ma[k] == mb[k], (k, ma[k], mb[k])
+
+
+def test_watertight_mode_closes_shared_edges(rt):
+    """GBSP_ISECT_WATERTIGHT: rays aimed at the shared edges and vertices of
+    a closed icosphere never miss, and every query agrees bit for bit with the
+    oracle's restatement of the same watertight test (brute force)."""
+    import pyoracle as po
+    from test_watertight_oracle import edge_rays
+
+    rays, v, i = edge_rays(level=3)
+    s = scenes.Scene(name="closed icosphere", meshes=[(v, i, False)],
+                     objects=[scenes.SceneObject(0, 1, (0.0, 0.0, 0.0), scenes.IDENTITY_QUAT,
+                                                 (1.0, 1.0, 1.0))],
+                     materials={1: scenes.material(albedo=(0.5, 0.5, 0.5))})
+    w = po.World("port")
+    w.set_build_bvh(False)
+    w.add_mesh(v, i)
+    w.add_object(0, 1, (0, 0, 0), (0, 0, 0, 1), (1, 1, 1))
+    w.build()
+    misses = {}
+    for mode, wt in ((gbsp.ISECT_REFERENCE_MT, False), (gbsp.ISECT_WATERTIGHT, True)):
+        t, tri, obj = gpu_closest(rt, s, rays, mode)
+        w.set_watertight(wt)
+        rt_, robj, rtri = w.closest_brute(rays)
+        assert np.array_equal(tri, rtri), f"mode {mode}: triangle ids differ from the oracle"
+        h = tri >= 0
+        assert np.array_equal(bits(t[h]), bits(rt_[h]))
+        misses[mode] = int((tri < 0).sum())
+    print(f"edge/vertex rays {len(rays)}: misses MT {misses[0]}, watertight {misses[1]}")
+    assert misses[gbsp.ISECT_WATERTIGHT] == 0

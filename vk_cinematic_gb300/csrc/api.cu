@@ -426,6 +426,15 @@ int gbsp_scene_create(gbsp_runtime *rt, gbsp_scene **out)
     return GBSP_OK;
 }
 
+int gbsp_scene_set_intersection(gbsp_scene *scene, uint32_t mode)
+{
+    if (!scene) return set_error(GBSP_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (mode != GBSP_ISECT_REFERENCE_MT && mode != GBSP_ISECT_WATERTIGHT)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "unknown intersection mode %u", mode);
+    scene->isectMode = mode;
+    return GBSP_OK;
+}
+
 int gbsp_scene_destroy(gbsp_scene *scene)
 {
     if (!scene) return GBSP_OK;

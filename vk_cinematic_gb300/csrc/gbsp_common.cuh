@@ -228,6 +228,58 @@ GBSP_HD TriHit ray_triangle_mt(V3 o, V3 d, V3 a, V3 b, V3 c, V3 n)
     return r;
 }
 
+// Watertight ray/triangle test (Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013): the vertices are translated
+// to the ray origin and sheared so the ray runs along +z, and the 2D edge
+// functions U, V, W decide the hit; an edge function that rounds to exactly
+// zero is recomputed in double precision, so a ray through a shared edge or
+// vertex hits at least one of the triangles that share it.  Two-sided edge
+// test, then the reference's face culling (dot(d, n) < 0 with the stored
+// n = cross(b - a, c - a)); u, v are the weights of b and c, as in
+// ray_triangle_mt.
+GBSP_HD float axis_of(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+GBSP_HD TriHit ray_triangle_watertight(V3 o, V3 d, V3 a, V3 b, V3 c, V3 n)
+{
+    TriHit r;
+    r.hit = false;
+    r.t = r.u = r.v = 0.0f;
+    float ax_ = fabsf(d.x), ay_ = fabsf(d.y), az_ = fabsf(d.z);
+    int kz = ax_ > ay_ ? (ax_ > az_ ? 0 : 2) : (ay_ > az_ ? 1 : 2);
+    int kx = kz == 2 ? 0 : kz + 1;
+    int ky = kx == 2 ? 0 : kx + 1;
+    float dz = axis_of(d, kz);
+    if (dz < 0.0f) {
+        int tmp = kx;
+        kx = ky;
+        ky = tmp;
+    }
+    float sx = axis_of(d, kx) / dz, sy = axis_of(d, ky) / dz, sz = 1.0f / dz;
+    V3 A = sub(a, o), B = sub(b, o), C = sub(c, o);
+    float Az = axis_of(A, kz), Bz = axis_of(B, kz), Cz = axis_of(C, kz);
+    float Ax = axis_of(A, kx) - sx * Az, Ay = axis_of(A, ky) - sy * Az;
+    float Bx = axis_of(B, kx) - sx * Bz, By = axis_of(B, ky) - sy * Bz;
+    float Cx = axis_of(C, kx) - sx * Cz, Cy = axis_of(C, ky) - sy * Cz;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return r;
+    float det = U + V + W;
+    if (det == 0.0f) return r;
+    float T = (U * (sz * Az) + V * (sz * Bz)) + W * (sz * Cz);
+    float inv = 1.0f / det;
+    r.t = T * inv;
+    r.u = V * inv;
+    r.v = W * inv;
+    r.hit = dot(d, n) < 0.0f;
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Device scene layout
 // ---------------------------------------------------------------------------
@@ -310,6 +362,7 @@ struct SceneView {
     const Instance *instances;
     uint32_t tlasRoot;           // node index of the object BVH root, or kEmptyChild
     uint32_t instanceCount;
+    uint32_t watertight;         // 1: ray_triangle_watertight, 0: the reference's MT
 };
 
 struct MaterialView {

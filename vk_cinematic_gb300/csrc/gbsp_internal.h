@@ -155,6 +155,7 @@ struct gbsp_scene {
     uint32_t tlasDepth = 0;
     uint32_t maxDepth = 0;
     bool committed = false;
+    uint32_t isectMode = GBSP_ISECT_REFERENCE_MT;
     std::vector<uint32_t> leafOrder;  // object-BVH leaf position -> object index
     // resolved material slots depend on the material system; objects keep ids
     gbsp::SceneView view() const
@@ -167,6 +168,7 @@ struct gbsp_scene {
         v.instances = instances.ptr;
         v.tlasRoot = tlasRoot;
         v.instanceCount = (uint32_t)objects.size();
+        v.watertight = isectMode == GBSP_ISECT_WATERTIGHT ? 1u : 0u;
         return v;
     }
 };

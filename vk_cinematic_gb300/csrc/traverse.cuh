@@ -117,7 +117,8 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
         // the reference only reaches triangles whose own box passes
         V3 bl = vmin(a, vmin(b, c)), bh = vmax(a, vmax(b, c));
         if (slab_entry(bl, bh, lo, linvd) < 0.0f) continue;
-        TriHit h = ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
+        TriHit h = sv.watertight ? ray_triangle_watertight(lo, ld, a, b, c, v3(A.w, B.w, C.w))
+                                 : ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
         if (!h.hit || !(h.t > 0.0f)) continue;
         bool take = h.t < bestT;
         if (!take && h.t == bestT && bestPrim >= 0)

@@ -53,7 +53,7 @@ EXPORTS = [
     "gbsp_dn_filter", "gbsp_dn_relmse_backward", "gbsp_dn_adam", "gbsp_tonemap",
     "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
     "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
-    "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status",
+    "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status", "gbsp_scene_set_intersection",
 ]
 
 
@@ -67,6 +67,8 @@ FLAG_STAGE_TIMING = 1
 FLAG_AOV = 2
 FLAG_TRACE_PER_LANE = 4
 FLAG_TRACE_PER_WARP = 8
+ISECT_REFERENCE_MT = 0
+ISECT_WATERTIGHT = 1
 
 
 class ImagePlane(ctypes.Structure):
@@ -233,6 +235,10 @@ class Scene:
         h = _vp()
         _check(self.L.gbsp_scene_create(rt.h, ctypes.byref(h)))
         self.h = h
+
+    def set_intersection(self, mode: int):
+        """ISECT_REFERENCE_MT (default) or ISECT_WATERTIGHT."""
+        _check(self.L.gbsp_scene_set_intersection(self.h, _u32(mode)))
 
     def create_mesh(self, vertices: np.ndarray, indices: np.ndarray, smooth=False) -> int:
         v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 8)
