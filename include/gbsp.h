@@ -447,6 +447,16 @@ int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uin
 /* Reads and clears the denoiser kernels' device status word (1 = a tensor-core
  * completion wait ran out); GBSP_ERR_DEVICE_STATUS when it was set. */
 int gbsp_dn_status(uint32_t *status);
+/* Plain path tracing as the judge of the denoiser: A (the denoiser's input)
+ * and C are independent plain renders with the same spp, denoised = D(A);
+ * per tile x tile block (tile <= 16) the tile's relMSE is estimated as
+ * mean(((D - C)^2 - (A - C)^2 / 2) / (D^2 + 0.01)) (the second term removes
+ * C's own variance), and a tile above `bound` is served from the plain
+ * samples (A + C) / 2.  Frames are RGBA32F (B x H x W); tileErr / flags
+ * receive one value per tile (row-major per image). */
+int gbsp_dn_tile_fallback(void *stream, const float *denoised, const float *plainA,
+    const float *plainC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile, float bound,
+    float *out, float *tileErr, uint32_t *flags);
 /* wt[8-tap][ci][co] = w[tap][co][ci]: weights of the data-gradient conv. */
 int gbsp_dn_flip_transpose(void *stream, const uint16_t *w, uint32_t cout, uint32_t cin,
     uint16_t *wt);

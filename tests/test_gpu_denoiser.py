@@ -220,3 +220,39 @@ def test_short_training_reduces_loss(gpu_lib):
     den = net.denoise(noisy, aov)
     assert torch.isfinite(den).all()
     torch.cuda.set_stream(torch.cuda.default_stream())
+
+
+def test_tile_fallback_serves_bad_tiles_from_plain_samples(gpu_lib):
+    """gbsp_dn_tile_fallback: a tile where the 'denoised' image is wrong is
+    detected from two independent plain renders and replaced by their mean;
+    tiles where it is right keep it."""
+    import torch
+
+    from vk_cinematic_gb300.denoiser import _ptr, _stream
+
+    g = torch.Generator(device="cuda").manual_seed(5)
+    B, H, W, tile = 2, 40, 56, 16
+    mu = torch.full((B, H, W, 4), 1.0, device="cuda")
+    A = mu + 0.3 * torch.randn((B, H, W, 4), device="cuda", generator=g)
+    C = mu + 0.3 * torch.randn((B, H, W, 4), device="cuda", generator=g)
+    D = mu.clone()
+    D[1, 16:32, 32:48, :3] += 2.0  # one wrong tile: image 1, tile row 1, column 2
+    out = torch.empty_like(D)
+    tiles = B * ((H + tile - 1) // tile) * ((W + tile - 1) // tile)
+    err = torch.empty(tiles, dtype=torch.float32, device="cuda")
+    flags = torch.empty(tiles, dtype=torch.int32, device="cuda")
+    L = gbsp.load()
+    rc = L.gbsp_dn_tile_fallback(_stream(), _ptr(D), _ptr(A), _ptr(C), B, H, W, tile,
+                                 ctypes.c_float(0.05), _ptr(out), _ptr(err), _ptr(flags))
+    assert rc == 0, L.gbsp_last_error_string()
+    torch.cuda.synchronize()
+    f = flags.cpu().numpy().reshape(B, 3, 4)
+    bad = np.zeros((B, 3, 4), bool)
+    bad[1, 1, 2] = True
+    print("tile estimates", err.cpu().numpy().round(3).reshape(B, 3, 4))
+    assert np.array_equal(f.astype(bool), bad)
+    o = out.cpu()
+    assert torch.equal(o[1, 16:32, 32:48, :3], (0.5 * (A + C))[1, 16:32, 32:48, :3].cpu())
+    keep = torch.ones((B, H, W), dtype=torch.bool)
+    keep[1, 16:32, 32:48] = False
+    assert torch.equal(o[..., :3][keep], D.cpu()[..., :3][keep])

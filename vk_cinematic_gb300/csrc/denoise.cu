@@ -565,6 +565,67 @@ __global__ void k_filter(const float *__restrict__ logits, const float4 *__restr
     out[p] = make_float4(o.x, o.y, o.z, 1.0f);
 }
 
+// Per-tile error check of a denoised frame, judged by the plain path tracer.
+// A (the denoiser's input) and C are two independent plain renders with the
+// same spp, D the denoised A.  For unbiased plain estimates with variance s^2,
+// E[(D - C)^2] = (D - mu)^2 + s^2 and E[(A - C)^2] = 2 s^2, so per pixel and
+// channel (D - C)^2 - (A - C)^2 / 2 estimates the denoiser's squared error;
+// divided by D^2 + 0.01 and averaged over a tile it estimates the tile's
+// relMSE.  A tile whose estimate exceeds the bound is served from the plain
+// samples, (A + C) / 2; the others keep D.  One CTA of 256 threads per tile
+// (tile <= 16 x 16).  tileErr[t] receives the estimate, flags[t] 1 when the
+// tile fell back.
+__global__ void __launch_bounds__(256) k_tile_fallback(const float4 *__restrict__ D,
+    const float4 *__restrict__ A, const float4 *__restrict__ C, int B, int H, int W, int tile,
+    float bound, float4 *__restrict__ out, float *__restrict__ tileErr, uint32_t *__restrict__ flags)
+{
+    const int tilesX = (W + tile - 1) / tile, tilesY = (H + tile - 1) / tile;
+    const int t = blockIdx.x;
+    const int b = t / (tilesX * tilesY), ty = (t / tilesX) % tilesY, tx = t % tilesX;
+    const int lx = threadIdx.x % tile, ly = threadIdx.x / tile;
+    const int x = tx * tile + lx, y = ty * tile + ly;
+    const bool in = threadIdx.x < tile * tile && x < W && y < H;
+    const size_t p = ((size_t)b * H + y) * W + x;
+    float e = 0.0f, n = 0.0f;
+    float4 d = make_float4(0, 0, 0, 0), a = d, c = d;
+    if (in) {
+        d = D[p];
+        a = A[p];
+        c = C[p];
+        float dv[3] = {d.x, d.y, d.z}, av[3] = {a.x, a.y, a.z}, cv[3] = {c.x, c.y, c.z};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            float dc = dv[k] - cv[k], ac = av[k] - cv[k];
+            e += (dc * dc - 0.5f * ac * ac) / (dv[k] * dv[k] + 0.01f);
+        }
+        n = 3.0f;
+    }
+    __shared__ float sE[8], sN[8];
+    for (int off = 16; off; off >>= 1) {
+        e += __shfl_xor_sync(0xFFFFFFFFu, e, off);
+        n += __shfl_xor_sync(0xFFFFFFFFu, n, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sE[threadIdx.x >> 5] = e;
+        sN[threadIdx.x >> 5] = n;
+    }
+    __syncthreads();
+    float te = 0.0f, tn = 0.0f;
+    for (int k = 0; k < 8; k++) {
+        te += sE[k];
+        tn += sN[k];
+    }
+    const float est = tn > 0.0f ? te / tn : 0.0f;
+    const bool fallback = est > bound;
+    if (threadIdx.x == 0) {
+        tileErr[t] = est;
+        flags[t] = fallback ? 1u : 0u;
+    }
+    if (in)
+        out[p] = fallback ? make_float4(0.5f * (a.x + c.x), 0.5f * (a.y + c.y), 0.5f * (a.z + c.z), 1.0f)
+                          : d;
+}
+
 // relMSE = mean over pixels and channels of (out - ref)^2 / (ref^2 + 0.01);
 // writes dLogits (BF16, 32 channels, zeros beyond 25) and adds the loss sum.
 __global__ void k_relmse_bwd(const float *__restrict__ logits, const float4 *__restrict__ noisy,
@@ -766,6 +827,22 @@ int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32
     uint64_t n = (uint64_t)B * H * W;
     k_filter<<<blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(logits,
         reinterpret_cast<const float4 *>(noisy), B, H, W, reinterpret_cast<float4 *>(out));
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_tile_fallback(void *stream, const float *denoised, const float *plainA,
+    const float *plainC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile, float bound,
+    float *out, float *tileErr, uint32_t *flags)
+{
+    if (!denoised || !plainA || !plainC || !out || !tileErr || !flags || !B || !H || !W)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad fallback args");
+    if (tile < 1 || tile > 16) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile must be 1..16");
+    uint64_t tiles = (uint64_t)B * ((H + tile - 1) / tile) * ((W + tile - 1) / tile);
+    k_tile_fallback<<<(unsigned)tiles, 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(denoised), reinterpret_cast<const float4 *>(plainA),
+        reinterpret_cast<const float4 *>(plainC), (int)B, (int)H, (int)W, (int)tile, bound,
+        reinterpret_cast<float4 *>(out), tileErr, flags);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }

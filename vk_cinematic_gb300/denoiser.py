@@ -136,6 +136,26 @@ class KPCNN:
         logits, _ = self.forward(self.features(radiance, aov))
         return self.filter(logits, radiance)
 
+    def denoise_checked(self, radiance, aov, plain_check, bound=0.01, tile=16):
+        """Denoises `radiance` and lets the plain path tracer judge every
+        tile x tile block with an independent render `plain_check` of the same
+        spp (gbsp_dn_tile_fallback): blocks whose estimated relMSE exceeds
+        `bound` are served from the plain samples.  Returns (image,
+        per-tile estimates, per-tile fallback flags)."""
+        import torch
+
+        den = self.denoise(radiance, aov)
+        B, H, W, _ = radiance.shape
+        tiles = B * ((H + tile - 1) // tile) * ((W + tile - 1) // tile)
+        out = torch.empty_like(den)
+        err = torch.empty(tiles, dtype=torch.float32, device="cuda")
+        flags = torch.empty(tiles, dtype=torch.int32, device="cuda")
+        _check(self.L.gbsp_dn_tile_fallback(_stream(), _ptr(den), _ptr(radiance),
+                                            _ptr(plain_check), _u32(B), _u32(H), _u32(W),
+                                            _u32(tile), _f32(bound), _ptr(out), _ptr(err),
+                                            _ptr(flags)))
+        return out, err, flags
+
     # ---- training ------------------------------------------------------------------
     def data_grad(self, li, d):
         """dIn of layer li from its output gradient d (BF16), FP32."""

@@ -54,6 +54,7 @@ EXPORTS = [
     "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
     "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
     "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status", "gbsp_scene_set_intersection",
+    "gbsp_dn_tile_fallback",
 ]
 
 
