@@ -629,6 +629,8 @@ def run_config5(args):
     in_spps = [4, 8, 16]  # denoiser input spp candidates (trained on 4)
     plain = {k: [] for k in spps}
     den = {k: [] for k in in_spps}
+    checked = {k: [] for k in in_spps}
+    fell_back = {k: [] for k in in_spps}
     rng = np.random.default_rng(99)
     for e in range(args.dn_eval_seeds):
         se = denoiser.denoise_scene(20_000 + e)
@@ -643,6 +645,13 @@ def run_config5(args):
             rk, ak = sre.render(x0, y0, crop, crop, k, seed=5 + k, aov=True)
             d = net.denoise(rk.unsqueeze(0).contiguous(), ak.unsqueeze(0).contiguous())[0]
             den[k].append(denoiser.relmse(d, ref))
+            # the plain path tracer as the judge: an independent render of the same spp
+            ck, _ = sre.render(x0, y0, crop, crop, k, seed=1000 + k)
+            dc, _, fl = net.denoise_checked(rk.unsqueeze(0).contiguous(),
+                                            ak.unsqueeze(0).contiguous(),
+                                            ck.unsqueeze(0).contiguous(), bound=0.01)
+            checked[k].append(denoiser.relmse(dc[0], ref))
+            fell_back[k].append(float(fl.float().mean().item()))
     plain_mean = {k: float(np.mean(v)) for k, v in plain.items()}
     den_mean = {k: float(np.mean(v)) for k, v in den.items()}
     # spp plain path tracing needs for relMSE 0.01 (log-log interpolation)
@@ -700,6 +709,9 @@ def run_config5(args):
                    "eval_seeds": args.dn_eval_seeds, "eval_crop": crop,
                    "oracle_spp": args.dn_oracle_spp, "conv": net.conv_impl},
         "denoised_relmse_by_input_spp": den_mean, "denoiser_input_spp": in_spp,
+        "checked_by_plain_tiles": {k: {"relmse": float(np.mean(checked[k])),
+                                       "fallback_tile_fraction": float(np.mean(fell_back[k]))}
+                                   for k in in_spps},
         "plain_relmse_by_spp": plain_mean, "plain_spp_for_0.01": need,
         "ms_plain_per_spp_1080p": ms_per_spp, "ms_input_render_1080p": tin_ms,
         "ms_denoise_1080p": dn_ms, "denoiser_tflops": flops / (dn_ms * 1e-3) / 1e12,

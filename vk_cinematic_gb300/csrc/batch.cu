@@ -42,6 +42,7 @@ struct BatchItemDev {
 // single-scene render: images are bit-identical.
 // ---------------------------------------------------------------------------
 struct ManyScenes {
+    static constexpr bool kStageTlas = false;  // every path may have its own scene
     const BatchItemDev *items;
     const uint32_t *pathItem;
     __device__ __forceinline__ const SceneView &scene(uint32_t p) const

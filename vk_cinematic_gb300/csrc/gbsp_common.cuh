@@ -363,6 +363,7 @@ struct SceneView {
     uint32_t tlasRoot;           // node index of the object BVH root, or kEmptyChild
     uint32_t instanceCount;
     uint32_t watertight;         // 1: ray_triangle_watertight, 0: the reference's MT
+    uint32_t tlasFirst, tlasCount;  // the object BVH's nodes in the pool
 };
 
 struct MaterialView {

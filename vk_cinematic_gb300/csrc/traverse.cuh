@@ -42,21 +42,30 @@ struct TraceCounters {
 
 __device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765625f; }
 
-// Tests the 8 children of a node against the ray, pushing hits nearest-last.
-template <bool kCount>
-__device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
-    V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp, uint32_t *status,
-    TraceCounters &cnt)
+// Node loads: read-only global path, or shared memory (the staged object BVH).
+template <bool kShared>
+__device__ __forceinline__ float4 node_ld(const float4 *p)
 {
-    const float4 *p = reinterpret_cast<const float4 *>(nodes + ref);
+    if (kShared) return *p;
+    return __ldg(p);
+}
+
+// Tests the 8 children of a node against the ray, pushing hits nearest-last.
+// p: the node's 14 float4 (in global memory, or in shared memory with kShared).
+template <bool kCount, bool kShared = false>
+__device__ __forceinline__ void visit_node_at(const float4 *p, V3 o, V3 invd, float bound,
+    uint32_t *stackRef, float *stackT, int &sp, uint32_t *status, TraceCounters &cnt)
+{
     uint32_t nearRef = kEmptyChild;
     float nearT = kInf;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
-        float4 lx = __ldg(p + 0 + half), hx = __ldg(p + 2 + half);
-        float4 ly = __ldg(p + 4 + half), hy = __ldg(p + 6 + half);
-        float4 lz = __ldg(p + 8 + half), hz = __ldg(p + 10 + half);
-        uint4 ch = __ldg(reinterpret_cast<const uint4 *>(p + 12 + half));
+        float4 lx = node_ld<kShared>(p + 0 + half), hx = node_ld<kShared>(p + 2 + half);
+        float4 ly = node_ld<kShared>(p + 4 + half), hy = node_ld<kShared>(p + 6 + half);
+        float4 lz = node_ld<kShared>(p + 8 + half), hz = node_ld<kShared>(p + 10 + half);
+        float4 chf = node_ld<kShared>(p + 12 + half);
+        uint4 ch = make_uint4(__float_as_uint(chf.x), __float_as_uint(chf.y),
+            __float_as_uint(chf.z), __float_as_uint(chf.w));
         float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, hxs[4] = {hx.x, hx.y, hx.z, hx.w};
         float lys[4] = {ly.x, ly.y, ly.z, ly.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
         float lzs[4] = {lz.x, lz.y, lz.z, lz.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
@@ -102,6 +111,36 @@ __device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint
     }
 }
 
+template <bool kCount>
+__device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
+    V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp, uint32_t *status,
+    TraceCounters &cnt)
+{
+    visit_node_at<kCount, false>(reinterpret_cast<const float4 *>(nodes + ref), o, invd, bound,
+        stackRef, stackT, sp, status, cnt);
+}
+
+// The object BVH staged in shared memory by the trace kernels of a one-scene
+// launch (nodes [first, first + count) of the pool), or count 0.
+struct SmemTlas {
+    const float4 *nodes;
+    uint32_t first, count;
+};
+constexpr uint32_t kSmemTlasNodes = 64;  // 14,336 bytes of shared memory
+
+// An object-level node visit: from shared memory when staged.
+template <bool kCount>
+__device__ __forceinline__ void visit_top_node(const SmemTlas &st, const Node8 *__restrict__ nodes,
+    uint32_t ref, V3 o, V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp,
+    uint32_t *status, TraceCounters &cnt)
+{
+    if (ref - st.first < st.count)
+        visit_node_at<kCount, true>(st.nodes + (size_t)(ref - st.first) * 14, o, invd, bound,
+            stackRef, stackT, sp, status, cnt);
+    else
+        visit_node<kCount>(nodes, ref, o, invd, bound, stackRef, stackT, sp, status, cnt);
+}
+
 // Triangle candidates of one mesh leaf, in object space.
 template <bool kCount>
 __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
@@ -134,7 +173,7 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
 
 template <bool kCount>
 __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *status,
-    TraceCounters &cnt)
+    TraceCounters &cnt, const SmemTlas &st = SmemTlas{nullptr, 0, 0})
 {
     RayHit best;
     best.t = kInf;
@@ -163,8 +202,8 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
         if (te > prune_bound(best.t)) continue;
         if (!child_is_leaf(ref)) {
             if (kCount) cnt.topNodes++;
-            visit_node<kCount>(nodes, ref, o, invd, prune_bound(best.t), stackRef, stackT, sp,
-                status, cnt);
+            visit_top_node<kCount>(st, nodes, ref, o, invd, prune_bound(best.t), stackRef, stackT,
+                sp, status, cnt);
             continue;
         }
         // an object whose world box passed: descend into its mesh

@@ -50,6 +50,7 @@ struct WaveParams {
 // Scene source of the wave kernels: everything a path needs from its scene.
 // OneScene: one scene for the whole launch (a frame or a tile).
 struct OneScene {
+    static constexpr bool kStageTlas = true;  // one object BVH for the launch
     SceneView sv;
     MaterialView mv;
     uint32_t maxBounces;
@@ -100,6 +101,18 @@ __global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
+    // one-scene launches stage the object BVH in shared memory
+    __shared__ float4 sTlas[kSmemTlasNodes * 14];
+    SmemTlas st = {sTlas, 0, 0};
+    if constexpr (Src::kStageTlas) {
+        const SceneView &sv0 = src.scene(0);
+        uint32_t n = sv0.tlasCount <= kSmemTlasNodes ? sv0.tlasCount : 0u;
+        const float4 *g = reinterpret_cast<const float4 *>(sv0.nodes + sv0.tlasFirst);
+        for (uint32_t i = threadIdx.x; i < n * 14; i += blockDim.x) sTlas[i] = __ldg(g + i);
+        __syncthreads();
+        st.first = sv0.tlasFirst;
+        st.count = n;
+    }
     int lane = threadIdx.x & 31;
     uint32_t count = *queueCount;
     TraceCounters cnt = {0, 0, 0, 0, 0};
@@ -114,7 +127,7 @@ __global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict
             float4 o4 = rayO[i], d4 = rayD[i];
             const SceneView &sv = src.scene((uint32_t)__float_as_int(o4.w));
             RayHit h = trace_closest<true>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z), status,
-                cnt);
+                cnt, st);
             hitA[i] = make_int4(__float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v),
                 h.prim);
             hitInst[i] = h.inst;
@@ -157,6 +170,18 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
+    // one-scene launches stage the object BVH in shared memory
+    __shared__ float4 sTlas[kSmemTlasNodes * 14];
+    SmemTlas st = {sTlas, 0, 0};
+    if constexpr (Src::kStageTlas) {
+        const SceneView &sv0 = src.scene(0);
+        uint32_t n = sv0.tlasCount <= kSmemTlasNodes ? sv0.tlasCount : 0u;
+        const float4 *g = reinterpret_cast<const float4 *>(sv0.nodes + sv0.tlasFirst);
+        for (uint32_t i = threadIdx.x; i < n * 14; i += blockDim.x) sTlas[i] = __ldg(g + i);
+        __syncthreads();
+        st.first = sv0.tlasFirst;
+        st.count = n;
+    }
     const int lane = threadIdx.x & 31;
     const uint32_t laneMaskLt = (1u << lane) - 1u;
     const uint32_t count = *queueCount;
@@ -248,8 +273,12 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                     cnt.topNodes++;
                 else
                     cnt.meshNodes++;
-                visit_node<true>(src.scene(pathId).nodes, ref, mode == 1 ? o : lo, mode == 1 ? invd : linvd,
-                    bound, stackRef, stackT, sp, status, cnt);
+                if (mode == 1)
+                    visit_top_node<true>(st, src.scene(pathId).nodes, ref, o, invd, bound, stackRef,
+                        stackT, sp, status, cnt);
+                else
+                    visit_node<true>(src.scene(pathId).nodes, ref, lo, linvd, bound, stackRef,
+                        stackT, sp, status, cnt);
             } else if (mode == 1) {
                 // an object whose world box passed: enter its mesh
                 inst = leaf_first(ref);
