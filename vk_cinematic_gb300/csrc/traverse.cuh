@@ -126,7 +126,7 @@ struct SmemTlas {
     const float4 *nodes;
     uint32_t first, count;
 };
-constexpr uint32_t kSmemTlasNodes = 64;  // 14,336 bytes of shared memory
+constexpr uint32_t kSmemTlasNodes = 96;  // 21,504 bytes of shared memory
 
 // An object-level node visit: from shared memory when staged.
 template <bool kCount>
