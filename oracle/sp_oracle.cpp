@@ -1463,7 +1463,9 @@ int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
             for (size_t oi = 0; oi < w.objects.size(); oi++)
             {
                 const Object &obj = w.objects[oi];
-                if (!slab_hit(obj.aabbMin, obj.aabbMax, o, invd)) continue;
+                // the box gates are rounded slab tests; the watertight mode tests
+                // every triangle so that no gate can reject an edge or vertex ray
+                if (!w.watertight && !slab_hit(obj.aabbMin, obj.aabbMax, o, invd)) continue;
                 const Mesh &mesh = w.meshes[obj.mesh];
                 F3 lo = transform_point(o, obj.invModel);
                 F3 ld = normalize3(transform_vector(d, obj.invModel));
@@ -1475,7 +1477,9 @@ int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
                 {
                     F3 a = mesh.pos[mesh.idx[3 * t]], b = mesh.pos[mesh.idx[3 * t + 1]],
                        c = mesh.pos[mesh.idx[3 * t + 2]];
-                    if (!slab_hit(vmin3(a, vmin3(b, c)), vmax3(a, vmax3(b, c)), lo, linvd)) continue;
+                    if (!w.watertight &&
+                        !slab_hit(vmin3(a, vmin3(b, c)), vmax3(a, vmax3(b, c)), lo, linvd))
+                        continue;
                     TriHit h = w.watertight ? ray_triangle_watertight(lo, ld, a, b, c)
                                             : ray_triangle_mt(lo, ld, a, b, c);
                     if (h.t > 0.0f && (h.t < lbest || lbest < 0.0f))

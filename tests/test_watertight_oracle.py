@@ -67,7 +67,11 @@ def edge_rays(level=2, seed=3):
     origins = np.array(origins, np.float32)
     d = pts - origins
     d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
-    return np.concatenate([origins, d], axis=1).astype(np.float32), v, i
+    # keep rays that cross the surface: a ray grazing the silhouette may touch
+    # only a back face there, which culling rightly rejects
+    normal = pts / np.linalg.norm(pts, axis=1, keepdims=True)
+    keep = -(d * normal).sum(axis=1) > 0.3
+    return np.concatenate([origins, d], axis=1)[keep].astype(np.float32), v, i
 
 
 def test_no_ray_slips_through_shared_edges(port):

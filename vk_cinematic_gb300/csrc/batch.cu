@@ -42,7 +42,6 @@ struct BatchItemDev {
 // single-scene render: images are bit-identical.
 // ---------------------------------------------------------------------------
 struct ManyScenes {
-    static constexpr bool kStageTlas = false;  // every path may have its own scene
     const BatchItemDev *items;
     const uint32_t *pathItem;
     __device__ __forceinline__ const SceneView &scene(uint32_t p) const
@@ -161,6 +160,7 @@ __global__ void k_batch_reset(unsigned long long *work, unsigned long long *coun
     if (threadIdx.x < GBSP_METRIC_COUNT) counters[threadIdx.x] = 0;
 }
 
+template <bool kWT>
 __global__ void __launch_bounds__(256) k_batch(const BatchItemDev *__restrict__ items,
     uint32_t itemCount, uint64_t totalPixels, uint32_t chunk, unsigned long long *work,
     unsigned long long *counters, uint32_t *status)
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) k_batch(const BatchItemDev *__restrict__ 
             CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
             for (uint32_t s = 0; s < it.spp; s++) {
                 uint32_t rng = sample_seed(it.seed, x, y, s);
-                V3 r = trace_full_path<kBatchMaxBounces>(it.sv, it.mv, it.cam, x, y, rng,
+                V3 r = trace_full_path<kBatchMaxBounces, kWT>(it.sv, it.mv, it.cam, x, y, rng,
                     it.maxBounces, it.clampValue, status, cnt, rays, hits);
                 paths++;
                 if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
@@ -245,6 +245,7 @@ constexpr uint32_t kMaxRaySteps = 1u << 22;
 constexpr uint64_t kMaxBatchIterations = 1ull << 34;
 constexpr int kSmShade = 16;
 
+template <bool kWT>
 __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict__ items,
     uint32_t itemCount, uint64_t totalPixels, unsigned long long *work,
     unsigned long long *counters, uint32_t *status)
@@ -449,7 +450,8 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                     cnt.meshNodes++;
                 V3 ro = tmode == 1 ? o : lo;
                 V3 ri = tmode == 1 ? invd : linvd;
-                visit_node<true>(sv.nodes, ref, ro, ri, bound, stackRef, stackT, sp, status, cnt);
+                visit_node<true, kWT>(sv.nodes, ref, ro, ri, bound, stackRef, stackT, sp, status,
+                    cnt);
                 return;
             }
             if (tmode == 1) {
@@ -476,7 +478,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                 tmode = 2;
                 return;
             }
-            visit_leaf<true>(sv, ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+            visit_leaf<true, kWT>(sv, ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
         };
         if (doShade && phase == 2)
             shade_step();
@@ -517,6 +519,7 @@ struct gbsp_batch {
     uint64_t totalPixels = 0, totalPaths = 0;
     gbsp_batch_config cfg = {128, 1, 8, 1, GBSP_BATCH_WAVEFRONT, 0};
     cudaGraphExec_t exec = nullptr;
+    bool watertight = false;  // every item's scene uses the same triangle test
     // batched wavefront
     std::vector<BatchItemDev> hostItems;
     std::vector<BatchWave> waves;
@@ -608,12 +611,8 @@ static void enqueue_wavefront(gbsp_batch *b)
             const float4 *qD = wb.rayD + ((bn & 1) ? wb.cap : 0);
             k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
             // primary rays per warp, bounce rays per lane (the frame renderer's default)
-            if (bn == 0)
-                k_trace<<<grid, 128, 0, s>>>(src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl,
-                    counters, rt->dStatus);
-            else
-                k_trace_lane<<<grid, 128, 0, s>>>(src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl,
-                    counters, rt->dStatus);
+            launch_trace_stage(bn > 0, b->watertight, grid, s, src, qO, qD, ctl + inQ, wb.hitA,
+                wb.hitInst, ctl, counters, rt->dStatus);
             k_shade<<<grid, 128, 0, s>>>(src, wb, bn, inQ, ctl, counters);
         }
         k_baccumulate<<<(w.pixels + 255) / 256, 256, 0, s>>>(b->dItems.ptr, n, w, wb, counters);
@@ -635,10 +634,12 @@ static int enqueue(gbsp_batch *b)
     if (b->cfg.kernel == GBSP_BATCH_WAVEFRONT)
         enqueue_wavefront(b);
     else if (b->cfg.kernel == GBSP_BATCH_PATH_STATE)
-        k_batch_sm<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(),
+        (b->watertight ? k_batch_sm<true> : k_batch_sm<false>)<<<grid, b->cfg.block, 0, s>>>(
+            b->dItems.ptr, (uint32_t)b->items.size(),
             b->totalPixels, b->dWork.ptr, rt->dCounters, rt->dStatus);
     else
-        k_batch<<<grid, b->cfg.block, 0, s>>>(b->dItems.ptr, (uint32_t)b->items.size(),
+        (b->watertight ? k_batch<true> : k_batch<false>)<<<grid, b->cfg.block, 0, s>>>(
+            b->dItems.ptr, (uint32_t)b->items.size(),
             b->totalPixels, b->cfg.chunk, b->dWork.ptr, rt->dCounters, rt->dStatus);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
@@ -717,6 +718,13 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
             rc = set_error(GBSP_ERR_INVALID_ARGUMENT,
                 "batch item %u: hash-per-sample seeding and at most %d bounces", i,
                 kBatchMaxBounces);
+            break;
+        }
+        bool wt = it.scene->isectMode == GBSP_ISECT_WATERTIGHT;
+        if (i == 0) b->watertight = wt;
+        if (wt != b->watertight) {
+            rc = set_error(GBSP_ERR_INVALID_ARGUMENT,
+                "batch item %u: all items must use the same intersection mode", i);
             break;
         }
         MaterialView mv;

@@ -201,6 +201,22 @@ GBSP_HD float slab_entry(V3 lo, V3 hi, V3 o, V3 invd)
     return tn <= tf ? tn : -1.0f;
 }
 
+// The same test with the exit distance scaled by 1 + 2 gamma(3) (Ize, "Robust
+// BVH Ray Traversal", JCGT 2(2), 2013): a rounded slab test can no longer
+// reject a ray that touches the box, which the watertight mode relies on.
+GBSP_HD float slab_entry_robust(V3 lo, V3 hi, V3 o, V3 invd)
+{
+    float t0x = (lo.x - o.x) * invd.x, t1x = (hi.x - o.x) * invd.x;
+    float t0y = (lo.y - o.y) * invd.y, t1y = (hi.y - o.y) * invd.y;
+    float t0z = (lo.z - o.z) * invd.z, t1z = (hi.z - o.z) * invd.z;
+    float mnx = t0x < t1x ? t0x : t1x, mxx = t0x > t1x ? t0x : t1x;
+    float mny = t0y < t1y ? t0y : t1y, mxy = t0y > t1y ? t0y : t1y;
+    float mnz = t0z < t1z ? t0z : t1z, mxz = t0z > t1z ? t0z : t1z;
+    float tn = rmax(0.0f, rmax(mnx, rmax(mny, mnz)));
+    float tf = rmin(mxx, rmin(mxy, mxz)) * 1.0000004f;
+    return tn <= tf ? tn : -1.0f;
+}
+
 struct TriHit {
     float t, u, v;
     bool hit;
@@ -363,7 +379,6 @@ struct SceneView {
     uint32_t tlasRoot;           // node index of the object BVH root, or kEmptyChild
     uint32_t instanceCount;
     uint32_t watertight;         // 1: ray_triangle_watertight, 0: the reference's MT
-    uint32_t tlasFirst, tlasCount;  // the object BVH's nodes in the pool
 };
 
 struct MaterialView {

@@ -169,8 +169,6 @@ struct gbsp_scene {
         v.tlasRoot = tlasRoot;
         v.instanceCount = (uint32_t)objects.size();
         v.watertight = isectMode == GBSP_ISECT_WATERTIGHT ? 1u : 0u;
-        v.tlasFirst = meshNodeCount;
-        v.tlasCount = tlasRoot == gbsp::kEmptyChild ? 0u : totalNodeCount - meshNodeCount;
         return v;
     }
 };

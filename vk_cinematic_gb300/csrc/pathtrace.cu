@@ -34,6 +34,7 @@ namespace gbsp {
 // ---------------------------------------------------------------------------
 constexpr int kMaxSeqBounces = 16;
 
+template <bool kWT>
 __global__ void __launch_bounds__(64) k_tile_sequential(SceneView sv, MaterialView mv,
     CameraParams cam, const uint4 *tiles, uint32_t tileCount, uint32_t *rngStates, uint32_t spp,
     uint32_t maxBounces, float clampValue, float4 *image, uint32_t imageWidth,
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(64) k_tile_sequential(SceneView sv, MaterialVi
                 camera_ray(cam, x, y, rng, o, d);
                 uint32_t len = 0;
                 for (uint32_t b = 0; b < maxBounces; b++) {
-                    RayHit h = trace_closest<true>(sv, o, d, status, cnt);
+                    RayHit h = trace_closest<true, kWT>(sv, o, d, status, cnt);
                     rays++;
                     float4 ec, aa;
                     if (h.prim >= 0 && h.t > 0.0f) {
@@ -149,7 +150,8 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
             (rc = dStates.upload(states.data(), states.size(), s)))
             return rc;
         uint32_t n = (uint32_t)tiles.size();
-        k_tile_sequential<<<(n + 63) / 64, 64, 0, s>>>(sv, mv, cam, dTiles.ptr, n, dStates.ptr, spp,
+        auto seqKernel = sv.watertight ? k_tile_sequential<true> : k_tile_sequential<false>;
+        seqKernel<<<(n + 63) / 64, 64, 0, s>>>(sv, mv, cam, dTiles.ptr, n, dStates.ptr, spp,
             maxBounces, opt.radiance_clamp, dImage, imageWidth, counters, rt->dStatus);
         GBSP_CUDA_TRY(cudaGetLastError());
         rt->launches += 1;
@@ -221,12 +223,8 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
                 int e0 = timing ? rt->stage_event(s) : -1;
                 bool perLane = (opt.flags & GBSP_FLAG_TRACE_PER_LANE) ||
                     (!(opt.flags & GBSP_FLAG_TRACE_PER_WARP) && b > 0);
-                if (perLane)
-                    k_trace_lane<<<persistentGrid, 128, 0, s>>>(one, qO, qD, ctl + inQ, wb.hitA,
-                        wb.hitInst, ctl, counters, rt->dStatus);
-                else
-                    k_trace<<<persistentGrid, 128, 0, s>>>(one, qO, qD, ctl + inQ, wb.hitA,
-                        wb.hitInst, ctl, counters, rt->dStatus);
+                launch_trace_stage(perLane, sv.watertight != 0, persistentGrid, s, one, qO, qD,
+                    ctl + inQ, wb.hitA, wb.hitInst, ctl, counters, rt->dStatus);
                 int e1 = timing ? rt->stage_event(s) : -1;
                 k_shade<<<persistentGrid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
                 int e2 = timing ? rt->stage_event(s) : -1;
@@ -420,9 +418,9 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
                 int inQ = (b & 1) ? kCtlQueue1 : kCtlQueue0;
                 int outQ = (b & 1) ? kCtlQueue0 : kCtlQueue1;
                 k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
-                k_trace<<<grid, 128, 0, s>>>(one, wb.rayO + ((b & 1) ? wb.cap : 0),
-                    wb.rayD + ((b & 1) ? wb.cap : 0), ctl + inQ, wb.hitA, wb.hitInst, ctl,
-                    counters, status);
+                launch_trace_stage(b > 0, one.sv.watertight != 0, grid, s, one,
+                    wb.rayO + ((b & 1) ? wb.cap : 0), wb.rayD + ((b & 1) ? wb.cap : 0), ctl + inQ,
+                    wb.hitA, wb.hitInst, ctl, counters, status);
                 k_shade<<<grid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
             }
         }

@@ -129,7 +129,7 @@ __device__ __forceinline__ V3 path_radiance(const float4 *vertE, const float4 *v
 // One whole path in one thread: the body of the reference's per-sample loop
 // (src/simd_path_tracer.cpp:208-324) - jitter and camera ray drawn from
 // `rng`, up to maxBounces closest-hit queries, per-vertex terms, reverse pass.
-template <int kMaxBounces>
+template <int kMaxBounces, bool kWT = false>
 __device__ __forceinline__ V3 trace_full_path(const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, uint32_t x, uint32_t y, uint32_t &rng, uint32_t maxBounces,
     float clampValue, uint32_t *status, TraceCounters &cnt, uint32_t &rays, uint32_t &hits)
@@ -140,7 +140,7 @@ __device__ __forceinline__ V3 trace_full_path(const SceneView &sv, const Materia
     uint32_t len = 0;
     if (maxBounces > (uint32_t)kMaxBounces) maxBounces = kMaxBounces;
     for (uint32_t b = 0; b < maxBounces; b++) {
-        RayHit h = trace_closest<true>(sv, o, d, status, cnt);
+        RayHit h = trace_closest<true, kWT>(sv, o, d, status, cnt);
         rays++;
         float4 ec, aa;
         if (h.prim >= 0 && h.t > 0.0f) {

@@ -29,6 +29,7 @@ __device__ __forceinline__ void warp_add_counters(unsigned long long *counters,
     }
 }
 
+template <bool kWT>
 __global__ void __launch_bounds__(128) k_intersect(SceneView sv, const float4 *__restrict__ rays,
     uint32_t count, float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut,
     uint32_t *matOut, unsigned int *work, unsigned long long *counters, uint32_t *status)
@@ -44,7 +45,7 @@ __global__ void __launch_bounds__(128) k_intersect(SceneView sv, const float4 *_
         uint32_t i = base + lane;
         if (i < count) {
             float4 o4 = __ldg(rays + 2 * (size_t)i), d4 = __ldg(rays + 2 * (size_t)i + 1);
-            RayHit h = trace_closest<true>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z), status,
+            RayHit h = trace_closest<true, kWT>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z), status,
                 cnt);
             bool hit = h.prim >= 0;
             rays_done++;
@@ -87,7 +88,8 @@ int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const 
     int grid = smCount * 8;
     uint64_t needed = ((uint64_t)count + 127) / 128;
     if ((uint64_t)grid > needed) grid = (int)needed;
-    k_intersect<<<grid, 128, 0, s>>>(sv, rays, count, tOut, triOut, objOut, attrOut, matOut, work,
+    auto kern = sv.watertight ? k_intersect<true> : k_intersect<false>;
+    kern<<<grid, 128, 0, s>>>(sv, rays, count, tOut, triOut, objOut, attrOut, matOut, work,
         counters, dStatus);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;

@@ -42,30 +42,22 @@ struct TraceCounters {
 
 __device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765625f; }
 
-// Node loads: read-only global path, or shared memory (the staged object BVH).
-template <bool kShared>
-__device__ __forceinline__ float4 node_ld(const float4 *p)
-{
-    if (kShared) return *p;
-    return __ldg(p);
-}
-
 // Tests the 8 children of a node against the ray, pushing hits nearest-last.
-// p: the node's 14 float4 (in global memory, or in shared memory with kShared).
-template <bool kCount, bool kShared = false>
-__device__ __forceinline__ void visit_node_at(const float4 *p, V3 o, V3 invd, float bound,
-    uint32_t *stackRef, float *stackT, int &sp, uint32_t *status, TraceCounters &cnt)
+// kWT: the watertight mode's robust slab test.
+template <bool kCount, bool kWT = false>
+__device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
+    V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp, uint32_t *status,
+    TraceCounters &cnt)
 {
+    const float4 *p = reinterpret_cast<const float4 *>(nodes + ref);
     uint32_t nearRef = kEmptyChild;
     float nearT = kInf;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
-        float4 lx = node_ld<kShared>(p + 0 + half), hx = node_ld<kShared>(p + 2 + half);
-        float4 ly = node_ld<kShared>(p + 4 + half), hy = node_ld<kShared>(p + 6 + half);
-        float4 lz = node_ld<kShared>(p + 8 + half), hz = node_ld<kShared>(p + 10 + half);
-        float4 chf = node_ld<kShared>(p + 12 + half);
-        uint4 ch = make_uint4(__float_as_uint(chf.x), __float_as_uint(chf.y),
-            __float_as_uint(chf.z), __float_as_uint(chf.w));
+        float4 lx = __ldg(p + 0 + half), hx = __ldg(p + 2 + half);
+        float4 ly = __ldg(p + 4 + half), hy = __ldg(p + 6 + half);
+        float4 lz = __ldg(p + 8 + half), hz = __ldg(p + 10 + half);
+        uint4 ch = __ldg(reinterpret_cast<const uint4 *>(p + 12 + half));
         float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, hxs[4] = {hx.x, hx.y, hx.z, hx.w};
         float lys[4] = {ly.x, ly.y, ly.z, ly.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
         float lzs[4] = {lz.x, lz.y, lz.z, lz.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
@@ -75,7 +67,8 @@ __device__ __forceinline__ void visit_node_at(const float4 *p, V3 o, V3 invd, fl
             uint32_t c = chs[k];
             if (c == kEmptyChild) continue;
             if (kCount) cnt.boxTests++;
-            float te = slab_entry(v3(lxs[k], lys[k], lzs[k]), v3(hxs[k], hys[k], hzs[k]), o, invd);
+            V3 bl = v3(lxs[k], lys[k], lzs[k]), bh = v3(hxs[k], hys[k], hzs[k]);
+            float te = kWT ? slab_entry_robust(bl, bh, o, invd) : slab_entry(bl, bh, o, invd);
             if (te < 0.0f || te > bound) continue;
             if (te < nearT) {
                 if (nearRef != kEmptyChild) {
@@ -111,38 +104,10 @@ __device__ __forceinline__ void visit_node_at(const float4 *p, V3 o, V3 invd, fl
     }
 }
 
-template <bool kCount>
-__device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
-    V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp, uint32_t *status,
-    TraceCounters &cnt)
-{
-    visit_node_at<kCount, false>(reinterpret_cast<const float4 *>(nodes + ref), o, invd, bound,
-        stackRef, stackT, sp, status, cnt);
-}
-
-// The object BVH staged in shared memory by the trace kernels of a one-scene
-// launch (nodes [first, first + count) of the pool), or count 0.
-struct SmemTlas {
-    const float4 *nodes;
-    uint32_t first, count;
-};
-constexpr uint32_t kSmemTlasNodes = 96;  // 21,504 bytes of shared memory
-
-// An object-level node visit: from shared memory when staged.
-template <bool kCount>
-__device__ __forceinline__ void visit_top_node(const SmemTlas &st, const Node8 *__restrict__ nodes,
-    uint32_t ref, V3 o, V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp,
-    uint32_t *status, TraceCounters &cnt)
-{
-    if (ref - st.first < st.count)
-        visit_node_at<kCount, true>(st.nodes + (size_t)(ref - st.first) * 14, o, invd, bound,
-            stackRef, stackT, sp, status, cnt);
-    else
-        visit_node<kCount>(nodes, ref, o, invd, bound, stackRef, stackT, sp, status, cnt);
-}
-
-// Triangle candidates of one mesh leaf, in object space.
-template <bool kCount>
+// Triangle candidates of one mesh leaf, in object space.  kWT: the
+// watertight test on every candidate (no box gate: a rounded box test could
+// reject an edge ray); otherwise the reference's gate and MT test.
+template <bool kCount, bool kWT = false>
 __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
     V3 linvd, float &bestT, float &bestU, float &bestV, int32_t &bestPrim, TraceCounters &cnt)
 {
@@ -153,11 +118,15 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
         float4 A = __ldg(tp + 0), B = __ldg(tp + 1), C = __ldg(tp + 2);
         V3 a = v3(A.x, A.y, A.z), b = v3(B.x, B.y, B.z), c = v3(C.x, C.y, C.z);
         if (kCount) cnt.triTests++;
-        // the reference only reaches triangles whose own box passes
-        V3 bl = vmin(a, vmin(b, c)), bh = vmax(a, vmax(b, c));
-        if (slab_entry(bl, bh, lo, linvd) < 0.0f) continue;
-        TriHit h = sv.watertight ? ray_triangle_watertight(lo, ld, a, b, c, v3(A.w, B.w, C.w))
-                                 : ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
+        TriHit h;
+        if constexpr (kWT) {
+            h = ray_triangle_watertight(lo, ld, a, b, c, v3(A.w, B.w, C.w));
+        } else {
+            // the reference only reaches triangles whose own box passes
+            V3 bl = vmin(a, vmin(b, c)), bh = vmax(a, vmax(b, c));
+            if (slab_entry(bl, bh, lo, linvd) < 0.0f) continue;
+            h = ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
+        }
         if (!h.hit || !(h.t > 0.0f)) continue;
         bool take = h.t < bestT;
         if (!take && h.t == bestT && bestPrim >= 0)
@@ -171,9 +140,9 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
     }
 }
 
-template <bool kCount>
+template <bool kCount, bool kWT = false>
 __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *status,
-    TraceCounters &cnt, const SmemTlas &st = SmemTlas{nullptr, 0, 0})
+    TraceCounters &cnt)
 {
     RayHit best;
     best.t = kInf;
@@ -202,7 +171,7 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
         if (te > prune_bound(best.t)) continue;
         if (!child_is_leaf(ref)) {
             if (kCount) cnt.topNodes++;
-            visit_top_node<kCount>(st, nodes, ref, o, invd, prune_bound(best.t), stackRef, stackT,
+            visit_node<kCount, kWT>(nodes, ref, o, invd, prune_bound(best.t), stackRef, stackT,
                 sp, status, cnt);
             continue;
         }
@@ -236,9 +205,10 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
             if (t2 > bound) continue;
             if (!child_is_leaf(r2)) {
                 if (kCount) cnt.meshNodes++;
-                visit_node<kCount>(nodes, r2, lo, linvd, bound, stackRef, stackT, sp, status, cnt);
+                visit_node<kCount, kWT>(nodes, r2, lo, linvd, bound, stackRef, stackT, sp, status,
+                    cnt);
             } else {
-                visit_leaf<kCount>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+                visit_leaf<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
             }
         }
         sp = base;

@@ -50,7 +50,6 @@ struct WaveParams {
 // Scene source of the wave kernels: everything a path needs from its scene.
 // OneScene: one scene for the whole launch (a frame or a tile).
 struct OneScene {
-    static constexpr bool kStageTlas = true;  // one object BVH for the launch
     SceneView sv;
     MaterialView mv;
     uint32_t maxBounces;
@@ -96,23 +95,11 @@ static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuff
     wb.pathLen[p] = 0;
 }
 
-template <class Src>
+template <class Src, bool kWT>
 __global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
-    // one-scene launches stage the object BVH in shared memory
-    __shared__ float4 sTlas[kSmemTlasNodes * 14];
-    SmemTlas st = {sTlas, 0, 0};
-    if constexpr (Src::kStageTlas) {
-        const SceneView &sv0 = src.scene(0);
-        uint32_t n = sv0.tlasCount <= kSmemTlasNodes ? sv0.tlasCount : 0u;
-        const float4 *g = reinterpret_cast<const float4 *>(sv0.nodes + sv0.tlasFirst);
-        for (uint32_t i = threadIdx.x; i < n * 14; i += blockDim.x) sTlas[i] = __ldg(g + i);
-        __syncthreads();
-        st.first = sv0.tlasFirst;
-        st.count = n;
-    }
     int lane = threadIdx.x & 31;
     uint32_t count = *queueCount;
     TraceCounters cnt = {0, 0, 0, 0, 0};
@@ -126,8 +113,8 @@ __global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict
         if (i < count) {
             float4 o4 = rayO[i], d4 = rayD[i];
             const SceneView &sv = src.scene((uint32_t)__float_as_int(o4.w));
-            RayHit h = trace_closest<true>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z), status,
-                cnt, st);
+            RayHit h = trace_closest<true, kWT>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z),
+                status, cnt);
             hitA[i] = make_int4(__float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v),
                 h.prim);
             hitInst[i] = h.inst;
@@ -165,23 +152,11 @@ __global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict
 constexpr uint32_t kMaxLaneRaySteps = 1u << 22;
 constexpr uint32_t kMaxLaneIterations = 1u << 28;
 
-template <class Src>
+template <class Src, bool kWT>
 __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
-    // one-scene launches stage the object BVH in shared memory
-    __shared__ float4 sTlas[kSmemTlasNodes * 14];
-    SmemTlas st = {sTlas, 0, 0};
-    if constexpr (Src::kStageTlas) {
-        const SceneView &sv0 = src.scene(0);
-        uint32_t n = sv0.tlasCount <= kSmemTlasNodes ? sv0.tlasCount : 0u;
-        const float4 *g = reinterpret_cast<const float4 *>(sv0.nodes + sv0.tlasFirst);
-        for (uint32_t i = threadIdx.x; i < n * 14; i += blockDim.x) sTlas[i] = __ldg(g + i);
-        __syncthreads();
-        st.first = sv0.tlasFirst;
-        st.count = n;
-    }
     const int lane = threadIdx.x & 31;
     const uint32_t laneMaskLt = (1u << lane) - 1u;
     const uint32_t count = *queueCount;
@@ -273,12 +248,8 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                     cnt.topNodes++;
                 else
                     cnt.meshNodes++;
-                if (mode == 1)
-                    visit_top_node<true>(st, src.scene(pathId).nodes, ref, o, invd, bound, stackRef,
-                        stackT, sp, status, cnt);
-                else
-                    visit_node<true>(src.scene(pathId).nodes, ref, lo, linvd, bound, stackRef,
-                        stackT, sp, status, cnt);
+                visit_node<true, kWT>(src.scene(pathId).nodes, ref, mode == 1 ? o : lo,
+                    mode == 1 ? invd : linvd, bound, stackRef, stackT, sp, status, cnt);
             } else if (mode == 1) {
                 // an object whose world box passed: enter its mesh
                 inst = leaf_first(ref);
@@ -303,7 +274,8 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                     mode = 2;
                 }
             } else {
-                visit_leaf<true>(src.scene(pathId), ref, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+                visit_leaf<true, kWT>(src.scene(pathId), ref, lo, ld, linvd, lBestT, lU, lV, lPrim,
+                    cnt);
             }
         }
     }
@@ -458,6 +430,31 @@ static __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBu
     for (int off = 16; off; off >>= 1) nans += __shfl_xor_sync(0xFFFFFFFFu, nans, off);
     if ((threadIdx.x & 31) == 0 && nans)
         atomicAdd(&counters[GBSP_METRIC_NAN_SAMPLES], (unsigned long long)nans);
+}
+
+// Launches the closest-hit kernel of one bounce: per-warp or per-lane
+// scheduling, reference MT or watertight triangle test (template arguments,
+// so neither choice costs the other anything).
+template <class Src>
+void launch_trace_stage(bool perLane, bool watertight, int grid, cudaStream_t s, const Src &src,
+    const float4 *qO, const float4 *qD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
+    unsigned int *ctl, unsigned long long *counters, uint32_t *status)
+{
+    if (perLane) {
+        if (watertight)
+            k_trace_lane<Src, true><<<grid, 128, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst,
+                ctl, counters, status);
+        else
+            k_trace_lane<Src, false><<<grid, 128, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst,
+                ctl, counters, status);
+    } else {
+        if (watertight)
+            k_trace<Src, true><<<grid, 128, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst, ctl,
+                counters, status);
+        else
+            k_trace<Src, false><<<grid, 128, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst, ctl,
+                counters, status);
+    }
 }
 
 }  // namespace gbsp
