@@ -358,3 +358,40 @@ def test_watertight_mode_closes_shared_edges(rt):
         misses[mode] = int((tri < 0).sum())
     print(f"edge/vertex rays {len(rays)}: misses MT {misses[0]}, watertight {misses[1]}")
     assert misses[gbsp.ISECT_WATERTIGHT] == 0
+
+
+@pytest.mark.parametrize("kind", ["config1", "config3_crop"])
+def test_fp64_reference_image_matches_oracle(rt, kind):
+    """The high-spp oracle image of the benchmarks (denoiser.SceneRenderer.
+    reference: FP32 passes of the GPU path tracer summed in FP64) against the
+    CPU oracle running the same passes (same seeds), at low spp: config 1 in
+    full and a 64x64 crop of a config-3-style scene."""
+    import torch
+
+    from vk_cinematic_gb300 import denoiser
+
+    if kind == "config1":
+        s = scenes.config1_scene()
+        x0, y0, w, h = 0, 0, s.width, s.height
+    else:
+        s = scenes.config3_scene(width=320, height=180, spp=4, n_spheres=48, level=3, seed=9)
+        x0, y0, w, h = 150, 90, 64, 64
+    passes, per_pass, seed = 3, 2, 77
+    sr = denoiser.SceneRenderer(rt, s)
+    got = sr.reference(x0, y0, w, h, passes * per_pass, per_pass=per_pass, seed=seed)
+    got = got.cpu().numpy()
+    wo = build_world("port", s)
+    if s.sky is not None:
+        wo.set_sky(s.sky)
+    wo.set_options(spp=per_pass, max_bounces=s.max_bounces, max_broadphase=4096,
+                   max_midphase=65536)
+    acc = np.zeros((h, w, 4), np.float64)
+    for k in range(passes):
+        img, _, _, _ = wo.path_trace_hashed(s.width, s.height, s.camera_position,
+                                            s.camera_rotation, s.film_distance, seed + k,
+                                            region=(x0, y0, x0 + w, y0 + h))
+        acc += img[y0:y0 + h, x0:x0 + w].astype(np.float64)
+    ref = acc / passes
+    err = mean_rel_err(got.astype(np.float32), ref.astype(np.float32))
+    print(f"FP64-accumulated reference ({kind}) vs oracle passes: mean rel err {err:.3e}")
+    assert err <= IMAGE_TOL
