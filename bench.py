@@ -645,7 +645,7 @@ def run_config5(args):
             rk, ak = sre.render(x0, y0, crop, crop, k, seed=5 + k, aov=True)
             d = net.denoise(rk.unsqueeze(0).contiguous(), ak.unsqueeze(0).contiguous())[0]
             den[k].append(denoiser.relmse(d, ref))
-            # the plain path tracer as the judge: an independent render of the same spp
+            # the plain path tracer checks the denoiser: an independent render of the same spp
             ck, _ = sre.render(x0, y0, crop, crop, k, seed=1000 + k)
             dc, _, fl = net.denoise_checked(rk.unsqueeze(0).contiguous(),
                                             ak.unsqueeze(0).contiguous(),

@@ -447,7 +447,7 @@ int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uin
 /* Reads and clears the denoiser kernels' device status word (1 = a tensor-core
  * completion wait ran out); GBSP_ERR_DEVICE_STATUS when it was set. */
 int gbsp_dn_status(uint32_t *status);
-/* Plain path tracing as the judge of the denoiser: A (the denoiser's input)
+/* Plain path tracing checks the denoiser: A (the denoiser's input)
  * and C are independent plain renders with the same spp, denoised = D(A);
  * per tile x tile block (tile <= 16) the tile's relMSE is estimated as
  * mean(((D - C)^2 - (A - C)^2 / 2) / (D^2 + 0.01)) (the second term removes
