@@ -67,6 +67,7 @@ def parse_args():
     ap.add_argument("--dn-eval-crop", type=int, default=256)
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--dn-conv", choices=["tcgen05", "mma"], default="tcgen05")
+    ap.add_argument("--dn-wgrad", choices=["mma", "simt"], default="mma")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
     ap.add_argument("--trace", choices=["hybrid", "warp", "lane"], default="hybrid",
@@ -605,7 +606,7 @@ def run_config5(args):
         rt, n_scenes=args.dn_scenes, crops_per_scene=args.dn_crops, crop=128, spp_in=4,
         spp_ref=args.dn_ref_spp, seed0=0, log=log)
     data_s = time.time() - t0
-    net = denoiser.KPCNN(seed=0, conv=args.dn_conv)
+    net = denoiser.KPCNN(seed=0, conv=args.dn_conv, wgrad=args.dn_wgrad)
     feats_all = net.features(noisy, aov)
     n = noisy.shape[0]
     g = torch.Generator(device="cpu").manual_seed(0)
@@ -622,6 +623,12 @@ def run_config5(args):
     torch.cuda.synchronize()
     train_ms = ev0.elapsed_time(ev1)
     log("training", losses)
+    # FLOPs of one training step (batch 16 x 128 x 128): forward, data gradient of
+    # layers 1..7 and weight gradient of every layer, each 2 x 9 x cin x cout per pixel
+    px = 16 * 128 * 128
+    layer_flops = [2.0 * px * 9 * ci * co for ci, co, _ in denoiser.LAYERS]
+    train_step_flops = 3 * sum(layer_flops) - layer_flops[0]
+    wgrad_ms = time_weight_grad(net, stream)
 
     # ---- quality on held-out scenes (crops, FP64-accumulated oracle)
     crop = args.dn_eval_crop
@@ -720,11 +727,43 @@ def run_config5(args):
                      "peak_source": bf16_peak[1], "unit": "TFLOP/s",
                      "frac": flops / (dn_ms * 1e-3) / 1e12 / bf16_peak[0], "traffic": None},
         "plain_ms_to_0.01": plain_ms, "denoised_ms_to_0.01": den_total_ms if in_spp else None,
-        "train_ms": train_ms, "dataset_s": data_s, "losses": losses,
+        "train_ms": train_ms, "train_ms_per_step": train_ms / args.dn_steps,
+        "train_tflops": train_step_flops * args.dn_steps / (train_ms * 1e-3) / 1e12,
+        "weight_grad_impl": net.wgrad_impl, "weight_grad_48x48_ms": wgrad_ms,
+        "dataset_s": data_s, "losses": losses,
         "params": net.parameters_count(),
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def time_weight_grad(net, stream, reps=20):
+    """Device time of one 48 -> 48 weight gradient on a 16 x 128 x 128 batch,
+    per implementation (tensor-core mma.sync and the FP32 SIMT kernel), in ms."""
+    import torch
+    from vk_cinematic_gb300 import denoiser
+
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.randn((16, 128, 128, 48), device="cuda", generator=g).to(torch.bfloat16)
+    d = torch.randn((16, 128, 128, 48), device="cuda", generator=g).to(torch.bfloat16)
+    dw = torch.zeros((9, 48, 48), device="cuda")
+    db = torch.zeros(48, device="cuda")
+    out = {}
+    for impl, fn in (("mma", net.L.gbsp_dn_conv3x3_weight_grad_tc),
+                     ("simt", net.L.gbsp_dn_conv3x3_weight_grad)):
+        args = (denoiser._stream(), denoiser._ptr(x), denoiser._ptr(d), denoiser._u32(16),
+                denoiser._u32(128), denoiser._u32(128), denoiser._u32(48), denoiser._u32(48),
+                denoiser._ptr(dw), denoiser._ptr(db))
+        for _ in range(3):
+            denoiser._check(fn(*args))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            denoiser._check(fn(*args))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[impl] = e0.elapsed_time(e1) / reps
+    return out
 
 
 def run_compute_pt(args):

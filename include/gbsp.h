@@ -466,6 +466,11 @@ int gbsp_dn_relu_backward(void *stream, const float *dAct, const uint16_t *act, 
 /* dW[tap][co][ci] += sum_p dOut[p][co] * in[p+off(tap)][ci]; dBias[co] += sum_p dOut[p][co]. */
 int gbsp_dn_conv3x3_weight_grad(void *stream, const uint16_t *in, const uint16_t *dOut,
     uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
+/* The same gradient on the tensor cores (mma.sync m16n8k16, BF16 operands, FP32
+ * accumulators): per-CTA partial sums added in a fixed order, so repeated calls give
+ * identical results.  Same shapes as gbsp_dn_conv3x3_weight_grad. */
+int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
 /* out[p] = sum_k softmax(logits[p][0..24])_k * noisy[p + off5x5(k)] (edge-clamped);
  * logits have 32 channels per pixel. */
 int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32_t B, uint32_t H,

@@ -178,8 +178,9 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // accumulator slot; every wait is bounded and a timeout sets g_dnStatus.
 // ---------------------------------------------------------------------------
 constexpr int kTcTileP = 128;
+constexpr int kTcThreads = 256;  // 8 warps: TMEM lane quarter = warp % 4, column half = warp / 4
 constexpr int kTcSpx = kTcTileP + 2;
-constexpr int kTcRing = 4;
+constexpr int kTcRing = 5;  // rows y-1..y+1 in use, y+2 and y+3 in flight
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 __device__ uint32_t g_dnStatus;
@@ -228,7 +229,7 @@ __device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 
     int H, int W, int x0, int tid)
 {
     const bool rowIn = gy >= 0 && gy < H;
-    for (int i = tid; i < KG * kTcSpx; i += 128) {
+    for (int i = tid; i < KG * kTcSpx; i += kTcThreads) {
         int px = i % kTcSpx, kg = i / kTcSpx;
         int gx = x0 + px - 1;
         bool ok = rowIn && gx >= 0 && gx < W;
@@ -241,48 +242,50 @@ __device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 
 }
 
 template <int CIN, int COUT, int EPI>
-__device__ __forceinline__ void conv_epilogue(uint32_t tmem, int warp, int lane, int x, int W,
+__device__ __forceinline__ void conv_epilogue(uint32_t tmem, int quarter, int half, int x, int W,
     size_t p, const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB,
     float *__restrict__ outF)
 {
+    // this thread's pixel (TMEM lane 32 quarter + lane), accumulator columns
+    // [half * COUT / 2, (half + 1) * COUT / 2): loaded 8 at a time, one wait
+    constexpr int HALF = COUT / 2;
+    static_assert(HALF % 8 == 0, "epilogue column split");
+    const int cBase = half * HALF;
+    uint32_t r[HALF];
 #pragma unroll
-    for (int c0 = 0; c0 < COUT; c0 += 16) {
-        uint32_t r[16];
-        uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+    for (int c = 0; c < HALF; c += 8) {
+        uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cBase + c);
         asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-            "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]),
-              "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]),
-              "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=r"(r[c + 0]), "=r"(r[c + 1]), "=r"(r[c + 2]), "=r"(r[c + 3]), "=r"(r[c + 4]),
+              "=r"(r[c + 5]), "=r"(r[c + 6]), "=r"(r[c + 7])
             : "r"(taddr));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (x < W) {
-            float v[16];
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    if (x >= W) return;
 #pragma unroll
-            for (int k = 0; k < 16; k++) {
-                v[k] = __uint_as_float(r[k]);
-                if (EPI != kEpiF32) v[k] += bias[c0 + k];
-                if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
-            }
-            if (EPI == kEpiBf16BiasRelu) {
-                uint4 *o = reinterpret_cast<uint4 *>(outB + p * COUT + c0);
-                o[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]),
-                    pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
-                o[1] = make_uint4(pack_bf16(v[8], v[9]), pack_bf16(v[10], v[11]),
-                    pack_bf16(v[12], v[13]), pack_bf16(v[14], v[15]));
-            } else {
-                float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + c0);
+    for (int c = 0; c < HALF; c += 8) {
+        float v[8];
 #pragma unroll
-                for (int k = 0; k < 4; k++)
-                    o[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-            }
+        for (int k = 0; k < 8; k++) {
+            v[k] = __uint_as_float(r[c + k]);
+            if (EPI != kEpiF32) v[k] += __ldg(bias + cBase + c + k);
+            if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
+        }
+        if (EPI == kEpiBf16BiasRelu) {
+            *reinterpret_cast<uint4 *>(outB + p * COUT + cBase + c) = make_uint4(
+                pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                pack_bf16(v[6], v[7]));
+        } else {
+            float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + cBase + c);
+            o[0] = make_float4(v[0], v[1], v[2], v[3]);
+            o[1] = make_float4(v[4], v[5], v[6], v[7]);
         }
     }
 }
 
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, int B,
+__global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, int B,
     int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
 {
@@ -292,14 +295,14 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restr
     constexpr int TMEM_COLS = 2 * ACC_COLS;  // two accumulator slots
     extern __shared__ __align__(128) unsigned char smemRaw[];
     uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [9][KG][COUT]
-    uint4 *sRing = sW + 9 * KG * COUT;               // [4][KG][kTcSpx]
+    uint4 *sRing = sW + 9 * KG * COUT;               // [kTcRing][KG][kTcSpx]
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmemBase;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
 
     // weights -> canonical layout: (tap, kg, co) holds w[tap][co][8 kg .. 8 kg + 7]
-    for (int i = tid; i < 9 * KG * COUT; i += 128) {
+    for (int i = tid; i < 9 * KG * COUT; i += kTcThreads) {
         int co = i % COUT, kg = (i / COUT) % KG, tap = i / (COUT * KG);
         sW[i] = reinterpret_cast<const uint4 *>(w)[((size_t)tap * COUT + co) * KG + kg];
     }
@@ -320,6 +323,10 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restr
     const uint32_t tmem = tmemBase;
     const uint32_t idesc = instr_desc_bf16<kTcTileP, COUT>();
     const uint32_t ringAddr = smem_u32(sRing), wAddr = smem_u32(sW);
+    // descriptors of ring slot 0 / tap 0; the 14-bit start-address field takes
+    // the (16-byte unit) offset of every other operand by plain addition
+    const uint64_t aDesc0 = smem_desc(ringAddr, kTcSpx * 16, 128);
+    const uint64_t bDesc0 = smem_desc(wAddr, COUT * 16, 128);
     const uint32_t bar[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
     uint32_t phase[2] = {0, 0};
 
@@ -332,31 +339,37 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restr
         const int b = strip / (stripsPerCol * segs);
         const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;
         const int y1 = min(H, y0 + rowsPerStrip);
-        // prologue: rows y0-1, y0, y0+1 into ring slots (row + 4) % 4
-        for (int gy = y0 - 1; gy <= y0 + 1; gy++)
+        // prologue: rows y0-1 .. y0+2 into ring slots (row + kTcRing) % kTcRing,
+        // one cp.async group per row
+        for (int gy = y0 - 1; gy <= y0 + 2 && gy <= y1; gy++)
             stage_row<KG>(ringAddr, (gy + kTcRing) % kTcRing, in4, b, gy, H, W, x0, tid);
         for (int y = y0; y <= y1 && !failed; y++) {
             const int acc = y & 1;
             if (y < y1) {
-                // rows y-1..y+1 are staged: make them visible to the tensor core
-                asm volatile("cp.async.wait_group 0;" ::: "memory");
+                // rows y-1..y+1 are staged (row y+2, when it exists, may still be
+                // in flight): make them visible to the tensor core
+                if (y + 2 <= y1)
+                    asm volatile("cp.async.wait_group 1;" ::: "memory");
+                else
+                    asm volatile("cp.async.wait_group 0;" ::: "memory");
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;");
                 __syncthreads();
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 if (tid == 0) {
                     const uint32_t dAcc = tmem + (uint32_t)(acc * ACC_COLS);
-#pragma unroll 1
+                    const int s0 = (y - 1 + kTcRing) % kTcRing;
+                    const int slots[3] = {s0, s0 + 1 == kTcRing ? 0 : s0 + 1,
+                        s0 + 2 >= kTcRing ? s0 + 2 - kTcRing : s0 + 2};
+#pragma unroll
                     for (int tap = 0; tap < 9; tap++) {
                         const int ty = tap / 3, tx = tap % 3;
-                        const int slot = (y + ty - 1 + kTcRing) % kTcRing;
+                        const uint64_t aRow = aDesc0 + (uint64_t)(slots[ty] * KG * kTcSpx + tx);
 #pragma unroll
                         for (int kc = 0; kc < CIN / 16; kc++) {
-                            uint32_t aAddr = ringAddr +
-                                (uint32_t)(((slot * KG + 2 * kc) * kTcSpx + tx) * 16);
-                            uint32_t bAddr = wAddr + (uint32_t)(((tap * KG + 2 * kc) * COUT) * 16);
-                            uint64_t aDesc = smem_desc(aAddr, kTcSpx * 16, 128);
-                            uint64_t bDesc = smem_desc(bAddr, COUT * 16, 128);
+                            // 16-byte units: slot row, channel group 2 kc, pixel tx
+                            uint64_t aDesc = aRow + (uint64_t)(2 * kc * kTcSpx);
+                            uint64_t bDesc = bDesc0 + (uint64_t)((tap * KG + 2 * kc) * COUT);
                             uint32_t accumulate = (tap | kc) ? 1u : 0u;
                             asm volatile(
                                 "{\n\t.reg .pred p;\n\t"
@@ -379,14 +392,14 @@ __global__ void __launch_bounds__(128) k_conv3x3_tc(const __nv_bfloat16 *__restr
                 if (failed) break;
                 phase[pa] ^= 1u;
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                const int x = x0 + warp * 32 + lane;
-                conv_epilogue<CIN, COUT, EPI>(tmem + (uint32_t)(pa * ACC_COLS), warp, lane, x, W,
-                    ((size_t)(b * H + (y - 1)) * W + x), bias, outB, outF);
+                const int x = x0 + (warp & 3) * 32 + lane;
+                conv_epilogue<CIN, COUT, EPI>(tmem + (uint32_t)(pa * ACC_COLS), warp & 3,
+                    warp >> 2, x, W, ((size_t)(b * H + (y - 1)) * W + x), bias, outB, outF);
                 asm volatile("tcgen05.fence::before_thread_sync;");
             }
-            // prefetch row y+2 into the slot of row y-2 (its last reader, row y-1, is done)
-            if (y < y1 - 1)
-                stage_row<KG>(ringAddr, (y + 2) % kTcRing, in4, b, y + 2, H, W, x0, tid);
+            // prefetch row y+3 into the slot of row y-2 (its last reader, row y-1, is done)
+            if (y + 3 <= y1)
+                stage_row<KG>(ringAddr, (y + 3) % kTcRing, in4, b, y + 3, H, W, x0, tid);
         }
         // the next strip's prologue overwrites the ring
         asm volatile("cp.async.wait_group 0;" ::: "memory");
@@ -416,7 +429,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     rows = rows < 4 ? 4 : (rows > H ? H : rows);
     int strips = cols * ((H + rows - 1) / rows);
     int grid = strips < ctas ? strips : ctas;
-    kern<<<grid, 128, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
+    kern<<<grid, kTcThreads, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
         reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
         outF);
     GBSP_CUDA_TRY(cudaGetLastError());
@@ -518,6 +531,119 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const __nv_bfloat16 *__re
         for (int c = 0; c < TI; c++)
             atomicAdd(&dW[((size_t)tap * COUT + tco * TC + a) * CIN + tci * TI + c], acc[a][c]);
     if (tap == 4 && threadIdx.x < COUT) atomicAdd(&dBias[threadIdx.x], bacc);
+}
+
+// Weight gradient on the tensor cores (mma.sync m16n8k16, BF16 in, FP32
+// accumulate): per tap, dW[tap][co][ci] = sum_p d[p][co] * x[p + off(tap)][ci]
+// is a GEMM with M = COUT, N = CIN and K = pixels.  A CTA of 9 warps (warp =
+// tap) walks 64-pixel row segments: it stages d transposed ([co][pixel]) and
+// the three input rows around the segment transposed ([row][ci][pixel], one
+// pixel of halo on each side), then every warp multiplies its tap's shifted
+// view, holding all COUT/16 x CIN/8 accumulator tiles in registers.  Each CTA
+// writes its partial sums (and the bias gradient sum_p d[p][co]) to its own
+// slice of a scratch buffer; k_wgrad_reduce adds the slices in a fixed order,
+// so the result is deterministic.
+constexpr int kWgTile = 64;
+constexpr int kWgStride = kWgTile + 8;  // padded pixel stride of the staged rows
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(288) k_conv3x3_wgrad_tc(const __nv_bfloat16 *__restrict__ in,
+    const __nv_bfloat16 *__restrict__ d, int B, int H, int W, float *__restrict__ partial)
+{
+    static_assert(CIN % 8 == 0 && COUT % 16 == 0, "tile shape");
+    constexpr int MT = COUT / 16, NT = CIN / 8;
+    __shared__ __align__(16) __nv_bfloat16 sD[COUT][kWgStride];
+    __shared__ __align__(16) __nv_bfloat16 sX[3][CIN][kWgStride];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    const int tap = warp, ty = tap / 3, tx = tap % 3;
+    float acc[MT][NT][4];
+#pragma unroll
+    for (int m = 0; m < MT; m++)
+#pragma unroll
+        for (int n = 0; n < NT; n++) acc[m][n][0] = acc[m][n][1] = acc[m][n][2] = acc[m][n][3] = 0.0f;
+    float bacc = 0.0f;  // threads 0..COUT-1: bias gradient of channel tid
+    const int segs = (W + kWgTile - 1) / kWgTile;
+    const int tiles = segs * B * H;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int row = tile / segs, x0 = (tile % segs) * kWgTile;
+        const int b = row / H, y = row % H;
+        __syncthreads();
+        for (int i = tid; i < kWgTile * COUT; i += 288) {
+            int k = i / COUT, co = i % COUT;
+            int x = x0 + k;
+            sD[co][k] = x < W ? d[((size_t)row * W + x) * COUT + co] : __float2bfloat16_rn(0.0f);
+        }
+        for (int i = tid; i < 3 * (kWgTile + 2) * CIN; i += 288) {
+            int ci = i % CIN, px = (i / CIN) % (kWgTile + 2), ry = i / (CIN * (kWgTile + 2));
+            int gy = y + ry - 1, gx = x0 + px - 1;
+            __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+                v = in[((size_t)(b * H + gy) * W + gx) * CIN + ci];
+            sX[ry][ci][px] = v;
+        }
+        __syncthreads();
+        if (tid < COUT) {
+            for (int k = 0; k < kWgTile; k++) bacc += __bfloat162float(sD[tid][k]);
+        }
+#pragma unroll
+        for (int k0 = 0; k0 < kWgTile; k0 += 16) {
+            uint32_t a[MT][4];
+#pragma unroll
+            for (int m = 0; m < MT; m++) {
+                const __nv_bfloat16 *r0 = &sD[m * 16 + g][k0 + 2 * t];
+                const __nv_bfloat16 *r1 = &sD[m * 16 + g + 8][k0 + 2 * t];
+                a[m][0] = *reinterpret_cast<const uint32_t *>(r0);
+                a[m][1] = *reinterpret_cast<const uint32_t *>(r1);
+                a[m][2] = *reinterpret_cast<const uint32_t *>(r0 + 8);
+                a[m][3] = *reinterpret_cast<const uint32_t *>(r1 + 8);
+            }
+#pragma unroll
+            for (int n = 0; n < NT; n++) {
+                // B[k][ci] = x[pixel k + tx - 1 of the segment][ci]: the staged row ty
+                // at halo index k + tx (odd for tx = 1: two 16-bit loads per pair)
+                const __nv_bfloat16 *c = &sX[ty][n * 8 + g][k0 + 2 * t + tx];
+                __nv_bfloat162 p0, p1;
+                p0.x = c[0];
+                p0.y = c[1];
+                p1.x = c[8];
+                p1.y = c[9];
+                uint32_t b0 = *reinterpret_cast<uint32_t *>(&p0);
+                uint32_t b1 = *reinterpret_cast<uint32_t *>(&p1);
+#pragma unroll
+                for (int m = 0; m < MT; m++)
+                    mma_bf16_16816(acc[m][n], a[m][0], a[m][1], a[m][2], a[m][3], b0, b1);
+            }
+        }
+    }
+    // C fragment: rows g / g + 8 (co), columns 2t, 2t + 1 (ci) of each tile
+    float *out = partial + (size_t)blockIdx.x * (9 * COUT * CIN + COUT);
+#pragma unroll
+    for (int m = 0; m < MT; m++)
+#pragma unroll
+        for (int n = 0; n < NT; n++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                int co = m * 16 + g + 8 * h, ci = n * 8 + 2 * t;
+                float *o = out + ((size_t)tap * COUT + co) * CIN + ci;
+                o[0] = acc[m][n][2 * h];
+                o[1] = acc[m][n][2 * h + 1];
+            }
+    if (tid < COUT) out[9 * COUT * CIN + tid] = bacc;
+}
+
+// dW[i] += sum over CTA slices of partial[slice][i], slices in order; the
+// last COUT entries of a slice are the bias gradient.
+__global__ void k_wgrad_reduce(const float *__restrict__ partial, int slices, int perSlice,
+    int wCount, float *dW, float *dBias)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= perSlice) return;
+    float sum = 0.0f;
+    for (int k = 0; k < slices; k++) sum += partial[(size_t)k * perSlice + i];
+    if (i < wCount)
+        dW[i] += sum;
+    else
+        dBias[i - wCount] += sum;
 }
 
 // Per-pixel 5x5 filter from softmax(logits[0..24]) applied to the noisy
@@ -707,6 +833,31 @@ int sm_count()
 using namespace gbsp;
 using namespace gbsp::dn;
 
+template <int CIN, int COUT>
+static int launch_wgrad_tc(cudaStream_t s, const __nv_bfloat16 *in, const __nv_bfloat16 *d, int B,
+    int H, int W, float *dW, float *dBias)
+{
+    const int tiles = ((W + kWgTile - 1) / kWgTile) * B * H;
+    int perSm = 1;
+    GBSP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm,
+        k_conv3x3_wgrad_tc<CIN, COUT>, 288, 0));
+    int grid = sm_count() * (perSm > 0 ? perSm : 1);
+    if (grid > tiles) grid = tiles;
+    const int perSlice = 9 * COUT * CIN + COUT;
+    float *partial = nullptr;
+    GBSP_CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(float) * (size_t)grid * perSlice, s));
+    k_conv3x3_wgrad_tc<CIN, COUT><<<grid, 288, 0, s>>>(in, d, B, H, W, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_wgrad_reduce<<<(perSlice + 255) / 256, 256, 0, s>>>(partial, grid, perSlice,
+            9 * COUT * CIN, dW, dBias);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(partial, s);
+    if (e != cudaSuccess) return cuda_error(e, "weight gradient");
+    return GBSP_OK;
+}
+
 extern "C" {
 
 int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
@@ -798,6 +949,20 @@ int gbsp_dn_relu_backward(void *stream, const float *dAct, const uint16_t *act, 
         reinterpret_cast<const __nv_bfloat16 *>(act), n, reinterpret_cast<__nv_bfloat16 *>(out));
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
+}
+
+int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!in || !dOut || !dW || !dBias || !B || !H || !W)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad weight-gradient args");
+    const __nv_bfloat16 *i16 = reinterpret_cast<const __nv_bfloat16 *>(in);
+    const __nv_bfloat16 *d16 = reinterpret_cast<const __nv_bfloat16 *>(dOut);
+    if (cin == 16 && cout == 48) return launch_wgrad_tc<16, 48>(s, i16, d16, B, H, W, dW, dBias);
+    if (cin == 48 && cout == 48) return launch_wgrad_tc<48, 48>(s, i16, d16, B, H, W, dW, dBias);
+    if (cin == 48 && cout == 32) return launch_wgrad_tc<48, 32>(s, i16, d16, B, H, W, dW, dBias);
+    return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
 }
 
 int gbsp_dn_conv3x3_weight_grad(void *stream, const uint16_t *in, const uint16_t *dOut,

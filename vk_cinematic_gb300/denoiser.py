@@ -55,15 +55,20 @@ def relmse(x, ref):
 class KPCNN:
     """conv: "tcgen05" (5th-generation tensor cores, accumulator in tensor
     memory) or "mma" (mma.sync BF16 fragments) for the forward and
-    data-gradient convolutions."""
+    data-gradient convolutions.  wgrad: "mma" (tensor cores, deterministic
+    per-CTA partial sums) or "simt" (FP32 FMA with atomics) for the weight
+    gradient."""
 
-    def __init__(self, seed: int = 0, conv: str = "tcgen05"):
+    def __init__(self, seed: int = 0, conv: str = "tcgen05", wgrad: str = "mma"):
         import torch
 
         self.L = gbsp.load()
         self._conv = {"tcgen05": self.L.gbsp_dn_conv3x3_forward_tc,
                       "mma": self.L.gbsp_dn_conv3x3_forward}[conv]
+        self._wgrad = {"mma": self.L.gbsp_dn_conv3x3_weight_grad_tc,
+                       "simt": self.L.gbsp_dn_conv3x3_weight_grad}[wgrad]
         self.conv_impl = conv
+        self.wgrad_impl = wgrad
         g = torch.Generator().manual_seed(seed)
         self.w, self.b, self.wb, self.state = [], [], [], []
         for li, (cin, cout, epi) in enumerate(LAYERS):
@@ -174,9 +179,8 @@ class KPCNN:
     def weight_grad(self, li, x, d, dw, db):
         B, H, W, cin = x.shape
         cout = d.shape[-1]
-        _check(self.L.gbsp_dn_conv3x3_weight_grad(_stream(), _ptr(x), _ptr(d), _u32(B), _u32(H),
-                                                  _u32(W), _u32(cin), _u32(cout), _ptr(dw),
-                                                  _ptr(db)))
+        _check(self._wgrad(_stream(), _ptr(x), _ptr(d), _u32(B), _u32(H), _u32(W), _u32(cin),
+                           _u32(cout), _ptr(dw), _ptr(db)))
 
     def gradients(self, feats, noisy, target):
         """Loss and parameter gradients for one batch."""
