@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const __nv_bfloat16 *__res
     static_assert(CIN % 16 == 0 && COUT % 8 == 0, "channel padding");
     constexpr int SIN = CIN + 8;  // padded element stride per pixel (bank-conflict free)
     constexpr int SPX = kTileP + 2;
-    extern __shared__ __align__(16) unsigned char smemRaw[];
+    extern __shared__ __align__(128) unsigned char smemRaw[];
     __nv_bfloat16 *sW = reinterpret_cast<__nv_bfloat16 *>(smemRaw);   // [9][COUT][SIN]
     __nv_bfloat16 *sIn = sW + 9 * COUT * SIN;                          // [3][SPX][SIN]
     const int tid = threadIdx.x;
@@ -168,19 +168,29 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // [COUT][16 B].  Descriptor strides: leading (K) = next channel group,
 // stride (M or N) = next 8 rows = 128 B.
 //
-// A CTA walks a vertical strip (one 128-pixel column segment, a run of
-// rows).  Per output row y: issue the MMAs of row y into accumulator slot
-// y & 1 (rows y-1..y+1 are in the ring), then - while they run - wait for
-// row y-1's accumulator, read it back with tcgen05.ld (warp w owns lanes
-// 32w..32w+31 = pixels 32w..32w+31) for the bias / ReLU / store epilogue,
-// and prefetch input row y+2 with cp.async into the ring slot row y-2 left.
-// MMA completion is signalled by tcgen05.commit on one mbarrier per
-// accumulator slot; every wait is bounded and a timeout sets g_dnStatus.
+// A CTA walks vertical strips (one 128-pixel column segment, a run of rows)
+// with its warps specialised and coupled only by mbarriers:
+//   * warps 1-3 (producers) stage input rows into a ring of kTcRing slots
+//     with cp.async, two rows in flight; a row's slot is reused once the
+//     MMAs of the last output row that reads it have completed (rowEmpty,
+//     signalled by tcgen05.commit), and a staged row is published on
+//     rowFull after cp.async.wait_group + fence.proxy.async;
+//   * lane 0 of warp 0 issues, per output row y, the 9 taps x CIN/16 MMAs
+//     reading rows y-1..y+1 into one of kTcAccSlots TMEM accumulators, then
+//     commits to that accumulator's accFull and to the rowEmpty of row y-1;
+//   * warps 4-7 (epilogue; warp 4 + k owns TMEM lanes 32k..32k+31 = pixels)
+//     wait on accFull, read the accumulator with tcgen05.ld, release it on
+//     accEmpty and apply bias / ReLU / BF16 packing while the tensor core
+//     already works on the next rows.
+// Every wait is bounded; a timeout raises a shared abort flag that ends the
+// other roles' waits, and sets g_dnStatus.
 // ---------------------------------------------------------------------------
 constexpr int kTcTileP = 128;
-constexpr int kTcThreads = 256;  // 8 warps: TMEM lane quarter = warp % 4, column half = warp / 4
+constexpr int kTcThreads = 256;  // warp 0: MMA issue; warps 1-3: producers; 4-7: epilogue
+constexpr int kTcProducers = 96;
+constexpr int kTcAccSlots = 4;
 constexpr int kTcSpx = kTcTileP + 2;
-constexpr int kTcRing = 5;  // rows y-1..y+1 in use, y+2 and y+3 in flight
+constexpr int kTcRing = 5;  // rows y-1..y+1 read by the MMAs, two more in flight
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 __device__ uint32_t g_dnStatus;
@@ -188,6 +198,46 @@ __device__ uint32_t g_dnStatus;
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
     return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Bounded mbarrier wait (at most kTcWaitLimit polls and kTcWaitNs of
+// wall time) that also gives up when another role has aborted.
+constexpr uint64_t kTcWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, volatile uint32_t *abortFlag)
+{
+    const uint64_t t0 = global_ns();
+    for (uint32_t it = 0; it < kTcWaitLimit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+        if (*abortFlag) return false;
+        if ((it & 255u) == 255u && global_ns() - t0 > kTcWaitNs) break;
+    }
+    *abortFlag = 1u;
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(bar) : "memory");
 }
 
 // Shared-memory matrix descriptor: start >> 4 (bits 0-13), leading-dimension
@@ -208,28 +258,14 @@ __device__ __forceinline__ uint32_t instr_desc_bf16()
         ((uint32_t)(M >> 4) << 24);
 }
 
-// Bounded wait on an mbarrier phase; returns 1 when the phase completed.
-__device__ __forceinline__ uint32_t mbar_wait(uint32_t bar, uint32_t phase)
-{
-    uint32_t done = 0;
-    for (uint32_t it = 0; it < kTcWaitLimit && !done; it++) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done) : "r"(bar), "r"(phase) : "memory");
-    }
-    return done;
-}
-
 // Stages input row gy (zero outside the image) into ring slot `slot` with
 // cp.async (16 B per copy, zero-filled when the source size is 0).
-template <int KG>
+template <int KG, int NT>
 __device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 *in, int b, int gy,
     int H, int W, int x0, int tid)
 {
     const bool rowIn = gy >= 0 && gy < H;
-    for (int i = tid; i < KG * kTcSpx; i += kTcThreads) {
+    for (int i = tid; i < KG * kTcSpx; i += NT) {
         int px = i % kTcSpx, kg = i / kTcSpx;
         int gx = x0 + px - 1;
         bool ok = rowIn && gx >= 0 && gx < W;
@@ -241,43 +277,25 @@ __device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-template <int CIN, int COUT, int EPI>
-__device__ __forceinline__ void conv_epilogue(uint32_t tmem, int quarter, int half, int x, int W,
-    size_t p, const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB,
-    float *__restrict__ outF)
+// Bias / ReLU / BF16 packing of one pixel's COUT accumulators and the store.
+template <int COUT, int EPI>
+__device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
+    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
 {
-    // this thread's pixel (TMEM lane 32 quarter + lane), accumulator columns
-    // [half * COUT / 2, (half + 1) * COUT / 2): loaded 8 at a time, one wait
-    constexpr int HALF = COUT / 2;
-    static_assert(HALF % 8 == 0, "epilogue column split");
-    const int cBase = half * HALF;
-    uint32_t r[HALF];
 #pragma unroll
-    for (int c = 0; c < HALF; c += 8) {
-        uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(cBase + c);
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-            : "=r"(r[c + 0]), "=r"(r[c + 1]), "=r"(r[c + 2]), "=r"(r[c + 3]), "=r"(r[c + 4]),
-              "=r"(r[c + 5]), "=r"(r[c + 6]), "=r"(r[c + 7])
-            : "r"(taddr));
-    }
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    if (x >= W) return;
-#pragma unroll
-    for (int c = 0; c < HALF; c += 8) {
+    for (int c = 0; c < COUT; c += 8) {
         float v[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             v[k] = __uint_as_float(r[c + k]);
-            if (EPI != kEpiF32) v[k] += __ldg(bias + cBase + c + k);
+            if (EPI != kEpiF32) v[k] += __ldg(bias + c + k);
             if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
         }
         if (EPI == kEpiBf16BiasRelu) {
-            *reinterpret_cast<uint4 *>(outB + p * COUT + cBase + c) = make_uint4(
-                pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
-                pack_bf16(v[6], v[7]));
+            *reinterpret_cast<uint4 *>(outB + p * COUT + c) = make_uint4(pack_bf16(v[0], v[1]),
+                pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
         } else {
-            float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + cBase + c);
+            float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + c);
             o[0] = make_float4(v[0], v[1], v[2], v[3]);
             o[1] = make_float4(v[4], v[5], v[6], v[7]);
         }
@@ -285,19 +303,22 @@ __device__ __forceinline__ void conv_epilogue(uint32_t tmem, int quarter, int ha
 }
 
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, int B,
-    int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
+__global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in,
+    int B, int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
 {
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tcgen05 tile shape");
     constexpr int KG = CIN / 8;  // 16-byte channel groups
     constexpr int ACC_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
-    constexpr int TMEM_COLS = 2 * ACC_COLS;  // two accumulator slots
+    constexpr int TMEM_COLS = kTcAccSlots * ACC_COLS;
+    static_assert(TMEM_COLS <= 512, "tensor memory");
     extern __shared__ __align__(128) unsigned char smemRaw[];
     uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [9][KG][COUT]
     uint4 *sRing = sW + 9 * KG * COUT;               // [kTcRing][KG][kTcSpx]
-    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ __align__(8) uint64_t rowFull[kTcRing], rowEmpty[kTcRing];
+    __shared__ __align__(8) uint64_t accFull[kTcAccSlots], accEmpty[kTcAccSlots], drain;
     __shared__ uint32_t tmemBase;
+    __shared__ volatile uint32_t abortFlag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
 
@@ -312,8 +333,17 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar[0])));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&mbar[1])));
+        for (int i = 0; i < kTcRing; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
+                         :: "r"(smem_u32(&rowFull[i])), "r"(kTcProducers));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&rowEmpty[i])));
+        }
+        for (int i = 0; i < kTcAccSlots; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&accFull[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" :: "r"(smem_u32(&accEmpty[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&drain)));
+        abortFlag = 0u;
         asm volatile("fence.mbarrier_init.release.cluster;");
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -321,50 +351,52 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmemBase;
-    const uint32_t idesc = instr_desc_bf16<kTcTileP, COUT>();
-    const uint32_t ringAddr = smem_u32(sRing), wAddr = smem_u32(sW);
-    // descriptors of ring slot 0 / tap 0; the 14-bit start-address field takes
-    // the (16-byte unit) offset of every other operand by plain addition
-    const uint64_t aDesc0 = smem_desc(ringAddr, kTcSpx * 16, 128);
-    const uint64_t bDesc0 = smem_desc(wAddr, COUT * 16, 128);
-    const uint32_t bar[2] = {smem_u32(&mbar[0]), smem_u32(&mbar[1])};
-    uint32_t phase[2] = {0, 0};
+    const uint32_t ringAddr = smem_u32(sRing);
 
     const int segs = (W + kTcTileP - 1) / kTcTileP;
     const int stripsPerCol = (H + rowsPerStrip - 1) / rowsPerStrip;
     const int numStrips = B * segs * stripsPerCol;
-    bool failed = false;
-    for (int strip = blockIdx.x; strip < numStrips && !failed; strip += gridDim.x) {
-        const int sy = strip % stripsPerCol, seg = (strip / stripsPerCol) % segs;
-        const int b = strip / (stripsPerCol * segs);
-        const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;
-        const int y1 = min(H, y0 + rowsPerStrip);
-        // prologue: rows y0-1 .. y0+2 into ring slots (row + kTcRing) % kTcRing,
-        // one cp.async group per row
-        for (int gy = y0 - 1; gy <= y0 + 2 && gy <= y1; gy++)
-            stage_row<KG>(ringAddr, (gy + kTcRing) % kTcRing, in4, b, gy, H, W, x0, tid);
-        for (int y = y0; y <= y1 && !failed; y++) {
-            const int acc = y & 1;
-            if (y < y1) {
-                // rows y-1..y+1 are staged (row y+2, when it exists, may still be
-                // in flight): make them visible to the tensor core
-                if (y + 2 <= y1)
-                    asm volatile("cp.async.wait_group 1;" ::: "memory");
-                else
-                    asm volatile("cp.async.wait_group 0;" ::: "memory");
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;");
-                __syncthreads();
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                if (tid == 0) {
-                    const uint32_t dAcc = tmem + (uint32_t)(acc * ACC_COLS);
-                    const int s0 = (y - 1 + kTcRing) % kTcRing;
-                    const int slots[3] = {s0, s0 + 1 == kTcRing ? 0 : s0 + 1,
-                        s0 + 2 >= kTcRing ? s0 + 2 - kTcRing : s0 + 2};
+    // strip geometry: segment origin x0, rows [y0, y1), image b
+#define GBSP_STRIP_GEOMETRY(strip)                                                       \
+    const int sy = (strip) % stripsPerCol, seg = ((strip) / stripsPerCol) % segs;        \
+    const int b = (strip) / (stripsPerCol * segs);                                        \
+    const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;                                \
+    const int y1 = min(H, y0 + rowsPerStrip);                                             \
+    (void)b;                                                                              \
+    (void)x0
+
+    if (warp == 0) {
+        if (lane == 0) {
+            // ---- MMA issue: rows of a strip have sequence numbers qBase + (gy - y0 + 1)
+            const uint32_t idesc = instr_desc_bf16<kTcTileP, COUT>();
+            const uint64_t aDesc0 = smem_desc(ringAddr, kTcSpx * 16, 128);
+            const uint64_t bDesc0 = smem_desc(smem_u32(sW), COUT * 16, 128);
+            uint32_t qBase = 0, outCount = 0;
+            bool ok = true;
+            for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
+                GBSP_STRIP_GEOMETRY(strip);
+                for (uint32_t q = qBase; q < qBase + 2 && ok; q++)
+                    ok = tc_wait(smem_u32(&rowFull[q % kTcRing]), (q / kTcRing) & 1u, &abortFlag);
+                for (int y = y0; y < y1 && ok; y++) {
+                    const uint32_t qTop = qBase + (uint32_t)(y - y0) + 2u;  // row y + 1
+                    if (!tc_wait(smem_u32(&rowFull[qTop % kTcRing]), (qTop / kTcRing) & 1u,
+                            &abortFlag)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    const uint32_t acc = outCount % kTcAccSlots, use = outCount / kTcAccSlots;
+                    if (use > 0 && !tc_wait(smem_u32(&accEmpty[acc]), (use - 1u) & 1u, &abortFlag)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t dAcc = tmem + acc * (uint32_t)ACC_COLS;
 #pragma unroll
                     for (int tap = 0; tap < 9; tap++) {
                         const int ty = tap / 3, tx = tap % 3;
-                        const uint64_t aRow = aDesc0 + (uint64_t)(slots[ty] * KG * kTcSpx + tx);
+                        const uint32_t slot = (qTop - 2u + (uint32_t)ty) % kTcRing;
+                        const uint64_t aRow = aDesc0 + (uint64_t)(slot * KG * kTcSpx + tx);
 #pragma unroll
                         for (int kc = 0; kc < CIN / 16; kc++) {
                             // 16-byte units: slot row, channel group 2 kc, pixel tx
@@ -379,37 +411,101 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
                                    "r"(accumulate));
                         }
                     }
-                    asm volatile(
-                        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                        :: "r"(bar[acc]) : "memory");
+                    tc_commit(smem_u32(&accFull[acc]));
+                    // row y - 1 has no later reader
+                    tc_commit(smem_u32(&rowEmpty[(qTop - 2u) % kTcRing]));
+                    outCount++;
                 }
+                if (!ok) break;
+                // rows y1 - 1 and y1 are free once the strip's last MMAs finish
+                const uint32_t qLast = qBase + (uint32_t)(y1 - y0) + 1u;
+                tc_commit(smem_u32(&rowEmpty[(qLast - 1u) % kTcRing]));
+                tc_commit(smem_u32(&rowEmpty[qLast % kTcRing]));
+                qBase = qLast + 1u;
             }
-            if (y > y0) {
-                // row y-1: its MMAs are done -> epilogue, and its oldest input row is free
-                const int pa = acc ^ 1;
-                uint32_t done = mbar_wait(bar[pa], phase[pa]);
-                failed = __syncthreads_or(!done) != 0;
-                if (failed) break;
-                phase[pa] ^= 1u;
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const int x = x0 + (warp & 3) * 32 + lane;
-                conv_epilogue<CIN, COUT, EPI>(tmem + (uint32_t)(pa * ACC_COLS), warp & 3,
-                    warp >> 2, x, W, ((size_t)(b * H + (y - 1)) * W + x), bias, outB, outF);
-                asm volatile("tcgen05.fence::before_thread_sync;");
-            }
-            // prefetch row y+3 into the slot of row y-2 (its last reader, row y-1, is done)
-            if (y + 3 <= y1)
-                stage_row<KG>(ringAddr, (y + 3) % kTcRing, in4, b, y + 3, H, W, x0, tid);
+            // every MMA issued has finished before the accumulators are freed
+            // (waited for even after an abort: the tensor memory is freed below)
+            tc_commit(smem_u32(&drain));
+            volatile uint32_t never = 0u;
+            if (!tc_wait(smem_u32(&drain), 0u, &never)) abortFlag = 1u;
+            if (!ok) abortFlag = 1u;
         }
-        // the next strip's prologue overwrites the ring
+        __syncwarp();
+    } else if (warp < 4) {
+        // ---- producers: rows y0 - 1 .. y1 of every strip, two in flight
+        const int ptid = tid - 32;
+        uint32_t q = 0;
+        int pend = 0;
+        uint32_t pendSlot[2] = {0u, 0u};
+        bool ok = true;
+        for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
+            GBSP_STRIP_GEOMETRY(strip);
+            for (int gy = y0 - 1; gy <= y1; gy++, q++) {
+                const uint32_t slot = q % kTcRing, use = q / kTcRing;
+                if (use > 0 && !tc_wait(smem_u32(&rowEmpty[slot]), (use - 1u) & 1u, &abortFlag)) {
+                    ok = false;
+                    break;
+                }
+                stage_row<KG, kTcProducers>(ringAddr, (int)slot, in4, b, gy, H, W, x0, ptid);
+                if (pend == 2) {
+                    // all but the two newest rows have landed: publish the oldest
+                    asm volatile("cp.async.wait_group 2;" ::: "memory");
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    mbar_arrive(smem_u32(&rowFull[pendSlot[0]]));
+                    pendSlot[0] = pendSlot[1];
+                    pend = 1;
+                }
+                pendSlot[pend++] = slot;
+            }
+        }
         asm volatile("cp.async.wait_group 0;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (ok)
+            for (int i = 0; i < pend; i++) mbar_arrive(smem_u32(&rowFull[pendSlot[i]]));
+    } else {
+        // ---- epilogue: warp 4 + k reads TMEM lanes 32k..32k+31 (pixels of the segment)
+        const int quarter = warp - 4;
+        uint32_t outCount = 0;
+        bool ok = true;
+        for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
+            GBSP_STRIP_GEOMETRY(strip);
+            for (int y = y0; y < y1; y++, outCount++) {
+                const uint32_t acc = outCount % kTcAccSlots, use = outCount / kTcAccSlots;
+                ok = tc_wait(smem_u32(&accFull[acc]), use & 1u, &abortFlag);
+                __syncwarp();
+                if (!__all_sync(0xFFFFFFFFu, ok)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                uint32_t r[COUT];
+#pragma unroll
+                for (int c = 0; c < COUT; c += 16) {
+                    uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) +
+                        acc * (uint32_t)ACC_COLS + (uint32_t)c;
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                        : "=r"(r[c + 0]), "=r"(r[c + 1]), "=r"(r[c + 2]), "=r"(r[c + 3]),
+                          "=r"(r[c + 4]), "=r"(r[c + 5]), "=r"(r[c + 6]), "=r"(r[c + 7]),
+                          "=r"(r[c + 8]), "=r"(r[c + 9]), "=r"(r[c + 10]), "=r"(r[c + 11]),
+                          "=r"(r[c + 12]), "=r"(r[c + 13]), "=r"(r[c + 14]), "=r"(r[c + 15])
+                        : "r"(taddr));
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                mbar_arrive(smem_u32(&accEmpty[acc]));
+                const int x = x0 + quarter * 32 + lane;
+                if (x < W)
+                    conv_store<COUT, EPI>(r, (size_t)(b * H + y) * W + x, bias, outB, outF);
+            }
+        }
     }
-    if (failed && tid == 0) atomicOr(&g_dnStatus, 1u);
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
+#undef GBSP_STRIP_GEOMETRY
+    asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && abortFlag) atomicOr(&g_dnStatus, 1u);
     if (warp == 0)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
                      :: "r"(tmem), "r"(TMEM_COLS));
