@@ -444,6 +444,14 @@ int gbsp_dn_conv3x3_forward(void *stream, const uint16_t *in, uint32_t B, uint32
 int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uint32_t H,
     uint32_t W, uint32_t cin, const uint16_t *weights, const float *bias, uint32_t cout,
     int epilogue, uint16_t *outBf16, float *outF32);
+/* The logits layer (cin -> 32, FP32 accumulators + bias) fused with the 5x5
+ * kernel-prediction filter: out[p] = sum_k softmax(logits[p][0..24])_k *
+ * noisy[p + off5x5(k)] (edge-clamped), RGBA32F, without storing the logits.
+ * Bit-identical to gbsp_dn_conv3x3_forward_tc (epilogue 1) + gbsp_dn_filter.
+ * cin = 48. */
+int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint32_t H,
+    uint32_t W, uint32_t cin, const uint16_t *weights, const float *bias, const float *noisy,
+    float *out);
 /* Reads and clears the denoiser kernels' device status word (1 = a tensor-core
  * completion wait ran out); GBSP_ERR_DEVICE_STATUS when it was set. */
 int gbsp_dn_status(uint32_t *status);

@@ -280,3 +280,22 @@ def test_tensor_core_weight_grad_is_deterministic(gpu_lib):
         outs.append((dw, db))
     torch.cuda.synchronize()
     assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize("B,H,W", [(1, 37, 200), (2, 4, 129), (1, 1, 3)])
+def test_fused_logits_and_filter_match_unfused(gpu_lib, B, H, W):
+    """The logits conv fused with the kernel-prediction filter gives the same
+    bits as the logits conv followed by the separate filter kernel."""
+    import torch
+
+    from vk_cinematic_gb300.denoiser import KPCNN
+
+    torch.manual_seed(11 + W)
+    net = KPCNN(seed=4)
+    rad = torch.rand((B, H, W, 4), device="cuda") * 3.0
+    aov = torch.rand((B, H, W, 8), device="cuda")
+    fused = net.denoise(rad, aov)
+    logits, _ = net.forward(net.features(rad, aov))
+    unfused = net.filter(logits, rad)
+    torch.cuda.synchronize()
+    assert torch.equal(fused, unfused)

@@ -261,8 +261,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
     float4 vE[kBatchMaxBounces], vA[kBatchMaxBounces];
     V3 o = v3(0, 0, 0), d = v3(0, 0, 0), invd = v3(0, 0, 0);
     // traversal state
-    uint32_t stackRef[kStackSize];
-    float stackT[kStackSize];
+    StackEntry stack[kStackSize];
     int sp = 0, tmode = 1, base = 0;
     float bestT = kInf, bestU = 0, bestV = 0;
     int32_t bestPrim = -1, bestInst = -1;
@@ -281,8 +280,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
         bestPrim = bestInst = -1;
         sp = 0;
         if (sv.tlasRoot != kEmptyChild) {
-            stackRef[0] = sv.tlasRoot;
-            stackT[0] = 0.0f;
+            stack[0] = StackEntry{sv.tlasRoot, 0.0f};
             sp = 1;
         }
         tmode = 1;
@@ -439,8 +437,9 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                 return;
             }
             sp--;
-            uint32_t ref = stackRef[sp];
-            float te = stackT[sp];
+            const StackEntry top = stack[sp];
+            uint32_t ref = top.ref;
+            float te = top.t;
             float bound = tmode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * llen));
             if (te > bound) return;
             if (!child_is_leaf(ref)) {
@@ -450,7 +449,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                     cnt.meshNodes++;
                 V3 ro = tmode == 1 ? o : lo;
                 V3 ri = tmode == 1 ? invd : linvd;
-                visit_node<true, kWT>(sv.nodes, ref, ro, ri, bound, stackRef, stackT, sp, status,
+                visit_node<true, kWT>(sv.nodes, ref, ro, ri, bound, stack, sp, status,
                     cnt);
                 return;
             }
@@ -472,8 +471,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                     atomicOr(status, kStatusStackOverflow);
                     return;
                 }
-                stackRef[sp] = __ldg(&in.blasRoot);
-                stackT[sp] = 0.0f;
+                stack[sp] = StackEntry{__ldg(&in.blasRoot), 0.0f};
                 sp++;
                 tmode = 2;
                 return;

@@ -42,7 +42,8 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
-enum Epilogue : int { kEpiBf16BiasRelu = 0, kEpiF32Bias = 1, kEpiF32 = 2 };
+// 3: FP32 logits + bias fed straight into the 5x5 kernel-prediction filter
+enum Epilogue : int { kEpiBf16BiasRelu = 0, kEpiF32Bias = 1, kEpiF32 = 2, kEpiFilter = 3 };
 
 // out[p][co] = sum_{tap, ci} in[p + off(tap)][ci] * w[tap][co][ci] (+ bias, ReLU)
 template <int CIN, int COUT, int EPI>
@@ -277,6 +278,28 @@ __device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 
     asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
+__device__ __forceinline__ void softmax25(const float *l, float *w)
+{
+    float m = l[0];
+#pragma unroll
+    for (int k = 1; k < 25; k++) m = fmaxf(m, l[k]);
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 25; k++) {
+        w[k] = __expf(l[k] - m);
+        s += w[k];
+    }
+    float inv = 1.0f / s;
+#pragma unroll
+    for (int k = 0; k < 25; k++) w[k] *= inv;
+}
+
+__device__ __forceinline__ uint64_t tap_pixel(uint64_t p, int x, int y, int W, int H, int k)
+{
+    int gx = min(max(x + k % 5 - 2, 0), W - 1), gy = min(max(y + k / 5 - 2, 0), H - 1);
+    return p - (uint64_t)x - (uint64_t)y * W + (uint64_t)gy * W + gx;
+}
+
 // Bias / ReLU / BF16 packing of one pixel's COUT accumulators and the store.
 template <int COUT, int EPI>
 __device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
@@ -302,10 +325,35 @@ __device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
     }
 }
 
+// Softmax of the 25 kernel logits (accumulators + bias) and the 5x5 filter of
+// the noisy radiance around pixel p = (x, y): the same arithmetic as k_filter
+// on stored logits, so the fused and unfused results are bit-identical.
+template <int COUT>
+__device__ __forceinline__ void conv_filter_store(const uint32_t (&r)[COUT], size_t p, int x, int y,
+    int W, int H, const float *__restrict__ bias, const float4 *__restrict__ noisy,
+    float4 *__restrict__ out)
+{
+    static_assert(COUT >= 25, "kernel logits");
+    float l[25], wk[25];
+#pragma unroll
+    for (int k = 0; k < 25; k++) l[k] = __uint_as_float(r[k]) + __ldg(bias + k);
+    softmax25(l, wk);
+    float3 o = make_float3(0, 0, 0);
+#pragma unroll
+    for (int k = 0; k < 25; k++) {
+        float4 c = __ldg(noisy + tap_pixel(p, x, y, W, H, k));
+        o.x += wk[k] * c.x;
+        o.y += wk[k] * c.y;
+        o.z += wk[k] * c.z;
+    }
+    out[p] = make_float4(o.x, o.y, o.z, 1.0f);
+}
+
 template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in,
     int B, int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
-    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
+    const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF,
+    const float4 *__restrict__ noisy, float4 *__restrict__ outFilt)
 {
     static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tcgen05 tile shape");
     constexpr int KG = CIN / 8;  // 16-byte channel groups
@@ -496,8 +544,13 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
                 asm volatile("tcgen05.fence::before_thread_sync;");
                 mbar_arrive(smem_u32(&accEmpty[acc]));
                 const int x = x0 + quarter * 32 + lane;
-                if (x < W)
-                    conv_store<COUT, EPI>(r, (size_t)(b * H + y) * W + x, bias, outB, outF);
+                if (x < W) {
+                    const size_t p = (size_t)(b * H + y) * W + x;
+                    if constexpr (EPI == kEpiFilter)
+                        conv_filter_store<COUT>(r, p, x, y, W, H, bias, noisy, outFilt);
+                    else
+                        conv_store<COUT, EPI>(r, p, bias, outB, outF);
+                }
             }
         }
     }
@@ -513,7 +566,8 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
 
 template <int CIN, int COUT, int EPI>
 int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, int W, const void *w,
-    const float *bias, void *outB, float *outF)
+    const float *bias, void *outB, float *outF, const float4 *noisy = nullptr,
+    float4 *outFilt = nullptr)
 {
     size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
@@ -527,7 +581,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     int grid = strips < ctas ? strips : ctas;
     kern<<<grid, kTcThreads, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
         reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
-        outF);
+        outF, noisy, outFilt);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }
@@ -744,28 +798,6 @@ __global__ void k_wgrad_reduce(const float *__restrict__ partial, int slices, in
 
 // Per-pixel 5x5 filter from softmax(logits[0..24]) applied to the noisy
 // radiance (clamped to the image edge).
-__device__ __forceinline__ void softmax25(const float *l, float *w)
-{
-    float m = l[0];
-#pragma unroll
-    for (int k = 1; k < 25; k++) m = fmaxf(m, l[k]);
-    float s = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 25; k++) {
-        w[k] = __expf(l[k] - m);
-        s += w[k];
-    }
-    float inv = 1.0f / s;
-#pragma unroll
-    for (int k = 0; k < 25; k++) w[k] *= inv;
-}
-
-__device__ __forceinline__ uint64_t tap_pixel(uint64_t p, int x, int y, int W, int H, int k)
-{
-    int gx = min(max(x + k % 5 - 2, 0), W - 1), gy = min(max(y + k / 5 - 2, 0), H - 1);
-    return p - (uint64_t)x - (uint64_t)y * W + (uint64_t)gy * W + gx;
-}
-
 __global__ void k_filter(const float *__restrict__ logits, const float4 *__restrict__ noisy, int B,
     int H, int W, float4 *__restrict__ out)
 {
@@ -1014,6 +1046,22 @@ int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uin
 #undef GBSP_CONV_CASE
     return set_error(GBSP_ERR_INVALID_ARGUMENT, "conv3x3 %u->%u epilogue %d not instantiated", cin,
         cout, epilogue);
+}
+
+int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint32_t H,
+    uint32_t W, uint32_t cin, const uint16_t *weights, const float *bias, const float *noisy,
+    float *out)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!in || !weights || !bias || !noisy || !out || !B || !H || !W)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad fused conv/filter args");
+    if (((uintptr_t)in | (uintptr_t)weights | (uintptr_t)noisy | (uintptr_t)out) & 15u)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "conv tensors must be 16-byte aligned");
+    if (cin != 48)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "fused conv/filter %u->32 not instantiated", cin);
+    return launch_conv_tc<48, 32, kEpiFilter>(s, sm_count(), in, (int)B, (int)H, (int)W, weights,
+        bias, nullptr, nullptr, reinterpret_cast<const float4 *>(noisy),
+        reinterpret_cast<float4 *>(out));
 }
 
 int gbsp_dn_status(uint32_t *status)

@@ -27,6 +27,13 @@
 namespace gbsp {
 
 constexpr int kStackSize = 96;
+
+// One traversal stack entry: a node or leaf reference and its entry
+// distance, kept together so that a push or a pop is one 8-byte access.
+struct __align__(8) StackEntry {
+    uint32_t ref;
+    float t;
+};
 constexpr float kInf = __builtin_huge_valf();
 
 struct RayHit {
@@ -46,7 +53,7 @@ __device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765
 // kWT: the watertight mode's robust slab test.
 template <bool kCount, bool kWT = false>
 __device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
-    V3 invd, float bound, uint32_t *stackRef, float *stackT, int &sp, uint32_t *status,
+    V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
     TraceCounters &cnt)
 {
     const float4 *p = reinterpret_cast<const float4 *>(nodes + ref);
@@ -73,8 +80,7 @@ __device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint
             if (te < nearT) {
                 if (nearRef != kEmptyChild) {
                     if (sp < kStackSize) {
-                        stackRef[sp] = nearRef;
-                        stackT[sp] = nearT;
+                        stack[sp] = StackEntry{nearRef, nearT};
                         sp++;
                     } else {
                         atomicOr(status, kStatusStackOverflow);
@@ -84,8 +90,7 @@ __device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint
                 nearT = te;
             } else {
                 if (sp < kStackSize) {
-                    stackRef[sp] = c;
-                    stackT[sp] = te;
+                    stack[sp] = StackEntry{c, te};
                     sp++;
                 } else {
                     atomicOr(status, kStatusStackOverflow);
@@ -95,8 +100,7 @@ __device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint
     }
     if (nearRef != kEmptyChild) {
         if (sp < kStackSize) {
-            stackRef[sp] = nearRef;
-            stackT[sp] = nearT;
+            stack[sp] = StackEntry{nearRef, nearT};
             sp++;
         } else {
             atomicOr(status, kStatusStackOverflow);
@@ -150,12 +154,10 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
     best.prim = -1;
     best.inst = -1;
     if (sv.tlasRoot == kEmptyChild) return best;
-    uint32_t stackRef[kStackSize];
-    float stackT[kStackSize];
+    StackEntry stack[kStackSize];
     int sp = 0;
     V3 invd = inverse(d);
-    stackRef[sp] = sv.tlasRoot;
-    stackT[sp] = 0.0f;
+    stack[sp] = StackEntry{sv.tlasRoot, 0.0f};
     sp++;
     const Node8 *__restrict__ nodes = sv.nodes;
     // trees are validated at build time (children after parents), so the
@@ -166,12 +168,13 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
             break;
         }
         sp--;
-        uint32_t ref = stackRef[sp];
-        float te = stackT[sp];
+        const StackEntry top = stack[sp];
+        uint32_t ref = top.ref;
+        float te = top.t;
         if (te > prune_bound(best.t)) continue;
         if (!child_is_leaf(ref)) {
             if (kCount) cnt.topNodes++;
-            visit_node<kCount, kWT>(nodes, ref, o, invd, prune_bound(best.t), stackRef, stackT,
+            visit_node<kCount, kWT>(nodes, ref, o, invd, prune_bound(best.t), stack,
                 sp, status, cnt);
             continue;
         }
@@ -194,18 +197,18 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
             atomicOr(status, kStatusStackOverflow);
             continue;
         }
-        stackRef[sp] = __ldg(&in.blasRoot);
-        stackT[sp] = 0.0f;
+        stack[sp] = StackEntry{__ldg(&in.blasRoot), 0.0f};
         sp++;
         for (int guard = 0; sp > base && guard < (1 << 22); guard++) {
             sp--;
-            uint32_t r2 = stackRef[sp];
-            float t2 = stackT[sp];
+            const StackEntry top = stack[sp];
+            uint32_t r2 = top.ref;
+            float t2 = top.t;
             float bound = prune_bound(rmin(lBestT, localBound));
             if (t2 > bound) continue;
             if (!child_is_leaf(r2)) {
                 if (kCount) cnt.meshNodes++;
-                visit_node<kCount, kWT>(nodes, r2, lo, linvd, bound, stackRef, stackT, sp, status,
+                visit_node<kCount, kWT>(nodes, r2, lo, linvd, bound, stack, sp, status,
                     cnt);
             } else {
                 visit_leaf<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);

@@ -163,8 +163,7 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
     unsigned int *work = &ctl[kCtlTraceWork];
     TraceCounters cnt = {0, 0, 0, 0, 0};
     uint32_t done = 0, hits = 0;
-    uint32_t stackRef[kStackSize];
-    float stackT[kStackSize];
+    StackEntry stack[kStackSize];
     int sp = 0, base = 0;
     int mode = 0;  // 0 needs a ray, 1 object level, 2 mesh level
     uint32_t slot = 0, steps = 0, inst = 0;
@@ -200,8 +199,7 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
             bestPrim = bestInst = -1;
             sp = 0;
             if (src.scene(pathId).tlasRoot != kEmptyChild) {
-                stackRef[0] = src.scene(pathId).tlasRoot;
-                stackT[0] = 0.0f;
+                stack[0] = StackEntry{src.scene(pathId).tlasRoot, 0.0f};
                 sp = 1;
             }
             mode = 1;
@@ -238,8 +236,9 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
             mode = 0;
         } else {
             sp--;
-            uint32_t ref = stackRef[sp];
-            float te = stackT[sp];
+            const StackEntry top = stack[sp];
+            uint32_t ref = top.ref;
+            float te = top.t;
             float bound = mode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * len));
             if (te > bound) {
                 // pruned
@@ -249,7 +248,7 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                 else
                     cnt.meshNodes++;
                 visit_node<true, kWT>(src.scene(pathId).nodes, ref, mode == 1 ? o : lo,
-                    mode == 1 ? invd : linvd, bound, stackRef, stackT, sp, status, cnt);
+                    mode == 1 ? invd : linvd, bound, stack, sp, status, cnt);
             } else if (mode == 1) {
                 // an object whose world box passed: enter its mesh
                 inst = leaf_first(ref);
@@ -268,8 +267,7 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                 if (sp >= kStackSize) {
                     atomicOr(status, kStatusStackOverflow);
                 } else {
-                    stackRef[sp] = __ldg(&in.blasRoot);
-                    stackT[sp] = 0.0f;
+                    stack[sp] = StackEntry{__ldg(&in.blasRoot), 0.0f};
                     sp++;
                     mode = 2;
                 }

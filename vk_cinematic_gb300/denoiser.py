@@ -138,8 +138,25 @@ class KPCNN:
         return out
 
     def denoise(self, radiance, aov):
-        logits, _ = self.forward(self.features(radiance, aov))
-        return self.filter(logits, radiance)
+        """Denoised RGBA32F frame.  On the tcgen05 path the logits layer and the
+        5x5 filter run as one kernel (the logits never reach memory); the
+        result is bit-identical to forward() + filter()."""
+        import torch
+
+        if self.conv_impl != "tcgen05":
+            logits, _ = self.forward(self.features(radiance, aov))
+            return self.filter(logits, radiance)
+        x = self.features(radiance, aov)
+        last = len(LAYERS) - 1
+        for li in range(last):
+            x = self.conv(li, x)
+        B, H, W, cin = x.shape
+        noisy = radiance.contiguous()
+        out = torch.empty((B, H, W, 4), dtype=torch.float32, device="cuda")
+        _check(self.L.gbsp_dn_conv3x3_filter_tc(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W),
+                                                _u32(cin), _ptr(self.wb[last]), _ptr(self.b[last]),
+                                                _ptr(noisy), _ptr(out)))
+        return out
 
     def denoise_checked(self, radiance, aov, plain_check, bound=0.01, tile=16):
         """Denoises `radiance` and lets the plain path tracer judge every
