@@ -169,29 +169,36 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // [COUT][16 B].  Descriptor strides: leading (K) = next channel group,
 // stride (M or N) = next 8 rows = 128 B.
 //
-// A CTA walks vertical strips (one 128-pixel column segment, a run of rows)
-// with its warps specialised and coupled only by mbarriers:
+// One persistent CTA per SM walks vertical strips (one 128-pixel column
+// segment, a run of rows) with its warps specialised and coupled only by
+// mbarriers:
 //   * warps 1-3 (producers) stage input rows into a ring of kTcRing slots
-//     with cp.async, two rows in flight; a row's slot is reused once the
+//     with cp.async, kTcInFlight rows in flight (the memory-level
+//     parallelism that hides DRAM latency); a row's slot is reused once the
 //     MMAs of the last output row that reads it have completed (rowEmpty,
 //     signalled by tcgen05.commit), and a staged row is published on
 //     rowFull after cp.async.wait_group + fence.proxy.async;
 //   * lane 0 of warp 0 issues, per output row y, the 9 taps x CIN/16 MMAs
 //     reading rows y-1..y+1 into one of kTcAccSlots TMEM accumulators, then
 //     commits to that accumulator's accFull and to the rowEmpty of row y-1;
-//   * warps 4-7 (epilogue; warp 4 + k owns TMEM lanes 32k..32k+31 = pixels)
-//     wait on accFull, read the accumulator with tcgen05.ld, release it on
-//     accEmpty and apply bias / ReLU / BF16 packing while the tensor core
+//   * warps 4-11 are two epilogue groups taking alternate output rows (warp
+//     w owns TMEM lanes 32 (w % 4) .. + 31 = pixels): wait on accFull, read
+//     the accumulator with tcgen05.ld, release it on accEmpty and apply bias
+//     / ReLU / BF16 packing (or the fused filter) while the tensor core
 //     already works on the next rows.
 // Every wait is bounded; a timeout raises a shared abort flag that ends the
 // other roles' waits, and sets g_dnStatus.
 // ---------------------------------------------------------------------------
 constexpr int kTcTileP = 128;
-constexpr int kTcThreads = 256;  // warp 0: MMA issue; warps 1-3: producers; 4-7: epilogue
+// One CTA per SM: warp 0 issues the MMAs, warps 1-3 produce, warps 4-11 are
+// two epilogue groups that take alternate output rows.
+constexpr int kTcThreads = 384;
 constexpr int kTcProducers = 96;
-constexpr int kTcAccSlots = 4;
+constexpr int kTcEpiGroups = 2;
+constexpr int kTcAccSlots = 4;  // accumulator a is drained by epilogue group a % 2
 constexpr int kTcSpx = kTcTileP + 2;
-constexpr int kTcRing = 5;  // rows y-1..y+1 read by the MMAs, two more in flight
+constexpr int kTcRing = 14;     // input row slots
+constexpr int kTcInFlight = 10; // rows staged but not yet published (kTcRing >= kTcInFlight + 3)
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 __device__ uint32_t g_dnStatus;
@@ -311,7 +318,7 @@ __device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             v[k] = __uint_as_float(r[c + k]);
-            if (EPI != kEpiF32) v[k] += __ldg(bias + c + k);
+            if (EPI != kEpiF32) v[k] += bias[c + k];
             if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
         }
         if (EPI == kEpiBf16BiasRelu) {
@@ -336,7 +343,7 @@ __device__ __forceinline__ void conv_filter_store(const uint32_t (&r)[COUT], siz
     static_assert(COUT >= 25, "kernel logits");
     float l[25], wk[25];
 #pragma unroll
-    for (int k = 0; k < 25; k++) l[k] = __uint_as_float(r[k]) + __ldg(bias + k);
+    for (int k = 0; k < 25; k++) l[k] = __uint_as_float(r[k]) + bias[k];
     softmax25(l, wk);
     float3 o = make_float3(0, 0, 0);
 #pragma unroll
@@ -350,7 +357,7 @@ __device__ __forceinline__ void conv_filter_store(const uint32_t (&r)[COUT], siz
 }
 
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in,
+__global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in,
     int B, int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF,
     const float4 *__restrict__ noisy, float4 *__restrict__ outFilt)
@@ -367,8 +374,10 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
     __shared__ __align__(8) uint64_t accFull[kTcAccSlots], accEmpty[kTcAccSlots], drain;
     __shared__ uint32_t tmemBase;
     __shared__ volatile uint32_t abortFlag;
+    __shared__ __align__(16) float sBias[COUT];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
+    if (tid < COUT) sBias[tid] = EPI != kEpiF32 ? bias[tid] : 0.0f;
 
     // weights -> canonical layout: (tap, kg, co) holds w[tap][co][8 kg .. 8 kg + 7]
     for (int i = tid; i < 9 * KG * COUT; i += kTcThreads) {
@@ -483,8 +492,6 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
         // ---- producers: rows y0 - 1 .. y1 of every strip, two in flight
         const int ptid = tid - 32;
         uint32_t q = 0;
-        int pend = 0;
-        uint32_t pendSlot[2] = {0u, 0u};
         bool ok = true;
         for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
             GBSP_STRIP_GEOMETRY(strip);
@@ -495,29 +502,30 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
                     break;
                 }
                 stage_row<KG, kTcProducers>(ringAddr, (int)slot, in4, b, gy, H, W, x0, ptid);
-                if (pend == 2) {
-                    // all but the two newest rows have landed: publish the oldest
-                    asm volatile("cp.async.wait_group 2;" ::: "memory");
+                if (q >= (uint32_t)kTcInFlight) {
+                    // every row but the kTcInFlight newest has landed: publish row q - kTcInFlight
+                    static_assert(kTcInFlight == 10, "wait_group immediate");
+                    asm volatile("cp.async.wait_group 10;" ::: "memory");
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_arrive(smem_u32(&rowFull[pendSlot[0]]));
-                    pendSlot[0] = pendSlot[1];
-                    pend = 1;
+                    mbar_arrive(smem_u32(&rowFull[(q - kTcInFlight) % kTcRing]));
                 }
-                pendSlot[pend++] = slot;
             }
         }
         asm volatile("cp.async.wait_group 0;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         if (ok)
-            for (int i = 0; i < pend; i++) mbar_arrive(smem_u32(&rowFull[pendSlot[i]]));
+            for (uint32_t r = q > (uint32_t)kTcInFlight ? q - kTcInFlight : 0u; r < q; r++)
+                mbar_arrive(smem_u32(&rowFull[r % kTcRing]));
     } else {
-        // ---- epilogue: warp 4 + k reads TMEM lanes 32k..32k+31 (pixels of the segment)
-        const int quarter = warp - 4;
+        // ---- epilogue: group g = (warp - 4) / 4 takes the output rows with
+        // outCount % 2 == g; warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels)
+        const int quarter = warp & 3, group = (warp - 4) >> 2;
         uint32_t outCount = 0;
         bool ok = true;
         for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
             GBSP_STRIP_GEOMETRY(strip);
             for (int y = y0; y < y1; y++, outCount++) {
+                if ((int)(outCount % kTcEpiGroups) != group) continue;
                 const uint32_t acc = outCount % kTcAccSlots, use = outCount / kTcAccSlots;
                 ok = tc_wait(smem_u32(&accFull[acc]), use & 1u, &abortFlag);
                 __syncwarp();
@@ -547,9 +555,9 @@ __global__ void __launch_bounds__(kTcThreads) k_conv3x3_tc(const __nv_bfloat16 *
                 if (x < W) {
                     const size_t p = (size_t)(b * H + y) * W + x;
                     if constexpr (EPI == kEpiFilter)
-                        conv_filter_store<COUT>(r, p, x, y, W, H, bias, noisy, outFilt);
+                        conv_filter_store<COUT>(r, p, x, y, W, H, sBias, noisy, outFilt);
                     else
-                        conv_store<COUT, EPI>(r, p, bias, outB, outF);
+                        conv_store<COUT, EPI>(r, p, sBias, outB, outF);
                 }
             }
         }
@@ -572,10 +580,11 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int ctas = smCount * 2;
+    const int ctas = smCount;  // one CTA per SM (the row ring takes most of shared memory)
     const int cols = B * ((W + kTcTileP - 1) / kTcTileP);
-    // rows per strip: enough strips to fill every CTA slot, at least 4 rows
-    int rows = (int)(((int64_t)cols * H + ctas - 1) / ctas);
+    // rows per strip: about six strips per CTA (strips go round-robin, so
+    // the last round is nearly full), at least 4 rows
+    int rows = (int)(((int64_t)cols * H + 6 * ctas - 1) / (6 * ctas));
     rows = rows < 4 ? 4 : (rows > H ? H : rows);
     int strips = cols * ((H + rows - 1) / rows);
     int grid = strips < ctas ? strips : ctas;
