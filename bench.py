@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--dn-conv", choices=["tcgen05", "mma"], default="tcgen05")
     ap.add_argument("--dn-wgrad", choices=["mma", "simt"], default="mma")
+    ap.add_argument("--sort-dirs", action="store_true",
+                    help="sort bounce-ray queues by direction octant")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
     ap.add_argument("--trace", choices=["hybrid", "warp", "lane"], default="hybrid",
@@ -345,6 +347,8 @@ def run_gpu(args):
     s = make_scene(args.workload, rank)
     flags = gbsp.FLAG_STAGE_TIMING | {"hybrid": 0, "lane": gbsp.FLAG_TRACE_PER_LANE,
                                       "warp": gbsp.FLAG_TRACE_PER_WARP}[args.trace]
+    if args.sort_dirs:
+        flags |= gbsp.FLAG_SORT_DIRECTIONS
     opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed, flags=flags)
     scene, ms, rend = gbsp.upload_scene(rt, s, opt)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -451,6 +455,7 @@ def run_gpu(args):
             "data": "synthetic: seeded procedural scene", "config": workload_config(s, args.workload),
             "mrays_per_s": rays_all / (elapsed_ms / 1e3) / 1e6,
             "parallelism": f"replicas x{world}", "trace_scheduling": args.trace,
+            "sort_directions": bool(args.sort_dirs),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(M["kernel_launches"]), "clocks": clk,
             "metrics": {k: M[k] for k in ("paths_traced", "rays_traced", "ray_hit_count",

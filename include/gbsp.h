@@ -85,6 +85,9 @@ extern "C" {
  * its current one is done.  The flags force one scheduling for every bounce. */
 #define GBSP_FLAG_TRACE_PER_LANE 4u
 #define GBSP_FLAG_TRACE_PER_WARP 8u
+/* Sort each bounce's ray queue by direction octant before tracing it (same
+ * results; rays of a warp then share the tree's near-to-far child order). */
+#define GBSP_FLAG_SORT_DIRECTIONS 16u
 
 typedef struct gbsp_runtime gbsp_runtime;
 typedef struct gbsp_scene gbsp_scene;
@@ -459,9 +462,11 @@ int gbsp_dn_status(uint32_t *status);
  * and C are independent plain renders with the same spp, denoised = D(A);
  * per tile x tile block (tile <= 16) the tile's relMSE is estimated as
  * mean(((D - C)^2 - (A - C)^2 / 2) / (D^2 + 0.01)) (the second term removes
- * C's own variance), and a tile above `bound` is served from the plain
- * samples (A + C) / 2.  Frames are RGBA32F (B x H x W); tileErr / flags
- * receive one value per tile (row-major per image). */
+ * C's own variance); a tile whose estimate exceeds `bound` by more than two
+ * standard errors of the tile mean (from the spread of its per-pixel terms)
+ * is served from the plain samples (A + C) / 2.  Frames are RGBA32F
+ * (B x H x W); tileErr receives the estimate and flags 1 for a tile that
+ * fell back, one value per tile (row-major per image). */
 int gbsp_dn_tile_fallback(void *stream, const float *denoised, const float *plainA,
     const float *plainC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile, float bound,
     float *out, float *tileErr, uint32_t *flags);

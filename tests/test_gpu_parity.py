@@ -302,8 +302,9 @@ def test_tonemap_matches_oracle(rt, port):
 
 @pytest.mark.parametrize("kind", ["config1", "config3_small", "crop_spp64"])
 def test_per_lane_trace_matches_static(rt, kind):
-    """The closest-hit scheduling flags (per warp, per lane, the default mix)
-    change only scheduling: images and every counter match bit for bit."""
+    """The closest-hit scheduling flags (per warp, per lane, the default mix,
+    bounce queues sorted by direction octant) change only scheduling: images
+    and every counter match bit for bit."""
     from vk_cinematic_gb300 import scenes
 
     if kind == "config1":
@@ -316,7 +317,8 @@ def test_per_lane_trace_matches_static(rt, kind):
         s = scenes.config3_scene(width=1920, height=1080, spp=64, n_spheres=64, level=3, seed=0)
         region = (1578, 647, 1578 + 64, 647 + 64)
     out = []
-    for flags in (gbsp.FLAG_TRACE_PER_WARP, gbsp.FLAG_TRACE_PER_LANE, 0):
+    for flags in (gbsp.FLAG_TRACE_PER_WARP, gbsp.FLAG_TRACE_PER_LANE, 0,
+                  gbsp.FLAG_SORT_DIRECTIONS, gbsp.FLAG_SORT_DIRECTIONS | gbsp.FLAG_TRACE_PER_WARP):
         scene, ms, rend = gbsp.upload_scene(rt, s)
         rend.options.flags = flags
         img, _, m = rend.tile(region)

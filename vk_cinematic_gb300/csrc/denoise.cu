@@ -834,10 +834,14 @@ __global__ void k_filter(const float *__restrict__ logits, const float4 *__restr
 // E[(D - C)^2] = (D - mu)^2 + s^2 and E[(A - C)^2] = 2 s^2, so per pixel and
 // channel (D - C)^2 - (A - C)^2 / 2 estimates the denoiser's squared error;
 // divided by D^2 + 0.01 and averaged over a tile it estimates the tile's
-// relMSE.  A tile whose estimate exceeds the bound is served from the plain
-// samples, (A + C) / 2; the others keep D.  One CTA of 256 threads per tile
+// relMSE.  The per-pixel terms are noisy at low spp, so a tile falls back
+// only when the bound lies below the estimate by more than kFallbackZ
+// standard errors of the tile mean (a one-sided test at about 98%): then it
+// is served from the plain samples, (A + C) / 2; the others keep D.  One CTA of 256 threads per tile
 // (tile <= 16 x 16).  tileErr[t] receives the estimate, flags[t] 1 when the
 // tile fell back.
+constexpr float kFallbackZ = 2.0f;
+
 __global__ void __launch_bounds__(256) k_tile_fallback(const float4 *__restrict__ D,
     const float4 *__restrict__ A, const float4 *__restrict__ C, int B, int H, int W, int tile,
     float bound, float4 *__restrict__ out, float *__restrict__ tileErr, uint32_t *__restrict__ flags)
@@ -849,7 +853,7 @@ __global__ void __launch_bounds__(256) k_tile_fallback(const float4 *__restrict_
     const int x = tx * tile + lx, y = ty * tile + ly;
     const bool in = threadIdx.x < tile * tile && x < W && y < H;
     const size_t p = ((size_t)b * H + y) * W + x;
-    float e = 0.0f, n = 0.0f;
+    float e = 0.0f, e2 = 0.0f, n = 0.0f;
     float4 d = make_float4(0, 0, 0, 0), a = d, c = d;
     if (in) {
         d = D[p];
@@ -859,27 +863,35 @@ __global__ void __launch_bounds__(256) k_tile_fallback(const float4 *__restrict_
 #pragma unroll
         for (int k = 0; k < 3; k++) {
             float dc = dv[k] - cv[k], ac = av[k] - cv[k];
-            e += (dc * dc - 0.5f * ac * ac) / (dv[k] * dv[k] + 0.01f);
+            const float term = (dc * dc - 0.5f * ac * ac) / (dv[k] * dv[k] + 0.01f);
+            e += term;
+            e2 += term * term;
         }
         n = 3.0f;
     }
-    __shared__ float sE[8], sN[8];
+    __shared__ float sE[8], sE2[8], sN[8];
     for (int off = 16; off; off >>= 1) {
         e += __shfl_xor_sync(0xFFFFFFFFu, e, off);
+        e2 += __shfl_xor_sync(0xFFFFFFFFu, e2, off);
         n += __shfl_xor_sync(0xFFFFFFFFu, n, off);
     }
     if ((threadIdx.x & 31) == 0) {
         sE[threadIdx.x >> 5] = e;
+        sE2[threadIdx.x >> 5] = e2;
         sN[threadIdx.x >> 5] = n;
     }
     __syncthreads();
-    float te = 0.0f, tn = 0.0f;
+    float te = 0.0f, te2 = 0.0f, tn = 0.0f;
     for (int k = 0; k < 8; k++) {
         te += sE[k];
+        te2 += sE2[k];
         tn += sN[k];
     }
     const float est = tn > 0.0f ? te / tn : 0.0f;
-    const bool fallback = est > bound;
+    // standard error of the tile mean from the spread of its per-pixel terms
+    const float var = tn > 1.0f ? fmaxf(te2 - te * est, 0.0f) / (tn - 1.0f) : 0.0f;
+    const float se = tn > 0.0f ? sqrtf(var / tn) : 0.0f;
+    const bool fallback = est - kFallbackZ * se > bound;
     if (threadIdx.x == 0) {
         tileErr[t] = est;
         flags[t] = fallback ? 1u : 0u;

@@ -85,6 +85,7 @@ struct gbsp_runtime {
     gbsp::DeviceBuffer<float4> rayO, rayD;         // two queues back to back
     gbsp::DeviceBuffer<int4> hitA;                 // t, u, v, prim
     gbsp::DeviceBuffer<int> hitInst;
+    gbsp::DeviceBuffer<uint32_t> sortHist;       // octant histograms of the ray sort
     gbsp::DeviceBuffer<uint32_t> pathRng;
     gbsp::DeviceBuffer<uint32_t> pathLen;
     gbsp::DeviceBuffer<float4> vertE;              // emission xyz, cosine

@@ -203,6 +203,8 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     wp.aovImage = dAov;
     OneScene one = {sv, mv, maxBounces, opt.radiance_clamp};
     int persistentGrid = rt->smCount * 8;
+    const bool sortDirs = (opt.flags & GBSP_FLAG_SORT_DIRECTIONS) != 0 && maxBounces > 1;
+    if (sortDirs && (rc = rt->sortHist.reserve(8 * (size_t)kSortBlocks, s))) return rc;
     bool timing = rt->stageTiming;
     for (uint64_t pb = 0; pb < regionPixels; pb += pixelsPerWave) {
         wp.pixelBase = pb;
@@ -215,10 +217,12 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
             k_generate<<<(paths + 255) / 256, 256, 0, s>>>(wp, wb);
             rt->launches += 2;
             for (uint32_t b = 0; b < maxBounces; b++) {
-                int inQ = (b & 1) ? kCtlQueue1 : kCtlQueue0;
-                int outQ = (b & 1) ? kCtlQueue0 : kCtlQueue1;
-                const float4 *qO = wb.rayO + ((b & 1) ? cap : 0);
-                const float4 *qD = wb.rayD + ((b & 1) ? cap : 0);
+                // sorted queues: shade always writes queue 1, the sort moves it to queue 0
+                const uint32_t side = sortDirs ? 0u : (b & 1u);
+                int inQ = side ? kCtlQueue1 : kCtlQueue0;
+                int outQ = side ? kCtlQueue0 : kCtlQueue1;
+                const float4 *qO = wb.rayO + (side ? cap : 0);
+                const float4 *qD = wb.rayD + (side ? cap : 0);
                 k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
                 int e0 = timing ? rt->stage_event(s) : -1;
                 bool perLane = (opt.flags & GBSP_FLAG_TRACE_PER_LANE) ||
@@ -227,6 +231,14 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
                     ctl + inQ, wb.hitA, wb.hitInst, ctl, counters, rt->dStatus);
                 int e1 = timing ? rt->stage_event(s) : -1;
                 k_shade<<<persistentGrid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
+                if (sortDirs && b + 1 < maxBounces) {
+                    k_octant_count<<<kSortBlocks, 256, 0, s>>>(wb.rayD + cap, ctl, kCtlQueue1,
+                        rt->sortHist.ptr);
+                    k_octant_scan<<<1, 1024, 0, s>>>(rt->sortHist.ptr, ctl, kCtlQueue1, kCtlQueue0);
+                    k_octant_scatter<<<kSortBlocks, 256, 0, s>>>(wb.rayO + cap, wb.rayD + cap, ctl,
+                        kCtlQueue1, rt->sortHist.ptr, wb.rayO, wb.rayD);
+                    rt->launches += 3;
+                }
                 int e2 = timing ? rt->stage_event(s) : -1;
                 if (timing && e0 >= 0 && e1 >= 0 && e2 >= 0) {
                     rt->traceSpans.emplace_back(e0, e1);

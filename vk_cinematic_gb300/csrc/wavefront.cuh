@@ -77,6 +77,126 @@ static __global__ void k_reset_stage(unsigned int *ctl, int outQueue)
     ctl[outQueue] = 0;
 }
 
+// ---------------------------------------------------------------------------
+// Stable counting sort of a ray queue by direction octant (sign bits of d),
+// so that the lanes of a warp walk the tree with the same near-to-far child
+// order.  Queue order otherwise follows path order (neighbouring pixels'
+// samples), which the sort keeps within each octant.  Three launches over a
+// fixed grid of kSortBlocks blocks (the count lives on the device):
+// per-block octant histograms, one exclusive scan over (octant, block), and
+// the scatter, which ranks rays inside each 256-ray tile with warp ballots.
+constexpr int kSortBlocks = 512;
+
+__device__ __forceinline__ uint32_t dir_octant(float4 d)
+{
+    return (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+}
+
+__device__ __forceinline__ void sort_chunk(uint32_t n, uint32_t &begin, uint32_t &end)
+{
+    uint32_t chunk = (n + kSortBlocks - 1) / kSortBlocks;
+    chunk = (chunk + 255u) & ~255u;
+    begin = min(n, blockIdx.x * chunk);
+    end = min(n, begin + chunk);
+}
+
+static __global__ void __launch_bounds__(256) k_octant_count(const float4 *__restrict__ rayD,
+    const unsigned int *ctl, int queue, uint32_t *hist)
+{
+    __shared__ uint32_t sh[8];
+    if (threadIdx.x < 8) sh[threadIdx.x] = 0;
+    __syncthreads();
+    uint32_t begin, end;
+    sort_chunk(ctl[queue], begin, end);
+    for (uint32_t i = begin + threadIdx.x; i < end; i += 256) atomicAdd(&sh[dir_octant(rayD[i])], 1u);
+    __syncthreads();
+    if (threadIdx.x < 8) hist[threadIdx.x * kSortBlocks + blockIdx.x] = sh[threadIdx.x];
+}
+
+// Exclusive scan of hist[8][kSortBlocks] in (octant, block) order; also
+// publishes the count as the destination queue's length.
+static __global__ void __launch_bounds__(1024) k_octant_scan(uint32_t *hist, unsigned int *ctl,
+    int srcQueue, int dstQueue)
+{
+    constexpr int kPer = 8 * kSortBlocks / 1024;
+    __shared__ uint32_t warpSum[32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t v[kPer], sum = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        v[k] = hist[t * kPer + k];
+        sum += v[k];
+    }
+    uint32_t incl = sum;
+    for (int off = 1; off < 32; off <<= 1) {
+        uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) warpSum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warpSum[lane], wi = w;
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t o = __shfl_up_sync(0xFFFFFFFFu, wi, off);
+            if (lane >= off) wi += o;
+        }
+        warpSum[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warpSum[warp] + incl - sum;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        hist[t * kPer + k] = run;
+        run += v[k];
+    }
+    if (t == 0) ctl[dstQueue] = ctl[srcQueue];
+}
+
+static __global__ void __launch_bounds__(256) k_octant_scatter(const float4 *__restrict__ srcO,
+    const float4 *__restrict__ srcD, const unsigned int *ctl, int queue,
+    const uint32_t *__restrict__ offsets, float4 *__restrict__ dstO, float4 *__restrict__ dstD)
+{
+    __shared__ uint32_t base[8], warpCount[8][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 8) base[threadIdx.x] = offsets[threadIdx.x * kSortBlocks + blockIdx.x];
+    uint32_t begin, end;
+    sort_chunk(ctl[queue], begin, end);
+    __syncthreads();
+    for (uint32_t t0 = begin; t0 < end; t0 += 256) {
+        const uint32_t i = t0 + threadIdx.x;
+        const bool valid = i < end;
+        float4 o = make_float4(0, 0, 0, 0), d = o;
+        uint32_t oct = 8u;
+        if (valid) {
+            o = srcO[i];
+            d = srcD[i];
+            oct = dir_octant(d);
+        }
+        uint32_t rank = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < 8; k++) {
+            uint32_t m = __ballot_sync(0xFFFFFFFFu, oct == k);
+            if (lane == 0) warpCount[k][warp] = __popc(m);
+            if (oct == k) rank = __popc(m & ((1u << lane) - 1u));
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0;
+            for (int w = 0; w < warp; w++) before += warpCount[oct][w];
+            const uint32_t dst = base[oct] + before + rank;
+            dstO[dst] = o;
+            dstD[dst] = d;
+        }
+        __syncthreads();
+        if (threadIdx.x < 8) {
+            uint32_t tot = 0;
+            for (int w = 0; w < 8; w++) tot += warpCount[threadIdx.x][w];
+            base[threadIdx.x] += tot;
+        }
+        __syncthreads();
+    }
+}
+
 static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuffers wb)
 {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;

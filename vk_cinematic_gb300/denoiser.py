@@ -162,8 +162,9 @@ class KPCNN:
         """Denoises `radiance` and lets the plain path tracer judge every
         tile x tile block with an independent render `plain_check` of the same
         spp (gbsp_dn_tile_fallback): blocks whose estimated relMSE exceeds
-        `bound` are served from the plain samples.  Returns (image,
-        per-tile estimates, per-tile fallback flags)."""
+        `bound` by more than two standard errors are served from the plain
+        samples.  Returns (image, per-tile estimates, per-tile fallback
+        flags)."""
         import torch
 
         den = self.denoise(radiance, aov)

@@ -69,6 +69,7 @@ FLAG_STAGE_TIMING = 1
 FLAG_AOV = 2
 FLAG_TRACE_PER_LANE = 4
 FLAG_TRACE_PER_WARP = 8
+FLAG_SORT_DIRECTIONS = 16
 ISECT_REFERENCE_MT = 0
 ISECT_WATERTIGHT = 1
 
