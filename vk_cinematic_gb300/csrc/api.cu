@@ -298,6 +298,7 @@ static void runtime_teardown(gbsp_runtime *rt)
     rt->frame.release();
     rt->aov.release();
     rt->pathAov.release();
+    rt->sortHist.release();
     cudaStreamSynchronize(rt->stream);
     if (rt->dStatus) cudaFree(rt->dStatus);
     if (rt->dCounters) cudaFree(rt->dCounters);
