@@ -222,6 +222,18 @@ def test_soup_closest_hit_small_matches_reference_bvh_walk(rt):
     assert np.all(obj[tri >= 0] == 0)
 
 
+def test_intersect_batch_paths_agree(rt):
+    """Batches below 65,536 rays run the per-warp query kernel, larger ones
+    the wavefront's per-lane kernel: both give the same bits per ray."""
+    s, _ = soup_world(12000, seed=7)
+    rays = scenes.soup_rays(65536, seed=8)
+    t_big, tri_big, obj_big = gpu_closest(rt, s, rays)
+    t_small, tri_small, obj_small = gpu_closest(rt, s, rays[:65535])
+    assert np.array_equal(bits(t_big[:65535]), bits(t_small))
+    assert np.array_equal(tri_big[:65535], tri_small)
+    assert np.array_equal(obj_big[:65535], obj_small)
+
+
 def test_soup_closest_hit_full_size_vs_brute_force(rt):
     """Config 2 at full size (1,048,576 triangles, 4,194,304 rays) on the
     GPU; a seeded subset of the rays is checked against brute force over

@@ -1,12 +1,17 @@
 // Batched closest-hit ray casting (config 2 and sp_RayIntersectScene batches).
 //
-// Persistent kernel: a grid sized to the SM count; every warp takes 32 rays
-// at a time from a global atomic counter until the batch is exhausted (the
-// counter only grows, so each warp loops at most count/32 times).  Rays are
+// Small batches: k_intersect, a persistent kernel whose warps take 32 rays at
+// a time from a global atomic counter until the batch is exhausted (the
+// counter only grows, so each warp loops at most count/32 times).  Large
+// batches of (typically incoherent) rays go through the wavefront's per-lane
+// closest-hit kernel instead, where a lane fetches its next ray as soon as
+// its current one is done: the rays are split into the queue layout, traced,
+// and the queue-ordered hits turned into the requested outputs.  Rays are
 // (origin, pad, direction, pad) float4 pairs, read with 128-bit loads.
 
 #include "gbsp_internal.h"
 #include "traverse.cuh"
+#include "wavefront.cuh"
 
 namespace gbsp {
 
@@ -77,11 +82,97 @@ __global__ void __launch_bounds__(128) k_intersect(SceneView sv, const float4 *_
     warp_add_counters(counters, cnt, rays_done, hits);
 }
 
+// Ray pairs -> queue layout (origin with path id 0, direction).
+__global__ void __launch_bounds__(256) k_split_rays(const float4 *__restrict__ rays, uint32_t count,
+    float4 *__restrict__ o, float4 *__restrict__ d)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float4 a = __ldg(rays + 2 * (size_t)i), b = __ldg(rays + 2 * (size_t)i + 1);
+    o[i] = make_float4(a.x, a.y, a.z, 0.0f);
+    d[i] = make_float4(b.x, b.y, b.z, 0.0f);
+}
+
+// Queue-ordered hits -> the per-ray outputs of k_intersect (same values).
+__global__ void __launch_bounds__(256) k_intersect_outputs(SceneView sv, const int4 *__restrict__ hitA,
+    const int *__restrict__ hitInst, uint32_t count, float *tOut, int32_t *triOut, int32_t *objOut,
+    float *attrOut, uint32_t *matOut)
+{
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    int4 hA = hitA[i];
+    RayHit h;
+    h.t = __int_as_float(hA.x);
+    h.u = __int_as_float(hA.y);
+    h.v = __int_as_float(hA.z);
+    h.prim = hA.w;
+    h.inst = hitInst[i];
+    bool hit = h.prim >= 0;
+    if (tOut) tOut[i] = hit ? h.t : -1.0f;
+    if (triOut) triOut[i] = hit ? (int32_t)__ldg(sv.triIds + h.prim) : -1;
+    const Instance *in = hit ? sv.instances + h.inst : nullptr;
+    if (objOut) objOut[i] = hit ? (int32_t)__ldg(&in->objectIndex) : -1;
+    if (attrOut) {
+        float *a = attrOut + 6 * (size_t)i;
+        if (hit) {
+            V3 n;
+            float ux, uy;
+            hit_surface(sv, h, n, ux, uy);
+            a[0] = h.t;
+            a[1] = n.x;
+            a[2] = n.y;
+            a[3] = n.z;
+            a[4] = ux;
+            a[5] = uy;
+        } else {
+            a[0] = -1.0f;
+            a[1] = a[2] = a[3] = a[4] = a[5] = 0.0f;
+        }
+    }
+    if (matOut) matOut[i] = hit ? __ldg(&in->materialId) : 0u;
+}
+
+// Batches from this size on take the per-lane path.
+constexpr uint32_t kPerLaneBatch = 1u << 16;
+
+static int launch_intersect_per_lane(cudaStream_t s, const SceneView &sv, uint32_t count,
+    const float4 *rays, float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut,
+    uint32_t *matOut, int smCount, unsigned long long *counters, uint32_t *dStatus)
+{
+    // one allocation: O, D, hits (16 B each per ray), instance ids, control block
+    const size_t n = count;
+    const size_t bytes = n * (16 + 16 + 16 + 4) + sizeof(unsigned int) * kCtlCount + 64;
+    unsigned char *tmp = nullptr;
+    GBSP_CUDA_TRY(cudaMallocAsync((void **)&tmp, bytes, s));
+    float4 *o = reinterpret_cast<float4 *>(tmp);
+    float4 *d = o + n;
+    int4 *hitA = reinterpret_cast<int4 *>(d + n);
+    int *hitInst = reinterpret_cast<int *>(hitA + n);
+    unsigned int *ctl = reinterpret_cast<unsigned int *>(
+        (reinterpret_cast<uintptr_t>(hitInst + n) + 63) & ~(uintptr_t)63);
+    OneScene one = {};
+    one.sv = sv;
+    const int blocks = (int)((n + 255) / 256);
+    k_split_rays<<<blocks, 256, 0, s>>>(rays, count, o, d);
+    k_reset_ctl<<<1, 32, 0, s>>>(ctl, count);
+    launch_trace_stage(true, sv.watertight != 0, smCount * 8, s, one, o, d, ctl + kCtlQueue0, hitA,
+        hitInst, ctl, counters, dStatus);
+    k_intersect_outputs<<<blocks, 256, 0, s>>>(sv, hitA, hitInst, count, tOut, triOut, objOut,
+        attrOut, matOut);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(tmp, s);
+    GBSP_CUDA_TRY(e);
+    return GBSP_OK;
+}
+
 int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const float4 *rays,
     float *tOut, int32_t *triOut, int32_t *objOut, float *attrOut, uint32_t *matOut,
     const Instance *, int smCount, unsigned long long *counters, uint32_t *dStatus)
 {
     if (!count) return GBSP_OK;
+    if (count >= kPerLaneBatch)
+        return launch_intersect_per_lane(s, sv, count, rays, tOut, triOut, objOut, attrOut, matOut,
+            smCount, counters, dStatus);
     // the work counter lives in the last counter slot's neighbour block
     unsigned int *work = reinterpret_cast<unsigned int *>(counters + GBSP_METRIC_COUNT);
     GBSP_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(unsigned int), s));
