@@ -56,7 +56,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gbsp", "reference"], default="gbsp")
     ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4", "config5",
-                                           "compute_pt", "cubemap"],
+                                           "compute_pt", "cubemap", "tc_rate"],
                     default="config3")
     ap.add_argument("--dn-scenes", type=int, default=125)
     ap.add_argument("--dn-crops", type=int, default=16)
@@ -908,6 +908,37 @@ def run_cubemap(args):
     return 0
 
 
+def run_tc_rate(args):
+    """Cycles per 128 x N x 16 BF16 tcgen05.mma on one SM, back to back from one
+    or two issuing threads: the shape-limited tensor rate that bounds the
+    denoiser's 48-channel convolutions.  Prints its own line."""
+    import ctypes
+
+    from vk_cinematic_gb300 import gbsp
+
+    L = gbsp.load()
+    out = (ctypes.c_double * 2)()
+    rows = []
+    for issuers, ns in ((1, (16, 32, 48, 64, 96, 128, 144, 256)), (2, (48, 128))):
+        for n in ns:
+            rc = L.gbsp_dn_tc_rate(n, 1024, issuers, out)
+            if rc:
+                raise RuntimeError(L.gbsp_last_error_string().decode())
+            cyc = [out[k] for k in range(issuers)]
+            rows.append({"n": n, "issuers": issuers, "cycles_per_mma": cyc,
+                         "mac_per_cycle": issuers * 128 * n * 16 / max(cyc)})
+    peak = max(r["mac_per_cycle"] for r in rows)
+    n48 = next(r for r in rows if r["n"] == 48 and r["issuers"] == 1)
+    line = {"metric": "tcgen05.mma MAC per cycle per SM, M = 128, K = 16, BF16 -> FP32",
+            "value": n48["mac_per_cycle"], "unit": "MAC/cycle (N = 48, one issuer)",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "bf16", "vs_baseline": None,
+            "data": "zeroed operands in shared memory (no-swizzle K-major), 1,024 MMAs",
+            "config": {"workload": "tc_rate: one CTA, back-to-back MMAs, clock64"},
+            "shape_limited_fraction_n48": n48["mac_per_cycle"] / peak, "rows": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     _OVERRIDES.update(width=args.width, height=args.height, spp=args.spp)
@@ -923,6 +954,8 @@ def main():
         return run_compute_pt(args)
     if args.workload == "cubemap":
         return run_cubemap(args)
+    if args.workload == "tc_rate":
+        return run_tc_rate(args)
     return run_gpu(args)
 
 

@@ -455,6 +455,11 @@ int gbsp_dn_conv3x3_forward_tc(void *stream, const uint16_t *in, uint32_t B, uin
 int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint32_t H,
     uint32_t W, uint32_t cin, const uint16_t *weights, const float *bias, const float *noisy,
     float *out);
+/* Diagnostic: clock cycles per 128 x n x 16 BF16 tcgen05.mma when `issuers`
+ * (1 or 2) threads of one CTA each issue `iters` of them back to back into
+ * their own tensor-memory accumulator (n = 16, 32, 48, 64, 96, 128, 144, 256);
+ * cyclesPerMma receives one value per issuer.  Synchronises the device. */
+int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, double *cyclesPerMma);
 /* Reads and clears the denoiser kernels' device status word (1 = a tensor-core
  * completion wait ran out); GBSP_ERR_DEVICE_STATUS when it was set. */
 int gbsp_dn_status(uint32_t *status);

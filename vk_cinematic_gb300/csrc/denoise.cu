@@ -153,52 +153,58 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // ---------------------------------------------------------------------------
 // conv3x3 on the 5th-generation tensor cores (tcgen05).
 //
-// GEMM: M = 128 pixels of one image row, N = COUT, K = 9 taps x CIN.  One
-// elected thread issues tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 ->
-// FP32) for every (tap, 16-channel slice): 9 * CIN / 16 instructions of
-// 128 x COUT x 16 per output row, accumulating in tensor memory.  Both
-// operands are read straight from shared memory through matrix descriptors,
-// so the 3x3 neighbourhood is never expanded: a tap is a 16-byte-granular
-// offset of the A descriptor into the staged input rows.
+// GEMM: M = 128 pixels of one image row, K = 9 taps x CIN, and two output
+// rows y, y + 1 side by side along N (accumulator columns [0, COUT) and
+// [COUT, 2 COUT)).  One elected thread issues tcgen05.mma.cta_group::1
+// .kind::f16 (BF16 x BF16 -> FP32) per (horizontal tap, 16-channel slice):
+// input rows y and y + 1 feed both output rows at once (N = 2 COUT, the
+// weights of the two tap rows stacked), input rows y - 1 and y + 2 one row
+// each (N = COUT).  An M = 128 MMA costs about the same up to N = 96, so
+// pairing rows cuts the MMAs per output row from 9 CIN / 16 to 6 CIN / 16.
+// Both operands are read straight from shared memory through matrix
+// descriptors, so the 3x3 neighbourhood is never expanded: a horizontal tap
+// is a 16-byte-granular offset of the A descriptor into a staged input row.
 //
 // Shared memory holds the operands in the canonical no-swizzle K-major
 // layout: 8 x 16-byte core matrices (8 rows of 8 BF16 channels), rows
-// contiguous.  Input rows: a ring of 4 slots of [CIN/8 channel groups][130
-// pixels][16 B] (a core matrix = 8 consecutive pixels of one channel group,
-// so a pixel shift moves the start by 16 B); weights: [9 taps][CIN/8 groups]
-// [COUT][16 B].  Descriptor strides: leading (K) = next channel group,
-// stride (M or N) = next 8 rows = 128 B.
+// contiguous.  Input rows: ring slots of [CIN/8 channel groups][130 pixels]
+// [16 B] (a core matrix = 8 consecutive pixels of one channel group, so a
+// pixel shift moves the start by 16 B); weights: [2 tap-row pairs][3 taps]
+// [CIN/8 groups][2 COUT][16 B].  Descriptor strides: leading (K) = next
+// channel group, stride (M or N) = next 8 rows = 128 B.
 //
 // One persistent CTA per SM walks vertical strips (one 128-pixel column
 // segment, a run of rows) with its warps specialised and coupled only by
 // mbarriers:
 //   * warps 1-3 (producers) stage input rows into a ring of kTcRing slots
-//     with cp.async, kTcInFlight rows in flight (the memory-level
-//     parallelism that hides DRAM latency); a row's slot is reused once the
-//     MMAs of the last output row that reads it have completed (rowEmpty,
-//     signalled by tcgen05.commit), and a staged row is published on
-//     rowFull after cp.async.wait_group + fence.proxy.async;
-//   * lane 0 of warp 0 issues, per output row y, the 9 taps x CIN/16 MMAs
-//     reading rows y-1..y+1 into one of kTcAccSlots TMEM accumulators, then
-//     commits to that accumulator's accFull and to the rowEmpty of row y-1;
-//   * warps 4-11 are two epilogue groups taking alternate output rows (warp
-//     w owns TMEM lanes 32 (w % 4) .. + 31 = pixels): wait on accFull, read
+//     with cp.async, as many rows in flight as the ring allows (the
+//     memory-level parallelism that hides DRAM latency); a row's slot is
+//     reused once the MMAs of the last row pair that reads it have completed
+//     (rowEmpty, signalled by tcgen05.commit), and each producer thread's
+//     copies arrive on the row's rowFull by themselves when they land
+//     (cp.async.mbarrier.arrive.noinc); the MMA thread fences the async
+//     proxy after its wait;
+//   * lane 0 of warp 0 issues, per row pair (y, y + 1), the 12 CIN/16 MMAs
+//     reading rows y-1..y+2 into one of kTcAccSlots TMEM accumulators, then
+//     commits to that accumulator's accFull and to the rowEmpty of rows y-1
+//     and y;
+//   * warps 4-11 are two epilogue groups taking alternate row pairs (warp w
+//     owns TMEM lanes 32 (w % 4) .. + 31 = pixels): wait on accFull, read
 //     the accumulator with tcgen05.ld, release it on accEmpty and apply bias
 //     / ReLU / BF16 packing (or the fused filter) while the tensor core
-//     already works on the next rows.
+//     already works on the next pairs.
 // Every wait is bounded; a timeout raises a shared abort flag that ends the
 // other roles' waits, and sets g_dnStatus.
 // ---------------------------------------------------------------------------
 constexpr int kTcTileP = 128;
 // One CTA per SM: warp 0 issues the MMAs, warps 1-3 produce, warps 4-11 are
-// two epilogue groups that take alternate output rows.
+// two epilogue groups that take alternate row pairs.
 constexpr int kTcThreads = 384;
 constexpr int kTcProducers = 96;
 constexpr int kTcEpiGroups = 2;
 constexpr int kTcAccSlots = 4;  // accumulator a is drained by epilogue group a % 2
 constexpr int kTcSpx = kTcTileP + 2;
-constexpr int kTcRing = 14;     // input row slots
-constexpr int kTcInFlight = 10; // rows staged but not yet published (kTcRing >= kTcInFlight + 3)
+constexpr int kTcRing = 13;  // input row slots: 4 read by a row pair's MMAs, the rest in flight
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 __device__ uint32_t g_dnStatus;
@@ -307,6 +313,30 @@ __device__ __forceinline__ uint64_t tap_pixel(uint64_t p, int x, int y, int W, i
     return p - (uint64_t)x - (uint64_t)y * W + (uint64_t)gy * W + gx;
 }
 
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+
+// One tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 -> FP32 in tensor
+// memory); accumulate = 0 overwrites the accumulator.
+__device__ __forceinline__ void tc_mma(uint32_t dTmem, uint64_t aDesc, uint64_t bDesc,
+    uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :: "r"(dTmem), "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate));
+}
+
 // Bias / ReLU / BF16 packing of one pixel's COUT accumulators and the store.
 template <int COUT, int EPI>
 __device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
@@ -362,14 +392,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF,
     const float4 *__restrict__ noisy, float4 *__restrict__ outFilt)
 {
-    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && COUT <= 256, "tcgen05 tile shape");
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && 2 * COUT <= 128, "tcgen05 tile shape");
     constexpr int KG = CIN / 8;  // 16-byte channel groups
-    constexpr int ACC_COLS = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : (COUT <= 128 ? 128 : 256));
+    constexpr int ACC_COLS = 128;  // one row pair: 2 COUT columns
     constexpr int TMEM_COLS = kTcAccSlots * ACC_COLS;
     static_assert(TMEM_COLS <= 512, "tensor memory");
     extern __shared__ __align__(128) unsigned char smemRaw[];
-    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [9][KG][COUT]
-    uint4 *sRing = sW + 9 * KG * COUT;               // [kTcRing][KG][kTcSpx]
+    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [2][3][KG][2 COUT]
+    uint4 *sRing = sW + 12 * KG * COUT;              // [kTcRing][KG][kTcSpx]
     __shared__ __align__(8) uint64_t rowFull[kTcRing], rowEmpty[kTcRing];
     __shared__ __align__(8) uint64_t accFull[kTcAccSlots], accEmpty[kTcAccSlots], drain;
     __shared__ uint32_t tmemBase;
@@ -379,10 +409,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
     if (tid < COUT) sBias[tid] = EPI != kEpiF32 ? bias[tid] : 0.0f;
 
-    // weights -> canonical layout: (tap, kg, co) holds w[tap][co][8 kg .. 8 kg + 7]
-    for (int i = tid; i < 9 * KG * COUT; i += kTcThreads) {
-        int co = i % COUT, kg = (i / COUT) % KG, tap = i / (COUT * KG);
-        sW[i] = reinterpret_cast<const uint4 *>(w)[((size_t)tap * COUT + co) * KG + kg];
+    // weights -> pair-stacked canonical layout: block (pt, tx, kg) holds 2 COUT rows of
+    // 16 B, rows [0, COUT) tap row ty = pt + 1 and rows [COUT, 2 COUT) tap row ty = pt,
+    // each row w[3 ty + tx][co][8 kg .. 8 kg + 7]
+    for (int i = tid; i < 12 * KG * COUT; i += kTcThreads) {
+        const int r = i % (2 * COUT), blk = i / (2 * COUT);
+        const int kg = blk % KG, tx = (blk / KG) % 3, pt = blk / (3 * KG);
+        const int ty = r < COUT ? pt + 1 : pt, co = r % COUT;
+        sW[i] = reinterpret_cast<const uint4 *>(w)[((size_t)(3 * ty + tx) * COUT + co) * KG + kg];
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -413,69 +447,79 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     const int segs = (W + kTcTileP - 1) / kTcTileP;
     const int stripsPerCol = (H + rowsPerStrip - 1) / rowsPerStrip;
     const int numStrips = B * segs * stripsPerCol;
-    // strip geometry: segment origin x0, rows [y0, y1), image b
+    // strip geometry: segment origin x0, output rows [y0, y1) in P row pairs (the
+    // second row of the last pair lies past the image when H - y0 is odd); staged
+    // input rows y0 - 1 .. y0 + 2 P
 #define GBSP_STRIP_GEOMETRY(strip)                                                       \
     const int sy = (strip) % stripsPerCol, seg = ((strip) / stripsPerCol) % segs;        \
     const int b = (strip) / (stripsPerCol * segs);                                        \
     const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;                                \
     const int y1 = min(H, y0 + rowsPerStrip);                                             \
+    const int P = (y1 - y0 + 1) / 2;                                                      \
     (void)b;                                                                              \
-    (void)x0
+    (void)x0;                                                                             \
+    (void)y1
 
     if (warp == 0) {
         if (lane == 0) {
-            // ---- MMA issue: rows of a strip have sequence numbers qBase + (gy - y0 + 1)
-            const uint32_t idesc = instr_desc_bf16<kTcTileP, COUT>();
+            // ---- MMA issue.  Input row gy of a strip has sequence number qBase + gy - y0 + 1.
+            // Pair (y, y + 1) accumulates rows y and y + 1 side by side (columns [0, COUT)
+            // and [COUT, 2 COUT)): input rows y and y + 1 feed both with one N = 2 COUT MMA
+            // each, rows y - 1 and y + 2 feed one row each with an N = COUT MMA.
+            const uint32_t idesc2 = instr_desc_bf16<kTcTileP, 2 * COUT>();
+            const uint32_t idesc1 = instr_desc_bf16<kTcTileP, COUT>();
             const uint64_t aDesc0 = smem_desc(ringAddr, kTcSpx * 16, 128);
-            const uint64_t bDesc0 = smem_desc(smem_u32(sW), COUT * 16, 128);
-            uint32_t qBase = 0, outCount = 0;
+            const uint64_t bDesc0 = smem_desc(smem_u32(sW), 2 * COUT * 16, 128);
+            uint32_t qBase = 0, pairCount = 0;
             bool ok = true;
             for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
                 GBSP_STRIP_GEOMETRY(strip);
-                for (uint32_t q = qBase; q < qBase + 2 && ok; q++)
-                    ok = tc_wait(smem_u32(&rowFull[q % kTcRing]), (q / kTcRing) & 1u, &abortFlag);
-                for (int y = y0; y < y1 && ok; y++) {
-                    const uint32_t qTop = qBase + (uint32_t)(y - y0) + 2u;  // row y + 1
-                    if (!tc_wait(smem_u32(&rowFull[qTop % kTcRing]), (qTop / kTcRing) & 1u,
-                            &abortFlag)) {
-                        ok = false;
-                        break;
-                    }
+                for (int p = 0; p < P && ok; p++) {
+                    const uint32_t q0 = qBase + 2u * (uint32_t)p;  // input row y - 1
+                    for (uint32_t q = q0; q < q0 + 4u && ok; q++)
+                        ok = tc_wait(smem_u32(&rowFull[q % kTcRing]), (q / kTcRing) & 1u,
+                            &abortFlag);
+                    if (!ok) break;
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const uint32_t acc = outCount % kTcAccSlots, use = outCount / kTcAccSlots;
+                    const uint32_t acc = pairCount % kTcAccSlots, use = pairCount / kTcAccSlots;
                     if (use > 0 && !tc_wait(smem_u32(&accEmpty[acc]), (use - 1u) & 1u, &abortFlag)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const uint32_t dAcc = tmem + acc * (uint32_t)ACC_COLS;
+                    const uint32_t sM = q0 % kTcRing, s0 = (q0 + 1u) % kTcRing;
+                    const uint32_t s1 = (q0 + 2u) % kTcRing, s2 = (q0 + 3u) % kTcRing;
 #pragma unroll
-                    for (int tap = 0; tap < 9; tap++) {
-                        const int ty = tap / 3, tx = tap % 3;
-                        const uint32_t slot = (qTop - 2u + (uint32_t)ty) % kTcRing;
-                        const uint64_t aRow = aDesc0 + (uint64_t)(slot * KG * kTcSpx + tx);
+                    for (int tx = 0; tx < 3; tx++) {
 #pragma unroll
                         for (int kc = 0; kc < CIN / 16; kc++) {
                             // 16-byte units: slot row, channel group 2 kc, pixel tx
-                            uint64_t aDesc = aRow + (uint64_t)(2 * kc * kTcSpx);
-                            uint64_t bDesc = bDesc0 + (uint64_t)((tap * KG + 2 * kc) * COUT);
-                            uint32_t accumulate = (tap | kc) ? 1u : 0u;
-                            asm volatile(
-                                "{\n\t.reg .pred p;\n\t"
-                                "setp.ne.b32 p, %4, 0;\n\t"
-                                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
-                                :: "r"(dAcc), "l"(aDesc), "l"(bDesc), "r"(idesc),
-                                   "r"(accumulate));
+                            const uint64_t aOff = (uint64_t)(2 * kc * kTcSpx + tx);
+                            const uint64_t b0 = bDesc0 + (uint64_t)(((0 * 3 + tx) * KG + 2 * kc) * 2 * COUT);
+                            const uint64_t b1 = bDesc0 + (uint64_t)(((1 * 3 + tx) * KG + 2 * kc) * 2 * COUT);
+                            const uint32_t first = (tx | kc) ? 1u : 0u;
+                            // input row y: [ty 1 | ty 0] -> both rows (initialises the pair)
+                            tc_mma(dAcc, aDesc0 + (uint64_t)(s0 * KG * kTcSpx) + aOff, b0, idesc2, first);
+                            // input row y + 1: [ty 2 | ty 1] -> both rows
+                            tc_mma(dAcc, aDesc0 + (uint64_t)(s1 * KG * kTcSpx) + aOff, b1, idesc2, 1u);
+                            // input row y - 1: ty 0 -> row y
+                            tc_mma(dAcc, aDesc0 + (uint64_t)(sM * KG * kTcSpx) + aOff,
+                                b0 + (uint64_t)COUT, idesc1, 1u);
+                            // input row y + 2: ty 2 -> row y + 1
+                            tc_mma(dAcc + (uint32_t)COUT, aDesc0 + (uint64_t)(s2 * KG * kTcSpx) + aOff,
+                                b1, idesc1, 1u);
                         }
                     }
                     tc_commit(smem_u32(&accFull[acc]));
-                    // row y - 1 has no later reader
-                    tc_commit(smem_u32(&rowEmpty[(qTop - 2u) % kTcRing]));
-                    outCount++;
+                    // input rows y - 1 and y have no later reader
+                    tc_commit(smem_u32(&rowEmpty[sM]));
+                    tc_commit(smem_u32(&rowEmpty[s0]));
+                    pairCount++;
                 }
                 if (!ok) break;
-                // rows y1 - 1 and y1 are free once the strip's last MMAs finish
-                const uint32_t qLast = qBase + (uint32_t)(y1 - y0) + 1u;
+                // the strip's last two input rows are free once its last MMAs finish
+                const uint32_t qLast = qBase + 2u * (uint32_t)P + 1u;
                 tc_commit(smem_u32(&rowEmpty[(qLast - 1u) % kTcRing]));
                 tc_commit(smem_u32(&rowEmpty[qLast % kTcRing]));
                 qBase = qLast + 1u;
@@ -489,44 +533,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
         }
         __syncwarp();
     } else if (warp < 4) {
-        // ---- producers: rows y0 - 1 .. y1 of every strip, two in flight
+        // ---- producers: input rows y0 - 1 .. y0 + 2 P of every strip
         const int ptid = tid - 32;
         uint32_t q = 0;
         bool ok = true;
         for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
             GBSP_STRIP_GEOMETRY(strip);
-            for (int gy = y0 - 1; gy <= y1; gy++, q++) {
+            for (int gy = y0 - 1; gy <= y0 + 2 * P; gy++, q++) {
                 const uint32_t slot = q % kTcRing, use = q / kTcRing;
                 if (use > 0 && !tc_wait(smem_u32(&rowEmpty[slot]), (use - 1u) & 1u, &abortFlag)) {
                     ok = false;
                     break;
                 }
                 stage_row<KG, kTcProducers>(ringAddr, (int)slot, in4, b, gy, H, W, x0, ptid);
-                if (q >= (uint32_t)kTcInFlight) {
-                    // every row but the kTcInFlight newest has landed: publish row q - kTcInFlight
-                    static_assert(kTcInFlight == 10, "wait_group immediate");
-                    asm volatile("cp.async.wait_group 10;" ::: "memory");
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_arrive(smem_u32(&rowFull[(q - kTcInFlight) % kTcRing]));
-                }
+                // this thread's arrival on rowFull fires when its copies have landed
+                asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];"
+                             :: "r"(smem_u32(&rowFull[slot])) : "memory");
             }
         }
         asm volatile("cp.async.wait_group 0;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        if (ok)
-            for (uint32_t r = q > (uint32_t)kTcInFlight ? q - kTcInFlight : 0u; r < q; r++)
-                mbar_arrive(smem_u32(&rowFull[r % kTcRing]));
     } else {
-        // ---- epilogue: group g = (warp - 4) / 4 takes the output rows with
-        // outCount % 2 == g; warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels)
+        // ---- epilogue: group g = (warp - 4) / 4 takes the row pairs with pairCount % 2 == g;
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels)
         const int quarter = warp & 3, group = (warp - 4) >> 2;
-        uint32_t outCount = 0;
+        uint32_t pairCount = 0;
         bool ok = true;
         for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
             GBSP_STRIP_GEOMETRY(strip);
-            for (int y = y0; y < y1; y++, outCount++) {
-                if ((int)(outCount % kTcEpiGroups) != group) continue;
-                const uint32_t acc = outCount % kTcAccSlots, use = outCount / kTcAccSlots;
+            for (int p = 0; p < P; p++, pairCount++) {
+                if ((int)(pairCount % kTcEpiGroups) != group) continue;
+                const uint32_t acc = pairCount % kTcAccSlots, use = pairCount / kTcAccSlots;
                 ok = tc_wait(smem_u32(&accFull[acc]), use & 1u, &abortFlag);
                 __syncwarp();
                 if (!__all_sync(0xFFFFFFFFu, ok)) {
@@ -534,30 +570,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                uint32_t r[COUT];
+                uint32_t r0[COUT], r1[COUT];
+                const uint32_t cols = tmem + ((uint32_t)(quarter * 32) << 16) + acc * (uint32_t)ACC_COLS;
 #pragma unroll
                 for (int c = 0; c < COUT; c += 16) {
-                    uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) +
-                        acc * (uint32_t)ACC_COLS + (uint32_t)c;
-                    asm volatile(
-                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-                        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                        : "=r"(r[c + 0]), "=r"(r[c + 1]), "=r"(r[c + 2]), "=r"(r[c + 3]),
-                          "=r"(r[c + 4]), "=r"(r[c + 5]), "=r"(r[c + 6]), "=r"(r[c + 7]),
-                          "=r"(r[c + 8]), "=r"(r[c + 9]), "=r"(r[c + 10]), "=r"(r[c + 11]),
-                          "=r"(r[c + 12]), "=r"(r[c + 13]), "=r"(r[c + 14]), "=r"(r[c + 15])
-                        : "r"(taddr));
+                    tmem_ld16(cols + (uint32_t)c, *reinterpret_cast<uint32_t(*)[16]>(r0 + c));
+                    tmem_ld16(cols + (uint32_t)(COUT + c), *reinterpret_cast<uint32_t(*)[16]>(r1 + c));
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;");
                 mbar_arrive(smem_u32(&accEmpty[acc]));
                 const int x = x0 + quarter * 32 + lane;
+                const int y = y0 + 2 * p;
                 if (x < W) {
-                    const size_t p = (size_t)(b * H + y) * W + x;
-                    if constexpr (EPI == kEpiFilter)
-                        conv_filter_store<COUT>(r, p, x, y, W, H, sBias, noisy, outFilt);
-                    else
-                        conv_store<COUT, EPI>(r, p, sBias, outB, outF);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        if (y + h >= y1) break;
+                        const size_t px = (size_t)(b * H + y + h) * W + x;
+                        if constexpr (EPI == kEpiFilter)
+                            conv_filter_store<COUT>(h ? r1 : r0, px, x, y + h, W, H, sBias, noisy,
+                                outFilt);
+                        else
+                            conv_store<COUT, EPI>(h ? r1 : r0, px, sBias, outB, outF);
+                    }
                 }
             }
         }
@@ -572,12 +607,66 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
                      :: "r"(tmem), "r"(TMEM_COLS));
 }
 
+// Rate probe for the MMA shape the convolutions use: one CTA, `issuers`
+// threads (lane 0 of warps 0..issuers-1) each issue `iters` back-to-back
+// 128 x N x 16 BF16 MMAs from zeroed shared memory into their own TMEM
+// accumulator, then wait for completion.  cycles[k] = clock64 cycles of
+// issuer k from its first issue to the completion of its last MMA.
+template <int N>
+__global__ void __launch_bounds__(64) k_tc_rate(int iters, int issuers, unsigned long long *cycles)
+{
+    __shared__ __align__(1024) uint4 sA[2 * 128];
+    __shared__ __align__(1024) uint4 sB[2 * 256];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tmemBase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < 2 * 128; i += 64) sA[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < 2 * 256; i += 64) sB[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmemBase)), "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; i++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bar[i])));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmemBase;
+    if (lane == 0 && warp < issuers) {
+        const uint32_t idesc = instr_desc_bf16<128, N>();
+        const uint64_t a = smem_desc(smem_u32(sA), 128 * 16, 128);
+        const uint64_t b = smem_desc(smem_u32(sB), N * 16, 128);
+        const uint32_t d = tmem + (uint32_t)(256 * warp);
+        const long long t0 = clock64();
+        for (int i = 0; i < iters; i++) {
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                :: "r"(d), "l"(a), "l"(b), "r"(idesc), "r"(i ? 1u : 0u));
+        }
+        tc_commit(smem_u32(&bar[warp]));
+        volatile uint32_t never = 0u;
+        const bool done = tc_wait(smem_u32(&bar[warp]), 0u, &never);
+        cycles[warp] = done ? (unsigned long long)(clock64() - t0) : 0ull;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(512));
+}
+
 template <int CIN, int COUT, int EPI>
 int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, int W, const void *w,
     const float *bias, void *outB, float *outF, const float4 *noisy = nullptr,
     float4 *outFilt = nullptr)
 {
-    size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
+    size_t smem = (size_t)(12 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int ctas = smCount;  // one CTA per SM (the row ring takes most of shared memory)
@@ -586,6 +675,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     // the last round is nearly full), at least 4 rows
     int rows = (int)(((int64_t)cols * H + 6 * ctas - 1) / (6 * ctas));
     rows = rows < 4 ? 4 : (rows > H ? H : rows);
+    rows += rows & 1;  // strips of whole row pairs (only the image's last pair may be half)
     int strips = cols * ((H + rows - 1) / rows);
     int grid = strips < ctas ? strips : ctas;
     kern<<<grid, kTcThreads, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
@@ -1083,6 +1173,35 @@ int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint
     return launch_conv_tc<48, 32, kEpiFilter>(s, sm_count(), in, (int)B, (int)H, (int)W, weights,
         bias, nullptr, nullptr, reinterpret_cast<const float4 *>(noisy),
         reinterpret_cast<float4 *>(out));
+}
+
+int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, double *cyclesPerMma)
+{
+    if (!cyclesPerMma || !iters || issuers < 1 || issuers > 2)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad MMA rate probe args");
+    unsigned long long *d = nullptr;
+    GBSP_CUDA_TRY(cudaMalloc((void **)&d, 2 * sizeof(unsigned long long)));
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    switch (n) {
+    case 16: k_tc_rate<16><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 32: k_tc_rate<32><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 48: k_tc_rate<48><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 64: k_tc_rate<64><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 96: k_tc_rate<96><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 128: k_tc_rate<128><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 144: k_tc_rate<144><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 256: k_tc_rate<256><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    default:
+        cudaFree(d);
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "MMA rate probe: N = %u not instantiated", n);
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned long long h[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    GBSP_CUDA_TRY(e);
+    for (uint32_t k = 0; k < issuers; k++) cyclesPerMma[k] = (double)h[k] / (double)iters;
+    return h[0] ? GBSP_OK : set_error(GBSP_ERR_DEVICE_STATUS, "MMA rate probe timed out");
 }
 
 int gbsp_dn_status(uint32_t *status)

@@ -51,6 +51,7 @@ EXPORTS = [
     "gbsp_frame_copy_region", "gbsp_dn_features", "gbsp_dn_conv3x3_forward",
     "gbsp_dn_flip_transpose", "gbsp_dn_relu_backward", "gbsp_dn_conv3x3_weight_grad",
     "gbsp_dn_conv3x3_weight_grad_tc", "gbsp_dn_conv3x3_filter_tc",
+    "gbsp_dn_tc_rate",
     "gbsp_dn_filter", "gbsp_dn_relmse_backward", "gbsp_dn_adam", "gbsp_tonemap",
     "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
     "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
