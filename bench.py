@@ -919,14 +919,16 @@ def run_tc_rate(args):
     L = gbsp.load()
     out = (ctypes.c_double * 2)()
     rows = []
-    for issuers, ns in ((1, (16, 32, 48, 64, 96, 128, 144, 256)), (2, (48, 128))):
-        for n in ns:
-            rc = L.gbsp_dn_tc_rate(n, 1024, issuers, out)
-            if rc:
-                raise RuntimeError(L.gbsp_last_error_string().decode())
-            cyc = [out[k] for k in range(issuers)]
-            rows.append({"n": n, "issuers": issuers, "cycles_per_mma": cyc,
-                         "mac_per_cycle": issuers * 128 * n * 16 / max(cyc)})
+    cases = [(1, n, 0) for n in (16, 32, 48, 64, 96, 128, 144, 256)]
+    cases += [(2, 48, 0), (2, 128, 0)]
+    cases += [(1, n, off) for n in (48, 96) for off in (1, 2, 8)]
+    for issuers, n, off in cases:
+        rc = L.gbsp_dn_tc_rate(n, 1024, issuers, off, out)
+        if rc:
+            raise RuntimeError(L.gbsp_last_error_string().decode())
+        cyc = [out[k] for k in range(issuers)]
+        rows.append({"n": n, "issuers": issuers, "a_offset_bytes": 16 * off,
+                     "cycles_per_mma": cyc, "mac_per_cycle": issuers * 128 * n * 16 / max(cyc)})
     peak = max(r["mac_per_cycle"] for r in rows)
     n48 = next(r for r in rows if r["n"] == 48 and r["issuers"] == 1)
     line = {"metric": "tcgen05.mma MAC per cycle per SM, M = 128, K = 16, BF16 -> FP32",

@@ -458,8 +458,10 @@ int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint
 /* Diagnostic: clock cycles per 128 x n x 16 BF16 tcgen05.mma when `issuers`
  * (1 or 2) threads of one CTA each issue `iters` of them back to back into
  * their own tensor-memory accumulator (n = 16, 32, 48, 64, 96, 128, 144, 256);
+ * the A operand starts aOffset16 (<= 64) 16-byte units past a 1 KB boundary.
  * cyclesPerMma receives one value per issuer.  Synchronises the device. */
-int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, double *cyclesPerMma);
+int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, uint32_t aOffset16,
+    double *cyclesPerMma);
 /* Reads and clears the denoiser kernels' device status word (1 = a tensor-core
  * completion wait ran out); GBSP_ERR_DEVICE_STATUS when it was set. */
 int gbsp_dn_status(uint32_t *status);

@@ -610,17 +610,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
 // Rate probe for the MMA shape the convolutions use: one CTA, `issuers`
 // threads (lane 0 of warps 0..issuers-1) each issue `iters` back-to-back
 // 128 x N x 16 BF16 MMAs from zeroed shared memory into their own TMEM
-// accumulator, then wait for completion.  cycles[k] = clock64 cycles of
-// issuer k from its first issue to the completion of its last MMA.
+// accumulator, then wait for completion.  The A operand starts aOff16 16-byte
+// units past a 1,024-byte boundary (a pixel-shifted view of a staged row).
+// cycles[k] = clock64 cycles of issuer k from its first issue to the
+// completion of its last MMA.
 template <int N>
-__global__ void __launch_bounds__(64) k_tc_rate(int iters, int issuers, unsigned long long *cycles)
+__global__ void __launch_bounds__(64) k_tc_rate(int iters, int issuers, int aOff16,
+    unsigned long long *cycles)
 {
-    __shared__ __align__(1024) uint4 sA[2 * 128];
+    __shared__ __align__(1024) uint4 sA[2 * 128 + 64];
     __shared__ __align__(1024) uint4 sB[2 * 256];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tmemBase;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int i = tid; i < 2 * 128; i += 64) sA[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < 2 * 128 + 64; i += 64) sA[i] = make_uint4(0, 0, 0, 0);
     for (int i = tid; i < 2 * 256; i += 64) sB[i] = make_uint4(0, 0, 0, 0);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -639,7 +642,7 @@ __global__ void __launch_bounds__(64) k_tc_rate(int iters, int issuers, unsigned
     const uint32_t tmem = tmemBase;
     if (lane == 0 && warp < issuers) {
         const uint32_t idesc = instr_desc_bf16<128, N>();
-        const uint64_t a = smem_desc(smem_u32(sA), 128 * 16, 128);
+        const uint64_t a = smem_desc(smem_u32(sA + aOff16), 128 * 16, 128);
         const uint64_t b = smem_desc(smem_u32(sB), N * 16, 128);
         const uint32_t d = tmem + (uint32_t)(256 * warp);
         const long long t0 = clock64();
@@ -1175,22 +1178,23 @@ int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint
         reinterpret_cast<float4 *>(out));
 }
 
-int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, double *cyclesPerMma)
+int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, uint32_t aOffset16,
+    double *cyclesPerMma)
 {
-    if (!cyclesPerMma || !iters || issuers < 1 || issuers > 2)
+    if (!cyclesPerMma || !iters || issuers < 1 || issuers > 2 || aOffset16 > 64)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad MMA rate probe args");
     unsigned long long *d = nullptr;
     GBSP_CUDA_TRY(cudaMalloc((void **)&d, 2 * sizeof(unsigned long long)));
     cudaMemset(d, 0, 2 * sizeof(unsigned long long));
     switch (n) {
-    case 16: k_tc_rate<16><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 32: k_tc_rate<32><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 48: k_tc_rate<48><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 64: k_tc_rate<64><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 96: k_tc_rate<96><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 128: k_tc_rate<128><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 144: k_tc_rate<144><<<1, 64>>>((int)iters, (int)issuers, d); break;
-    case 256: k_tc_rate<256><<<1, 64>>>((int)iters, (int)issuers, d); break;
+    case 16: k_tc_rate<16><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 32: k_tc_rate<32><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 48: k_tc_rate<48><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 64: k_tc_rate<64><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 96: k_tc_rate<96><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 128: k_tc_rate<128><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 144: k_tc_rate<144><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
+    case 256: k_tc_rate<256><<<1, 64>>>((int)iters, (int)issuers, (int)aOffset16, d); break;
     default:
         cudaFree(d);
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "MMA rate probe: N = %u not instantiated", n);
