@@ -204,7 +204,8 @@ constexpr int kTcProducers = 96;
 constexpr int kTcEpiGroups = 2;
 constexpr int kTcAccSlots = 4;  // accumulator a is drained by epilogue group a % 2
 constexpr int kTcSpx = kTcTileP + 2;
-constexpr int kTcRing = 13;  // input row slots: 4 read by a row pair's MMAs, the rest in flight
+constexpr int kTcGroupRows = 4;  // output rows per accumulator
+constexpr int kTcRing = 14;  // input row slots: 6 read by a row group's MMAs, the rest in flight
 constexpr uint32_t kTcWaitLimit = 1u << 26;
 
 __device__ uint32_t g_dnStatus;
@@ -392,16 +393,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF,
     const float4 *__restrict__ noisy, float4 *__restrict__ outFilt)
 {
-    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && 2 * COUT <= 128, "tcgen05 tile shape");
+    constexpr int G = kTcGroupRows;
+    static_assert(CIN % 16 == 0 && COUT % 16 == 0 && 3 * COUT <= 256, "tcgen05 tile shape");
     constexpr int KG = CIN / 8;  // 16-byte channel groups
-    constexpr int ACC_COLS = 128;  // one row pair: 2 COUT columns
-    constexpr int TMEM_COLS = kTcAccSlots * ACC_COLS;
-    static_assert(TMEM_COLS <= 512, "tensor memory");
+    constexpr int ACC_COLS = G * COUT <= 128 ? 128 : 256;  // G output rows side by side
+    static_assert(G * COUT <= ACC_COLS, "accumulator");
+    // an even number of accumulators: accumulator a is always drained by epilogue group a % 2
+    constexpr int SLOTS = 512 / ACC_COLS >= kTcAccSlots ? kTcAccSlots : 512 / ACC_COLS;
+    static_assert(SLOTS % kTcEpiGroups == 0, "accumulator slots");
+    constexpr int TMEM_COLS = 512;
     extern __shared__ __align__(128) unsigned char smemRaw[];
-    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [2][3][KG][2 COUT]
-    uint4 *sRing = sW + 12 * KG * COUT;              // [kTcRing][KG][kTcSpx]
+    uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [3][KG][3 COUT]
+    uint4 *sRing = sW + 9 * KG * COUT;               // [kTcRing][KG][kTcSpx]
     __shared__ __align__(8) uint64_t rowFull[kTcRing], rowEmpty[kTcRing];
-    __shared__ __align__(8) uint64_t accFull[kTcAccSlots], accEmpty[kTcAccSlots], drain;
+    __shared__ __align__(8) uint64_t accFull[SLOTS], accEmpty[SLOTS], drain;
     __shared__ uint32_t tmemBase;
     __shared__ volatile uint32_t abortFlag;
     __shared__ __align__(16) float sBias[COUT];
@@ -409,13 +414,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
     if (tid < COUT) sBias[tid] = EPI != kEpiF32 ? bias[tid] : 0.0f;
 
-    // weights -> pair-stacked canonical layout: block (pt, tx, kg) holds 2 COUT rows of
-    // 16 B, rows [0, COUT) tap row ty = pt + 1 and rows [COUT, 2 COUT) tap row ty = pt,
-    // each row w[3 ty + tx][co][8 kg .. 8 kg + 7]
-    for (int i = tid; i < 12 * KG * COUT; i += kTcThreads) {
-        const int r = i % (2 * COUT), blk = i / (2 * COUT);
-        const int kg = blk % KG, tx = (blk / KG) % 3, pt = blk / (3 * KG);
-        const int ty = r < COUT ? pt + 1 : pt, co = r % COUT;
+    // weights -> stacked canonical layout: block (tx, kg) holds 3 COUT rows of 16 B, the
+    // tap rows ty = 2, 1, 0 one after the other, each row w[3 ty + tx][co][8 kg .. 8 kg + 7]
+    for (int i = tid; i < 9 * KG * COUT; i += kTcThreads) {
+        const int r = i % (3 * COUT), blk = i / (3 * COUT);
+        const int kg = blk % KG, tx = blk / KG;
+        const int ty = 2 - r / COUT, co = r % COUT;
         sW[i] = reinterpret_cast<const uint4 *>(w)[((size_t)(3 * ty + tx) * COUT + co) * KG + kg];
     }
     if (warp == 0) {
@@ -429,7 +433,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
                          :: "r"(smem_u32(&rowFull[i])), "r"(kTcProducers));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&rowEmpty[i])));
         }
-        for (int i = 0; i < kTcAccSlots; i++) {
+        for (int i = 0; i < SLOTS; i++) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&accFull[i])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" :: "r"(smem_u32(&accEmpty[i])));
         }
@@ -447,15 +451,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     const int segs = (W + kTcTileP - 1) / kTcTileP;
     const int stripsPerCol = (H + rowsPerStrip - 1) / rowsPerStrip;
     const int numStrips = B * segs * stripsPerCol;
-    // strip geometry: segment origin x0, output rows [y0, y1) in P row pairs (the
-    // second row of the last pair lies past the image when H - y0 is odd); staged
-    // input rows y0 - 1 .. y0 + 2 P
+    // strip geometry: segment origin x0, output rows [y0, y1) in P groups of G rows
+    // (the last group may reach past the image); staged input rows y0 - 1 .. y0 + G P
 #define GBSP_STRIP_GEOMETRY(strip)                                                       \
     const int sy = (strip) % stripsPerCol, seg = ((strip) / stripsPerCol) % segs;        \
     const int b = (strip) / (stripsPerCol * segs);                                        \
     const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;                                \
     const int y1 = min(H, y0 + rowsPerStrip);                                             \
-    const int P = (y1 - y0 + 1) / 2;                                                      \
+    const int P = (y1 - y0 + G - 1) / G;                                                  \
     (void)b;                                                                              \
     (void)x0;                                                                             \
     (void)y1
@@ -463,63 +466,68 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     if (warp == 0) {
         if (lane == 0) {
             // ---- MMA issue.  Input row gy of a strip has sequence number qBase + gy - y0 + 1.
-            // Pair (y, y + 1) accumulates rows y and y + 1 side by side (columns [0, COUT)
-            // and [COUT, 2 COUT)): input rows y and y + 1 feed both with one N = 2 COUT MMA
-            // each, rows y - 1 and y + 2 feed one row each with an N = COUT MMA.
-            const uint32_t idesc2 = instr_desc_bf16<kTcTileP, 2 * COUT>();
-            const uint32_t idesc1 = instr_desc_bf16<kTcTileP, COUT>();
+            // Group (y .. y + G - 1) accumulates its G output rows side by side (row y + j in
+            // columns [j COUT, (j + 1) COUT)).  Input row y - 1 + k feeds output rows
+            // j = max(0, k - 2) .. min(G - 1, k) through tap rows ty = k - j: one MMA whose
+            // B operand is the contiguous slice of the [ty 2 | ty 1 | ty 0] weight stack.
+            uint32_t idesc[4];
+            idesc[1] = instr_desc_bf16<kTcTileP, COUT>();
+            idesc[2] = instr_desc_bf16<kTcTileP, 2 * COUT>();
+            idesc[3] = instr_desc_bf16<kTcTileP, 3 * COUT>();
             const uint64_t aDesc0 = smem_desc(ringAddr, kTcSpx * 16, 128);
-            const uint64_t bDesc0 = smem_desc(smem_u32(sW), 2 * COUT * 16, 128);
-            uint32_t qBase = 0, pairCount = 0;
+            const uint64_t bDesc0 = smem_desc(smem_u32(sW), 3 * COUT * 16, 128);
+            // issue order per (tx, kc): k = 2 and k = G + 1 first (their outputs tile all G
+            // rows, so they can start the accumulator), then the rest
+            static_assert(G == 4, "issue order below is for groups of 4 rows");
+            constexpr int kOrder[G + 2] = {2, 5, 0, 1, 3, 4};
+            uint32_t qBase = 0, groupCount = 0;
             bool ok = true;
             for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
                 GBSP_STRIP_GEOMETRY(strip);
                 for (int p = 0; p < P && ok; p++) {
-                    const uint32_t q0 = qBase + 2u * (uint32_t)p;  // input row y - 1
-                    for (uint32_t q = q0; q < q0 + 4u && ok; q++)
+                    const uint32_t q0 = qBase + (uint32_t)(G * p);  // input row y - 1
+                    for (uint32_t q = q0; q < q0 + G + 2 && ok; q++)
                         ok = tc_wait(smem_u32(&rowFull[q % kTcRing]), (q / kTcRing) & 1u,
                             &abortFlag);
                     if (!ok) break;
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    const uint32_t acc = pairCount % kTcAccSlots, use = pairCount / kTcAccSlots;
+                    const uint32_t acc = groupCount % SLOTS, use = groupCount / SLOTS;
                     if (use > 0 && !tc_wait(smem_u32(&accEmpty[acc]), (use - 1u) & 1u, &abortFlag)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const uint32_t dAcc = tmem + acc * (uint32_t)ACC_COLS;
-                    const uint32_t sM = q0 % kTcRing, s0 = (q0 + 1u) % kTcRing;
-                    const uint32_t s1 = (q0 + 2u) % kTcRing, s2 = (q0 + 3u) % kTcRing;
 #pragma unroll
                     for (int tx = 0; tx < 3; tx++) {
 #pragma unroll
                         for (int kc = 0; kc < CIN / 16; kc++) {
-                            // 16-byte units: slot row, channel group 2 kc, pixel tx
-                            const uint64_t aOff = (uint64_t)(2 * kc * kTcSpx + tx);
-                            const uint64_t b0 = bDesc0 + (uint64_t)(((0 * 3 + tx) * KG + 2 * kc) * 2 * COUT);
-                            const uint64_t b1 = bDesc0 + (uint64_t)(((1 * 3 + tx) * KG + 2 * kc) * 2 * COUT);
-                            const uint32_t first = (tx | kc) ? 1u : 0u;
-                            // input row y: [ty 1 | ty 0] -> both rows (initialises the pair)
-                            tc_mma(dAcc, aDesc0 + (uint64_t)(s0 * KG * kTcSpx) + aOff, b0, idesc2, first);
-                            // input row y + 1: [ty 2 | ty 1] -> both rows
-                            tc_mma(dAcc, aDesc0 + (uint64_t)(s1 * KG * kTcSpx) + aOff, b1, idesc2, 1u);
-                            // input row y - 1: ty 0 -> row y
-                            tc_mma(dAcc, aDesc0 + (uint64_t)(sM * KG * kTcSpx) + aOff,
-                                b0 + (uint64_t)COUT, idesc1, 1u);
-                            // input row y + 2: ty 2 -> row y + 1
-                            tc_mma(dAcc + (uint32_t)COUT, aDesc0 + (uint64_t)(s2 * KG * kTcSpx) + aOff,
-                                b1, idesc1, 1u);
+#pragma unroll
+                            for (int o = 0; o < G + 2; o++) {
+                                const int k = kOrder[o];
+                                const int jlo = k - 2 > 0 ? k - 2 : 0, jhi = k < G - 1 ? k : G - 1;
+                                const uint32_t slot = (q0 + (uint32_t)k) % kTcRing;
+                                // 16-byte units: slot row, channel group 2 kc, pixel tx
+                                const uint64_t aDesc = aDesc0 +
+                                    (uint64_t)(slot * KG * kTcSpx + 2 * kc * kTcSpx + tx);
+                                // weight block (tx, 2 kc), starting at tap row ty = k - jlo
+                                const uint64_t bDesc = bDesc0 +
+                                    (uint64_t)((tx * KG + 2 * kc) * 3 * COUT + (2 - k + jlo) * COUT);
+                                const uint32_t accumulate = (tx | kc) || o >= 2 ? 1u : 0u;
+                                tc_mma(dAcc + (uint32_t)(jlo * COUT), aDesc, bDesc,
+                                    idesc[jhi - jlo + 1], accumulate);
+                            }
                         }
                     }
                     tc_commit(smem_u32(&accFull[acc]));
-                    // input rows y - 1 and y have no later reader
-                    tc_commit(smem_u32(&rowEmpty[sM]));
-                    tc_commit(smem_u32(&rowEmpty[s0]));
-                    pairCount++;
+                    // input rows y - 1 .. y + G - 2 have no later reader
+                    for (int k = 0; k < G; k++)
+                        tc_commit(smem_u32(&rowEmpty[(q0 + (uint32_t)k) % kTcRing]));
+                    groupCount++;
                 }
                 if (!ok) break;
                 // the strip's last two input rows are free once its last MMAs finish
-                const uint32_t qLast = qBase + 2u * (uint32_t)P + 1u;
+                const uint32_t qLast = qBase + (uint32_t)(G * P) + 1u;
                 tc_commit(smem_u32(&rowEmpty[(qLast - 1u) % kTcRing]));
                 tc_commit(smem_u32(&rowEmpty[qLast % kTcRing]));
                 qBase = qLast + 1u;
@@ -533,13 +541,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
         }
         __syncwarp();
     } else if (warp < 4) {
-        // ---- producers: input rows y0 - 1 .. y0 + 2 P of every strip
+        // ---- producers: input rows y0 - 1 .. y0 + G P of every strip
         const int ptid = tid - 32;
         uint32_t q = 0;
         bool ok = true;
         for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
             GBSP_STRIP_GEOMETRY(strip);
-            for (int gy = y0 - 1; gy <= y0 + 2 * P; gy++, q++) {
+            for (int gy = y0 - 1; gy <= y0 + G * P; gy++, q++) {
                 const uint32_t slot = q % kTcRing, use = q / kTcRing;
                 if (use > 0 && !tc_wait(smem_u32(&rowEmpty[slot]), (use - 1u) & 1u, &abortFlag)) {
                     ok = false;
@@ -553,16 +561,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
         }
         asm volatile("cp.async.wait_group 0;" ::: "memory");
     } else {
-        // ---- epilogue: group g = (warp - 4) / 4 takes the row pairs with pairCount % 2 == g;
+        // ---- epilogue: group g = (warp - 4) / 4 takes the row groups with groupCount % 2 == g;
         // warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels)
         const int quarter = warp & 3, group = (warp - 4) >> 2;
-        uint32_t pairCount = 0;
+        uint32_t groupCount = 0;
         bool ok = true;
         for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
             GBSP_STRIP_GEOMETRY(strip);
-            for (int p = 0; p < P; p++, pairCount++) {
-                if ((int)(pairCount % kTcEpiGroups) != group) continue;
-                const uint32_t acc = pairCount % kTcAccSlots, use = pairCount / kTcAccSlots;
+            for (int p = 0; p < P; p++, groupCount++) {
+                if ((int)(groupCount % kTcEpiGroups) != group) continue;
+                const uint32_t acc = groupCount % SLOTS, use = groupCount / SLOTS;
                 ok = tc_wait(smem_u32(&accFull[acc]), use & 1u, &abortFlag);
                 __syncwarp();
                 if (!__all_sync(0xFFFFFFFFu, ok)) {
@@ -570,30 +578,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
-                uint32_t r0[COUT], r1[COUT];
                 const uint32_t cols = tmem + ((uint32_t)(quarter * 32) << 16) + acc * (uint32_t)ACC_COLS;
-#pragma unroll
-                for (int c = 0; c < COUT; c += 16) {
-                    tmem_ld16(cols + (uint32_t)c, *reinterpret_cast<uint32_t(*)[16]>(r0 + c));
-                    tmem_ld16(cols + (uint32_t)(COUT + c), *reinterpret_cast<uint32_t(*)[16]>(r1 + c));
-                }
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                asm volatile("tcgen05.fence::before_thread_sync;");
-                mbar_arrive(smem_u32(&accEmpty[acc]));
                 const int x = x0 + quarter * 32 + lane;
-                const int y = y0 + 2 * p;
-                if (x < W) {
+#pragma unroll 1
+                for (int j = 0; j < G; j++) {
+                    const int y = y0 + G * p + j;
+                    uint32_t r[COUT];
 #pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        if (y + h >= y1) break;
-                        const size_t px = (size_t)(b * H + y + h) * W + x;
+                    for (int c = 0; c < COUT; c += 16)
+                        tmem_ld16(cols + (uint32_t)(j * COUT + c), *reinterpret_cast<uint32_t(*)[16]>(r + c));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (x < W && y < y1) {
+                        const size_t px = (size_t)(b * H + y) * W + x;
                         if constexpr (EPI == kEpiFilter)
-                            conv_filter_store<COUT>(h ? r1 : r0, px, x, y + h, W, H, sBias, noisy,
-                                outFilt);
+                            conv_filter_store<COUT>(r, px, x, y, W, H, sBias, noisy, outFilt);
                         else
-                            conv_store<COUT, EPI>(h ? r1 : r0, px, sBias, outB, outF);
+                            conv_store<COUT, EPI>(r, px, sBias, outB, outF);
                     }
                 }
+                asm volatile("tcgen05.fence::before_thread_sync;");
+                mbar_arrive(smem_u32(&accEmpty[acc]));
             }
         }
     }
@@ -669,7 +673,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     const float *bias, void *outB, float *outF, const float4 *noisy = nullptr,
     float4 *outFilt = nullptr)
 {
-    size_t smem = (size_t)(12 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
+    size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int ctas = smCount;  // one CTA per SM (the row ring takes most of shared memory)
@@ -678,7 +682,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     // the last round is nearly full), at least 4 rows
     int rows = (int)(((int64_t)cols * H + 6 * ctas - 1) / (6 * ctas));
     rows = rows < 4 ? 4 : (rows > H ? H : rows);
-    rows += rows & 1;  // strips of whole row pairs (only the image's last pair may be half)
+    rows = (rows + kTcGroupRows - 1) / kTcGroupRows * kTcGroupRows;  // whole row groups
     int strips = cols * ((H + rows - 1) / rows);
     int grid = strips < ctas ? strips : ctas;
     kern<<<grid, kTcThreads, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
