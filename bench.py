@@ -921,7 +921,7 @@ def run_tc_rate(args):
     rows = []
     cases = [(1, n, 0) for n in (16, 32, 48, 64, 96, 128, 144, 256)]
     cases += [(2, 48, 0), (2, 128, 0)]
-    cases += [(1, n, off) for n in (48, 96) for off in (1, 2, 8)]
+    cases += [(1, n, off) for n in (48, 96) for off in (1, 2, 8, 64, 65)]
     for issuers, n, off in cases:
         rc = L.gbsp_dn_tc_rate(n, 1024, issuers, off, out)
         if rc:

@@ -458,7 +458,8 @@ int gbsp_dn_conv3x3_filter_tc(void *stream, const uint16_t *in, uint32_t B, uint
 /* Diagnostic: clock cycles per 128 x n x 16 BF16 tcgen05.mma when `issuers`
  * (1 or 2) threads of one CTA each issue `iters` of them back to back into
  * their own tensor-memory accumulator (n = 16, 32, 48, 64, 96, 128, 144, 256);
- * the A operand starts aOffset16 (<= 64) 16-byte units past a 1 KB boundary.
+ * the A operand starts (aOffset16 % 64) 16-byte units past a 1 KB boundary,
+ * and from aOffset16 = 64 on the MMAs alternate between two A tiles 4 KB apart.
  * cyclesPerMma receives one value per issuer.  Synchronises the device. */
 int gbsp_dn_tc_rate(uint32_t n, uint32_t iters, uint32_t issuers, uint32_t aOffset16,
     double *cyclesPerMma);

@@ -16,7 +16,10 @@
 
 #include <cstdint>
 
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <mutex>
 
 #include "gbsp_internal.h"
 
@@ -153,57 +156,57 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // ---------------------------------------------------------------------------
 // conv3x3 on the 5th-generation tensor cores (tcgen05).
 //
-// GEMM: M = 128 pixels of one image row, K = 9 taps x CIN, and two output
-// rows y, y + 1 side by side along N (accumulator columns [0, COUT) and
-// [COUT, 2 COUT)).  One elected thread issues tcgen05.mma.cta_group::1
-// .kind::f16 (BF16 x BF16 -> FP32) per (horizontal tap, 16-channel slice):
-// input rows y and y + 1 feed both output rows at once (N = 2 COUT, the
-// weights of the two tap rows stacked), input rows y - 1 and y + 2 one row
-// each (N = COUT).  An M = 128 MMA costs about the same up to N = 96, so
-// pairing rows cuts the MMAs per output row from 9 CIN / 16 to 6 CIN / 16.
-// Both operands are read straight from shared memory through matrix
-// descriptors, so the 3x3 neighbourhood is never expanded: a horizontal tap
-// is a 16-byte-granular offset of the A descriptor into a staged input row.
+// GEMM: M = 128 pixels of one image row, K = 9 taps x CIN, and the G =
+// kTcGroupRows output rows y .. y + G - 1 of a group side by side along N
+// (row y + j in accumulator columns [j COUT, (j + 1) COUT)).  One elected
+// thread issues tcgen05.mma.cta_group::1.kind::f16 (BF16 x BF16 -> FP32) per
+// (input row, horizontal tap, 16-channel slice): input row y - 1 + k feeds
+// every output row j of the group with k - j in 0..2 at once, with the
+// matching tap rows of the [ty 2 | ty 1 | ty 0] weight stack as a
+// contiguous B slice (N = COUT, 2 COUT or 3 COUT).  An M = 128 MMA costs
+// about the same up to N = 96 and runs at the dense rate from N = 128, so
+// G = 4 takes 6 instead of 12 MMAs per (tap, slice) for 4 rows.  Both
+// operands are read straight from shared memory through matrix descriptors,
+// so the 3x3 neighbourhood is never expanded: a horizontal tap is a
+// 16-byte-granular offset of the A descriptor into a staged input row.
 //
 // Shared memory holds the operands in the canonical no-swizzle K-major
 // layout: 8 x 16-byte core matrices (8 rows of 8 BF16 channels), rows
-// contiguous.  Input rows: ring slots of [CIN/8 channel groups][130 pixels]
-// [16 B] (a core matrix = 8 consecutive pixels of one channel group, so a
-// pixel shift moves the start by 16 B); weights: [2 tap-row pairs][3 taps]
-// [CIN/8 groups][2 COUT][16 B].  Descriptor strides: leading (K) = next
+// contiguous.  Input rows: ring slots of [CIN/8 channel groups][kTcPlane
+// pixels][16 B] (a core matrix = 8 consecutive pixels of one channel group,
+// so a pixel shift moves the start by 16 B); weights: [3 taps][CIN/8
+// groups][3 tap rows x COUT][16 B].  Descriptor strides: leading (K) = next
 // channel group, stride (M or N) = next 8 rows = 128 B.
 //
 // One persistent CTA per SM walks vertical strips (one 128-pixel column
 // segment, a run of rows) with its warps specialised and coupled only by
 // mbarriers:
-//   * warps 1-3 (producers) stage input rows into a ring of kTcRing slots
-//     with cp.async, as many rows in flight as the ring allows (the
-//     memory-level parallelism that hides DRAM latency); a row's slot is
-//     reused once the MMAs of the last row pair that reads it have completed
-//     (rowEmpty, signalled by tcgen05.commit), and each producer thread's
-//     copies arrive on the row's rowFull by themselves when they land
-//     (cp.async.mbarrier.arrive.noinc); the MMA thread fences the async
-//     proxy after its wait;
-//   * lane 0 of warp 0 issues, per row pair (y, y + 1), the 12 CIN/16 MMAs
-//     reading rows y-1..y+2 into one of kTcAccSlots TMEM accumulators, then
-//     commits to that accumulator's accFull and to the rowEmpty of rows y-1
-//     and y;
-//   * warps 4-11 are two epilogue groups taking alternate row pairs (warp w
-//     owns TMEM lanes 32 (w % 4) .. + 31 = pixels): wait on accFull, read
-//     the accumulator with tcgen05.ld, release it on accEmpty and apply bias
-//     / ReLU / BF16 packing (or the fused filter) while the tensor core
-//     already works on the next pairs.
+//   * lane 0 of warp 1 (producer) loads input rows into a ring of kTcRing
+//     slots with TMA (cp.async.bulk.tensor, one 130-pixel x 8-channel box
+//     per channel group, zero outside the image), as many rows in flight as
+//     the ring allows; a row lands on its rowFull barrier by transaction
+//     count, and its slot is reused once the MMAs of the last row group that
+//     reads it have completed (rowEmpty, signalled by tcgen05.commit);
+//   * lane 0 of warp 0 issues, per group of kTcGroupRows output rows, the
+//     (kTcGroupRows + 2) x 3 x CIN/16 MMAs reading its input rows into one
+//     TMEM accumulator, then commits to that accumulator's accFull and to the
+//     rowEmpty of the input rows no later group reads;
+//   * warps 4-11 are two epilogue groups taking alternate row groups (warp
+//     w owns TMEM lanes 32 (w % 4) .. + 31 = pixels): wait on accFull, read
+//     the accumulator with tcgen05.ld, apply bias / ReLU / BF16 packing (or
+//     the fused filter), and release it on accEmpty, while the tensor core
+//     already works on the next group.
 // Every wait is bounded; a timeout raises a shared abort flag that ends the
 // other roles' waits, and sets g_dnStatus.
 // ---------------------------------------------------------------------------
 constexpr int kTcTileP = 128;
-// One CTA per SM: warp 0 issues the MMAs, warps 1-3 produce, warps 4-11 are
-// two epilogue groups that take alternate row pairs.
+// One CTA per SM: warp 0 issues the MMAs, lane 0 of warp 1 loads rows, warps 4-11 are
+// two epilogue groups that take alternate row groups.
 constexpr int kTcThreads = 384;
-constexpr int kTcProducers = 96;
 constexpr int kTcEpiGroups = 2;
 constexpr int kTcAccSlots = 4;  // accumulator a is drained by epilogue group a % 2
-constexpr int kTcSpx = kTcTileP + 2;
+constexpr int kTcSpx = kTcTileP + 2;     // staged pixels per row: x0 - 1 .. x0 + 128
+constexpr int kTcPlane = 136;            // pixels per channel-group plane (2,176 B, 128-B aligned)
 constexpr int kTcGroupRows = 4;  // output rows per accumulator
 constexpr int kTcRing = 14;  // input row slots: 6 read by a row group's MMAs, the rest in flight
 constexpr uint32_t kTcWaitLimit = 1u << 26;
@@ -271,25 +274,6 @@ __device__ __forceinline__ uint32_t instr_desc_bf16()
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
         ((uint32_t)(M >> 4) << 24);
-}
-
-// Stages input row gy (zero outside the image) into ring slot `slot` with
-// cp.async (16 B per copy, zero-filled when the source size is 0).
-template <int KG, int NT>
-__device__ __forceinline__ void stage_row(uint32_t sRing, int slot, const uint4 *in, int b, int gy,
-    int H, int W, int x0, int tid)
-{
-    const bool rowIn = gy >= 0 && gy < H;
-    for (int i = tid; i < KG * kTcSpx; i += NT) {
-        int px = i % kTcSpx, kg = i / kTcSpx;
-        int gx = x0 + px - 1;
-        bool ok = rowIn && gx >= 0 && gx < W;
-        const uint4 *src = ok ? in + ((size_t)(b * H + gy) * W + gx) * KG + kg : in;
-        uint32_t dst = sRing + (uint32_t)(((slot * KG + kg) * kTcSpx + px) * 16);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
-                     :: "r"(dst), "l"(src), "r"(ok ? 16 : 0) : "memory");
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
 __device__ __forceinline__ void softmax25(const float *l, float *w)
@@ -388,7 +372,7 @@ __device__ __forceinline__ void conv_filter_store(const uint32_t (&r)[COUT], siz
 }
 
 template <int CIN, int COUT, int EPI>
-__global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in,
+__global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmIn,
     int B, int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF,
     const float4 *__restrict__ noisy, float4 *__restrict__ outFilt)
@@ -404,14 +388,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     constexpr int TMEM_COLS = 512;
     extern __shared__ __align__(128) unsigned char smemRaw[];
     uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [3][KG][3 COUT]
-    uint4 *sRing = sW + 9 * KG * COUT;               // [kTcRing][KG][kTcSpx]
+    // ring slots of [KG][kTcPlane] 16-byte pixels, 128-byte aligned for TMA
+    const uint32_t ringAddr = (smem_u32(sW + 9 * KG * COUT) + 127u) & ~127u;
     __shared__ __align__(8) uint64_t rowFull[kTcRing], rowEmpty[kTcRing];
     __shared__ __align__(8) uint64_t accFull[SLOTS], accEmpty[SLOTS], drain;
     __shared__ uint32_t tmemBase;
     __shared__ volatile uint32_t abortFlag;
     __shared__ __align__(16) float sBias[COUT];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint4 *in4 = reinterpret_cast<const uint4 *>(in);
     if (tid < COUT) sBias[tid] = EPI != kEpiF32 ? bias[tid] : 0.0f;
 
     // weights -> stacked canonical layout: block (tx, kg) holds 3 COUT rows of 16 B, the
@@ -429,8 +413,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     }
     if (tid == 0) {
         for (int i = 0; i < kTcRing; i++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
-                         :: "r"(smem_u32(&rowFull[i])), "r"(kTcProducers));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&rowFull[i])));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&rowEmpty[i])));
         }
         for (int i = 0; i < SLOTS; i++) {
@@ -446,7 +429,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmemBase;
-    const uint32_t ringAddr = smem_u32(sRing);
 
     const int segs = (W + kTcTileP - 1) / kTcTileP;
     const int stripsPerCol = (H + rowsPerStrip - 1) / rowsPerStrip;
@@ -474,7 +456,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
             idesc[1] = instr_desc_bf16<kTcTileP, COUT>();
             idesc[2] = instr_desc_bf16<kTcTileP, 2 * COUT>();
             idesc[3] = instr_desc_bf16<kTcTileP, 3 * COUT>();
-            const uint64_t aDesc0 = smem_desc(ringAddr, kTcSpx * 16, 128);
+            const uint64_t aDesc0 = smem_desc(ringAddr, kTcPlane * 16, 128);
             const uint64_t bDesc0 = smem_desc(smem_u32(sW), 3 * COUT * 16, 128);
             // issue order per (tx, kc): k = 2 and k = G + 1 first (their outputs tile all G
             // rows, so they can start the accumulator), then the rest
@@ -509,7 +491,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
                                 const uint32_t slot = (q0 + (uint32_t)k) % kTcRing;
                                 // 16-byte units: slot row, channel group 2 kc, pixel tx
                                 const uint64_t aDesc = aDesc0 +
-                                    (uint64_t)(slot * KG * kTcSpx + 2 * kc * kTcSpx + tx);
+                                    (uint64_t)(slot * KG * kTcPlane + 2 * kc * kTcPlane + tx);
                                 // weight block (tx, 2 kc), starting at tap row ty = k - jlo
                                 const uint64_t bDesc = bDesc0 +
                                     (uint64_t)((tx * KG + 2 * kc) * 3 * COUT + (2 - k + jlo) * COUT);
@@ -541,25 +523,44 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __nv_bfloat1
         }
         __syncwarp();
     } else if (warp < 4) {
-        // ---- producers: input rows y0 - 1 .. y0 + G P of every strip
-        const int ptid = tid - 32;
-        uint32_t q = 0;
-        bool ok = true;
-        for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
-            GBSP_STRIP_GEOMETRY(strip);
-            for (int gy = y0 - 1; gy <= y0 + G * P; gy++, q++) {
-                const uint32_t slot = q % kTcRing, use = q / kTcRing;
-                if (use > 0 && !tc_wait(smem_u32(&rowEmpty[slot]), (use - 1u) & 1u, &abortFlag)) {
-                    ok = false;
-                    break;
+        // ---- producer (lane 0 of warp 1): input rows y0 - 1 .. y0 + G P of every strip,
+        // one TMA box (130 pixels x 8 channels, zero outside the image) per channel group,
+        // completing the row's rowFull transaction count
+        if (warp == 1 && lane == 0) {
+            constexpr uint32_t kRowBytes = (uint32_t)(KG * kTcSpx * 16);
+            uint32_t q = 0;
+            bool ok = true;
+            for (int strip = blockIdx.x; strip < numStrips && ok; strip += gridDim.x) {
+                GBSP_STRIP_GEOMETRY(strip);
+                for (int gy = y0 - 1; gy <= y0 + G * P; gy++, q++) {
+                    const uint32_t slot = q % kTcRing, use = q / kTcRing;
+                    if (use > 0 && !tc_wait(smem_u32(&rowEmpty[slot]), (use - 1u) & 1u, &abortFlag)) {
+                        ok = false;
+                        break;
+                    }
+                    const uint32_t bar = smem_u32(&rowFull[slot]);
+                    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                                 :: "r"(bar), "r"(kRowBytes) : "memory");
+                    for (int kg = 0; kg < KG; kg++) {
+                        const uint32_t dst = ringAddr + (uint32_t)((slot * KG + kg) * kTcPlane * 16);
+                        asm volatile(
+                            "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                            " [%0], [%1, {%2, %3, %4, %5}], [%6];"
+                            :: "r"(dst), "l"(reinterpret_cast<uint64_t>(&tmIn)), "r"(8 * kg),
+                               "r"(x0 - 1), "r"(gy), "r"(b), "r"(bar)
+                            : "memory");
+                    }
                 }
-                stage_row<KG, kTcProducers>(ringAddr, (int)slot, in4, b, gy, H, W, x0, ptid);
-                // this thread's arrival on rowFull fires when its copies have landed
-                asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];"
-                             :: "r"(smem_u32(&rowFull[slot])) : "memory");
             }
+            // every box issued has landed before the CTA's shared memory is released
+            volatile uint32_t never = 0u;
+            for (uint32_t s0 = 0; s0 < kTcRing && s0 < q; s0++) {
+                const uint32_t lastUse = (q - 1u - ((q - 1u - s0) % kTcRing)) / kTcRing;
+                if (!tc_wait(smem_u32(&rowFull[s0]), lastUse & 1u, &never)) abortFlag = 1u;
+            }
+            if (!ok) abortFlag = 1u;
         }
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncwarp();
     } else {
         // ---- epilogue: group g = (warp - 4) / 4 takes the row groups with groupCount % 2 == g;
         // warp w reads TMEM lanes 32 (w % 4) .. + 31 (pixels)
@@ -668,14 +669,53 @@ __global__ void __launch_bounds__(64) k_tc_rate(int iters, int issuers, int aOff
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(512));
 }
 
+// cuTensorMapEncodeTiled from the driver, looked up once through the runtime
+// (no link-time dependency on libcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                &q) == cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// TMA map of an NHWC BF16 activation tensor [B][H][W][cin]: boxes of 8
+// channels x kTcSpx pixels x 1 row x 1 image, zero outside the tensor.
+static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)W * cin * 2,
+        (cuuint64_t)H * W * cin * 2};
+    const cuuint32_t box[4] = {8, (cuuint32_t)kTcSpx, 1, 1};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), dims,
+        strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return GBSP_OK;
+}
+
 template <int CIN, int COUT, int EPI>
 int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, int W, const void *w,
     const float *bias, void *outB, float *outF, const float4 *noisy = nullptr,
     float4 *outFilt = nullptr)
 {
-    size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcSpx) * 16;
+    // weights, then the ring (rounded up to a 128-byte boundary inside the kernel)
+    size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcPlane) * 16 + 128;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUtensorMap map;
+    int rc = input_tensor_map(&map, in, B, H, W, CIN);
+    if (rc) return rc;
     const int ctas = smCount;  // one CTA per SM (the row ring takes most of shared memory)
     const int cols = B * ((W + kTcTileP - 1) / kTcTileP);
     // rows per strip: about six strips per CTA (strips go round-robin, so
@@ -685,7 +725,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     rows = (rows + kTcGroupRows - 1) / kTcGroupRows * kTcGroupRows;  // whole row groups
     int strips = cols * ((H + rows - 1) / rows);
     int grid = strips < ctas ? strips : ctas;
-    kern<<<grid, kTcThreads, smem, s>>>(reinterpret_cast<const __nv_bfloat16 *>(in), B, H, W, rows,
+    kern<<<grid, kTcThreads, smem, s>>>(map, B, H, W, rows,
         reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
         outF, noisy, outFilt);
     GBSP_CUDA_TRY(cudaGetLastError());
