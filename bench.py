@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--dn-scenes", type=int, default=125)
     ap.add_argument("--dn-crops", type=int, default=16)
     ap.add_argument("--dn-ref-spp", type=int, default=4096)
+    ap.add_argument("--dn-train-spp", default="2,4",
+                    help="input spp of the training crops (comma list: crops cycle through it)")
     ap.add_argument("--dn-steps", type=int, default=4000)
     ap.add_argument("--dn-lr", type=float, default=1e-4)
     ap.add_argument("--dn-eval-seeds", type=int, default=50)
@@ -593,11 +595,13 @@ def run_config2(args):
 
 
 def run_config5(args):
-    """Config 5: learned denoiser.  Train on path-traced pairs (4-spp inputs +
-    G-buffers, high-spp targets, 128x128 crops, batch 16, Adam, relMSE), then
-    on held-out scenes compare, at equal render resolution, the wall time for
-    plain path tracing to reach relMSE 0.01 against an FP64-accumulated
-    16,384-spp oracle with the time of 4 spp + denoising.  Prints its own line."""
+    """Config 5: learned denoiser.  Train on path-traced pairs (low-spp inputs,
+    2 and 4 spp by default, + G-buffers, high-spp targets, 128x128 crops, batch
+    16, Adam, relMSE), then on held-out scenes compare, at equal render
+    resolution, the wall time for plain path tracing to reach relMSE 0.01
+    against an FP64-accumulated 16,384-spp oracle with the time of the
+    cheapest input spp whose denoised result meets it + denoising.  Prints its
+    own line."""
     import torch
     from vk_cinematic_gb300 import denoiser, gbsp
 
@@ -607,8 +611,9 @@ def run_config5(args):
     rt = gbsp.Runtime(0, stream=stream.cuda_stream)
     log = lambda *a: print(*a, file=sys.stderr, flush=True)  # noqa: E731
     t0 = time.time()
+    train_spp = [int(v) for v in str(args.dn_train_spp).split(",") if v]
     noisy, aov, target = denoiser.make_dataset(
-        rt, n_scenes=args.dn_scenes, crops_per_scene=args.dn_crops, crop=128, spp_in=4,
+        rt, n_scenes=args.dn_scenes, crops_per_scene=args.dn_crops, crop=128, spp_in=train_spp,
         spp_ref=args.dn_ref_spp, seed0=0, log=log)
     data_s = time.time() - t0
     net = denoiser.KPCNN(seed=0, conv=args.dn_conv, wgrad=args.dn_wgrad)
@@ -638,7 +643,7 @@ def run_config5(args):
     # ---- quality on held-out scenes (crops, FP64-accumulated oracle)
     crop = args.dn_eval_crop
     spps = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024]
-    in_spps = [4, 8, 16]  # denoiser input spp candidates (trained on 4)
+    in_spps = [2, 4, 8, 16]  # denoiser input spp candidates
     plain = {k: [] for k in spps}
     den = {k: [] for k in in_spps}
     checked = {k: [] for k in in_spps}
@@ -717,7 +722,7 @@ def run_config5(args):
         "data": "synthetic: path-traced seeded config-3-style scenes",
         "config": {"workload": "config5: KPCNN 8 x conv3x3 (48 ch) + softmax 5x5 filter",
                    "train_crops": int(n), "crop": 128, "batch": 16, "steps": args.dn_steps,
-                   "lr": args.dn_lr, "train_input_spp": 4, "target_spp": args.dn_ref_spp,
+                   "lr": args.dn_lr, "train_input_spp": train_spp, "target_spp": args.dn_ref_spp,
                    "eval_seeds": args.dn_eval_seeds, "eval_crop": crop,
                    "oracle_spp": args.dn_oracle_spp, "conv": net.conv_impl},
         "denoised_relmse_by_input_spp": den_mean, "denoiser_input_spp": in_spp,

@@ -302,7 +302,7 @@ def test_fused_logits_and_filter_match_unfused(gpu_lib, B, H, W):
 
 
 def test_tile_fallback_ignores_noise_alone(gpu_lib):
-    """A correct denoised tile judged by very noisy plain renders: the point
+    """A correct denoised tile checked against very noisy plain renders: the point
     estimates scatter around 0 and often exceed the bound, but a tile falls
     back only when the bound lies two standard errors below its estimate."""
     import torch

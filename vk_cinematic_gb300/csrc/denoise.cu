@@ -206,7 +206,7 @@ constexpr int kTcThreads = 384;
 constexpr int kTcEpiGroups = 2;
 constexpr int kTcAccSlots = 4;  // accumulator a is drained by epilogue group a % 2
 constexpr int kTcSpx = kTcTileP + 2;     // staged pixels per row: x0 - 1 .. x0 + 128
-constexpr int kTcPlane = 136;            // pixels per channel-group plane (2,176 B, 128-B aligned)
+constexpr int kTcPlane = kTcSpx;         // pixels per channel-group plane of a ring slot
 constexpr int kTcGroupRows = 4;  // output rows per accumulator
 constexpr int kTcRing = 14;  // input row slots: 6 read by a row group's MMAs, the rest in flight
 constexpr uint32_t kTcWaitLimit = 1u << 26;
@@ -388,7 +388,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_const
     constexpr int TMEM_COLS = 512;
     extern __shared__ __align__(128) unsigned char smemRaw[];
     uint4 *sW = reinterpret_cast<uint4 *>(smemRaw);  // [3][KG][3 COUT]
-    // ring slots of [KG][kTcPlane] 16-byte pixels, 128-byte aligned for TMA
+    // ring slots of [KG][kTcPlane] 16-byte pixels, each slot 128-byte aligned for TMA
+    constexpr uint32_t kSlotBytes = (uint32_t)((KG * kTcPlane * 16 + 127) / 128 * 128);
     const uint32_t ringAddr = (smem_u32(sW + 9 * KG * COUT) + 127u) & ~127u;
     __shared__ __align__(8) uint64_t rowFull[kTcRing], rowEmpty[kTcRing];
     __shared__ __align__(8) uint64_t accFull[SLOTS], accEmpty[SLOTS], drain;
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_const
                                 const uint32_t slot = (q0 + (uint32_t)k) % kTcRing;
                                 // 16-byte units: slot row, channel group 2 kc, pixel tx
                                 const uint64_t aDesc = aDesc0 +
-                                    (uint64_t)(slot * KG * kTcPlane + 2 * kc * kTcPlane + tx);
+                                    (uint64_t)(slot * (kSlotBytes / 16) + 2 * kc * kTcPlane + tx);
                                 // weight block (tx, 2 kc), starting at tap row ty = k - jlo
                                 const uint64_t bDesc = bDesc0 +
                                     (uint64_t)((tx * KG + 2 * kc) * 3 * COUT + (2 - k + jlo) * COUT);
@@ -524,8 +525,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_const
         __syncwarp();
     } else if (warp < 4) {
         // ---- producer (lane 0 of warp 1): input rows y0 - 1 .. y0 + G P of every strip,
-        // one TMA box (130 pixels x 8 channels, zero outside the image) per channel group,
-        // completing the row's rowFull transaction count
+        // one TMA box per row (8 channels x 130 pixels x every channel group, zero outside
+        // the image, landing as [group][pixel][8 channels]), completing the row's rowFull
+        // transaction count
         if (warp == 1 && lane == 0) {
             constexpr uint32_t kRowBytes = (uint32_t)(KG * kTcSpx * 16);
             uint32_t q = 0;
@@ -541,15 +543,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_const
                     const uint32_t bar = smem_u32(&rowFull[slot]);
                     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                                  :: "r"(bar), "r"(kRowBytes) : "memory");
-                    for (int kg = 0; kg < KG; kg++) {
-                        const uint32_t dst = ringAddr + (uint32_t)((slot * KG + kg) * kTcPlane * 16);
-                        asm volatile(
-                            "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-                            " [%0], [%1, {%2, %3, %4, %5}], [%6];"
-                            :: "r"(dst), "l"(reinterpret_cast<uint64_t>(&tmIn)), "r"(8 * kg),
-                               "r"(x0 - 1), "r"(gy), "r"(b), "r"(bar)
-                            : "memory");
-                    }
+                    const uint32_t dst = ringAddr + slot * kSlotBytes;
+                    asm volatile(
+                        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                        :: "r"(dst), "l"(reinterpret_cast<uint64_t>(&tmIn)), "r"(0), "r"(x0 - 1),
+                           "r"(0), "r"(gy), "r"(b), "r"(bar)
+                        : "memory");
                 }
             }
             // every box issued has landed before the CTA's shared memory is released
@@ -685,18 +685,22 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// TMA map of an NHWC BF16 activation tensor [B][H][W][cin]: boxes of 8
-// channels x kTcSpx pixels x 1 row x 1 image, zero outside the tensor.
+// TMA map of an NHWC BF16 activation tensor [B][H][W][cin] viewed as
+// [B][H][cin / 8][W][8] (dimension order 8 channels, pixel, channel group,
+// row, image; the channel-group stride, 16 B, is below the pixel stride):
+// one box = 8 channels x kTcSpx pixels x every channel group of one row,
+// written to shared memory as [group][pixel][8 channels], zero outside the
+// tensor.
 static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin)
 {
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
-    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
-    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)W * cin * 2,
+    const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)cin / 8, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[4] = {(cuuint64_t)cin * 2, 16, (cuuint64_t)W * cin * 2,
         (cuuint64_t)H * W * cin * 2};
-    const cuuint32_t box[4] = {8, (cuuint32_t)kTcSpx, 1, 1};
-    const cuuint32_t elem[4] = {1, 1, 1, 1};
-    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), dims,
+    const cuuint32_t box[5] = {8, (cuuint32_t)kTcSpx, (cuuint32_t)cin / 8, 1, 1};
+    const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(in), dims,
         strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS)
@@ -710,7 +714,8 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     float4 *outFilt = nullptr)
 {
     // weights, then the ring (rounded up to a 128-byte boundary inside the kernel)
-    size_t smem = (size_t)(9 * (CIN / 8) * COUT + kTcRing * (CIN / 8) * kTcPlane) * 16 + 128;
+    size_t smem = (size_t)9 * (CIN / 8) * COUT * 16 +
+        (size_t)kTcRing * (((CIN / 8) * kTcPlane * 16 + 127) / 128 * 128) + 128;
     auto kern = k_conv3x3_tc<CIN, COUT, EPI>;
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CUtensorMap map;
@@ -965,7 +970,7 @@ __global__ void k_filter(const float *__restrict__ logits, const float4 *__restr
     out[p] = make_float4(o.x, o.y, o.z, 1.0f);
 }
 
-// Per-tile error check of a denoised frame, judged by the plain path tracer.
+// Per-tile error check of a denoised frame against the plain path tracer.
 // A (the denoiser's input) and C are two independent plain renders with the
 // same spp, D the denoised A.  For unbiased plain estimates with variance s^2,
 // E[(D - C)^2] = (D - mu)^2 + s^2 and E[(A - C)^2] = 2 s^2, so per pixel and

@@ -159,7 +159,7 @@ class KPCNN:
         return out
 
     def denoise_checked(self, radiance, aov, plain_check, bound=0.01, tile=16):
-        """Denoises `radiance` and lets the plain path tracer judge every
+        """Denoises `radiance` and lets the plain path tracer check every
         tile x tile block with an independent render `plain_check` of the same
         spp (gbsp_dn_tile_fallback): blocks whose estimated relMSE exceeds
         `bound` by more than two standard errors are served from the plain
@@ -282,9 +282,11 @@ class SceneRenderer:
 def make_dataset(rt, n_scenes, crops_per_scene, crop=128, spp_in=4, spp_ref=4096, seed0=0,
                  n_spheres=256, level=5, log=print):
     """Training pairs: random crops of config-3-style frames, low-spp inputs
-    (+ G-buffers) and independent high-spp targets."""
+    (+ G-buffers) and independent high-spp targets.  spp_in may be a sequence:
+    crop c then gets spp_in[c % len(spp_in)] samples (a mixed-noise dataset)."""
     import torch
 
+    spp_list = list(spp_in) if isinstance(spp_in, (list, tuple)) else [spp_in]
     rng = np.random.default_rng(seed0)
     feats_l, noisy_l, tgt_l = [], [], []
     t0 = time.time()
@@ -294,7 +296,8 @@ def make_dataset(rt, n_scenes, crops_per_scene, crop=128, spp_in=4, spp_ref=4096
         for c in range(crops_per_scene):
             x0 = int(rng.integers(0, s.width - crop))
             y0 = int(rng.integers(0, s.height - crop))
-            noisy, aov = sr.render(x0, y0, crop, crop, spp_in, seed=1000 * k + 2 * c, aov=True)
+            spp = spp_list[c % len(spp_list)]
+            noisy, aov = sr.render(x0, y0, crop, crop, spp, seed=1000 * k + 2 * c, aov=True)
             target, _ = sr.render(x0, y0, crop, crop, spp_ref, seed=1000 * k + 2 * c + 1)
             noisy_l.append(noisy)
             tgt_l.append(target)
