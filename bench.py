@@ -61,9 +61,9 @@ def parse_args():
     ap.add_argument("--dn-scenes", type=int, default=125)
     ap.add_argument("--dn-crops", type=int, default=16)
     ap.add_argument("--dn-ref-spp", type=int, default=4096)
-    ap.add_argument("--dn-train-spp", default="2,4",
+    ap.add_argument("--dn-train-spp", default="1,2",
                     help="input spp of the training crops (comma list: crops cycle through it)")
-    ap.add_argument("--dn-steps", type=int, default=4000)
+    ap.add_argument("--dn-steps", type=int, default=10000)
     ap.add_argument("--dn-lr", type=float, default=1e-4)
     ap.add_argument("--dn-eval-seeds", type=int, default=50)
     ap.add_argument("--dn-eval-crop", type=int, default=256)
@@ -596,8 +596,8 @@ def run_config2(args):
 
 def run_config5(args):
     """Config 5: learned denoiser.  Train on path-traced pairs (low-spp inputs,
-    2 and 4 spp by default, + G-buffers, high-spp targets, 128x128 crops, batch
-    16, Adam, relMSE), then on held-out scenes compare, at equal render
+    1 and 2 spp by default, + G-buffers, high-spp targets, 128x128 crops, batch
+    16, Adam, relMSE, 10,000 steps), then on held-out scenes compare, at equal render
     resolution, the wall time for plain path tracing to reach relMSE 0.01
     against an FP64-accumulated 16,384-spp oracle with the time of the
     cheapest input spp whose denoised result meets it + denoising.  Prints its
@@ -643,7 +643,7 @@ def run_config5(args):
     # ---- quality on held-out scenes (crops, FP64-accumulated oracle)
     crop = args.dn_eval_crop
     spps = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024]
-    in_spps = [2, 4, 8, 16]  # denoiser input spp candidates
+    in_spps = [1, 2, 4, 8, 16]  # denoiser input spp candidates
     plain = {k: [] for k in spps}
     den = {k: [] for k in in_spps}
     checked = {k: [] for k in in_spps}
