@@ -19,6 +19,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
+#include <atomic>
 #include <mutex>
 
 #include "gbsp_internal.h"
@@ -373,7 +374,7 @@ __device__ __forceinline__ void conv_filter_store(const uint32_t (&r)[COUT], siz
 
 template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmIn,
-    int B, int H, int W, int rowsPerStrip, const __nv_bfloat16 *__restrict__ w,
+    int B, int H, int W, int rowsPerStrip, int reverseStrips, const __nv_bfloat16 *__restrict__ w,
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF,
     const float4 *__restrict__ noisy, float4 *__restrict__ outFilt)
 {
@@ -437,8 +438,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_const
     // strip geometry: segment origin x0, output rows [y0, y1) in P groups of G rows
     // (the last group may reach past the image); staged input rows y0 - 1 .. y0 + G P
 #define GBSP_STRIP_GEOMETRY(strip)                                                       \
-    const int sy = (strip) % stripsPerCol, seg = ((strip) / stripsPerCol) % segs;        \
-    const int b = (strip) / (stripsPerCol * segs);                                        \
+    const int st = reverseStrips ? numStrips - 1 - (strip) : (strip);                     \
+    const int sy = st % stripsPerCol, seg = (st / stripsPerCol) % segs;                  \
+    const int b = st / (stripsPerCol * segs);                                             \
     const int x0 = seg * kTcTileP, y0 = sy * rowsPerStrip;                                \
     const int y1 = min(H, y0 + rowsPerStrip);                                             \
     const int P = (y1 - y0 + G - 1) / G;                                                  \
@@ -730,7 +732,11 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     rows = (rows + kTcGroupRows - 1) / kTcGroupRows * kTcGroupRows;  // whole row groups
     int strips = cols * ((H + rows - 1) / rows);
     int grid = strips < ctas ? strips : ctas;
-    kern<<<grid, kTcThreads, smem, s>>>(map, B, H, W, rows,
+    // consecutive convolutions walk the strips in opposite orders, so a layer
+    // starts on the rows its predecessor wrote last (still in L2)
+    static std::atomic<unsigned> launches{0};
+    const int reverse = (int)(launches.fetch_add(1, std::memory_order_relaxed) & 1u);
+    kern<<<grid, kTcThreads, smem, s>>>(map, B, H, W, rows, reverse,
         reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
         outF, noisy, outFilt);
     GBSP_CUDA_TRY(cudaGetLastError());
