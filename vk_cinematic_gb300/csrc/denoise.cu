@@ -671,6 +671,9 @@ __global__ void __launch_bounds__(64) k_tc_rate(int iters, int issuers, int aOff
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(512));
 }
 
+// tcgen05 convolutions launched so far (all shapes): its parity picks the strip order.
+static std::atomic<unsigned> g_convLaunches{0};
+
 // cuTensorMapEncodeTiled from the driver, looked up once through the runtime
 // (no link-time dependency on libcuda).
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
@@ -734,8 +737,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
     int grid = strips < ctas ? strips : ctas;
     // consecutive convolutions walk the strips in opposite orders, so a layer
     // starts on the rows its predecessor wrote last (still in L2)
-    static std::atomic<unsigned> launches{0};
-    const int reverse = (int)(launches.fetch_add(1, std::memory_order_relaxed) & 1u);
+    const int reverse = (int)(g_convLaunches.fetch_add(1, std::memory_order_relaxed) & 1u);
     kern<<<grid, kTcThreads, smem, s>>>(map, B, H, W, rows, reverse,
         reinterpret_cast<const __nv_bfloat16 *>(w), bias, reinterpret_cast<__nv_bfloat16 *>(outB),
         outF, noisy, outFilt);
