@@ -425,16 +425,21 @@ int gbsp_tonemap(void *stream, const float *frame, uint64_t pixels, uint32_t *ou
 /* ---- learned denoiser ----------------------------------------------------------- */
 /* Kernels of a kernel-predicting CNN denoiser (8 conv3x3 layers, 48 channels,
  * softmax 5x5 filter) trained on this path tracer's low/high-spp frames.
- * No reference counterpart.  All pointers are device memory, tensors are
- * NHWC, BF16 values travel as uint16_t.  `stream` is a cudaStream_t (NULL =
- * default stream).  Calls are asynchronous. */
+ * No reference counterpart.  All pointers are device memory, BF16 values
+ * travel as uint16_t.  `stream` is a cudaStream_t (NULL = default stream).
+ * Calls are asynchronous.  Layouts: frames (radiance RGBA32F, G-buffers,
+ * denoised output) and FP32 logits are NHWC; activations and their gradients
+ * (features, conv inputs and BF16 / FP32-gradient outputs, dLogits) are
+ * channel-group-planar, [B][H][C/8][W][8]: each 8-channel group of an image
+ * row is one contiguous plane of W pixels. */
 #define GBSP_DN_EPI_BF16_BIAS_RELU 0  /* BF16 out = relu(conv + bias) */
 #define GBSP_DN_EPI_F32_BIAS 1        /* FP32 out = conv + bias */
 #define GBSP_DN_EPI_F32 2             /* FP32 out = conv */
 /* features[p] = log1p(radiance), albedo, normal, depth/(1+depth), 6 zeros
- * (16 BF16) from an RGBA32F frame and its G-buffers (8 floats per pixel). */
+ * (16 BF16, planar) from an RGBA32F frame and its G-buffers (8 floats per
+ * pixel); `pixels` is a whole number of rows of `width` pixels. */
 int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
-    uint16_t *out);
+    uint32_t width, uint16_t *out);
 /* out[p][co] = sum_tap,ci in[p+off(tap)][ci] * w[tap][co][ci] (zero padded),
  * with the epilogue above.  Instantiated for (cin, cout) = (16,48), (48,48),
  * (48,32) and, for data gradients, (48,48)/(32,48) with GBSP_DN_EPI_F32. */

@@ -36,27 +36,33 @@ def close(a, b, rtol=2e-2):
 def test_conv3x3_forward_matches_torch(gpu_lib, cin, cout, epi):
     import torch
 
-    from vk_cinematic_gb300.denoiser import _ptr, _stream
+    from vk_cinematic_gb300.denoiser import _ptr, _stream, from_planar, to_planar
 
     torch.manual_seed(cin * 100 + cout + epi)
     B, H, W = 2, 9, 70
     x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+    xp = to_planar(x)
     w = (torch.randn((9, cout, cin), device="cuda") * 0.2).to(torch.bfloat16)
     bias = torch.randn(cout, device="cuda")
     L = gbsp.load()
     if epi == 0:
-        out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device="cuda")
-        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), B, H, W, cin, _ptr(w), _ptr(bias), cout,
-                                       epi, _ptr(out), None)
+        out = torch.empty((B, H, cout // 8, W, 8), dtype=torch.bfloat16, device="cuda")
+        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), _ptr(bias),
+                                       cout, epi, _ptr(out), None)
         ref = torch.relu(torch_conv(x, w, bias))
-    else:
+    elif epi == 1:
         out = torch.empty((B, H, W, cout), dtype=torch.float32, device="cuda")
-        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(x), B, H, W, cin, _ptr(w),
-                                       _ptr(bias) if epi == 1 else None, cout, epi, None, _ptr(out))
-        ref = torch_conv(x, w, bias if epi == 1 else None)
+        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), _ptr(bias),
+                                       cout, epi, None, _ptr(out))
+        ref = torch_conv(x, w, bias)
+    else:
+        out = torch.empty((B, H, cout // 8, W, 8), dtype=torch.float32, device="cuda")
+        rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), None, cout,
+                                       epi, None, _ptr(out))
+        ref = torch_conv(x, w)
     assert rc == 0, L.gbsp_last_error_string()
     torch.cuda.synchronize()
-    err, ok = close(out, ref)
+    err, ok = close(out if epi == 1 else from_planar(out), ref)
     print(f"conv {cin}->{cout} epi {epi}: max rel err {err:.2e}")
     assert ok
 
@@ -70,23 +76,29 @@ def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, B, H, W)
     300-row image gives every CTA strips of 8 rows (the row ring wraps)."""
     import torch
 
-    from vk_cinematic_gb300.denoiser import _ptr, _stream
+    from vk_cinematic_gb300.denoiser import _ptr, _stream, from_planar, to_planar
 
     torch.manual_seed(cin * 100 + cout + epi + W)
     x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
+    xp = to_planar(x)
     w = (torch.randn((9, cout, cin), device="cuda") * 0.2).to(torch.bfloat16)
     bias = torch.randn(cout, device="cuda")
     L = gbsp.load()
     outs = []
     for fn in (L.gbsp_dn_conv3x3_forward_tc, L.gbsp_dn_conv3x3_forward):
         if epi == 0:
-            out = torch.full((B, H, W, cout), 7.0, dtype=torch.bfloat16, device="cuda")
-            rc = fn(_stream(), _ptr(x), B, H, W, cin, _ptr(w), _ptr(bias), cout, epi, _ptr(out),
+            out = torch.full((B, H, cout // 8, W, 8), 7.0, dtype=torch.bfloat16, device="cuda")
+            rc = fn(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), _ptr(bias), cout, epi, _ptr(out),
                     None)
-        else:
+            out = from_planar(out)
+        elif epi == 1:
             out = torch.full((B, H, W, cout), 7.0, dtype=torch.float32, device="cuda")
-            rc = fn(_stream(), _ptr(x), B, H, W, cin, _ptr(w), _ptr(bias) if epi == 1 else None,
-                    cout, epi, None, _ptr(out))
+            rc = fn(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), _ptr(bias), cout, epi, None,
+                    _ptr(out))
+        else:
+            out = torch.full((B, H, cout // 8, W, 8), 7.0, dtype=torch.float32, device="cuda")
+            rc = fn(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), None, cout, epi, None, _ptr(out))
+            out = from_planar(out)
         assert rc == 0, L.gbsp_last_error_string()
         outs.append(out)
     torch.cuda.synchronize()
@@ -107,7 +119,7 @@ def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, B, H, W)
 def test_conv_gradients_match_autograd(gpu_lib, wgrad, shape):
     import torch
 
-    from vk_cinematic_gb300.denoiser import KPCNN, _ptr, _stream
+    from vk_cinematic_gb300.denoiser import KPCNN, from_planar, to_planar
 
     torch.manual_seed(3)
     net = KPCNN(seed=1, wgrad=wgrad)
@@ -118,7 +130,7 @@ def test_conv_gradients_match_autograd(gpu_lib, wgrad, shape):
         d = (torch.randn((B, H, W, cout), device="cuda") * 0.1).to(torch.bfloat16)
         dw = torch.zeros((9, cout, cin), device="cuda")
         db = torch.zeros(cout, device="cuda")
-        net.weight_grad(li, x, d, dw, db)
+        net.weight_grad(li, to_planar(x), to_planar(d), dw, db)
         xr = x.float().clone().requires_grad_(True)
         wr = net.wb[li].float().clone().requires_grad_(True)
         br = torch.zeros(cout, device="cuda", requires_grad=True)
@@ -130,7 +142,7 @@ def test_conv_gradients_match_autograd(gpu_lib, wgrad, shape):
         print(f"{wgrad} {shape} layer {li}: dW rel err {err_w:.2e}, dB rel err {err_b:.2e}")
         assert ok_w and ok_b
         if li > 0:
-            dx = net.data_grad(li, d)
+            dx = from_planar(net.data_grad(li, to_planar(d)))
             torch.cuda.synchronize()
             err_x, ok_x = close(dx, xr.grad)
             print(f"layer {li}: dX rel err {err_x:.2e}")
@@ -140,7 +152,7 @@ def test_conv_gradients_match_autograd(gpu_lib, wgrad, shape):
 def test_filter_and_relmse_gradient_match_autograd(gpu_lib):
     import torch
 
-    from vk_cinematic_gb300.denoiser import KPCNN, _ptr, _stream
+    from vk_cinematic_gb300.denoiser import KPCNN, _ptr, _stream, from_planar
 
     torch.manual_seed(5)
     B, H, W = 2, 7, 9
@@ -149,11 +161,12 @@ def test_filter_and_relmse_gradient_match_autograd(gpu_lib):
     target = torch.rand((B, H, W, 4), device="cuda") * 2
     net = KPCNN(seed=0)
     out = net.filter(logits, noisy)
-    dlog = torch.empty((B, H, W, 32), dtype=torch.bfloat16, device="cuda")
+    dlog = torch.empty((B, H, 4, W, 8), dtype=torch.bfloat16, device="cuda")
     loss = torch.zeros(1, device="cuda")
     L = gbsp.load()
     assert L.gbsp_dn_relmse_backward(_stream(), _ptr(logits), _ptr(noisy), _ptr(target), B, H, W,
                                      _ptr(dlog), _ptr(loss)) == 0
+    dlog = from_planar(dlog)
     # reference
     lr = logits[..., :25].clone().requires_grad_(True)
     wts = torch.softmax(lr, dim=-1)
@@ -265,13 +278,13 @@ def test_tensor_core_weight_grad_is_deterministic(gpu_lib):
     order: two calls on the same inputs give bit-identical dW and dBias."""
     import torch
 
-    from vk_cinematic_gb300.denoiser import KPCNN
+    from vk_cinematic_gb300.denoiser import KPCNN, to_planar
 
     torch.manual_seed(5)
     net = KPCNN(seed=2, wgrad="mma")
     B, H, W, cin, cout = 2, 64, 96, 48, 48
-    x = torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16)
-    d = (torch.randn((B, H, W, cout), device="cuda") * 0.1).to(torch.bfloat16)
+    x = to_planar(torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16))
+    d = to_planar((torch.randn((B, H, W, cout), device="cuda") * 0.1).to(torch.bfloat16))
     outs = []
     for _ in range(2):
         dw = torch.zeros((9, cout, cin), device="cuda")

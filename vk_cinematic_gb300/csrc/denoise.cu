@@ -46,6 +46,15 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
     return *reinterpret_cast<uint32_t *>(&v);
 }
 
+// Activations and their gradients use a channel-group-planar layout,
+// [B][H][C/8][W][8]: each 8-channel group of an image row is a contiguous
+// plane of W x 16 bytes (BF16), so that one TMA box of a row's pixels is one
+// contiguous read.  Element (row = b H + y, x, c):
+__device__ __forceinline__ size_t cg_index(size_t row, int x, int c, int W, int C)
+{
+    return ((row * (size_t)(C / 8) + (size_t)(c / 8)) * (size_t)W + (size_t)x) * 8 + (size_t)(c % 8);
+}
+
 // 3: FP32 logits + bias fed straight into the 5x5 kernel-prediction filter
 enum Epilogue : int { kEpiBf16BiasRelu = 0, kEpiF32Bias = 1, kEpiF32 = 2, kEpiFilter = 3 };
 
@@ -82,7 +91,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const __nv_bfloat16 *__res
             int gy = y + ry - 1, gx = x0 + px - 1;
             uint32_t v = 0;
             if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                v = reinterpret_cast<const uint32_t *>(in)[((size_t)(b * H + gy) * W + gx) * (CIN / 2) + c2];
+                v = reinterpret_cast<const uint32_t *>(in)[cg_index((size_t)(b * H + gy), gx, 2 * c2, W, CIN) / 2];
             reinterpret_cast<uint32_t *>(sIn + (ry * SPX + px) * SIN)[c2] = v;
         }
         __syncthreads();
@@ -115,7 +124,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const __nv_bfloat16 *__res
         for (int half = 0; half < 2; half++) {
             int x = x0 + m0 + g + 8 * half;
             if (x >= W) continue;
-            size_t p = (size_t)row * W + x;
+            size_t p = (size_t)row * W + x;  // logits (FP32, NHWC)
 #pragma unroll
             for (int n = 0; n < COUT / 8; n++) {
                 int co = n * 8 + 2 * t;
@@ -127,9 +136,13 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const __nv_bfloat16 *__res
                 if (EPI == kEpiBf16BiasRelu) {
                     v0 = fmaxf(v0, 0.0f);
                     v1 = fmaxf(v1, 0.0f);
-                    reinterpret_cast<uint32_t *>(outB + p * COUT)[co / 2] = pack_bf16(v0, v1);
-                } else {
+                    reinterpret_cast<uint32_t *>(outB)[cg_index(row, x, co, W, COUT) / 2] =
+                        pack_bf16(v0, v1);
+                } else if (EPI == kEpiF32Bias) {
                     *reinterpret_cast<float2 *>(outF + p * COUT + co) = make_float2(v0, v1);
+                } else {
+                    *reinterpret_cast<float2 *>(outF + cg_index(row, x, co, W, COUT)) =
+                        make_float2(v0, v1);
                 }
             }
         }
@@ -323,9 +336,10 @@ __device__ __forceinline__ void tc_mma(uint32_t dTmem, uint64_t aDesc, uint64_t 
         :: "r"(dTmem), "l"(aDesc), "l"(bDesc), "r"(idesc), "r"(accumulate));
 }
 
-// Bias / ReLU / BF16 packing of one pixel's COUT accumulators and the store.
+// Bias / ReLU / BF16 packing of one pixel's COUT accumulators and the store:
+// BF16 activations and FP32 gradients channel-group-planar, FP32 logits NHWC.
 template <int COUT, int EPI>
-__device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
+__device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t row, int x, int W,
     const float *__restrict__ bias, __nv_bfloat16 *__restrict__ outB, float *__restrict__ outF)
 {
 #pragma unroll
@@ -338,10 +352,12 @@ __device__ __forceinline__ void conv_store(const uint32_t (&r)[COUT], size_t p,
             if (EPI == kEpiBf16BiasRelu) v[k] = fmaxf(v[k], 0.0f);
         }
         if (EPI == kEpiBf16BiasRelu) {
-            *reinterpret_cast<uint4 *>(outB + p * COUT + c) = make_uint4(pack_bf16(v[0], v[1]),
-                pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
+            *reinterpret_cast<uint4 *>(outB + cg_index(row, x, c, W, COUT)) = make_uint4(
+                pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]),
+                pack_bf16(v[6], v[7]));
         } else {
-            float4 *o = reinterpret_cast<float4 *>(outF + p * COUT + c);
+            float4 *o = reinterpret_cast<float4 *>(
+                EPI == kEpiF32Bias ? outF + (row * W + x) * COUT + c : outF + cg_index(row, x, c, W, COUT));
             o[0] = make_float4(v[0], v[1], v[2], v[3]);
             o[1] = make_float4(v[4], v[5], v[6], v[7]);
         }
@@ -592,11 +608,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_conv3x3_tc(const __grid_const
                         tmem_ld16(cols + (uint32_t)(j * COUT + c), *reinterpret_cast<uint32_t(*)[16]>(r + c));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
                     if (x < W && y < y1) {
-                        const size_t px = (size_t)(b * H + y) * W + x;
+                        const size_t row = (size_t)(b * H + y);
                         if constexpr (EPI == kEpiFilter)
-                            conv_filter_store<COUT>(r, px, x, y, W, H, sBias, noisy, outFilt);
+                            conv_filter_store<COUT>(r, row * W + x, x, y, W, H, sBias, noisy,
+                                outFilt);
                         else
-                            conv_store<COUT, EPI>(r, px, sBias, outB, outF);
+                            conv_store<COUT, EPI>(r, row, x, W, sBias, outB, outF);
                     }
                 }
                 asm volatile("tcgen05.fence::before_thread_sync;");
@@ -690,18 +707,17 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// TMA map of an NHWC BF16 activation tensor [B][H][W][cin] viewed as
-// [B][H][cin / 8][W][8] (dimension order 8 channels, pixel, channel group,
-// row, image; the channel-group stride, 16 B, is below the pixel stride):
-// one box = 8 channels x kTcSpx pixels x every channel group of one row,
-// written to shared memory as [group][pixel][8 channels], zero outside the
-// tensor.
+// TMA map of a channel-group-planar BF16 activation tensor [B][H][cin/8][W][8]
+// (dimension order: 8 channels, pixel, channel group, row, image): one box =
+// 8 channels x kTcSpx pixels x every channel group of one row, i.e. cin/8
+// contiguous 2,080-byte runs, written to shared memory as [group][pixel][8
+// channels], zero outside the tensor.
 static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin)
 {
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)cin / 8, (cuuint64_t)H, (cuuint64_t)B};
-    const cuuint64_t strides[4] = {(cuuint64_t)cin * 2, 16, (cuuint64_t)W * cin * 2,
+    const cuuint64_t strides[4] = {16, (cuuint64_t)W * 16, (cuuint64_t)W * cin * 2,
         (cuuint64_t)H * W * cin * 2};
     const cuuint32_t box[5] = {8, (cuuint32_t)kTcSpx, (cuuint32_t)cin / 8, 1, 1};
     const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
@@ -748,7 +764,7 @@ int launch_conv_tc(cudaStream_t s, int smCount, const void *in, int B, int H, in
 // Input features: log(1 + radiance), albedo, normal, depth/(1 + depth),
 // zero-padded to 16 channels.
 __global__ void k_features(const float4 *__restrict__ rad, const float4 *__restrict__ aov,
-    uint64_t n, __nv_bfloat16 *__restrict__ out)
+    uint64_t n, int W, __nv_bfloat16 *__restrict__ out)
 {
     uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (p >= n) return;
@@ -757,9 +773,13 @@ __global__ void k_features(const float4 *__restrict__ rad, const float4 *__restr
     float d = fmaxf(a.w, 0.0f);
     float f[16] = {log1pf(fmaxf(r.x, 0.0f)), log1pf(fmaxf(r.y, 0.0f)), log1pf(fmaxf(r.z, 0.0f)),
         a.x, a.y, a.z, nn.x, nn.y, nn.z, d / (1.0f + d), 0, 0, 0, 0, 0, 0};
-    uint32_t *o = reinterpret_cast<uint32_t *>(out + p * 16);
+    const size_t row = p / (uint64_t)W;
+    const int x = (int)(p % (uint64_t)W);
 #pragma unroll
-    for (int i = 0; i < 8; i++) o[i] = pack_bf16(f[2 * i], f[2 * i + 1]);
+    for (int g = 0; g < 2; g++)
+        *reinterpret_cast<uint4 *>(out + cg_index(row, x, 8 * g, W, 16)) = make_uint4(
+            pack_bf16(f[8 * g], f[8 * g + 1]), pack_bf16(f[8 * g + 2], f[8 * g + 3]),
+            pack_bf16(f[8 * g + 4], f[8 * g + 5]), pack_bf16(f[8 * g + 6], f[8 * g + 7]));
 }
 
 // w'[8 - tap][ci][co] = w[tap][co][ci]: weights of the data-gradient conv.
@@ -806,7 +826,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const __nv_bfloat16 *__re
         for (int i = threadIdx.x; i < STAGE * COUT; i += 128) {
             int k = i / COUT, co = i % COUT;
             uint64_t p = p0 + base + k;
-            sD[k][co] = p < N ? __bfloat162float(d[p * COUT + co]) : 0.0f;
+            sD[k][co] = p < N ? __bfloat162float(d[cg_index(p / W, (int)(p % W), co, W, COUT)]) : 0.0f;
         }
         for (int i = threadIdx.x; i < STAGE * CIN; i += 128) {
             int k = i / CIN, ci = i % CIN;
@@ -816,7 +836,7 @@ __global__ void __launch_bounds__(128) k_conv3x3_wgrad(const __nv_bfloat16 *__re
                 int x = (int)(p % W), y = (int)((p / W) % H);
                 int gx = x + dx, gy = y + dy;
                 if (gx >= 0 && gx < W && gy >= 0 && gy < H)
-                    v = __bfloat162float(in[(p + (int64_t)dy * W + dx) * CIN + ci]);
+                    v = __bfloat162float(in[cg_index(p / W + dy, gx, ci, W, CIN)]);
             }
             sI[k][ci] = v;
         }
@@ -880,14 +900,14 @@ __global__ void __launch_bounds__(288) k_conv3x3_wgrad_tc(const __nv_bfloat16 *_
         for (int i = tid; i < kWgTile * COUT; i += 288) {
             int k = i / COUT, co = i % COUT;
             int x = x0 + k;
-            sD[co][k] = x < W ? d[((size_t)row * W + x) * COUT + co] : __float2bfloat16_rn(0.0f);
+            sD[co][k] = x < W ? d[cg_index((size_t)row, x, co, W, COUT)] : __float2bfloat16_rn(0.0f);
         }
         for (int i = tid; i < 3 * (kWgTile + 2) * CIN; i += 288) {
             int ci = i % CIN, px = (i / CIN) % (kWgTile + 2), ry = i / (CIN * (kWgTile + 2));
             int gy = y + ry - 1, gx = x0 + px - 1;
             __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
             if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                v = in[((size_t)(b * H + gy) * W + gx) * CIN + ci];
+                v = in[cg_index((size_t)(b * H + gy), gx, ci, W, CIN)];
             sX[ry][ci][px] = v;
         }
         __syncthreads();
@@ -1089,12 +1109,12 @@ __global__ void k_relmse_bwd(const float *__restrict__ logits, const float4 *__r
             gk[k] = gx * c.x + gy * c.y + gz * c.z;
             dot += w[k] * gk[k];
         }
-        uint32_t *o32 = reinterpret_cast<uint32_t *>(dLogits + p * 32);
+        const size_t row = p / (uint64_t)W;
 #pragma unroll
         for (int k = 0; k < 32; k += 2) {
             float v0 = k < 25 ? w[k] * (gk[k] - dot) : 0.0f;
             float v1 = k + 1 < 25 ? w[k + 1] * (gk[k + 1] - dot) : 0.0f;
-            o32[k / 2] = pack_bf16(v0, v1);
+            reinterpret_cast<uint32_t *>(dLogits)[cg_index(row, x, k, W, 32) / 2] = pack_bf16(v0, v1);
         }
     }
     for (int off = 16; off; off >>= 1) loss += __shfl_xor_sync(0xFFFFFFFFu, loss, off);
@@ -1160,13 +1180,15 @@ static int launch_wgrad_tc(cudaStream_t s, const __nv_bfloat16 *in, const __nv_b
 extern "C" {
 
 int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
-    uint16_t *out)
+    uint32_t width, uint16_t *out)
 {
     if (!radiance || !aov || !out) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!pixels) return GBSP_OK;
+    if (!width || pixels % width)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "pixels must be whole rows of `width`");
     k_features<<<blocks(pixels, 256), 256, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<const float4 *>(radiance), reinterpret_cast<const float4 *>(aov), pixels,
-        reinterpret_cast<__nv_bfloat16 *>(out));
+        (int)width, reinterpret_cast<__nv_bfloat16 *>(out));
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }

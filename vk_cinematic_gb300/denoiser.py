@@ -43,6 +43,24 @@ def _check(rc):
     gbsp._check(rc)
 
 
+def to_planar(t):
+    """NHWC (B, H, W, C) -> the kernels' channel-group-planar (B, H, C/8, W, 8)."""
+    B, H, W, C = t.shape
+    return t.reshape(B, H, W, C // 8, 8).permute(0, 1, 3, 2, 4).contiguous()
+
+
+def from_planar(t):
+    """Channel-group-planar (B, H, C/8, W, 8) -> NHWC (B, H, W, C)."""
+    B, H, G, W, _ = t.shape
+    return t.permute(0, 1, 3, 2, 4).reshape(B, H, W, G * 8)
+
+
+def _dims(t):
+    """(B, H, W, C) of a channel-group-planar activation tensor."""
+    B, H, G, W, _ = t.shape
+    return B, H, W, G * 8
+
+
 def relmse(x, ref):
     """mean over pixels and RGB of (x - ref)^2 / (ref^2 + 0.01)."""
     import torch
@@ -96,19 +114,19 @@ class KPCNN:
         import torch
 
         B, H, W, _ = radiance.shape
-        f = torch.empty((B, H, W, FEATURE_CHANNELS), dtype=torch.bfloat16, device="cuda")
+        f = torch.empty((B, H, FEATURE_CHANNELS // 8, W, 8), dtype=torch.bfloat16, device="cuda")
         _check(self.L.gbsp_dn_features(_stream(), _ptr(radiance), _ptr(aov), _u64(B * H * W),
-                                       _ptr(f)))
+                                       _u32(W), _ptr(f)))
         return f
 
     def conv(self, li, x, keep_f32=False):
         import torch
 
-        B, H, W, cin = x.shape
+        B, H, W, cin = _dims(x)
         _, cout, _ = self.wb[li].shape
         epi = LAYERS[li][2]
         if epi == 0:
-            out = torch.empty((B, H, W, cout), dtype=torch.bfloat16, device="cuda")
+            out = torch.empty((B, H, cout // 8, W, 8), dtype=torch.bfloat16, device="cuda")
             _check(self._conv(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W), _u32(cin),
                               _ptr(self.wb[li]), _ptr(self.b[li]), _u32(cout), _int(0), _ptr(out),
                               None))
@@ -150,7 +168,7 @@ class KPCNN:
         last = len(LAYERS) - 1
         for li in range(last):
             x = self.conv(li, x)
-        B, H, W, cin = x.shape
+        B, H, W, cin = _dims(x)
         noisy = radiance.contiguous()
         out = torch.empty((B, H, W, 4), dtype=torch.float32, device="cuda")
         _check(self.L.gbsp_dn_conv3x3_filter_tc(_stream(), _ptr(x), _u32(B), _u32(H), _u32(W),
@@ -181,22 +199,23 @@ class KPCNN:
 
     # ---- training ------------------------------------------------------------------
     def data_grad(self, li, d):
-        """dIn of layer li from its output gradient d (BF16), FP32."""
+        """dIn of layer li from its output gradient d (BF16), FP32; both
+        channel-group-planar."""
         import torch
 
-        B, H, W, cout = d.shape
+        B, H, W, cout = _dims(d)
         _, _, cin = self.wb[li].shape
         wt = torch.empty((9, cin, cout), dtype=torch.bfloat16, device="cuda")
         _check(self.L.gbsp_dn_flip_transpose(_stream(), _ptr(self.wb[li]), _u32(cout), _u32(cin),
                                              _ptr(wt)))
-        out = torch.empty((B, H, W, cin), dtype=torch.float32, device="cuda")
+        out = torch.empty((B, H, cin // 8, W, 8), dtype=torch.float32, device="cuda")
         _check(self._conv(_stream(), _ptr(d), _u32(B), _u32(H), _u32(W), _u32(cout), _ptr(wt),
                           None, _u32(cin), _int(2), None, _ptr(out)))
         return out
 
     def weight_grad(self, li, x, d, dw, db):
-        B, H, W, cin = x.shape
-        cout = d.shape[-1]
+        B, H, W, cin = _dims(x)
+        cout = _dims(d)[3]
         _check(self._wgrad(_stream(), _ptr(x), _ptr(d), _u32(B), _u32(H), _u32(W), _u32(cin),
                            _u32(cout), _ptr(dw), _ptr(db)))
 
@@ -206,7 +225,7 @@ class KPCNN:
 
         B, H, W, _ = noisy.shape
         logits, acts = self.forward(feats, keep=True)
-        dlog = torch.empty((B, H, W, 32), dtype=torch.bfloat16, device="cuda")
+        dlog = torch.empty((B, H, 4, W, 8), dtype=torch.bfloat16, device="cuda")
         loss = torch.zeros(1, dtype=torch.float32, device="cuda")
         _check(self.L.gbsp_dn_relmse_backward(_stream(), _ptr(logits), _ptr(noisy), _ptr(target),
                                               _u32(B), _u32(H), _u32(W), _ptr(dlog), _ptr(loss)))
