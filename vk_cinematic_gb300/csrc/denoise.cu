@@ -897,18 +897,27 @@ __global__ void __launch_bounds__(288) k_conv3x3_wgrad_tc(const __nv_bfloat16 *_
         const int row = tile / segs, x0 = (tile % segs) * kWgTile;
         const int b = row / H, y = row % H;
         __syncthreads();
-        for (int i = tid; i < kWgTile * COUT; i += 288) {
-            int k = i / COUT, co = i % COUT;
-            int x = x0 + k;
-            sD[co][k] = x < W ? d[cg_index((size_t)row, x, co, W, COUT)] : __float2bfloat16_rn(0.0f);
+        // staging: one 16-byte load per (pixel, 8-channel group) of the planar
+        // tensors (consecutive threads take consecutive pixels of one plane),
+        // spread over the transposed [channel][pixel] tiles
+        for (int i = tid; i < kWgTile * (COUT / 8); i += 288) {
+            const int k = i % kWgTile, cg = i / kWgTile, x = x0 + k;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (x < W) v = *reinterpret_cast<const uint4 *>(d + cg_index((size_t)row, x, 8 * cg, W, COUT));
+            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) sD[8 * cg + j][k] = e[j];
         }
-        for (int i = tid; i < 3 * (kWgTile + 2) * CIN; i += 288) {
-            int ci = i % CIN, px = (i / CIN) % (kWgTile + 2), ry = i / (CIN * (kWgTile + 2));
-            int gy = y + ry - 1, gx = x0 + px - 1;
-            __nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+        for (int i = tid; i < 3 * (kWgTile + 2) * (CIN / 8); i += 288) {
+            const int px = i % (kWgTile + 2), cg = (i / (kWgTile + 2)) % (CIN / 8);
+            const int ry = i / ((kWgTile + 2) * (CIN / 8));
+            const int gy = y + ry - 1, gx = x0 + px - 1;
+            uint4 v = make_uint4(0, 0, 0, 0);
             if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                v = in[cg_index((size_t)(b * H + gy), gx, ci, W, CIN)];
-            sX[ry][ci][px] = v;
+                v = *reinterpret_cast<const uint4 *>(in + cg_index((size_t)(b * H + gy), gx, 8 * cg, W, CIN));
+            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+            for (int j = 0; j < 8; j++) sX[ry][8 * cg + j][px] = e[j];
         }
         __syncthreads();
         if (tid < COUT) {
