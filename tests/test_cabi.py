@@ -88,3 +88,22 @@ def test_invalid_arguments_return_status():
     assert b"NULL" in lib.gbsp_last_error_string()
     assert lib.gbsp_scene_create(None, None) == -1
     assert lib.gbsp_icosphere(11, None, None, None, None) == -3
+
+
+def test_denoiser_planar_layout_round_trip():
+    """The denoiser kernels take activations channel-group-planar,
+    [B][H][C/8][W][8]; the host helpers convert NHWC to that layout and back,
+    and element (b, y, x, c) lands at ((b H + y) C/8 + c/8) W + x) 8 + c % 8."""
+    import torch
+
+    from vk_cinematic_gb300.denoiser import from_planar, to_planar
+
+    B, H, W, C = 2, 3, 5, 24
+    t = torch.arange(B * H * W * C, dtype=torch.float32).reshape(B, H, W, C)
+    p = to_planar(t)
+    assert p.shape == (B, H, C // 8, W, 8) and p.is_contiguous()
+    assert torch.equal(from_planar(p), t)
+    flat = p.reshape(-1)
+    for b, y, x, c in ((0, 0, 0, 0), (1, 2, 4, 23), (0, 1, 3, 9), (1, 0, 2, 16)):
+        idx = (((b * H + y) * (C // 8) + c // 8) * W + x) * 8 + c % 8
+        assert flat[idx].item() == t[b, y, x, c].item()
