@@ -196,11 +196,13 @@ int launch_conv(cudaStream_t s, int smCount, const void *in, int B, int H, int W
 // segment, a run of rows) with its warps specialised and coupled only by
 // mbarriers:
 //   * lane 0 of warp 1 (producer) loads input rows into a ring of kTcRing
-//     slots with TMA (cp.async.bulk.tensor, one 130-pixel x 8-channel box
-//     per channel group, zero outside the image), as many rows in flight as
-//     the ring allows; a row lands on its rowFull barrier by transaction
-//     count, and its slot is reused once the MMAs of the last row group that
-//     reads it have completed (rowEmpty, signalled by tcgen05.commit);
+//     slots with TMA (cp.async.bulk.tensor: one box of 130 pixels x every
+//     channel group per row, which in the channel-group-planar activation
+//     layout is CIN/8 contiguous 2,080-byte runs; zero outside the image),
+//     as many rows in flight as the ring allows; a row lands on its rowFull
+//     barrier by transaction count, and its slot is reused once the MMAs of
+//     the last row group that reads it have completed (rowEmpty, signalled
+//     by tcgen05.commit);
 //   * lane 0 of warp 0 issues, per group of kTcGroupRows output rows, the
 //     (kTcGroupRows + 2) x 3 x CIN/16 MMAs reading its input rows into one
 //     TMEM accumulator, then commits to that accumulator's accFull and to the
@@ -218,7 +220,7 @@ constexpr int kTcTileP = 128;
 // two epilogue groups that take alternate row groups.
 constexpr int kTcThreads = 384;
 constexpr int kTcEpiGroups = 2;
-constexpr int kTcAccSlots = 4;  // accumulator a is drained by epilogue group a % 2
+constexpr int kTcAccSlots = 4;  // at most; accumulator a is drained by epilogue group a % 2
 constexpr int kTcSpx = kTcTileP + 2;     // staged pixels per row: x0 - 1 .. x0 + 128
 constexpr int kTcPlane = kTcSpx;         // pixels per channel-group plane of a ring slot
 constexpr int kTcGroupRows = 4;  // output rows per accumulator
