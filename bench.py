@@ -135,18 +135,50 @@ def measured_bf16_peak():
     return 1900.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per ray of the closest-hit kernels from the committed ncu
-    summary profiles/trace_kernel_dram.md (its `dram_bytes_per_ray:` line);
-    the bench scales it to this run's rays per launch.  None if absent."""
-    p = os.path.join(ROOT, "profiles", "trace_kernel_dram.md")
+def profiled_counters():
+    """Per-ray counters of the closest-hit kernels (k_trace + k_trace_lane)
+    from the committed ncu summary profiles/trace_kernel_counters.md: its
+    `name: value` lines (dram_bytes_per_ray, l2_bytes_per_ray,
+    issue_slots_busy, threads_per_inst, ...).  The bench scales the per-ray
+    byte counts to this run's rays per launch.  Empty if absent."""
+    p = os.path.join(ROOT, "profiles", "trace_kernel_counters.md")
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
     with open(p) as f:
         for line in f:
-            if line.strip().startswith("dram_bytes_per_ray:"):
-                return {"dram_bytes_per_ray": float(line.split(":", 1)[1])}
-    return None
+            k, sep, v = line.strip().partition(":")
+            if sep and k and " " not in k:
+                try:
+                    out[k] = float(v)
+                except ValueError:
+                    pass
+    return out
+
+
+def measure_l2_peak(stream, reps=50):
+    """L2-resident copy bandwidth (GB/s, read + write bytes): a 24 MB buffer
+    copied back and forth between two device buffers that together fit in the
+    129 MB L2, timed with CUDA events on `stream` after a warm-up.  The
+    denominator of the closest-hit kernels' L2 fraction."""
+    import torch
+
+    n = 24 << 20
+    a = torch.empty(n, dtype=torch.uint8, device="cuda")
+    b = torch.empty(n, dtype=torch.uint8, device="cuda")
+    a.fill_(1)
+    for _ in range(5):
+        b.copy_(a)
+        a.copy_(b)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.copy_(a)
+        a.copy_(b)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return 2 * reps * 2 * n / (ms * 1e-3) / 1e9
 
 
 class ClockSampler:
@@ -232,46 +264,69 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_baseline_run(s, seconds_target, threads=None):
-    """The oracle port in the reference's tile mode (64x64 tiles, RNG reset to
-    0xF51C0E49 per tile, src/main.cpp:731-759) on a bounded, evenly spread
-    subset of the frame's tiles.  Returns a dict in the bench format."""
+def spread_tiles(total, n):
+    """n distinct tile ids spread evenly over the frame's `total` tiles
+    (row-major tile order), so that a sample sees sky, spheres and ground in
+    the frame's own proportions."""
+    n = max(1, min(total, n))
+    return [int((k + 0.5) * total / n) for k in range(n)]
+
+
+def cpu_tile_count(per_tile_s, seconds_target, threads, total):
+    """Tiles per CPU sample: about `seconds_target` of work, rounded up to a
+    whole number of waves of `threads` tiles so no thread idles at the end."""
+    n = max(1, int(seconds_target / max(per_tile_s, 1e-6) * threads))
+    n = -(-n // threads) * threads
+    return min(total, n)
+
+
+def _cpu_world(s):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import pyoracle as po
     from golden_scenes import build_world
 
     po.build_port()
-    threads = threads or os.cpu_count() or 1
-    t0 = time.time()
     w = build_world("port", s)
     if s.sky is not None:
         w.set_sky(s.sky)
     w.set_options(spp=s.spp, max_bounces=s.max_bounces, max_broadphase=1 << 16,
                   max_midphase=1 << 20)
-    setup_s = time.time() - t0
+    return w
+
+
+def _cpu_calibrate(w, s, threads, pixels):
+    """Seconds per tile per thread, from one wave of `threads` spread tiles."""
     tiles_x = (s.width + 63) // 64
-    tiles_y = (s.height + 63) // 64
-    total_tiles = tiles_x * tiles_y
+    total = tiles_x * ((s.height + 63) // 64)
+    ids = spread_tiles(total, threads)
+    dt, _, _ = w.render_tile_list(s.width, s.height, s.camera_position, s.camera_rotation,
+                                  s.film_distance, 64, ids, threads, pixels)
+    return dt * threads / len(ids), total
+
+
+def cpu_baseline_run(s, seconds_target, threads=None):
+    """The oracle port in the reference's tile mode (64x64 tiles, RNG reset to
+    0xF51C0E49 per tile, src/main.cpp:731-759) on a bounded sample of the
+    frame's tiles spread evenly over the frame.  Returns a dict in the bench
+    format."""
+    threads = threads or os.cpu_count() or 1
+    t0 = time.time()
+    w = _cpu_world(s)
+    setup_s = time.time() - t0
     pixels = np.zeros((s.height, s.width, 4), np.float32)
-    # calibrate on a few tiles in the middle of the frame
-    cal = max(1, min(threads, total_tiles))
-    first = total_tiles // 2
-    dt, _, m = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
-                                 s.film_distance, 64, first, cal, threads, pixels)
-    per_tile = dt / cal
-    n = int(max(cal, min(total_tiles, seconds_target / max(per_tile, 1e-6))))
-    # evenly spread contiguous runs: render n tiles starting at a centred offset
-    start = max(0, (total_tiles - n) // 2)
-    dt, _, m = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
-                                 s.film_distance, 64, start, n, threads, pixels)
+    per_tile, total_tiles = _cpu_calibrate(w, s, threads, pixels)
+    n = cpu_tile_count(per_tile, seconds_target, threads, total_tiles)
+    ids = spread_tiles(total_tiles, n)
+    dt, _, m = w.render_tile_list(s.width, s.height, s.camera_position, s.camera_rotation,
+                                  s.film_distance, 64, ids, threads, pixels)
     paths, rays = int(m[1]), int(m[2])
     return {
         "value": paths / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
         "mrays_per_s": rays / dt / 1e6,
-        "sample": (f"{n} of {total_tiles} 64x64 tiles (tiles {start}..{start + n - 1}) at "
-                   f"{s.spp} spp, {paths} paths, {rays} rays in {dt:.2f} s; "
-                   f"reference tile-mode RNG; BVH/scene setup {setup_s:.1f} s untimed"),
+        "sample": (f"{n} of {total_tiles} 64x64 tiles spread evenly over the frame "
+                   f"({n // threads} per thread) at {s.spp} spp, {paths} paths, {rays} rays in "
+                   f"{dt:.2f} s; reference tile-mode RNG; BVH/scene setup {setup_s:.1f} s untimed"),
         "seconds": dt,
     }
 
@@ -281,35 +336,21 @@ def run_reference(args):
     if world > 1 and rank != 0:
         return 0
     s = make_scene(args.workload)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import pyoracle as po
-    from golden_scenes import build_world
-
-    po.build_port()
     threads = os.cpu_count() or 1
-    w = build_world("port", s)
-    if s.sky is not None:
-        w.set_sky(s.sky)
-    w.set_options(spp=s.spp, max_bounces=s.max_bounces, max_broadphase=1 << 16,
-                  max_midphase=1 << 20)
-    tiles_x = (s.width + 63) // 64
-    total = tiles_x * ((s.height + 63) // 64)
+    w = _cpu_world(s)
     pixels = np.zeros((s.height, s.width, 4), np.float32)
-    dt, _, _ = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
-                                 s.film_distance, 64, total // 2, threads, threads, pixels)
-    per_tile = dt / threads
-    # each step renders a fixed run of tiles sized to about 4 s of work
-    n = int(max(threads, min(total, 4.0 / max(per_tile, 1e-6))))
-    start = max(0, (total - n) // 2)
+    per_tile, total = _cpu_calibrate(w, s, threads, pixels)
+    # each step renders the same spread tile sample, about 4 s of work
+    n = cpu_tile_count(per_tile, 4.0, threads, total)
+    ids = spread_tiles(total, n)
     for _ in range(args.warmup):
-        w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
-                          s.film_distance, 64, start, n, threads, pixels)
+        w.render_tile_list(s.width, s.height, s.camera_position, s.camera_rotation,
+                           s.film_distance, 64, ids, threads, pixels)
     paths = rays = 0
     elapsed = 0.0
     for _ in range(args.steps):
-        dt, _, m = w.render_tiles_mt(s.width, s.height, s.camera_position, s.camera_rotation,
-                                     s.film_distance, 64, start, n, threads, pixels)
+        dt, _, m = w.render_tile_list(s.width, s.height, s.camera_position, s.camera_rotation,
+                                      s.film_distance, 64, ids, threads, pixels)
         elapsed += dt
         paths += int(m[1])
         rays += int(m[2])
@@ -322,7 +363,8 @@ def run_reference(args):
         "data": "synthetic: seeded procedural scene", "config": workload_config(s, args.workload),
         "mrays_per_s": rays / elapsed / 1e6,
         "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port",
-                         "sample": f"{n} of {total} 64x64 tiles per step at {s.spp} spp "
+                         "sample": f"{n} of {total} 64x64 tiles per step spread evenly over the "
+                                   f"frame ({n // threads} per thread) at {s.spp} spp "
                                    f"(reference tile-mode RNG)"},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -390,14 +432,34 @@ def run_gpu(args):
                  + (M["broadphase_node_visits"] + M["midphase_node_visits"]) * NODE_BYTES
                  + M["triangle_tests"] * TRI_BYTES)
     achieved = (alg_bytes / launches) / (trace_s / launches) / 1e9 if trace_s > 0 else None
-    traffic = None
-    tp = profiled_traffic()
-    if tp and tp.get("dram_bytes_per_ray"):
-        traffic = tp["dram_bytes_per_ray"] * M["rays_traced"] / launches
+    prof = profiled_counters()
+    rays_per_launch = M["rays_traced"] / launches
+    mean_launch_s = trace_s / launches if trace_s > 0 else None
+    traffic = (prof["dram_bytes_per_ray"] * rays_per_launch
+               if "dram_bytes_per_ray" in prof else None)
+    l2_peak = measure_l2_peak(stream)
+    l2 = None
+    if "l2_bytes_per_ray" in prof and mean_launch_s:
+        l2_gbs = prof["l2_bytes_per_ray"] * rays_per_launch / mean_launch_s / 1e9
+        l2 = {"achieved": l2_gbs, "peak": l2_peak, "unit": "GB/s", "frac": l2_gbs / l2_peak,
+              "peak_source": "measured live: L2-resident 24 MB device copy (torch), read + write",
+              "bytes_per_ray_source": "ncu lts__t_bytes.sum per ray, "
+                                      "profiles/trace_kernel_counters.md"}
     roofline = {
-        "bound": "hbm", "kernel": "k_trace (closest hit)", "achieved": achieved, "peak": peak,
+        "bound": "latency/L2",
+        "bound_detail": ("closest-hit traversal of an L1/L2-resident BVH: bound by load "
+                         "latency and issue, not by HBM; `achieved`/`frac` are the kernel's "
+                         "algorithmic fetch rate against the HBM copy peak, `l2` its L2 "
+                         "traffic against the measured L2 copy rate, `issue` its issue-slot "
+                         "use from ncu"),
+        "kernel": "k_trace + k_trace_lane (closest hit)", "achieved": achieved, "peak": peak,
         "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
         "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+        "l2": l2,
+        "issue": ({"issue_slots_busy": prof.get("issue_slots_busy"),
+                   "threads_per_inst": prof.get("threads_per_inst"),
+                   "source": "ncu, profiles/trace_kernel_counters.md"}
+                  if "issue_slots_busy" in prof else None),
         "bytes_per_launch": alg_bytes / launches, "mean_launch_ms": 1e3 * trace_s / launches,
         "trace_share_of_frame": (M["intersect_scene_ns"] / 1e6) / max(elapsed_ms, 1e-9),
         "per_ray": {"node_visits": (M["broadphase_node_visits"] + M["midphase_node_visits"])
@@ -569,6 +631,8 @@ def run_config2(args):
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     total_ms = 0.0
+    clocks = ClockSampler(0)
+    clocks.start()
     for _ in range(args.steps):
         flush.zero_()
         ev0.record(stream)
@@ -576,8 +640,28 @@ def run_config2(args):
         ev1.record(stream)
         torch.cuda.synchronize()
         total_ms += ev0.elapsed_time(ev1)
+    clk = clocks.stop()
     rt.synchronize()
     hit_frac = float((tri >= 0).float().mean().item())
+    # the traversal's node visits and triangle tests for the same rays (the
+    # host-buffer query runs the same kernel and fills the metric counters)
+    _, _, mq = scene.intersect(rays)
+    M = mq.as_dict()
+    peak, peak_kind = measured_peaks()
+    alg_bytes = (n * TRACE_BYTES_PER_RAY
+                 + (M["broadphase_node_visits"] + M["midphase_node_visits"]) * NODE_BYTES
+                 + M["triangle_tests"] * TRI_BYTES)
+    launch_ms = total_ms / args.steps
+    achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+    roofline = {
+        "bound": "latency/L1-L2 (BVH fetches mostly on chip; view against the HBM copy peak)",
+        "kernel": "k_trace_lane (closest hit, one launch per step)", "achieved": achieved,
+        "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+        "peak_source": f"{peak_kind} hbm_gbs", "bytes_per_launch": alg_bytes,
+        "mean_launch_ms": launch_ms,
+        "per_ray": {"node_visits": (M["broadphase_node_visits"] + M["midphase_node_visits"]) / n,
+                    "triangle_tests": M["triangle_tests"] / n},
+    }
     line = {
         "metric": "Mrays/s closest hit (config 2)", "value": n * args.steps / total_ms / 1e3,
         "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -589,6 +673,7 @@ def run_config2(args):
                    "l2": "flushed (256 MB device write) before every timed step; kernel time "
                          "only (CUDA events around the launch)"},
         "hit_fraction": hit_frac, "device_bvh_build_and_upload_s": build_s,
+        "roofline": roofline, "clocks": clk, "gpu_launches": args.steps * 2,
     }
     print(json.dumps(line), flush=True)
     return 0

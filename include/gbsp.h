@@ -278,7 +278,13 @@ int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics);
  * array's device address (cudaGetSymbolAddress), so make that first call
  * before any stream capture.  All calls share the array: calls that overlap
  * on the GPU (other threads, other runtimes on the same device) race and
- * must be serialised by the caller.  The call waits for its own work. */
+ * must be serialised by the caller.  The call waits for its own work and
+ * leaves the caller's current device as it found it.  Options: the trace
+ * scheduling flags apply as in gbsp_path_trace_tile; GBSP_FLAG_AOV is
+ * rejected (GBSP_ERR_INVALID_ARGUMENT: no G-buffer output here);
+ * GBSP_FLAG_SORT_DIRECTIONS and GBSP_FLAG_STAGE_TIMING have no effect, so
+ * the ELAPSED_NS, INTERSECT_SCENE_NS and SHADE_NS metric slots stay zero;
+ * every other metric slot is filled as by gbsp_path_trace_tile. */
 int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile tile,
     float *deviceImage, gbsp_metrics *metrics);
 /* Device pointer of the runtime's last frame (width*height RGBA32F). */

@@ -23,7 +23,15 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libspref.so")
-DEFAULT_REFERENCE = "/root/reference"
+# Where the reference checkout is looked for: $VK_CINEMATIC_REFERENCE, else
+# the location it is mounted at in the build container.  Only the reference
+# harness build reads it; nothing on a GPU host needs the reference.
+REFERENCE_ENV = "VK_CINEMATIC_REFERENCE"
+MOUNTED_REFERENCE = "/root/reference"
+
+
+def reference_root() -> str:
+    return os.environ.get(REFERENCE_ENV) or MOUNTED_REFERENCE
 
 _f = ctypes.c_float
 _u32 = ctypes.c_uint32
@@ -39,11 +47,12 @@ def build_port() -> str:
     return PORT_LIB
 
 
-def build_ref(reference: str = DEFAULT_REFERENCE) -> str | None:
+def build_ref(reference: str | None = None) -> str | None:
     """Compile the reference harness when the reference tree is present on an
     x86-64 host; returns the library path or None."""
     import platform
 
+    reference = reference or reference_root()
     if not os.path.isdir(os.path.join(reference, "src")):
         return None
     if platform.machine() not in ("x86_64", "AMD64"):
@@ -122,7 +131,7 @@ class _Lib:
             fn = getattr(self.lib, self.prefix + name, None)
             if fn is not None:
                 fn.restype = res
-        for name in ("world_render_tiles_mt", "world_render_hashed_mt"):
+        for name in ("world_render_tiles_mt", "world_render_hashed_mt", "world_render_tile_list"):
             fn = getattr(self.lib, self.prefix + name, None)
             if fn is not None:
                 fn.restype = _d
@@ -318,17 +327,21 @@ class World:
             raise RuntimeError(f"intersect failed {rc}")
         return out, mat, metrics
 
-    def closest(self, rays):
+    def closest(self, rays, ties=False):
+        """(t, object, triangle) per ray through the reference's scene query;
+        with ties=True also a bool array flagging rays whose best t is an
+        exact tie between two candidates."""
         assert self.kind == "port"
         rays = _f32(rays).reshape(-1, 6)
         t = np.zeros(len(rays), np.float32)
         obj = np.zeros(len(rays), np.int32)
         tri = np.zeros(len(rays), np.int32)
+        tied = np.zeros(len(rays), np.int32)
         rc = self.L.fn("world_closest")(self.h, _u32(len(rays)), _p(rays), _p(t), _p(obj),
-                                        _p(tri))
+                                        _p(tri), _p(tied))
         if rc != 0:
             raise RuntimeError(f"closest failed {rc}")
-        return t, obj, tri
+        return (t, obj, tri, tied.astype(bool)) if ties else (t, obj, tri)
 
     def set_build_bvh(self, on: bool):
         assert self.kind == "port"
@@ -339,16 +352,18 @@ class World:
         assert self.kind == "port"
         self.L.fn("world_set_watertight")(self.h, _i32(int(on)))
 
-    def closest_brute(self, rays, threads=None):
+    def closest_brute(self, rays, threads=None, ties=False):
+        """Brute-force closest hit over every triangle; ties as in closest()."""
         assert self.kind == "port"
         rays = _f32(rays).reshape(-1, 6)
         t = np.zeros(len(rays), np.float32)
         obj = np.zeros(len(rays), np.int32)
         tri = np.zeros(len(rays), np.int32)
+        tied = np.zeros(len(rays), np.int32)
         threads = threads or os.cpu_count() or 1
         self.L.fn("world_closest_brute")(self.h, _u32(len(rays)), _p(rays), _u32(threads), _p(t),
-                                         _p(obj), _p(tri))
-        return t, obj, tri
+                                         _p(obj), _p(tri), _p(tied))
+        return (t, obj, tri, tied.astype(bool)) if ties else (t, obj, tri)
 
     def path_trace_tile(self, width, height, cam_pos, cam_rot, film, tile, rng_state, pixels=None):
         if pixels is None:
@@ -407,6 +422,23 @@ class World:
             _p(pixels), _p(metrics))
         if dt < 0:
             raise RuntimeError("render_tiles_mt: a capacity of the reference overflowed")
+        return dt, pixels, metrics
+
+    def render_tile_list(self, width, height, cam_pos, cam_rot, film, tile_size, tile_ids,
+                         threads, pixels=None):
+        """The reference's tile mode over an explicit list of tile ids (row-major
+        tile order), `threads` workers popping tiles from a shared counter."""
+        assert self.kind == "port"
+        if pixels is None:
+            pixels = np.zeros((height, width, 4), np.float32)
+        ids = np.ascontiguousarray(tile_ids, dtype=np.uint32)
+        metrics = np.zeros(12, np.uint64)
+        dt = self.L.fn("world_render_tile_list")(
+            self.h, _u32(width), _u32(height), _p(_f32(cam_pos, 3)), _p(_f32(cam_rot, 4)),
+            _f(film), _u32(tile_size), _p(ids), _u32(len(ids)), _u32(threads), _p(pixels),
+            _p(metrics))
+        if dt < 0:
+            raise RuntimeError("render_tile_list: a capacity of the reference overflowed")
         return dt, pixels, metrics
 
     def render_hashed_mt(self, width, height, cam_pos, cam_rot, film, seed, row_begin, row_end,

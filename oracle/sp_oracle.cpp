@@ -770,6 +770,9 @@ struct MeshHit
 {
     TriHit hit;
     int32_t triangle;
+    // another candidate of this mesh hit at exactly hit.t (the reference's
+    // strict '<' keeps the first one found, so the winner is order-dependent)
+    bool tied;
 };
 
 // sp_scene.cpp:127-227; returns -100 style errors through ok=false
@@ -779,6 +782,7 @@ MeshHit intersect_mesh(const World &w, const Mesh &mesh, F3 o, F3 d,
     MeshHit best = {};
     best.hit.t = -1.0f;
     best.triangle = -1;
+    best.tied = false;
     s.leaves.resize(w.opt.max_midphase);
     BvhQuery q = bvh_query(mesh.tree, o, d, s.leaves.data(), w.opt.max_midphase,
         &s.stackA, &s.stackB);
@@ -791,10 +795,12 @@ MeshHit intersect_mesh(const World &w, const Mesh &mesh, F3 o, F3 d,
         TriHit h = ray_triangle_mt(o, d, mesh.pos[i0], mesh.pos[i1], mesh.pos[i2]);
         if (h.t > 0.0f)
         {
+            if (h.t == best.hit.t) best.tied = true;
             if (h.t < best.hit.t || best.hit.t < 0.0f)
             {
                 best.hit = h;
                 best.triangle = (int32_t)tri;
+                best.tied = false;
                 float wgt = 1.0f - h.uv.x - h.uv.y;
                 F2 uv;
                 uv.x = mesh.uv[i0].x * wgt + mesh.uv[i1].x * h.uv.x + mesh.uv[i2].x * h.uv.y;
@@ -818,6 +824,9 @@ struct SceneHit
     F3 normal;
     F2 uv;
     int32_t object, triangle;
+    // the best t is an exact tie: two objects at the same world t, or two
+    // triangles of the winning object at the same object-space t
+    bool tied;
 };
 
 // sp_scene.cpp:229-339
@@ -828,6 +837,7 @@ SceneHit intersect_scene(const World &w, F3 o, F3 d, QueryScratch &s,
     r.t = -1.0f;
     r.object = -1;
     r.triangle = -1;
+    r.tied = false;
     s.objects.resize(w.opt.max_broadphase);
     BvhQuery q = bvh_query(w.broadphase, o, d, s.objects.data(), w.opt.max_broadphase,
         &s.stackA, &s.stackB);
@@ -846,8 +856,10 @@ SceneHit intersect_scene(const World &w, F3 o, F3 d, QueryScratch &s,
             F3 worldHit = transform_point(localHit, obj.model);
             float t = dot3(worldHit - o, d);
             F3 wn = normalize3(transform_vector(mh.hit.normal, obj.model));
+            if (r.t >= 0.0f && t == r.t) r.tied = true;
             if (t < r.t || r.t < 0.0f)
             {
+                r.tied = mh.tied;
                 r.t = t;
                 r.materialId = obj.material;
                 r.normal = wn;
@@ -1264,7 +1276,7 @@ int oracle_world_intersect(void *wp, uint32_t rayCount, const float *rays,
 }
 
 int oracle_world_closest(void *wp, uint32_t rayCount, const float *rays,
-    float *tOut, int32_t *objectOut, int32_t *triangleOut)
+    float *tOut, int32_t *objectOut, int32_t *triangleOut, int32_t *tiedOut)
 {
     World &w = *(World *)wp;
     QueryScratch s;
@@ -1275,6 +1287,7 @@ int oracle_world_closest(void *wp, uint32_t rayCount, const float *rays,
         tOut[r] = h.t;
         objectOut[r] = h.object;
         triangleOut[r] = h.triangle;
+        if (tiedOut) tiedOut[r] = h.tied ? 1 : 0;
     }
     return ok ? 0 : -100;
 }
@@ -1327,12 +1340,13 @@ void oracle_world_radiance_for_path(void *wp, const void *vertices,
     st3(out, radiance_for_path(w, path.data(), count));
 }
 
-double oracle_world_render_tiles_mt(void *wp, uint32_t width, uint32_t height,
-    const float *camPos, const float *camRot, float filmDistance,
-    uint32_t tileSize, uint32_t firstTile, uint32_t tileCount,
-    uint32_t threads, float *pixels, uint64_t *metrics)
+// Renders the listed 64x64-style tiles (ids in row-major tile order) on a
+// pool of threads that pop tile indices from an atomic counter, each tile
+// with the application's per-tile RNG reset (src/main.cpp:731-759).
+static double render_tile_ids(World &w, uint32_t width, uint32_t height, const float *camPos,
+    const float *camRot, float filmDistance, uint32_t tileSize, const uint32_t *ids,
+    uint32_t firstTile, uint32_t tileCount, uint32_t threads, float *pixels, uint64_t *metrics)
 {
-    World &w = *(World *)wp;
     Camera cam = configure_camera(width, height, ld3(camPos), ld4(camRot), filmDistance);
     uint32_t tilesX = (width + tileSize - 1) / tileSize;
     std::atomic<uint32_t> next(0);
@@ -1344,7 +1358,7 @@ double oracle_world_render_tiles_mt(void *wp, uint32_t width, uint32_t height,
         {
             uint32_t k = next.fetch_add(1);
             if (k >= tileCount) break;
-            uint32_t tid = firstTile + k;
+            uint32_t tid = ids ? ids[k] : firstTile + k;
             uint32_t tx = tid % tilesX, ty = tid / tilesX;
             uint32_t tile[4] = {tx * tileSize, ty * tileSize,
                 tx * tileSize + tileSize < width ? tx * tileSize + tileSize : width,
@@ -1366,6 +1380,24 @@ double oracle_world_render_tiles_mt(void *wp, uint32_t width, uint32_t height,
             for (int i = 0; i < 12; i++) metrics[i] += v[i];
     }
     return allOk ? dt : -dt;
+}
+
+double oracle_world_render_tiles_mt(void *wp, uint32_t width, uint32_t height,
+    const float *camPos, const float *camRot, float filmDistance,
+    uint32_t tileSize, uint32_t firstTile, uint32_t tileCount,
+    uint32_t threads, float *pixels, uint64_t *metrics)
+{
+    return render_tile_ids(*(World *)wp, width, height, camPos, camRot, filmDistance, tileSize,
+        nullptr, firstTile, tileCount, threads, pixels, metrics);
+}
+
+double oracle_world_render_tile_list(void *wp, uint32_t width, uint32_t height,
+    const float *camPos, const float *camRot, float filmDistance,
+    uint32_t tileSize, const uint32_t *tileIds, uint32_t tileCount,
+    uint32_t threads, float *pixels, uint64_t *metrics)
+{
+    return render_tile_ids(*(World *)wp, width, height, camPos, camRot, filmDistance, tileSize,
+        tileIds, 0, tileCount, threads, pixels, metrics);
 }
 
 double oracle_world_render_hashed_mt(void *wp, uint32_t width, uint32_t height,
@@ -1447,7 +1479,7 @@ void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out)
 // per object (ties to the lower triangle index), world t, smallest world t
 // (ties to the lower object index).  Threads split the rays.
 int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
-    uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut)
+    uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut, int32_t *tiedOut)
 {
     const World &w = *(const World *)wp;
     std::atomic<uint32_t> next(0);
@@ -1460,6 +1492,7 @@ int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
             F3 invd = inverse3(d);
             float best = INFINITY;
             int32_t bestObj = -1, bestTri = -1;
+            bool tied = false;
             for (size_t oi = 0; oi < w.objects.size(); oi++)
             {
                 const Object &obj = w.objects[oi];
@@ -1472,6 +1505,7 @@ int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
                 F3 linvd = inverse3(ld);
                 float lbest = -1.0f;
                 int32_t ltri = -1;
+                bool ltied = false;
                 uint32_t triCount = (uint32_t)(mesh.idx.size() / 3);
                 for (uint32_t t = 0; t < triCount; t++)
                 {
@@ -1482,25 +1516,30 @@ int oracle_world_closest_brute(void *wp, uint32_t rayCount, const float *rays,
                         continue;
                     TriHit h = w.watertight ? ray_triangle_watertight(lo, ld, a, b, c)
                                             : ray_triangle_mt(lo, ld, a, b, c);
+                    if (h.t > 0.0f && h.t == lbest) ltied = true;
                     if (h.t > 0.0f && (h.t < lbest || lbest < 0.0f))
                     {
                         lbest = h.t;
                         ltri = (int32_t)t;
+                        ltied = false;
                     }
                 }
                 if (ltri < 0) continue;
                 F3 worldHit = transform_point(lo + ld * lbest, obj.model);
                 float tw = dot3(worldHit - o, d);
+                if (tw == best) tied = true;
                 if (tw < best)
                 {
                     best = tw;
                     bestObj = (int32_t)oi;
                     bestTri = ltri;
+                    tied = ltied;
                 }
             }
             tOut[r] = bestObj >= 0 ? best : -1.0f;
             objectOut[r] = bestObj;
             triangleOut[r] = bestTri;
+            if (tiedOut) tiedOut[r] = tied ? 1 : 0;
         }
     };
     std::vector<std::thread> pool;

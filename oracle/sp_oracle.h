@@ -97,6 +97,12 @@ double oracle_world_render_tiles_mt(void *w, uint32_t width, uint32_t height,
     uint32_t tileSize, uint32_t firstTile, uint32_t tileCount,
     uint32_t threads, float *pixels, uint64_t *metrics);
 
+// Same, over an explicit list of tile ids (row-major tile order).
+double oracle_world_render_tile_list(void *w, uint32_t width, uint32_t height,
+    const float *camPos, const float *camRot, float filmDistance,
+    uint32_t tileSize, const uint32_t *tileIds, uint32_t tileCount,
+    uint32_t threads, float *pixels, uint64_t *metrics);
+
 // Same, hash-per-sample seeding (what the GPU path computes).
 double oracle_world_render_hashed_mt(void *w, uint32_t width, uint32_t height,
     const float *camPos, const float *camRot, float filmDistance,
@@ -104,9 +110,13 @@ double oracle_world_render_hashed_mt(void *w, uint32_t width, uint32_t height,
     float *out, uint64_t *metrics);
 
 // Closest hit for a ray batch through the reference's scene query: out per
-// ray is the world t (-1 miss), the winning object and its triangle index.
+// ray is the world t (-1 miss), the winning object and its triangle index;
+// tiedOut (optional) flags rays whose best t is an exact tie between two
+// candidates (two objects at the same world t, or two triangles of the
+// winning object at the same object-space t), where the reference's winner
+// depends on its BVH order.
 int oracle_world_closest(void *w, uint32_t rayCount, const float *rays,
-    float *tOut, int32_t *objectOut, int32_t *triangleOut);
+    float *tOut, int32_t *objectOut, int32_t *triangleOut, int32_t *tiedOut);
 
 // Meshes added after this call skip the reference's O(n^2 log n) BVH build
 // (they can then only be queried with oracle_world_closest_brute).
@@ -119,7 +129,7 @@ void oracle_ray_triangle_watertight(const float *o, const float *d, const float 
 // Display conversion: Reinhard + gamma 1/2.2, then 8-bit packing.
 void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out);
 int oracle_world_closest_brute(void *w, uint32_t rayCount, const float *rays,
-    uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut);
+    uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut, int32_t *tiedOut);
 
 #ifdef __cplusplus
 }

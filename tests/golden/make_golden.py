@@ -265,7 +265,7 @@ def gen_scenes(rng: np.random.Generator) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default=po.DEFAULT_REFERENCE)
+    ap.add_argument("--reference", default=po.reference_root())
     args = ap.parse_args()
     if po.build_ref(args.reference) is None:
         sys.exit("the reference tree (x86-64 host) is needed to make golden vectors")

@@ -1,6 +1,17 @@
-"""Denoiser kernels against PyTorch FP32 references of the same ops, on the
-same BF16-rounded tensors (tolerances: relative 2e-2 for BF16 outputs,
-accumulation order differs), plus a short training run on path-traced data."""
+"""Denoiser kernels against float64 references of the same ops on the same
+BF16-valued tensors (every BF16 input is exact in float64, so the reference
+carries no rounding of its own), plus a short training run on path-traced
+data.
+
+Tolerances, per element, with S = the sum of |a*b| over the K products that
+make up that output element (the scale FP32 accumulation error grows with):
+  * FP32 outputs (logits, data gradient, weight and bias gradients):
+    |out - ref| <= 1e-4 * S;
+  * BF16 outputs (ReLU activations, logit gradients): the same plus the BF16
+    rounding of the result, 2^-8 * |ref|.
+A wrong tap, a dropped 16-channel K slice or a misplaced pixel moves an
+element by a few percent of S and fails these bounds.
+"""
 
 import ctypes
 
@@ -11,24 +22,59 @@ from vk_cinematic_gb300 import gbsp, scenes
 
 pytestmark = pytest.mark.gpu
 
+FP32_TOL = 1e-4
+BF16_REL = 2.0 ** -8
 
-def torch_conv(x, w, b=None):
-    """x (B,H,W,Cin), w (9,Cout,Cin) -> (B,H,W,Cout), FP32."""
+
+def _wt(w):
+    """(9, Cout, Cin) -> conv2d weight (Cout, Cin, 3, 3), float64."""
+    _, cout, cin = w.shape
+    return w.double().reshape(3, 3, cout, cin).permute(2, 3, 0, 1).contiguous()
+
+
+def ref_conv(x, w, b=None):
+    """x (B,H,W,Cin), w (9,Cout,Cin) -> (y, S) as (B,H,W,Cout) float64: y the
+    exact convolution (zero padding) plus bias, S the sum of |x*w| (+ |bias|)."""
     import torch
 
-    B, H, W, cin = x.shape
-    cout = w.shape[1]
-    wt = w.float().reshape(3, 3, cout, cin).permute(2, 3, 0, 1).contiguous()
-    y = torch.nn.functional.conv2d(x.float().permute(0, 3, 1, 2), wt, b, padding=1)
-    return y.permute(0, 2, 3, 1).contiguous()
+    F = torch.nn.functional
+    xd = x.double().permute(0, 3, 1, 2)
+    wd = _wt(w)
+    bd = None if b is None else b.double()
+    y = F.conv2d(xd, wd, bd, padding=1)
+    sa = F.conv2d(xd.abs(), wd.abs(), None if bd is None else bd.abs(), padding=1)
+    return y.permute(0, 2, 3, 1), sa.permute(0, 2, 3, 1)
 
 
-def close(a, b, rtol=2e-2):
-    a = a.float().cpu()
-    b = b.float().cpu()
-    scale = b.abs().max().item() + 1e-6
-    err = (a - b).abs().max().item() / scale
-    return err, err <= rtol
+def ref_grads(x, w, d):
+    """Gradients of sum(conv(x, w, b) * d) in float64: (dW (9,Cout,Cin), dB,
+    dX (B,H,W,Cin)) with their sums of |products| (same shapes)."""
+    import torch
+
+    G = torch.nn.grad
+    xd = x.double().permute(0, 3, 1, 2)
+    dd = d.double().permute(0, 3, 1, 2)
+    wd = _wt(w)
+
+    def back(t):  # (Cout, Cin, 3, 3) -> (9, Cout, Cin)
+        cout, cin = t.shape[0], t.shape[1]
+        return t.permute(2, 3, 0, 1).reshape(9, cout, cin)
+
+    dw = back(G.conv2d_weight(xd, wd.shape, dd, padding=1))
+    dw_s = back(G.conv2d_weight(xd.abs(), wd.shape, dd.abs(), padding=1))
+    db = dd.sum(dim=(0, 2, 3))
+    db_s = dd.abs().sum(dim=(0, 2, 3))
+    dx = G.conv2d_input(xd.shape, wd, dd, padding=1).permute(0, 2, 3, 1)
+    dx_s = G.conv2d_input(xd.shape, wd.abs(), dd.abs(), padding=1).permute(0, 2, 3, 1)
+    return (dw, dw_s), (db, db_s), (dx, dx_s)
+
+
+def within(out, ref, scale, bf16=False, tol=FP32_TOL, bf16_rel=BF16_REL):
+    """(worst ratio of |out - ref| to its allowed bound, ok) per element."""
+    out = out.double()
+    bound = tol * scale + (bf16_rel * ref.abs() if bf16 else 0.0) + 1e-30
+    r = ((out - ref).abs() / bound).max().item()
+    return r, r <= 1.0
 
 
 @pytest.mark.parametrize("cin,cout,epi", [(16, 48, 0), (48, 48, 0), (48, 32, 1), (48, 48, 2),
@@ -49,21 +95,21 @@ def test_conv3x3_forward_matches_torch(gpu_lib, cin, cout, epi):
         out = torch.empty((B, H, cout // 8, W, 8), dtype=torch.bfloat16, device="cuda")
         rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), _ptr(bias),
                                        cout, epi, _ptr(out), None)
-        ref = torch.relu(torch_conv(x, w, bias))
     elif epi == 1:
         out = torch.empty((B, H, W, cout), dtype=torch.float32, device="cuda")
         rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), _ptr(bias),
                                        cout, epi, None, _ptr(out))
-        ref = torch_conv(x, w, bias)
     else:
         out = torch.empty((B, H, cout // 8, W, 8), dtype=torch.float32, device="cuda")
         rc = L.gbsp_dn_conv3x3_forward(_stream(), _ptr(xp), B, H, W, cin, _ptr(w), None, cout,
                                        epi, None, _ptr(out))
-        ref = torch_conv(x, w)
     assert rc == 0, L.gbsp_last_error_string()
     torch.cuda.synchronize()
-    err, ok = close(out if epi == 1 else from_planar(out), ref)
-    print(f"conv {cin}->{cout} epi {epi}: max rel err {err:.2e}")
+    ref, S = ref_conv(x, w, bias if epi != 2 else None)
+    if epi == 0:
+        ref = torch.relu(ref)
+    r, ok = within(out if epi == 1 else from_planar(out), ref, S, bf16=epi == 0)
+    print(f"mma.sync conv {cin}->{cout} epi {epi}: worst error / bound {r:.3f}")
     assert ok
 
 
@@ -104,13 +150,15 @@ def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, B, H, W)
     torch.cuda.synchronize()
     st = ctypes.c_uint32(0)
     assert L.gbsp_dn_status(ctypes.byref(st)) == 0, st.value
-    ref = torch_conv(x, w, bias if epi != 2 else None)
+    ref, S = ref_conv(x, w, bias if epi != 2 else None)
     if epi == 0:
         ref = torch.relu(ref)
-    err, ok = close(outs[0], ref)
-    err2, ok2 = close(outs[0], outs[1], rtol=1e-2 if epi == 0 else 1e-4)
-    print(f"tcgen05 conv {cin}->{cout} epi {epi} {B}x{H}x{W}: vs torch {err:.2e}, "
-          f"vs mma.sync {err2:.2e}")
+    r, ok = within(outs[0], ref, S, bf16=epi == 0)
+    # the two kernels: each within its bound of the exact result, hence of each
+    # other (two BF16 roundings of nearly equal values differ by one BF16 ulp)
+    r2, ok2 = within(outs[0], outs[1].double(), 2 * S, bf16=epi == 0, bf16_rel=2 * BF16_REL)
+    print(f"tcgen05 conv {cin}->{cout} epi {epi} {B}x{H}x{W}: worst error / bound {r:.3f}, "
+          f"vs mma.sync {r2:.3f}")
     assert ok and ok2
 
 
@@ -131,21 +179,17 @@ def test_conv_gradients_match_autograd(gpu_lib, wgrad, shape):
         dw = torch.zeros((9, cout, cin), device="cuda")
         db = torch.zeros(cout, device="cuda")
         net.weight_grad(li, to_planar(x), to_planar(d), dw, db)
-        xr = x.float().clone().requires_grad_(True)
-        wr = net.wb[li].float().clone().requires_grad_(True)
-        br = torch.zeros(cout, device="cuda", requires_grad=True)
-        y = torch_conv(xr, wr, br)
-        (y * d.float()).sum().backward()
         torch.cuda.synchronize()
-        err_w, ok_w = close(dw, wr.grad)
-        err_b, ok_b = close(db, br.grad)
-        print(f"{wgrad} {shape} layer {li}: dW rel err {err_w:.2e}, dB rel err {err_b:.2e}")
+        (rw, sw), (rb, sb), (rx, sx) = ref_grads(x, net.wb[li], d)
+        r_w, ok_w = within(dw, rw, sw)
+        r_b, ok_b = within(db, rb, sb)
+        print(f"{wgrad} {shape} layer {li}: worst error / bound dW {r_w:.3f}, dB {r_b:.3f}")
         assert ok_w and ok_b
         if li > 0:
             dx = from_planar(net.data_grad(li, to_planar(d)))
             torch.cuda.synchronize()
-            err_x, ok_x = close(dx, xr.grad)
-            print(f"layer {li}: dX rel err {err_x:.2e}")
+            r_x, ok_x = within(dx, rx, sx)
+            print(f"layer {li}: worst error / bound dX {r_x:.3f}")
             assert ok_x
 
 
@@ -167,25 +211,30 @@ def test_filter_and_relmse_gradient_match_autograd(gpu_lib):
     assert L.gbsp_dn_relmse_backward(_stream(), _ptr(logits), _ptr(noisy), _ptr(target), B, H, W,
                                      _ptr(dlog), _ptr(loss)) == 0
     dlog = from_planar(dlog)
-    # reference
-    lr = logits[..., :25].clone().requires_grad_(True)
+    # float64 reference
+    lr = logits[..., :25].double().clone().requires_grad_(True)
     wts = torch.softmax(lr, dim=-1)
-    pad = torch.nn.functional.pad(noisy[..., :3].permute(0, 3, 1, 2), (2, 2, 2, 2),
+    pad = torch.nn.functional.pad(noisy[..., :3].double().permute(0, 3, 1, 2), (2, 2, 2, 2),
                                   mode="replicate")
-    acc = torch.zeros((B, 3, H, W), device="cuda")
+    acc = torch.zeros((B, 3, H, W), dtype=torch.float64, device="cuda")
     for k in range(25):
         ky, kx = k // 5, k % 5
         acc = acc + wts[..., k].unsqueeze(1) * pad[:, :, ky:ky + H, kx:kx + W]
     ref_out = acc.permute(0, 2, 3, 1)
-    t3 = target[..., :3]
+    t3 = target[..., :3].double()
     ref_loss = ((ref_out - t3) ** 2 / (t3 * t3 + 0.01)).mean()
     ref_loss.backward()
     torch.cuda.synchronize()
-    err_o, ok_o = close(out[..., :3], ref_out.detach(), rtol=1e-4)
-    assert ok_o, err_o
+    # filter: a 25-term weighted sum of positive radiance, S = ref_out itself
+    r_o, ok_o = within(out[..., :3], ref_out.detach(), ref_out.detach().abs())
+    assert ok_o, r_o
     assert abs(loss.item() / (3 * B * H * W) - ref_loss.item()) <= 1e-4 * ref_loss.item()
-    err_g, ok_g = close(dlog[..., :25], lr.grad)
-    print(f"filter rel err {err_o:.2e}, dLogits rel err {err_g:.2e}")
+    # dLogits: w_k (g_k - sum_j w_j g_j) with g the per-tap loss gradient; scale
+    # it by w_k (|g_k| + sum_j w_j |g_j|), here bounded by the largest gradient
+    g = lr.grad
+    r_g, ok_g = within(dlog[..., :25], g, g.abs().amax(dim=-1, keepdim=True).expand_as(g),
+                       bf16=True)
+    print(f"filter worst error / bound {r_o:.3f}, dLogits {r_g:.3f}")
     assert ok_g
     assert torch.all(dlog[..., 25:] == 0)
 

@@ -164,3 +164,28 @@ def test_radiance_for_path(golden):
     # TestEvaluateLightPath (test_simd_path_tracer.cpp:278-306) is NaN at HEAD:
     # DistributionGGX is 0/0 at roughness 0 with N.H = 1
     assert np.all(np.isnan(g["path_radiance"][0]))
+
+
+def test_closest_flags_exact_ties(port):
+    """The oracle's tie flag (the only rays where a closest-hit id may differ
+    from the reference's, whose winner among equal-t candidates depends on its
+    BVH order): two coincident copies of a triangle tie, one copy does not, and
+    a second object at exactly the same world t ties across objects."""
+    tri = np.array([[-1, -1, 0, 0, 0, 1, 0, 0], [1, -1, 0, 0, 0, 1, 1, 0],
+                    [0, 1, 0, 0, 0, 1, 0, 1]], np.float32)
+    rays = np.array([[0, 0, 5, 0, 0, -1], [0.2, -0.3, 5, 0, 0, -1], [5, 5, 5, 0, 0, -1]],
+                    np.float32)
+    for copies, obj_count, expect_tie in ((1, 1, False), (2, 1, True), (1, 2, True)):
+        w = po.World("port")
+        v = np.concatenate([tri] * copies)
+        i = np.arange(3 * copies, dtype=np.uint32)
+        w.add_mesh(v, i)
+        for _ in range(obj_count):
+            w.add_object(0, 1, (0, 0, 0), (0, 0, 0, 1), (1, 1, 1))
+        w.build()
+        w.set_options(max_broadphase=64, max_midphase=64)
+        for fn in (w.closest, w.closest_brute):
+            t, obj, tr, tied = fn(rays, ties=True)
+            assert np.allclose(t[:2], 5.0) and t[2] == -1.0
+            assert tied.tolist() == [expect_tie, expect_tie, False], (copies, obj_count, fn)
+        w.close()

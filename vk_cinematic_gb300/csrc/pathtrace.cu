@@ -300,6 +300,26 @@ static int noalloc_scratch(int device, unsigned char **out)
     return GBSP_OK;
 }
 
+// Makes a device current for the scope of a call and restores the caller's
+// current device on every return.
+struct CurrentDeviceScope {
+    int previous = -1;
+    bool changed = false;
+    cudaError_t enter(int device)
+    {
+        cudaError_t e = cudaGetDevice(&previous);
+        if (e != cudaSuccess) return e;
+        if (previous == device) return cudaSuccess;
+        e = cudaSetDevice(device);
+        changed = e == cudaSuccess;
+        return e;
+    }
+    ~CurrentDeviceScope()
+    {
+        if (changed) cudaSetDevice(previous);
+    }
+};
+
 }  // namespace gbsp
 
 using namespace gbsp;
@@ -329,6 +349,9 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "scene, materials and context use different runtimes");
     if (opt.rng_mode != GBSP_RNG_HASH_PER_SAMPLE)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "the allocation-free entry renders hash-per-sample only");
+    if (opt.flags & GBSP_FLAG_AOV)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT,
+            "the allocation-free entry writes no G-buffers (GBSP_FLAG_AOV)");
     uint32_t spp = opt.spp ? opt.spp : 1;
     if (spp > kNoAllocMaxPaths || opt.max_bounces > kNoAllocMaxBounces ||
         sc->objects.size() > kNoAllocMaxObjects)
@@ -342,7 +365,8 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     uint32_t y1 = tile.maxY < ip->height ? tile.maxY : ip->height;
     if (x1 <= x0 || y1 <= y0) return GBSP_OK;
 
-    GBSP_CUDA_TRY(cudaSetDevice(rt->device));
+    CurrentDeviceScope deviceScope;
+    GBSP_CUDA_TRY(deviceScope.enter(rt->device));
     unsigned char *base = nullptr;
     int rc = noalloc_scratch(rt->device, &base);
     if (rc) return rc;
@@ -416,6 +440,7 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     float4 *image = reinterpret_cast<float4 *>(deviceImage);
     uint64_t regionPixels = (uint64_t)(x1 - x0) * (y1 - y0);
     int grid = rt->smCount * 8;
+    uint64_t launches = 0, traceLaunches = 0;
     for (uint64_t pb = 0; pb < regionPixels; pb += pixelsPerWave) {
         wp.pixelBase = pb;
         uint64_t left = regionPixels - pb;
@@ -426,17 +451,25 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
         } else {
             k_reset_ctl<<<1, 32, 0, s>>>(ctl, paths);
             k_generate<<<(paths + 255) / 256, 256, 0, s>>>(wp, wb);
+            launches += 2;
             for (uint32_t b = 0; b < opt.max_bounces; b++) {
                 int inQ = (b & 1) ? kCtlQueue1 : kCtlQueue0;
                 int outQ = (b & 1) ? kCtlQueue0 : kCtlQueue1;
                 k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
-                launch_trace_stage(b > 0, one.sv.watertight != 0, grid, s, one,
+                // the same per-bounce scheduling choice as the regular entry points
+                // (it changes the order of work, not the results)
+                bool perLane = (opt.flags & GBSP_FLAG_TRACE_PER_LANE) ||
+                    (!(opt.flags & GBSP_FLAG_TRACE_PER_WARP) && b > 0);
+                launch_trace_stage(perLane, one.sv.watertight != 0, grid, s, one,
                     wb.rayO + ((b & 1) ? wb.cap : 0), wb.rayD + ((b & 1) ? wb.cap : 0), ctl + inQ,
                     wb.hitA, wb.hitInst, ctl, counters, status);
                 k_shade<<<grid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
+                launches += 3;
+                traceLaunches += 1;
             }
         }
         k_accumulate<<<(wp.pixels + 255) / 256, 256, 0, s>>>(wp, wb, image, ip->width, counters);
+        launches += 1;
         GBSP_CUDA_TRY(cudaGetLastError());
     }
     unsigned long long hostCounters[GBSP_METRIC_COUNT];
@@ -446,6 +479,8 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     GBSP_CUDA_TRY(cudaStreamSynchronize(s));
     if (st)
         return set_error(GBSP_ERR_DEVICE_STATUS, "device status 0x%x in the allocation-free render", st);
+    hostCounters[GBSP_METRIC_TRACE_LAUNCHES] += traceLaunches;
+    hostCounters[GBSP_METRIC_KERNEL_LAUNCHES] += launches;
     if (metrics)
         for (int i = 0; i < GBSP_METRIC_COUNT; i++) metrics->values[i] += hostCounters[i];
     return GBSP_OK;
