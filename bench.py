@@ -580,6 +580,33 @@ def run_config4(args):
     clk = clocks.stop()
     batch_ms = ev0.elapsed_time(ev1) / args.steps
     m = batch.launch(metrics=True).as_dict()
+    widths = batch.node_widths()
+
+    # the single persistent launches against the tuned configuration, at the
+    # tuned node widths: one thread per pixel (k_batch) and the per-lane path
+    # state machine (k_batch_sm), each at its best blocks per SM
+    def time_config(**kw):
+        batch.set_config(**kw)
+        batch.launch(metrics=False)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            batch.launch(metrics=False)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps
+
+    kernels = {}
+    for name, kern, blocks in (("thread_per_pixel (k_batch)", gbsp.BATCH_THREAD_PER_PIXEL, 128),
+                               ("path_state (k_batch_sm)", gbsp.BATCH_PATH_STATE, 128)):
+        best_ms = min(time_config(block=blocks, chunk=1, blocks_per_sm=bps, use_graph=1,
+                                  kernel=kern, wave_paths=tuned.wavePaths) for bps in (2, 4, 8))
+        kernels[name] = {"ms_per_step": best_ms, "value": total / best_ms / 1e3,
+                         "unit": "Msamples/s"}
+    batch.set_config(block=tuned.block, chunk=tuned.chunk, blocks_per_sm=tuned.blocksPerSm,
+                     use_graph=tuned.useGraph, kernel=tuned.kernel, wave_paths=tuned.wavePaths)
+    kernels["tuned"] = {"ms_per_step": batch_ms, "value": total / batch_ms / 1e3,
+                        "unit": "Msamples/s"}
     line = {
         "metric": "aggregate spp/s, 32 uneven scenes (config 4)", "value": total / batch_ms / 1e3,
         "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -595,6 +622,7 @@ def run_config4(args):
                                           "ms_per_step": single_ms},
         "speedup_vs_per_scene": single_ms / batch_ms,
         "autotuned": tuned.as_dict(), "autotune_seconds": tune_s,
+        "node_width_per_scene": widths, "persistent_kernels": kernels,
         "mrays_per_s": m["rays_traced"] / batch_ms / 1e3, "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }

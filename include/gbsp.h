@@ -197,6 +197,15 @@ int gbsp_scene_destroy(gbsp_scene *scene);
 #define GBSP_ISECT_REFERENCE_MT 0u
 #define GBSP_ISECT_WATERTIGHT 1u
 int gbsp_scene_set_intersection(gbsp_scene *scene, uint32_t mode);
+/* Node width of the BVHs the scene's queries and renders walk: 8 (default)
+ * or 4 (the reference's width, src/bvh.h:4-12).  Every mesh and object BVH
+ * is built at both widths from one binary tree (same leaves, same triangle
+ * order), so switching is free and never changes a result: images, hit
+ * records and ids are bit-identical at either width; only the work per ray
+ * differs.  gbsp_batch_autotune picks it per batch item.  No reference
+ * counterpart (the reference's width is fixed at 4). */
+int gbsp_scene_set_node_width(gbsp_scene *scene, uint32_t width);
+uint32_t gbsp_scene_node_width(const gbsp_scene *scene);
 /* replaces sp_CreateMesh + sp_BuildMeshMidphase (src/sp_scene.cpp:8-54):
  * copies the vertices and indices to the device and builds the mesh BVH
  * there.  *meshOut receives the mesh handle used by add_object. */
@@ -344,11 +353,17 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
 int gbsp_batch_destroy(gbsp_batch *batch);
 int gbsp_batch_set_config(gbsp_batch *batch, const gbsp_batch_config *config);
 int gbsp_batch_get_config(const gbsp_batch *batch, gbsp_batch_config *config);
-/* Times every candidate configuration (36: thread-per-pixel block x chunk x
+/* First picks each item's BVH node width (8 or 4): the item's frame is
+ * timed alone at both widths (spp capped at 8) and the faster is kept; then
+ * times every candidate configuration (36: thread-per-pixel block x chunk x
  * blocks per SM, path-state block x blocks per SM, wavefront blocks per SM x
  * wave size 2^22..2^24) over `trials` launches each and keeps the fastest;
- * *best receives it. */
+ * *best receives it.  Items start at their scene's gbsp_scene_set_node_width. */
 int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best);
+/* Node width per item (`widths` has one entry per item: 4 or 8), as chosen by
+ * gbsp_batch_autotune or set by the caller.  Images do not depend on it. */
+int gbsp_batch_set_node_widths(gbsp_batch *batch, const uint32_t *widths);
+int gbsp_batch_get_node_widths(const gbsp_batch *batch, uint32_t *widths);
 /* Renders every item.  metrics NULL: asynchronous on the runtime's stream. */
 int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics);
 

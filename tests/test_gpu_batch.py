@@ -59,10 +59,23 @@ def test_batch_matches_single_scene_renders(gpu_lib):
                 got = t.cpu().numpy()
                 assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), \
                     f"item {k} differs (kernel={kernel}, graph={use_graph}, wave={wave})"
+    # every item on 4-wide BVHs, then mixed widths: the same bits
+    for widths in ([4] * len(ss), [4 if k % 2 else 8 for k in range(len(ss))]):
+        batch.set_node_widths(widths)
+        assert batch.node_widths() == widths
+        for t in imgs:
+            t.fill_(-1.0)
+        torch.cuda.synchronize()
+        batch.launch()
+        for k, (t, ref) in enumerate(zip(imgs, refs)):
+            assert np.array_equal(t.cpu().numpy().view(np.uint32), ref.view(np.uint32)), \
+                f"item {k} differs at node widths {widths}"
     best = batch.autotune(trials=1)
     assert best.block in (64, 128, 256)
     assert best.kernel in (gbsp.BATCH_THREAD_PER_PIXEL, gbsp.BATCH_PATH_STATE,
                            gbsp.BATCH_WAVEFRONT)
+    assert set(batch.node_widths()) <= {4, 8}
+    print("autotuned node widths", batch.node_widths())
     for t in imgs:
         t.fill_(-1.0)
     torch.cuda.synchronize()

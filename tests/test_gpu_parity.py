@@ -373,6 +373,51 @@ def test_config3_bench_scene_primary_hits_bit_exact(config3_bench):
     assert np.all(same_obj | rtied[h])
 
 
+@pytest.mark.parametrize("kind", ["config3_small", "soup"])
+def test_node_width_changes_nothing(rt, kind):
+    """The 4-wide BVHs (the reference's width) and the 8-wide ones index the
+    same triangles: frames, hit records and ray/hit counters are bit-identical
+    at both widths; only node visits and box tests differ."""
+    if kind == "config3_small":
+        s = scenes.config3_scene(width=96, height=64, spp=4, n_spheres=48, level=3, seed=13)
+        out = {}
+        for width in (8, 4):
+            scene, ms, rend = gbsp.upload_scene(rt, s)
+            scene.set_node_width(width)
+            assert scene.node_width == width
+            img, m = rend.frame()
+            out[width] = (img, m.as_dict())
+        a, ma = out[8]
+        b, mb = out[4]
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        for k in ("paths_traced", "rays_traced", "ray_hit_count", "triangle_tests"):
+            assert ma[k] == mb[k], (k, ma[k], mb[k])
+        print("node visits per ray, 8-wide vs 4-wide:",
+              (ma["broadphase_node_visits"] + ma["midphase_node_visits"]) / ma["rays_traced"],
+              (mb["broadphase_node_visits"] + mb["midphase_node_visits"]) / mb["rays_traced"])
+    else:
+        s, _ = soup_world(12000, seed=17, bvh=False)
+        rays = scenes.soup_rays(70000, seed=18)
+        res = {}
+        for width in (8, 4):
+            scene, ms, _ = gbsp.upload_scene(rt, s)
+            scene.set_node_width(width)
+            import torch
+
+            packed = np.zeros((len(rays), 8), np.float32)
+            packed[:, 0:3] = rays[:, 0:3]
+            packed[:, 4:7] = rays[:, 3:6]
+            dr = torch.from_numpy(packed).cuda()
+            t = torch.empty(len(rays), dtype=torch.float32, device="cuda")
+            tri = torch.empty(len(rays), dtype=torch.int32, device="cuda")
+            torch.cuda.synchronize()
+            scene.intersect_closest_device(len(rays), dr.data_ptr(), t.data_ptr(), tri.data_ptr())
+            rt.synchronize()
+            res[width] = (t.cpu().numpy(), tri.cpu().numpy())
+        assert np.array_equal(bits(res[8][0]), bits(res[4][0]))
+        assert np.array_equal(res[8][1], res[4][1])
+
+
 def test_tonemap_matches_oracle(rt, port):
     """Display conversion (post_processing.frag.glsl:19-26 + ToColor) of a
     path-traced frame against the C restatement; powf differs in the last

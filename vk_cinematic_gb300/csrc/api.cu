@@ -436,6 +436,20 @@ int gbsp_scene_set_intersection(gbsp_scene *scene, uint32_t mode)
     return GBSP_OK;
 }
 
+int gbsp_scene_set_node_width(gbsp_scene *scene, uint32_t width)
+{
+    if (!scene) return set_error(GBSP_ERR_INVALID_ARGUMENT, "scene is NULL");
+    if (width != 4 && width != 8)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "node width %u (4 or 8)", width);
+    scene->nodeWidth = width;
+    return GBSP_OK;
+}
+
+uint32_t gbsp_scene_node_width(const gbsp_scene *scene)
+{
+    return scene ? scene->nodeWidth : 0u;
+}
+
 int gbsp_scene_destroy(gbsp_scene *scene)
 {
     if (!scene) return GBSP_OK;
@@ -493,12 +507,13 @@ int gbsp_create_mesh(gbsp_scene *scene, const gbsp_vertex *vertices, uint32_t ve
         (rc = lo.reserve(triCount, s)) || (rc = hi.reserve(triCount, s)))
         return rc;
     if ((rc = mesh_prepare(s, dv.ptr, di.ptr, triCount, lo.ptr, hi.ptr))) return rc;
-    uint32_t nodeBase = scene->meshNodeCount, nodeCount = 0, depth = 0;
     // the object BVH lives after the mesh nodes and is rebuilt on commit
     scene->committed = false;
-    scene->tlasRoot = kEmptyChild;
-    if ((rc = build_wide_bvh(s, lo.ptr, hi.ptr, triCount, kMaxLeafPrims, &scene->nodes, nodeBase,
-             &nodeCount, &order, &depth, rt->dStatus)))
+    for (int w = 0; w < kNodeWidths; w++) scene->tlasRoot[w] = kEmptyChild;
+    const uint32_t nodeBase[kNodeWidths] = {scene->meshNodeCount[0], scene->meshNodeCount[1]};
+    WideTree trees[kNodeWidths];
+    if ((rc = build_wide_bvh(s, lo.ptr, hi.ptr, triCount, kMaxLeafPrims, scene->nodes, nodeBase,
+             trees, &order, rt->dStatus)))
         return rc;
     uint64_t triBase = scene->triCount;
     if ((rc = append_device(scene->tris, triBase, triCount, s)) ||
@@ -506,15 +521,20 @@ int gbsp_create_mesh(gbsp_scene *scene, const gbsp_vertex *vertices, uint32_t ve
         (rc = append_device(scene->triIds, triBase, triCount, s)))
         return rc;
     if ((rc = mesh_emit(s, dv.ptr, di.ptr, triCount, order.ptr, scene->tris.ptr + triBase,
-             scene->attrs.ptr + triBase, scene->triIds.ptr + triBase, nodeBase, scene->nodes.ptr,
-             nodeCount, (uint32_t)triBase)))
+             scene->attrs.ptr + triBase, scene->triIds.ptr + triBase, (uint32_t)triBase)))
         return rc;
+    for (int w = 0; w < kNodeWidths; w++)
+        if ((rc = offset_nodes(s, scene->nodes[w], trees[w].nodeCount, nodeBase[w],
+                 (uint32_t)triBase)))
+            return rc;
     gbsp_mesh_info mi;
-    mi.rootNode = nodeBase;
+    for (int w = 0; w < kNodeWidths; w++) {
+        mi.rootNode[w] = nodeBase[w];
+        mi.nodeCount[w] = trees[w].nodeCount;
+        mi.depth[w] = trees[w].depth;
+    }
     mi.triFirst = (uint32_t)triBase;
     mi.triCount = triCount;
-    mi.nodeCount = nodeCount;
-    mi.depth = depth;
     mi.smooth = useSmoothShading != 0;
     // vertex AABB over all vertices (src/sp_scene.cpp:57-75)
     V3 mn = ld3(vertices[0].position), mx = mn;
@@ -525,9 +545,11 @@ int gbsp_create_mesh(gbsp_scene *scene, const gbsp_vertex *vertices, uint32_t ve
     memcpy(mi.aabbMin, &mn, 12);
     memcpy(mi.aabbMax, &mx, 12);
     scene->meshes.push_back(mi);
-    scene->meshNodeCount += nodeCount;
+    for (int w = 0; w < kNodeWidths; w++) {
+        scene->meshNodeCount[w] += trees[w].nodeCount;
+        scene->maxDepth[w] = std::max(scene->maxDepth[w], trees[w].depth);
+    }
     scene->triCount += triCount;
-    scene->maxDepth = std::max(scene->maxDepth, depth);
     GBSP_CUDA_TRY(cudaStreamSynchronize(s));
     if (meshOut) *meshOut = (uint32_t)scene->meshes.size() - 1;
     return check_stream_status(rt);
@@ -560,7 +582,7 @@ int gbsp_add_object_to_scene(gbsp_scene *scene, uint32_t mesh, uint32_t material
     in.model = rows_of(model);
     memcpy(in.lo, &lo, 12);
     memcpy(in.hi, &hi, 12);
-    in.blasRoot = mi.rootNode;
+    in.blasRoot = mi.rootNode[0];  // per width when the instances are uploaded
     in.materialId = material;
     in.objectIndex = (uint32_t)scene->objects.size();
     in.smooth = mi.smooth ? 1u : 0u;
@@ -583,9 +605,11 @@ int gbsp_build_scene_broadphase(gbsp_scene *scene)
     gbsp_runtime *rt = scene->rt;
     cudaStream_t s = rt->stream;
     uint32_t n = (uint32_t)scene->objects.size();
-    scene->totalNodeCount = scene->meshNodeCount;
-    scene->tlasRoot = kEmptyChild;
-    scene->tlasDepth = 0;
+    for (int w = 0; w < kNodeWidths; w++) {
+        scene->totalNodeCount[w] = scene->meshNodeCount[w];
+        scene->tlasRoot[w] = kEmptyChild;
+        scene->tlasDepth[w] = 0;
+    }
     if (n == 0) {
         scene->committed = true;
         return GBSP_OK;
@@ -600,25 +624,30 @@ int gbsp_build_scene_broadphase(gbsp_scene *scene)
     DeviceBuffer<float4> dlo, dhi;
     DeviceBuffer<uint32_t> order;
     if ((rc = dlo.upload(lo.data(), n, s)) || (rc = dhi.upload(hi.data(), n, s))) return rc;
-    uint32_t nodeCount = 0, depth = 0;
-    if ((rc = build_wide_bvh(s, dlo.ptr, dhi.ptr, n, 1, &scene->nodes, scene->meshNodeCount,
-             &nodeCount, &order, &depth, rt->dStatus)))
+    WideTree trees[kNodeWidths];
+    if ((rc = build_wide_bvh(s, dlo.ptr, dhi.ptr, n, 1, scene->nodes, scene->meshNodeCount, trees,
+             &order, rt->dStatus)))
         return rc;
-    if ((rc = offset_nodes(s, scene->nodes.ptr + scene->meshNodeCount, nodeCount,
-             scene->meshNodeCount, 0)))
-        return rc;
+    for (int w = 0; w < kNodeWidths; w++)
+        if ((rc = offset_nodes(s, scene->nodes[w], trees[w].nodeCount, scene->meshNodeCount[w], 0)))
+            return rc;
     std::vector<uint32_t> ord(n);
     GBSP_CUDA_TRY(cudaMemcpyAsync(ord.data(), order.ptr, 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
     GBSP_CUDA_TRY(cudaStreamSynchronize(s));
     std::vector<Instance> inst(n);
-    for (uint32_t j = 0; j < n; j++) {
+    for (uint32_t j = 0; j < n; j++)
         if (ord[j] >= n) return set_error(GBSP_ERR_DEVICE_STATUS, "object order out of range");
-        inst[j] = scene->objects[ord[j]].inst;
+    for (int w = 0; w < kNodeWidths; w++) {
+        for (uint32_t j = 0; j < n; j++) {
+            const gbsp_object_info &o = scene->objects[ord[j]];
+            inst[j] = o.inst;
+            inst[j].blasRoot = scene->meshes[o.mesh].rootNode[w];
+        }
+        if ((rc = scene->instances[w].upload(inst.data(), n, s))) return rc;
+        scene->tlasRoot[w] = scene->meshNodeCount[w];
+        scene->tlasDepth[w] = trees[w].depth;
+        scene->totalNodeCount[w] = scene->meshNodeCount[w] + trees[w].nodeCount;
     }
-    if ((rc = scene->instances.upload(inst.data(), n, s))) return rc;
-    scene->tlasRoot = scene->meshNodeCount;
-    scene->tlasDepth = depth;
-    scene->totalNodeCount = scene->meshNodeCount + nodeCount;
     scene->leafOrder = ord;
     scene->committed = true;
     GBSP_CUDA_TRY(cudaStreamSynchronize(s));
@@ -635,8 +664,9 @@ int gbsp_scene_info(const gbsp_scene *scene, uint32_t *objects, uint64_t *triang
         for (const auto &o : scene->objects) t += scene->meshes[o.mesh].triCount;
         *triangles = t;
     }
-    if (meshNodes) *meshNodes = scene->meshNodeCount;
-    if (maxDepth) *maxDepth = scene->maxDepth + scene->tlasDepth;
+    int w = width_index(scene->nodeWidth);
+    if (meshNodes) *meshNodes = scene->meshNodeCount[w];
+    if (maxDepth) *maxDepth = scene->maxDepth[w] + scene->tlasDepth[w];
     return GBSP_OK;
 }
 

@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(128) k_batch_sm(const BatchItemDev *__restrict
                     cnt.meshNodes++;
                 V3 ro = tmode == 1 ? o : lo;
                 V3 ri = tmode == 1 ? invd : linvd;
-                visit_node<true, kWT>(sv.nodes, ref, ro, ri, bound, stack, sp, status,
+                visit_node<true, kWT>(sv.nodes, sv.nodeQuads, ref, ro, ri, bound, stack, sp, status,
                     cnt);
                 return;
             }
@@ -526,7 +526,60 @@ struct gbsp_batch {
     DeviceBuffer<int4> hitA;
     DeviceBuffer<int> hitInst;
     DeviceBuffer<uint32_t> pathRng, pathLen, pathItem;
+    std::vector<uint32_t> nodeWidth;  // per item: BVH node width its scene view walks
 };
+
+static void drop_graph(gbsp_batch *b);
+
+// Points every item's scene view at the BVHs of its chosen node width,
+// re-uploads the item table and drops the captured graph (re-captured on
+// the next launch).
+static int apply_node_widths(gbsp_batch *b)
+{
+    for (size_t i = 0; i < b->items.size(); i++)
+        b->hostItems[i].sv = b->items[i].scene->view(b->nodeWidth[i]);
+    drop_graph(b);
+    return b->dItems.upload(b->hostItems.data(), b->hostItems.size(), b->rt->stream);
+}
+
+// Node width per item, timed on the item's own frame: the frame renderer
+// draws the item at each width (its spp capped at 8 for the probe; per-ray
+// work does not depend on the sample count) and the faster width is kept.
+static int tune_node_widths(gbsp_batch *b, uint32_t trials)
+{
+    gbsp_runtime *rt = b->rt;
+    cudaStream_t s = rt->stream;
+    for (size_t i = 0; i < b->items.size(); i++) {
+        const gbsp_batch_item &it = b->items[i];
+        const BatchItemDev &d = b->hostItems[i];
+        gbsp_options o = it.options;
+        o.spp = std::min(o.spp ? o.spp : 1u, 8u);
+        o.flags = 0;
+        float bestMs = 3.0e38f;
+        uint32_t bestWidth = b->nodeWidth[i];
+        for (uint32_t width : {8u, 4u}) {
+            SceneView sv = it.scene->view(width);
+            int rc = render_frame(rt, sv, d.mv, d.cam, o, 0, 0, d.width, d.height, d.image, d.width,
+                nullptr);
+            if (rc) return rc;
+            GBSP_CUDA_TRY(cudaEventRecord(rt->ev[2], s));
+            for (uint32_t t = 0; t < trials; t++)
+                if ((rc = render_frame(rt, sv, d.mv, d.cam, o, 0, 0, d.width, d.height, d.image,
+                         d.width, nullptr)))
+                    return rc;
+            GBSP_CUDA_TRY(cudaEventRecord(rt->ev[3], s));
+            GBSP_CUDA_TRY(cudaEventSynchronize(rt->ev[3]));
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, rt->ev[2], rt->ev[3]);
+            if (ms < bestMs) {
+                bestMs = ms;
+                bestWidth = width;
+            }
+        }
+        b->nodeWidth[i] = bestWidth;
+    }
+    return apply_node_widths(b);
+}
 
 // Cuts the items' paths into waves of whole pixels of at most `cap` paths
 // and reserves the wave buffers (once).
@@ -772,6 +825,8 @@ int gbsp_batch_create(gbsp_runtime *rt, const gbsp_batch_item *items, uint32_t c
     if (!rc) {
         b->hostItems = dev;
         b->totalPixels = base;
+        b->nodeWidth.resize(count);
+        for (uint32_t i = 0; i < count; i++) b->nodeWidth[i] = items[i].scene->nodeWidth;
         rc = plan_waves(b);
     }
     if (!rc && cudaStreamSynchronize(s) != cudaSuccess)
@@ -843,12 +898,32 @@ int gbsp_batch_launch(gbsp_batch *batch, gbsp_metrics *metrics)
     return GBSP_OK;
 }
 
+int gbsp_batch_set_node_widths(gbsp_batch *batch, const uint32_t *widths)
+{
+    if (!batch || !widths) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (size_t i = 0; i < batch->items.size(); i++)
+        if (widths[i] != 4 && widths[i] != 8)
+            return set_error(GBSP_ERR_INVALID_ARGUMENT, "item %zu: node width %u (4 or 8)", i,
+                widths[i]);
+    batch->nodeWidth.assign(widths, widths + batch->items.size());
+    return apply_node_widths(batch);
+}
+
+int gbsp_batch_get_node_widths(const gbsp_batch *batch, uint32_t *widths)
+{
+    if (!batch || !widths) return set_error(GBSP_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (size_t i = 0; i < batch->items.size(); i++) widths[i] = batch->nodeWidth[i];
+    return GBSP_OK;
+}
+
 int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best)
 {
     if (!batch) return set_error(GBSP_ERR_INVALID_ARGUMENT, "batch is NULL");
     gbsp_runtime *rt = batch->rt;
     cudaStream_t s = rt->stream;
     if (trials == 0) trials = 1;
+    int wrc = tune_node_widths(batch, trials);
+    if (wrc) return wrc;
     gbsp_batch_config keep = batch->cfg;
     // candidates: thread-per-pixel (block x chunk x blocks per SM), path state
     // (block <= 128 x blocks per SM), wavefront (blocks per SM x wave size)

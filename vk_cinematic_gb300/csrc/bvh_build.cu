@@ -11,9 +11,12 @@
 //      per-block ranks from __match_any_sync);
 //   3. the binary radix tree of Karras (HPG 2012), one thread per node;
 //   4. bottom-up box refit with one atomic arrival counter per node;
-//   5. top-down collapse into 8-wide nodes: each wide node repeatedly opens
-//      its largest-area child until it has 8 children; subtrees of at most
-//      leafMax primitives become leaves.
+//   5. top-down collapse into wide nodes, once per node width (8 and 4)
+//      from the same binary tree: each wide node repeatedly opens its
+//      largest-area child until it has W children; subtrees of at most
+//      leafMax primitives become leaves.  Leaves index the primitives in the
+//      sorted Morton order, which both widths share, so one triangle pool
+//      serves the trees of both widths.
 // Every loop is bounded by the primitive count or log2 of it.
 
 #include <cstdio>
@@ -283,23 +286,54 @@ struct CollapseItem {
     uint32_t wide;  // output wide node (relative index)
 };
 
+// Writes one node of width 4 * quads (layout in gbsp_common.cuh).
+__device__ void store_node(float4 *dst, uint32_t quads, const float *lo, const float *hi,
+    const uint32_t *child)
+{
+    for (uint32_t q = 0; q < quads; q++) {
+        const uint32_t b = 4 * q;
+        dst[0 * quads + q] = make_float4(lo[3 * b + 0], lo[3 * (b + 1) + 0], lo[3 * (b + 2) + 0],
+            lo[3 * (b + 3) + 0]);
+        dst[1 * quads + q] = make_float4(hi[3 * b + 0], hi[3 * (b + 1) + 0], hi[3 * (b + 2) + 0],
+            hi[3 * (b + 3) + 0]);
+        dst[2 * quads + q] = make_float4(lo[3 * b + 1], lo[3 * (b + 1) + 1], lo[3 * (b + 2) + 1],
+            lo[3 * (b + 3) + 1]);
+        dst[3 * quads + q] = make_float4(hi[3 * b + 1], hi[3 * (b + 1) + 1], hi[3 * (b + 2) + 1],
+            hi[3 * (b + 3) + 1]);
+        dst[4 * quads + q] = make_float4(lo[3 * b + 2], lo[3 * (b + 1) + 2], lo[3 * (b + 2) + 2],
+            lo[3 * (b + 3) + 2]);
+        dst[5 * quads + q] = make_float4(hi[3 * b + 2], hi[3 * (b + 1) + 2], hi[3 * (b + 2) + 2],
+            hi[3 * (b + 3) + 2]);
+        dst[6 * quads + q] = make_float4(__uint_as_float(child[b]), __uint_as_float(child[b + 1]),
+            __uint_as_float(child[b + 2]), __uint_as_float(child[b + 3]));
+    }
+}
+
+__device__ __forceinline__ uint32_t node_child(const float4 *node, uint32_t quads, uint32_t c)
+{
+    const float4 v = node[6 * quads + c / 4];
+    const float f = (c & 3) == 0 ? v.x : (c & 3) == 1 ? v.y : (c & 3) == 2 ? v.z : v.w;
+    return __float_as_uint(f);
+}
+
+template <int W>
 __global__ void collapse_level(const CollapseItem *in, uint32_t inCount, CollapseItem *out,
     uint32_t *outCount, uint32_t *nodeCounter, uint32_t nodeCapacity, const uint32_t *left,
     const uint32_t *right, const uint32_t *first, const uint32_t *last, const float4 *nodeLo,
     const float4 *nodeHi, const float4 *primLo, const float4 *primHi, const uint32_t *order,
-    uint32_t leafMax, Node8 *nodes, uint32_t *status)
+    uint32_t leafMax, float4 *nodes, uint32_t *status)
 {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= inCount) return;
     CollapseItem item = in[k];
-    uint32_t ch[8];
-    float4 clo[8], chi[8];
+    uint32_t ch[W];
+    float4 clo[W], chi[W];
     int cnt = 2;
     ch[0] = left[item.bin];
     ch[1] = right[item.bin];
     child_box(ch[0], nodeLo, nodeHi, primLo, primHi, order, clo[0], chi[0]);
     child_box(ch[1], nodeLo, nodeHi, primLo, primHi, order, clo[1], chi[1]);
-    while (cnt < 8) {
+    while (cnt < W) {
         int best = -1;
         float bestArea = -1.0f;
         for (int c = 0; c < cnt; c++) {
@@ -318,38 +352,39 @@ __global__ void collapse_level(const CollapseItem *in, uint32_t inCount, Collaps
         child_box(ch[cnt], nodeLo, nodeHi, primLo, primHi, order, clo[cnt], chi[cnt]);
         cnt++;
     }
-    Node8 node;
-    for (int c = 0; c < 8; c++) {
+    float lo[3 * W], hi[3 * W];
+    uint32_t child[W];
+    for (int c = 0; c < W; c++) {
         if (c >= cnt) {
-            node.lox[c] = node.loy[c] = node.loz[c] = 1.0f;
-            node.hix[c] = node.hiy[c] = node.hiz[c] = 0.0f;
-            node.child[c] = kEmptyChild;
+            lo[3 * c] = lo[3 * c + 1] = lo[3 * c + 2] = 1.0f;
+            hi[3 * c] = hi[3 * c + 1] = hi[3 * c + 2] = 0.0f;
+            child[c] = kEmptyChild;
             continue;
         }
-        node.lox[c] = clo[c].x;
-        node.loy[c] = clo[c].y;
-        node.loz[c] = clo[c].z;
-        node.hix[c] = chi[c].x;
-        node.hiy[c] = chi[c].y;
-        node.hiz[c] = chi[c].z;
+        lo[3 * c] = clo[c].x;
+        lo[3 * c + 1] = clo[c].y;
+        lo[3 * c + 2] = clo[c].z;
+        hi[3 * c] = chi[c].x;
+        hi[3 * c + 1] = chi[c].y;
+        hi[3 * c + 2] = chi[c].z;
         uint32_t r = ch[c];
         if (r & kBinLeaf) {
-            node.child[c] = make_leaf(r & ~kBinLeaf, 1u);
+            child[c] = make_leaf(r & ~kBinLeaf, 1u);
         } else if (last[r] - first[r] + 1u <= leafMax) {
-            node.child[c] = make_leaf(first[r], last[r] - first[r] + 1u);
+            child[c] = make_leaf(first[r], last[r] - first[r] + 1u);
         } else {
             uint32_t w = atomicAdd(nodeCounter, 1u);
             if (w >= nodeCapacity) {
                 atomicOr(status, kStatusBuildLoop);
-                node.child[c] = kEmptyChild;
+                child[c] = kEmptyChild;
                 continue;
             }
-            node.child[c] = w;
+            child[c] = w;
             uint32_t slot = atomicAdd(outCount, 1u);
             out[slot] = CollapseItem{r, w};
         }
     }
-    nodes[item.wide] = node;
+    store_node(nodes + node_offset(item.wide, W / 4), W / 4, lo, hi, child);
 }
 
 // Structural check of a freshly built tree (relative indices): every
@@ -357,14 +392,14 @@ __global__ void collapse_level(const CollapseItem *in, uint32_t inCount, Collaps
 // count, every leaf range lies inside the primitives.  Children are always
 // allocated after their parent, so this rules out cycles and makes every
 // traversal loop finite.
-__global__ void validate_nodes(const Node8 *nodes, uint32_t count, uint32_t prims,
-    uint32_t *status)
+__global__ void validate_nodes(const float4 *nodes, uint32_t quads, uint32_t count,
+    uint32_t prims, uint32_t *status)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    const Node8 &n = nodes[i];
-    for (int c = 0; c < 8; c++) {
-        uint32_t r = n.child[c];
+    const float4 *n = nodes + node_offset(i, quads);
+    for (uint32_t c = 0; c < 4 * quads; c++) {
+        uint32_t r = node_child(n, quads, c);
         if (r == kEmptyChild) continue;
         bool ok = child_is_leaf(r) ? (leaf_first(r) + leaf_count(r) <= prims)
                                    : (r > i && r < count);
@@ -372,34 +407,29 @@ __global__ void validate_nodes(const Node8 *nodes, uint32_t count, uint32_t prim
     }
 }
 
-__global__ void single_leaf_root(const float4 *lo, const float4 *hi, Node8 *nodes)
+__global__ void single_leaf_root(const float4 *lo, const float4 *hi, float4 *nodes, uint32_t quads)
 {
-    Node8 node;
+    float l[24], h[24];
+    uint32_t child[8];
     for (int c = 0; c < 8; c++) {
-        node.lox[c] = node.loy[c] = node.loz[c] = 1.0f;
-        node.hix[c] = node.hiy[c] = node.hiz[c] = 0.0f;
-        node.child[c] = kEmptyChild;
+        l[3 * c] = l[3 * c + 1] = l[3 * c + 2] = 1.0f;
+        h[3 * c] = h[3 * c + 1] = h[3 * c + 2] = 0.0f;
+        child[c] = kEmptyChild;
     }
-    node.lox[0] = lo[0].x;
-    node.loy[0] = lo[0].y;
-    node.loz[0] = lo[0].z;
-    node.hix[0] = hi[0].x;
-    node.hiy[0] = hi[0].y;
-    node.hiz[0] = hi[0].z;
-    node.child[0] = make_leaf(0, 1);
-    nodes[0] = node;
+    l[0] = lo[0].x;
+    l[1] = lo[0].y;
+    l[2] = lo[0].z;
+    h[0] = hi[0].x;
+    h[1] = hi[0].y;
+    h[2] = hi[0].z;
+    child[0] = make_leaf(0, 1);
+    store_node(nodes, quads, l, h, child);
 }
 
 __global__ void init_bounds(int *b)
 {
     if (threadIdx.x < 3) b[threadIdx.x] = 0x7FFFFFFF;  // ordered +max
     else if (threadIdx.x < 6) b[threadIdx.x] = (int)0x80000000;
-}
-
-__global__ void copy_nodes(const Node8 *src, Node8 *dst, uint32_t count)
-{
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) dst[i] = src[i];
 }
 
 inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
@@ -460,73 +490,84 @@ __global__ void k_mesh_emit(const gbsp_vertex *v, const uint32_t *idx, uint32_t 
     triIds[j] = t;
 }
 
-__global__ void k_offset_nodes(Node8 *nodes, uint32_t count, uint32_t nodeBase, uint32_t leafBase)
+__global__ void k_offset_nodes(float4 *nodes, uint32_t quads, uint32_t count, uint32_t nodeBase,
+    uint32_t leafBase)
 {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    Node8 &n = nodes[i];
-    for (int c = 0; c < 8; c++) {
-        uint32_t r = n.child[c];
-        if (r == kEmptyChild) continue;
-        if (child_is_leaf(r))
-            n.child[c] = make_leaf(leaf_first(r) + leafBase, leaf_count(r));
-        else
-            n.child[c] = r + nodeBase;
+    float4 *n = nodes + node_offset(i, quads);
+    for (uint32_t q = 0; q < quads; q++) {
+        float4 &v = n[6 * quads + q];
+        float *w = &v.x;
+        for (int k = 0; k < 4; k++) {
+            uint32_t r = __float_as_uint(w[k]);
+            if (r == kEmptyChild) continue;
+            r = child_is_leaf(r) ? make_leaf(leaf_first(r) + leafBase, leaf_count(r)) : r + nodeBase;
+            w[k] = __uint_as_float(r);
+        }
     }
 }
 
-int offset_nodes(cudaStream_t s, Node8 *dNodes, uint32_t nodeCount, uint32_t nodeBase,
+int offset_nodes(cudaStream_t s, NodePool &pool, uint32_t nodeCount, uint32_t nodeBase,
     uint32_t leafBase)
 {
     if (!nodeCount) return GBSP_OK;
-    k_offset_nodes<<<blocks_for(nodeCount, 128), 128, 0, s>>>(dNodes, nodeCount, nodeBase, leafBase);
+    k_offset_nodes<<<blocks_for(nodeCount, 128), 128, 0, s>>>(pool.node(nodeBase), pool.quads,
+        nodeCount, nodeBase, leafBase);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }
 
 int mesh_emit(cudaStream_t s, const gbsp_vertex *dVerts, const uint32_t *dIdx, uint32_t triCount,
-    const uint32_t *dOrder, TriRecord *dTris, TriAttr *dAttrs, uint32_t *dTriIds,
-    uint32_t nodeBase, Node8 *dNodes, uint32_t nodeCount, uint32_t triBase)
+    const uint32_t *dOrder, TriRecord *dTris, TriAttr *dAttrs, uint32_t *dTriIds, uint32_t triBase)
 {
     k_mesh_emit<<<blocks_for(triCount, 256), 256, 0, s>>>(dVerts, dIdx, triCount, dOrder, dTris,
         dAttrs, dTriIds);
     GBSP_CUDA_TRY(cudaGetLastError());
-    return offset_nodes(s, dNodes + nodeBase, nodeCount, nodeBase, triBase);
+    return GBSP_OK;
+}
+
+// Grows a node pool to at least `nodes` nodes, keeping its contents.
+static int grow_pool(cudaStream_t s, NodePool &pool, size_t nodes)
+{
+    size_t want = nodes * kNodeComponents * pool.quads;
+    if (want <= pool.buf.count && pool.buf.ptr) return GBSP_OK;
+    DeviceBuffer<float4> grown;
+    int rc = grown.reserve(want * 3 / 2 + 64, s);
+    if (rc) return rc;
+    if (pool.buf.ptr && pool.buf.count)
+        GBSP_CUDA_TRY(cudaMemcpyAsync(grown.ptr, pool.buf.ptr, pool.buf.count * sizeof(float4),
+            cudaMemcpyDeviceToDevice, s));
+    pool.buf.release();
+    pool.buf.ptr = grown.ptr;
+    pool.buf.count = grown.count;
+    pool.buf.stream = s;
+    grown.ptr = nullptr;
+    grown.count = 0;
+    return GBSP_OK;
 }
 
 int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_t n,
-    uint32_t leafMax, DeviceBuffer<Node8> *nodes, uint32_t nodeBase, uint32_t *nodeCountOut,
-    DeviceBuffer<uint32_t> *orderOut, uint32_t *depthOut, uint32_t *dStatus)
+    uint32_t leafMax, NodePool *pools, const uint32_t *nodeBase, WideTree *trees,
+    DeviceBuffer<uint32_t> *orderOut, uint32_t *dStatus)
 {
     if (n == 0) return set_error(GBSP_ERR_INVALID_ARGUMENT, "BVH over zero primitives");
     if (n >= (1u << 27)) return set_error(GBSP_ERR_CAPACITY, "BVH over %u primitives (max 2^27)", n);
     int rc;
     uint32_t capacity = n > 1 ? n - 1 : 1;  // wide nodes never exceed binary internal nodes
-    // grow the pool, keeping the existing nodes
-    if ((size_t)nodeBase + capacity > nodes->count) {
-        DeviceBuffer<Node8> grown;
-        size_t want = ((size_t)nodeBase + capacity) * 3 / 2 + 16;
-        if ((rc = grown.reserve(want, s))) return rc;
-        if (nodeBase)
-            copy_nodes<<<blocks_for(nodeBase, 128), 128, 0, s>>>(nodes->ptr, grown.ptr, nodeBase);
-        GBSP_CUDA_TRY(cudaGetLastError());
-        nodes->release();
-        nodes->ptr = grown.ptr;
-        nodes->count = grown.count;
-        nodes->stream = s;
-        grown.ptr = nullptr;
-        grown.count = 0;
-    }
+    for (int w = 0; w < kNodeWidths; w++)
+        if ((rc = grow_pool(s, pools[w], (size_t)nodeBase[w] + capacity))) return rc;
     if ((rc = orderOut->reserve(n, s))) return rc;
-    Node8 *out = nodes->ptr + nodeBase;
     if (n == 1) {
-        single_leaf_root<<<1, 1, 0, s>>>(dLo, dHi, out);
+        for (int w = 0; w < kNodeWidths; w++) {
+            single_leaf_root<<<1, 1, 0, s>>>(dLo, dHi, pools[w].node(nodeBase[w]), pools[w].quads);
+            trees[w].nodeCount = 1;
+            trees[w].depth = 1;
+        }
         GBSP_CUDA_TRY(cudaGetLastError());
         uint32_t zero = 0;
         GBSP_CUDA_TRY(cudaMemcpyAsync(orderOut->ptr, &zero, 4, cudaMemcpyHostToDevice, s));
         GBSP_CUDA_TRY(cudaStreamSynchronize(s));
-        *nodeCountOut = 1;
-        *depthOut = 1;
         return GBSP_OK;
     }
 
@@ -571,33 +612,42 @@ int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_
         order, nodeLo.ptr, nodeHi.ptr, arrivals.ptr, dStatus);
     GBSP_CUDA_TRY(cudaGetLastError());
 
-    // collapse, level by level; counters: [0] node counter, [1..2] queue counts
-    uint32_t init[4] = {1, 0, 0, 0};
-    GBSP_CUDA_TRY(cudaMemcpyAsync(counters.ptr, init, 16, cudaMemcpyHostToDevice, s));
-    CollapseItem rootItem = {0, 0};
-    GBSP_CUDA_TRY(cudaMemcpyAsync(q[0].ptr, &rootItem, sizeof(rootItem), cudaMemcpyHostToDevice, s));
-    uint32_t inCount = 1, depth = 0;
-    int qi = 0;
-    while (inCount > 0) {
-        if (depth > 200) return set_error(GBSP_ERR_DEVICE_STATUS, "BVH collapse exceeded 200 levels");
-        GBSP_CUDA_TRY(cudaMemsetAsync(counters.ptr + 1 + (qi ^ 1), 0, 4, s));
-        collapse_level<<<blocks_for(inCount, 128), 128, 0, s>>>(q[qi].ptr, inCount, q[qi ^ 1].ptr,
-            counters.ptr + 1 + (qi ^ 1), counters.ptr, capacity, left.ptr, right.ptr, first.ptr,
-            last.ptr, nodeLo.ptr, nodeHi.ptr, dLo, dHi, order, leafMax, out, dStatus);
-        GBSP_CUDA_TRY(cudaGetLastError());
-        GBSP_CUDA_TRY(cudaMemcpyAsync(&inCount, counters.ptr + 1 + (qi ^ 1), 4,
-            cudaMemcpyDeviceToHost, s));
+    // collapse the same binary tree once per width, level by level;
+    // counters: [0] node counter, [1..2] queue counts
+    for (int w = 0; w < kNodeWidths; w++) {
+        float4 *out = pools[w].node(nodeBase[w]);
+        uint32_t init[4] = {1, 0, 0, 0};
+        GBSP_CUDA_TRY(cudaMemcpyAsync(counters.ptr, init, 16, cudaMemcpyHostToDevice, s));
+        CollapseItem rootItem = {0, 0};
+        GBSP_CUDA_TRY(cudaMemcpyAsync(q[0].ptr, &rootItem, sizeof(rootItem), cudaMemcpyHostToDevice,
+            s));
+        uint32_t inCount = 1, depth = 0;
+        int qi = 0;
+        while (inCount > 0) {
+            if (depth > 200)
+                return set_error(GBSP_ERR_DEVICE_STATUS, "BVH collapse exceeded 200 levels");
+            GBSP_CUDA_TRY(cudaMemsetAsync(counters.ptr + 1 + (qi ^ 1), 0, 4, s));
+            auto kern = pools[w].quads == 2 ? collapse_level<8> : collapse_level<4>;
+            kern<<<blocks_for(inCount, 128), 128, 0, s>>>(q[qi].ptr, inCount, q[qi ^ 1].ptr,
+                counters.ptr + 1 + (qi ^ 1), counters.ptr, capacity, left.ptr, right.ptr,
+                first.ptr, last.ptr, nodeLo.ptr, nodeHi.ptr, dLo, dHi, order, leafMax, out, dStatus);
+            GBSP_CUDA_TRY(cudaGetLastError());
+            GBSP_CUDA_TRY(cudaMemcpyAsync(&inCount, counters.ptr + 1 + (qi ^ 1), 4,
+                cudaMemcpyDeviceToHost, s));
+            GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+            qi ^= 1;
+            depth++;
+        }
+        uint32_t used = 0;
+        GBSP_CUDA_TRY(cudaMemcpyAsync(&used, counters.ptr, 4, cudaMemcpyDeviceToHost, s));
         GBSP_CUDA_TRY(cudaStreamSynchronize(s));
-        qi ^= 1;
-        depth++;
+        if (used > capacity) used = capacity;
+        validate_nodes<<<blocks_for(used, 128), 128, 0, s>>>(out, pools[w].quads, used, n, dStatus);
+        GBSP_CUDA_TRY(cudaGetLastError());
+        trees[w].nodeCount = used;
+        trees[w].depth = depth;
     }
-    uint32_t used = 0;
-    GBSP_CUDA_TRY(cudaMemcpyAsync(&used, counters.ptr, 4, cudaMemcpyDeviceToHost, s));
     GBSP_CUDA_TRY(cudaMemcpyAsync(orderOut->ptr, order, 4 * (size_t)n, cudaMemcpyDeviceToDevice, s));
-    GBSP_CUDA_TRY(cudaStreamSynchronize(s));
-    if (used > capacity) used = capacity;
-    validate_nodes<<<blocks_for(used, 128), 128, 0, s>>>(out, used, n, dStatus);
-    GBSP_CUDA_TRY(cudaGetLastError());
     uint32_t st = 0;
     GBSP_CUDA_TRY(cudaMemcpyAsync(&st, dStatus, 4, cudaMemcpyDeviceToHost, s));
     GBSP_CUDA_TRY(cudaStreamSynchronize(s));
@@ -605,8 +655,6 @@ int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_
         return set_error(GBSP_ERR_DEVICE_STATUS, "BVH build exceeded its node capacity");
     if (st & kStatusBadIndex)
         return set_error(GBSP_ERR_DEVICE_STATUS, "BVH build produced an invalid child reference");
-    *nodeCountOut = used;
-    *depthOut = depth;
     return GBSP_OK;
 }
 

@@ -299,11 +299,22 @@ GBSP_HD TriHit ray_triangle_watertight(V3 o, V3 d, V3 a, V3 b, V3 c, V3 n)
 // ---------------------------------------------------------------------------
 // Device scene layout
 // ---------------------------------------------------------------------------
-// 8-wide BVH node, structure of arrays inside the node: 224 bytes = 7 x 32 B
-// sectors, loaded with 128-bit loads.  child[k]:
-//   < 0x80000000  internal node index
+// BVH node of width 4 * Q children, Q = 2 (8-wide) or Q = 1 (4-wide, the
+// reference's width, src/bvh.h:4-12): structure of arrays inside the node,
+// 7 * Q float4 loaded with 128-bit loads.  Float4 number c * Q + q of a node
+// holds component c of its children 4q .. 4q+3, with c = 0..5 the child
+// boxes' lo.x, hi.x, lo.y, hi.y, lo.z, hi.z and c = 6 the child words:
+//   < 0x80000000  internal node index (in nodes of the same width)
 //   0xFFFFFFFF    empty slot
 //   otherwise     leaf: bits 30..3 first primitive, bits 2..0 count - 1
+// An 8-wide node is 224 bytes = 7 x 32 B sectors, a 4-wide node 112 bytes.
+constexpr uint32_t kNodeComponents = 7;
+constexpr uint32_t kMaxNodeQuads = 2;
+GBSP_HD size_t node_offset(uint32_t ref, uint32_t quads)
+{
+    return (size_t)ref * kNodeComponents * quads;
+}
+// The 8-wide node as a struct (the same bytes as Q = 2 above).
 struct __align__(16) Node8 {
     float lox[8], hix[8], loy[8], hiy[8], loz[8], hiz[8];
     uint32_t child[8];
@@ -371,7 +382,8 @@ struct SkyParams {
 
 // Everything a kernel needs to trace and shade against one scene.
 struct SceneView {
-    const Node8 *nodes;          // node pool (all mesh BVHs + object BVH)
+    const float4 *nodes;         // node pool (all mesh BVHs + object BVH), nodeQuads wide
+    uint32_t nodeQuads;          // 2: 8-wide nodes, 1: 4-wide nodes
     const TriRecord *tris;       // leaf-ordered triangles of all meshes
     const TriAttr *attrs;        // per triangle, same order
     const uint32_t *triIds;      // leaf order -> the mesh's own triangle index

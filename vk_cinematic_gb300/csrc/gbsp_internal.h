@@ -67,6 +67,24 @@ struct DeviceBuffer {
 
 struct Counters;  // device metric block
 
+// BVH node widths the library builds for every mesh and object BVH: index 0
+// holds the 8-wide trees (2 quads per node), index 1 the 4-wide trees.
+constexpr int kNodeWidths = 2;
+constexpr uint32_t kWidthQuads[kNodeWidths] = {2, 1};
+inline int width_index(uint32_t width) { return width == 4 ? 1 : 0; }
+
+// Device node pool of one width (layout in gbsp_common.cuh).
+struct NodePool {
+    DeviceBuffer<float4> buf;
+    uint32_t quads = 2;
+    float4 *node(uint32_t i) const { return buf.ptr + node_offset(i, quads); }
+};
+
+struct WideTree {
+    uint32_t nodeCount = 0;
+    uint32_t depth = 0;
+};
+
 }  // namespace gbsp
 
 // A runtime lives until gbsp_runtime_destroy has been called AND every scene
@@ -123,11 +141,11 @@ struct gbsp_runtime {
 };
 
 struct gbsp_mesh_info {
-    uint32_t rootNode;     // in the scene's node pool
+    uint32_t rootNode[gbsp::kNodeWidths];   // in the scene's node pool of each width
     uint32_t triFirst;     // first triangle in the pool
     uint32_t triCount;
-    uint32_t nodeCount;
-    uint32_t depth;
+    uint32_t nodeCount[gbsp::kNodeWidths];
+    uint32_t depth[gbsp::kNodeWidths];
     bool smooth;
     float aabbMin[3], aabbMax[3];  // vertex AABB (src/sp_scene.cpp:57-75)
 };
@@ -143,31 +161,41 @@ struct gbsp_scene {
     gbsp_runtime *rt = nullptr;
     std::vector<gbsp_mesh_info> meshes;
     std::vector<gbsp_object_info> objects;
-    // node pool: mesh BVHs first, then the object BVH (rebuilt per commit)
-    gbsp::DeviceBuffer<gbsp::Node8> nodes;
-    uint32_t meshNodeCount = 0;   // nodes used by meshes
-    uint32_t totalNodeCount = 0;
+    // node pools, one per width: mesh BVHs first, then the object BVH
+    // (rebuilt per commit); renders use the pool of nodeWidth
+    gbsp::NodePool nodes[gbsp::kNodeWidths];
+    uint32_t meshNodeCount[gbsp::kNodeWidths] = {0, 0};   // nodes used by meshes
+    uint32_t totalNodeCount[gbsp::kNodeWidths] = {0, 0};
     gbsp::DeviceBuffer<gbsp::TriRecord> tris;
     gbsp::DeviceBuffer<gbsp::TriAttr> attrs;
     gbsp::DeviceBuffer<uint32_t> triIds;
     uint64_t triCount = 0;
-    gbsp::DeviceBuffer<gbsp::Instance> instances;
-    uint32_t tlasRoot = gbsp::kEmptyChild;
-    uint32_t tlasDepth = 0;
-    uint32_t maxDepth = 0;
+    // instances in object-BVH leaf order, one array per width (they differ
+    // only in the mesh root node index)
+    gbsp::DeviceBuffer<gbsp::Instance> instances[gbsp::kNodeWidths];
+    uint32_t tlasRoot[gbsp::kNodeWidths] = {gbsp::kEmptyChild, gbsp::kEmptyChild};
+    uint32_t tlasDepth[gbsp::kNodeWidths] = {0, 0};
+    uint32_t maxDepth[gbsp::kNodeWidths] = {0, 0};
+    uint32_t nodeWidth = 8;       // 8 or 4
     bool committed = false;
     uint32_t isectMode = GBSP_ISECT_REFERENCE_MT;
     std::vector<uint32_t> leafOrder;  // object-BVH leaf position -> object index
-    // resolved material slots depend on the material system; objects keep ids
-    gbsp::SceneView view() const
+    gbsp_scene()
     {
+        for (int w = 0; w < gbsp::kNodeWidths; w++) nodes[w].quads = gbsp::kWidthQuads[w];
+    }
+    // resolved material slots depend on the material system; objects keep ids
+    gbsp::SceneView view(uint32_t width = 0) const
+    {
+        int w = gbsp::width_index(width ? width : nodeWidth);
         gbsp::SceneView v;
-        v.nodes = nodes.ptr;
+        v.nodes = nodes[w].buf.ptr;
+        v.nodeQuads = nodes[w].quads;
         v.tris = tris.ptr;
         v.attrs = attrs.ptr;
         v.triIds = triIds.ptr;
-        v.instances = instances.ptr;
-        v.tlasRoot = tlasRoot;
+        v.instances = instances[w].ptr;
+        v.tlasRoot = tlasRoot[w];
         v.instanceCount = (uint32_t)objects.size();
         v.watertight = isectMode == GBSP_ISECT_WATERTIGHT ? 1u : 0u;
         return v;
@@ -193,20 +221,24 @@ struct gbsp_material_system {
 namespace gbsp {
 
 // bvh_build.cu
-// Builds an 8-wide BVH over n primitive boxes on the device.  Appends the
-// nodes to *nodes starting at nodeBase (growing the pool, keeping its
-// contents) and returns the primitive order (sorted position -> primitive).
+// Builds the wide BVHs (8- and 4-wide, from one binary tree) over n
+// primitive boxes on the device.  Tree w is appended to pools[w] at
+// nodeBase[w] (growing the pool, keeping its contents), with node indices
+// relative to nodeBase[w]; trees[w] receives its node count and depth.
+// Returns the primitive order (sorted position -> primitive) both trees'
+// leaves index.
 int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_t n,
-    uint32_t leafMax, DeviceBuffer<Node8> *nodes, uint32_t nodeBase, uint32_t *nodeCountOut,
-    DeviceBuffer<uint32_t> *orderOut, uint32_t *depthOut, uint32_t *dStatus);
+    uint32_t leafMax, NodePool *pools, const uint32_t *nodeBase, WideTree *trees,
+    DeviceBuffer<uint32_t> *orderOut, uint32_t *dStatus);
 // Triangle boxes + records for a mesh: positions from VertexPNT, indices.
 int mesh_prepare(cudaStream_t s, const gbsp_vertex *dVerts, const uint32_t *dIdx,
     uint32_t triCount, float4 *dLo, float4 *dHi);
 int mesh_emit(cudaStream_t s, const gbsp_vertex *dVerts, const uint32_t *dIdx,
     uint32_t triCount, const uint32_t *dOrder, TriRecord *dTris, TriAttr *dAttrs,
-    uint32_t *dTriIds, uint32_t nodeBase, Node8 *dNodes, uint32_t nodeCount,
-    uint32_t triBase);
-int offset_nodes(cudaStream_t s, Node8 *dNodes, uint32_t nodeCount, uint32_t nodeBase,
+    uint32_t *dTriIds, uint32_t triBase);
+// Moves nodeCount nodes at nodeBase of a pool from relative to absolute
+// indices (child node indices += nodeBase, leaf first += leafBase).
+int offset_nodes(cudaStream_t s, NodePool &pool, uint32_t nodeCount, uint32_t nodeBase,
     uint32_t leafBase);
 
 // trace.cu

@@ -49,22 +49,26 @@ struct TraceCounters {
 
 __device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765625f; }
 
-// Tests the 8 children of a node against the ray, pushing hits nearest-last.
-// kWT: the watertight mode's robust slab test.
-template <bool kCount, bool kWT = false>
-__device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint32_t ref, V3 o,
-    V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
-    TraceCounters &cnt)
+// Tests the children of a node (4 per quad, `quads` = 1 or 2) against the
+// ray, pushing hits nearest-last.  kWT: the watertight mode's robust slab
+// test.  With kKeepNearest the nearest hit child is not pushed but returned
+// in *next (ref kEmptyChild when no child is hit), for the caller to visit
+// straight away: one stack store and load fewer per node visit.
+template <bool kCount, bool kWT = false, bool kKeepNearest = false>
+__device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint32_t quads,
+    uint32_t ref, V3 o, V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
+    TraceCounters &cnt, StackEntry *next = nullptr)
 {
-    const float4 *p = reinterpret_cast<const float4 *>(nodes + ref);
+    const float4 *p = pool + node_offset(ref, quads);
     uint32_t nearRef = kEmptyChild;
     float nearT = kInf;
 #pragma unroll
-    for (int half = 0; half < 2; half++) {
-        float4 lx = __ldg(p + 0 + half), hx = __ldg(p + 2 + half);
-        float4 ly = __ldg(p + 4 + half), hy = __ldg(p + 6 + half);
-        float4 lz = __ldg(p + 8 + half), hz = __ldg(p + 10 + half);
-        uint4 ch = __ldg(reinterpret_cast<const uint4 *>(p + 12 + half));
+    for (int half = 0; half < (int)kMaxNodeQuads; half++) {
+        if (half >= (int)quads) break;
+        float4 lx = __ldg(p + 0 * quads + half), hx = __ldg(p + 1 * quads + half);
+        float4 ly = __ldg(p + 2 * quads + half), hy = __ldg(p + 3 * quads + half);
+        float4 lz = __ldg(p + 4 * quads + half), hz = __ldg(p + 5 * quads + half);
+        uint4 ch = __ldg(reinterpret_cast<const uint4 *>(p + 6 * quads + half));
         float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, hxs[4] = {hx.x, hx.y, hx.z, hx.w};
         float lys[4] = {ly.x, ly.y, ly.z, ly.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
         float lzs[4] = {lz.x, lz.y, lz.z, lz.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
@@ -98,7 +102,9 @@ __device__ __forceinline__ void visit_node(const Node8 *__restrict__ nodes, uint
             }
         }
     }
-    if (nearRef != kEmptyChild) {
+    if constexpr (kKeepNearest) {
+        *next = StackEntry{nearRef, nearT};
+    } else if (nearRef != kEmptyChild) {
         if (sp < kStackSize) {
             stack[sp] = StackEntry{nearRef, nearT};
             sp++;
@@ -157,25 +163,33 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
     StackEntry stack[kStackSize];
     int sp = 0;
     V3 invd = inverse(d);
-    stack[sp] = StackEntry{sv.tlasRoot, 0.0f};
-    sp++;
-    const Node8 *__restrict__ nodes = sv.nodes;
+    // the entry to visit next (the nearest child of the last node visit),
+    // kept out of the stack
+    StackEntry next = StackEntry{sv.tlasRoot, 0.0f};
+    const float4 *__restrict__ nodes = sv.nodes;
+    const uint32_t quads = sv.nodeQuads;
     // trees are validated at build time (children after parents), so the
     // walk is finite; the guard only bounds it against corrupted memory
-    for (int guard = 0; sp > 0; guard++) {
+    for (int guard = 0; next.ref != kEmptyChild || sp > 0; guard++) {
         if (guard >= (1 << 20)) {
             atomicOr(status, kStatusStackOverflow);
             break;
         }
-        sp--;
-        const StackEntry top = stack[sp];
+        StackEntry top;
+        if (next.ref != kEmptyChild) {
+            top = next;
+            next.ref = kEmptyChild;
+        } else {
+            sp--;
+            top = stack[sp];
+        }
         uint32_t ref = top.ref;
         float te = top.t;
         if (te > prune_bound(best.t)) continue;
         if (!child_is_leaf(ref)) {
             if (kCount) cnt.topNodes++;
-            visit_node<kCount, kWT>(nodes, ref, o, invd, prune_bound(best.t), stack,
-                sp, status, cnt);
+            visit_node<kCount, kWT, true>(nodes, quads, ref, o, invd, prune_bound(best.t), stack,
+                sp, status, cnt, &next);
             continue;
         }
         // an object whose world box passed: descend into its mesh
@@ -192,24 +206,25 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
         float lBestT = kInf, lU = 0.0f, lV = 0.0f;
         int32_t lPrim = -1;
         float localBound = best.t * len;
-        int base = sp;
-        if (sp >= kStackSize) {
-            atomicOr(status, kStatusStackOverflow);
-            continue;
-        }
-        stack[sp] = StackEntry{__ldg(&in.blasRoot), 0.0f};
-        sp++;
-        for (int guard = 0; sp > base && guard < (1 << 22); guard++) {
-            sp--;
-            const StackEntry top = stack[sp];
-            uint32_t r2 = top.ref;
-            float t2 = top.t;
+        const int base = sp;
+        StackEntry lnext = StackEntry{__ldg(&in.blasRoot), 0.0f};
+        for (int guard = 0; (lnext.ref != kEmptyChild || sp > base) && guard < (1 << 22); guard++) {
+            StackEntry top2;
+            if (lnext.ref != kEmptyChild) {
+                top2 = lnext;
+                lnext.ref = kEmptyChild;
+            } else {
+                sp--;
+                top2 = stack[sp];
+            }
+            uint32_t r2 = top2.ref;
+            float t2 = top2.t;
             float bound = prune_bound(rmin(lBestT, localBound));
             if (t2 > bound) continue;
             if (!child_is_leaf(r2)) {
                 if (kCount) cnt.meshNodes++;
-                visit_node<kCount, kWT>(nodes, r2, lo, linvd, bound, stack, sp, status,
-                    cnt);
+                visit_node<kCount, kWT, true>(nodes, quads, r2, lo, linvd, bound, stack, sp, status,
+                    cnt, &lnext);
             } else {
                 visit_leaf<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
             }

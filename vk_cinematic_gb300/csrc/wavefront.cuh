@@ -284,6 +284,9 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
     TraceCounters cnt = {0, 0, 0, 0, 0};
     uint32_t done = 0, hits = 0;
     StackEntry stack[kStackSize];
+    // next: the entry to visit next (the nearest child of the last node
+    // visit, or a root), kept out of the stack; ref kEmptyChild when none
+    StackEntry next = StackEntry{kEmptyChild, 0.0f};
     int sp = 0, base = 0;
     int mode = 0;  // 0 needs a ray, 1 object level, 2 mesh level
     uint32_t slot = 0, steps = 0, inst = 0;
@@ -318,18 +321,17 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
             bestU = bestV = 0.0f;
             bestPrim = bestInst = -1;
             sp = 0;
-            if (src.scene(pathId).tlasRoot != kEmptyChild) {
-                stack[0] = StackEntry{src.scene(pathId).tlasRoot, 0.0f};
-                sp = 1;
-            }
+            next = StackEntry{src.scene(pathId).tlasRoot, 0.0f};
             mode = 1;
         }
         if (++steps > kMaxLaneRaySteps) {
             atomicOr(status, kStatusRayStepLimit);
             mode = 1;
             sp = 0;  // store the best hit found so far
+            next.ref = kEmptyChild;
         }
-        if (mode == 2 && sp == base) {
+        const bool levelDone = sp == (mode == 2 ? base : 0) && next.ref == kEmptyChild;
+        if (mode == 2 && levelDone) {
             // leaving an object: its closest triangle goes back to world space
             if (lPrim >= 0) {
                 const Instance &in = src.scene(pathId).instances[inst];
@@ -347,7 +349,7 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                 }
             }
             mode = 1;
-        } else if (mode == 1 && sp == 0) {
+        } else if (mode == 1 && levelDone) {
             hitA[slot] = make_int4(__float_as_int(bestT), __float_as_int(bestU),
                 __float_as_int(bestV), bestPrim);
             hitInst[slot] = bestInst;
@@ -355,8 +357,14 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
             hits += (bestPrim >= 0 && bestT > 0.0f) ? 1u : 0u;
             mode = 0;
         } else {
-            sp--;
-            const StackEntry top = stack[sp];
+            StackEntry top;
+            if (next.ref != kEmptyChild) {
+                top = next;
+                next.ref = kEmptyChild;
+            } else {
+                sp--;
+                top = stack[sp];
+            }
             uint32_t ref = top.ref;
             float te = top.t;
             float bound = mode == 1 ? prune_bound(bestT) : prune_bound(rmin(lBestT, bestT * len));
@@ -367,8 +375,9 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                     cnt.topNodes++;
                 else
                     cnt.meshNodes++;
-                visit_node<true, kWT>(src.scene(pathId).nodes, ref, mode == 1 ? o : lo,
-                    mode == 1 ? invd : linvd, bound, stack, sp, status, cnt);
+                visit_node<true, kWT, true>(src.scene(pathId).nodes, src.scene(pathId).nodeQuads,
+                    ref, mode == 1 ? o : lo, mode == 1 ? invd : linvd, bound, stack, sp, status,
+                    cnt, &next);
             } else if (mode == 1) {
                 // an object whose world box passed: enter its mesh
                 inst = leaf_first(ref);
@@ -384,13 +393,8 @@ __global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__res
                 lU = lV = 0.0f;
                 lPrim = -1;
                 base = sp;
-                if (sp >= kStackSize) {
-                    atomicOr(status, kStatusStackOverflow);
-                } else {
-                    stack[sp] = StackEntry{__ldg(&in.blasRoot), 0.0f};
-                    sp++;
-                    mode = 2;
-                }
+                next = StackEntry{__ldg(&in.blasRoot), 0.0f};
+                mode = 2;
             } else {
                 visit_leaf<true, kWT>(src.scene(pathId), ref, lo, ld, linvd, lBestT, lU, lV, lPrim,
                     cnt);

@@ -56,7 +56,8 @@ EXPORTS = [
     "gbsp_cpt_scene_create", "gbsp_cpt_scene_destroy", "gbsp_cpt_render_tiles",
     "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
     "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status", "gbsp_scene_set_intersection",
-    "gbsp_dn_tile_fallback",
+    "gbsp_dn_tile_fallback", "gbsp_scene_set_node_width", "gbsp_scene_node_width",
+    "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths",
 ]
 
 
@@ -140,6 +141,7 @@ def load(build_if_missing: bool = True):
     lib.gbsp_calculate_film_positions.restype = _u32
     lib.gbsp_xorshift32_jump.restype = _u32
     lib.gbsp_xorshift32_jump.argtypes = [_u32, ctypes.c_uint64]
+    lib.gbsp_scene_node_width.restype = _u32
     for name in EXPORTS:
         getattr(lib, name)  # raises if a declared symbol is not exported
     _LIB = lib
@@ -243,6 +245,14 @@ class Scene:
     def set_intersection(self, mode: int):
         """ISECT_REFERENCE_MT (default) or ISECT_WATERTIGHT."""
         _check(self.L.gbsp_scene_set_intersection(self.h, _u32(mode)))
+
+    def set_node_width(self, width: int):
+        """BVH node width of this scene's queries and renders: 8 (default) or 4."""
+        _check(self.L.gbsp_scene_set_node_width(self.h, _u32(width)))
+
+    @property
+    def node_width(self) -> int:
+        return int(self.L.gbsp_scene_node_width(self.h))
 
     def create_mesh(self, vertices: np.ndarray, indices: np.ndarray, smooth=False) -> int:
         v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 8)
@@ -485,6 +495,17 @@ class Batch:
         c = BatchConfig()
         _check(self.L.gbsp_batch_autotune(self.h, _u32(trials), ctypes.byref(c)))
         return c
+
+    def node_widths(self) -> list:
+        n = len(self._keep[0])
+        w = (_u32 * n)()
+        _check(self.L.gbsp_batch_get_node_widths(self.h, w))
+        return [int(v) for v in w]
+
+    def set_node_widths(self, widths):
+        n = len(self._keep[0])
+        w = (_u32 * n)(*[int(v) for v in widths])
+        _check(self.L.gbsp_batch_set_node_widths(self.h, w))
 
     def launch(self, metrics: bool = True):
         m = Metrics() if metrics else None
