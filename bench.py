@@ -58,11 +58,12 @@ def parse_args():
     ap.add_argument("--workload", choices=["config3", "config1", "config2", "config4", "config5",
                                            "compute_pt", "cubemap", "tc_rate"],
                     default="config3")
-    ap.add_argument("--dn-scenes", type=int, default=125)
-    ap.add_argument("--dn-crops", type=int, default=16)
+    ap.add_argument("--dn-scenes", type=int, default=2000)
+    ap.add_argument("--dn-crops", type=int, default=1)
     ap.add_argument("--dn-ref-spp", type=int, default=4096)
-    ap.add_argument("--dn-train-spp", default="1,2",
-                    help="input spp of the training crops (comma list: crops cycle through it)")
+    ap.add_argument("--dn-train-spp", default="4",
+                    help="input spp of the training crops (comma list: crops cycle through it; "
+                         "the last one is the quoted protocol's input spp)")
     ap.add_argument("--dn-steps", type=int, default=10000)
     ap.add_argument("--dn-lr", type=float, default=1e-4)
     ap.add_argument("--dn-eval-seeds", type=int, default=50)
@@ -77,6 +78,8 @@ def parse_args():
     ap.add_argument("--trace", choices=["hybrid", "warp", "lane"], default="hybrid",
                     help="closest-hit scheduling: per-warp for primary and per-lane for bounce "
                          "rays (library default), or one of the two for every bounce")
+    ap.add_argument("--node-width", type=int, choices=[4, 8], default=8,
+                    help="BVH node width of the rendered scene (8: library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override (profiling cases only)")
@@ -395,6 +398,7 @@ def run_gpu(args):
         flags |= gbsp.FLAG_SORT_DIRECTIONS
     opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed, flags=flags)
     scene, ms, rend = gbsp.upload_scene(rt, s, opt)
+    scene.set_node_width(args.node_width)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
     def barrier():
@@ -519,6 +523,7 @@ def run_gpu(args):
             "data": "synthetic: seeded procedural scene", "config": workload_config(s, args.workload),
             "mrays_per_s": rays_all / (elapsed_ms / 1e3) / 1e6,
             "parallelism": f"replicas x{world}", "trace_scheduling": args.trace,
+            "node_width": args.node_width,
             "sort_directions": bool(args.sort_dirs),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(M["kernel_launches"]), "clocks": clk,
@@ -708,13 +713,14 @@ def run_config2(args):
 
 
 def run_config5(args):
-    """Config 5: learned denoiser.  Train on path-traced pairs (low-spp inputs,
-    1 and 2 spp by default, + G-buffers, high-spp targets, 128x128 crops, batch
-    16, Adam, relMSE, 10,000 steps), then on held-out scenes compare, at equal render
-    resolution, the wall time for plain path tracing to reach relMSE 0.01
-    against an FP64-accumulated 16,384-spp oracle with the time of the
-    cheapest input spp whose denoised result meets it + denoising.  Prints its
-    own line."""
+    """Config 5: learned denoiser.  Train on path-traced pairs (by default the
+    quoted protocol: 2,000 seeded scenes, one 128x128 crop each, 4-spp inputs
+    + G-buffers, 4096-spp targets, batch 16, Adam lr 1e-4, relMSE loss), then
+    on 50 held-out scenes measure the served output - denoised, checked tile by
+    tile against an independent plain render, failing tiles served from plain
+    samples topped up to the bound - against an FP64-accumulated 16,384-spp
+    oracle, and compare at 1920x1080 the wall time of that served output with
+    plain path tracing to relMSE 0.01.  Prints its own line."""
     import torch
     from vk_cinematic_gb300 import denoiser, gbsp
 
@@ -735,6 +741,8 @@ def run_config5(args):
     g = torch.Generator(device="cpu").manual_seed(0)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     losses = []
+    clocks = ClockSampler(0)
+    clocks.start()
     ev0.record(stream)
     for step in range(args.dn_steps):
         idx = torch.randint(0, n, (16,), generator=g).cuda()
@@ -744,8 +752,9 @@ def run_config5(args):
             losses.append((step, float(loss.item())))
     ev1.record(stream)
     torch.cuda.synchronize()
+    train_clk = clocks.stop()
     train_ms = ev0.elapsed_time(ev1)
-    log("training", losses)
+    log("training", losses[::10])
     # FLOPs of one training step (batch 16 x 128 x 128): forward, data gradient of
     # layers 1..7 and weight gradient of every layer, each 2 x 9 x cin x cout per pixel
     px = 16 * 128 * 128
@@ -756,11 +765,12 @@ def run_config5(args):
     # ---- quality on held-out scenes (crops, FP64-accumulated oracle)
     crop = args.dn_eval_crop
     spps = [1, 2, 4, 8, 16, 32, 64, 128, 256, 512, 1024]
-    in_spps = [1, 2, 4, 8, 16]  # denoiser input spp candidates
+    in_spps = sorted(set([1, 2, 4, 8] + train_spp))
     plain = {k: [] for k in spps}
     den = {k: [] for k in in_spps}
-    checked = {k: [] for k in in_spps}
-    fell_back = {k: [] for k in in_spps}
+    served = {k: [] for k in in_spps}
+    flagged = {k: [] for k in in_spps}
+    fb_spp = {k: [] for k in in_spps}
     rng = np.random.default_rng(99)
     for e in range(args.dn_eval_seeds):
         se = denoiser.denoise_scene(20_000 + e)
@@ -772,18 +782,14 @@ def run_config5(args):
             img, _ = sre.render(x0, y0, crop, crop, k, seed=7 + k)
             plain[k].append(denoiser.relmse(img, ref))
         for k in in_spps:
-            rk, ak = sre.render(x0, y0, crop, crop, k, seed=5 + k, aov=True)
-            d = net.denoise(rk.unsqueeze(0).contiguous(), ak.unsqueeze(0).contiguous())[0]
-            den[k].append(denoiser.relmse(d, ref))
-            # the plain path tracer checks the denoiser: an independent render of the same spp
-            ck, _ = sre.render(x0, y0, crop, crop, k, seed=1000 + k)
-            dc, _, fl = net.denoise_checked(rk.unsqueeze(0).contiguous(),
-                                            ak.unsqueeze(0).contiguous(),
-                                            ck.unsqueeze(0).contiguous(), bound=0.01)
-            checked[k].append(denoiser.relmse(dc[0], ref))
-            fell_back[k].append(float(fl.float().mean().item()))
+            out, st = net.serve(sre, x0, y0, crop, crop, k, seed=5 + 31 * k, bound=0.01)
+            den[k].append(denoiser.relmse(st["denoised"], ref))
+            served[k].append(denoiser.relmse(out, ref))
+            flagged[k].append(st["flagged"] / st["tiles"])
+            fb_spp[k].append(st["fallback_samples"] / float(crop * crop))
     plain_mean = {k: float(np.mean(v)) for k, v in plain.items()}
     den_mean = {k: float(np.mean(v)) for k, v in den.items()}
+    served_mean = {k: float(np.mean(v)) for k, v in served.items()}
     # spp plain path tracing needs for relMSE 0.01 (log-log interpolation)
     need = None
     for a, b in zip(spps, spps[1:]):
@@ -795,66 +801,88 @@ def run_config5(args):
     if need is None and plain_mean[spps[-1]] > 0.01:
         # extrapolate with the Monte Carlo rate relMSE ~ 1/spp from the last point
         need = spps[-1] * plain_mean[spps[-1]] / 0.01
-    # cheapest denoiser input that meets the target on the held-out crops
-    in_spp = next((k for k in in_spps if den_mean[k] <= 0.01), None)
+    # the quoted protocol's input spp, and the cheapest input whose served output
+    # meets the bound on the held-out crops
+    quoted_spp = train_spp[-1]
+    cheapest = next((k for k in in_spps if served_mean[k] <= 0.01), None)
 
-    # ---- timing at 1920x1080: plain path tracing vs in_spp + denoise
+    # ---- timing at 1920x1080: plain path tracing vs the served output
     s = denoiser.denoise_scene(10_000)
     sr = denoiser.SceneRenderer(rt, s)
     W, H = s.width, s.height
-    timed_spp = in_spp or in_spps[-1]
-    sr.render(0, 0, W, H, timed_spp, seed=1, aov=True)  # warm-up
-    ev0.record(stream)
-    radk, aovk = sr.render(0, 0, W, H, timed_spp, seed=2, aov=True)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    tin_ms = ev0.elapsed_time(ev1)
-    xk = radk.unsqueeze(0).contiguous()
-    ak = aovk.unsqueeze(0).contiguous()
-    net.denoise(xk, ak)
-    ev0.record(stream)
-    net.denoise(xk, ak)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    dn_ms = ev0.elapsed_time(ev1)
+    clocks = ClockSampler(0)
+    clocks.start()
     ev0.record(stream)
     sr.render(0, 0, W, H, 64, seed=3)
     ev1.record(stream)
     torch.cuda.synchronize()
     ms_per_spp = ev0.elapsed_time(ev1) / 64.0
+    timing = {}
+    for k in sorted(set([quoted_spp] + ([cheapest] if cheapest else []))):
+        net.serve(sr, 0, 0, W, H, k, seed=1)  # warm-up
+        torch.cuda.synchronize()
+        reps = 5
+        t1 = time.perf_counter()
+        stats = []
+        for r in range(reps):
+            _, st = net.serve(sr, 0, 0, W, H, k, seed=11 + r)
+            stats.append(st)
+        torch.cuda.synchronize()
+        served_ms = (time.perf_counter() - t1) * 1e3 / reps
+        timing[k] = {"served_ms": served_ms,
+                     "flagged_tile_fraction": float(np.mean([x["flagged"] / x["tiles"]
+                                                             for x in stats])),
+                     "fallback_spp_per_pixel": float(np.mean([x["fallback_samples"] / (W * H)
+                                                              for x in stats]))}
+    xk, ak = sr.render(0, 0, W, H, quoted_spp, seed=2, aov=True)
+    net.denoise(xk.unsqueeze(0).contiguous(), ak.unsqueeze(0).contiguous())
+    ev0.record(stream)
+    net.denoise(xk.unsqueeze(0).contiguous(), ak.unsqueeze(0).contiguous())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dn_ms = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
     flops = 2.0 * W * H * sum(9 * ci * co for ci, co, _ in [(10, 48, 0)] + [(48, 48, 0)] * 6 +
                               [(48, 25, 1)])
     plain_ms = need * ms_per_spp if need else None
-    den_total_ms = tin_ms + dn_ms
+    headline_spp = quoted_spp if served_mean[quoted_spp] <= 0.01 else cheapest
+    served_ms = timing[headline_spp]["served_ms"] if headline_spp in timing else None
     bf16_peak = measured_bf16_peak()
-    value = (plain_ms / den_total_ms) if (plain_ms and in_spp) else None
+    value = (plain_ms / served_ms) if (plain_ms and served_ms) else None
     line = {
-        "metric": "time-to-relMSE 0.01 at 1080p: plain PT / (low spp + denoiser) (config 5)",
+        "metric": "time-to-relMSE 0.01 at 1080p: plain PT / served denoised output (config 5)",
         "value": value, "unit": "x (higher is better)",
         "n_gpus": 1, "higher_is_better": True, "dtype": "bf16 (conv) / f32", "vs_baseline": None,
         "data": "synthetic: path-traced seeded config-3-style scenes",
         "config": {"workload": "config5: KPCNN 8 x conv3x3 (48 ch) + softmax 5x5 filter",
+                   "train_scenes": args.dn_scenes, "crops_per_scene": args.dn_crops,
                    "train_crops": int(n), "crop": 128, "batch": 16, "steps": args.dn_steps,
                    "lr": args.dn_lr, "train_input_spp": train_spp, "target_spp": args.dn_ref_spp,
                    "eval_seeds": args.dn_eval_seeds, "eval_crop": crop,
-                   "oracle_spp": args.dn_oracle_spp, "conv": net.conv_impl},
-        "denoised_relmse_by_input_spp": den_mean, "denoiser_input_spp": in_spp,
-        "checked_by_plain_tiles": {k: {"relmse": float(np.mean(checked[k])),
-                                       "fallback_tile_fraction": float(np.mean(fell_back[k]))}
-                                   for k in in_spps},
+                   "oracle_spp": args.dn_oracle_spp, "conv": net.conv_impl,
+                   "served": "denoised; 16x16 tiles checked against an independent plain render "
+                             "of the same spp; failing tiles served from all their plain "
+                             "samples topped up to the spp the check estimates for the bound"},
+        "served_input_spp": headline_spp, "quoted_input_spp": quoted_spp,
+        "served_relmse_by_input_spp": served_mean,
+        "denoised_unchecked_relmse_by_input_spp": den_mean,
+        "flagged_tile_fraction_by_input_spp": {k: float(np.mean(v)) for k, v in flagged.items()},
+        "fallback_spp_per_pixel_by_input_spp": {k: float(np.mean(v)) for k, v in fb_spp.items()},
+        "served_relmse_max_over_crops": {k: float(np.max(v)) for k, v in served.items()},
         "plain_relmse_by_spp": plain_mean, "plain_spp_for_0.01": need,
-        "ms_plain_per_spp_1080p": ms_per_spp, "ms_input_render_1080p": tin_ms,
+        "ms_plain_per_spp_1080p": ms_per_spp, "plain_ms_to_0.01": plain_ms,
+        "served_ms_1080p": {str(k): v for k, v in timing.items()},
+        "served_ms_to_0.01": served_ms,
         "ms_denoise_1080p": dn_ms, "denoiser_tflops": flops / (dn_ms * 1e-3) / 1e12,
         "roofline": {"bound": "tensor", "kernel": "denoiser inference (8 x k_conv3x3_tc + filter)",
                      "achieved": flops / (dn_ms * 1e-3) / 1e12, "peak": bf16_peak[0],
                      "peak_source": bf16_peak[1], "unit": "TFLOP/s",
                      "frac": flops / (dn_ms * 1e-3) / 1e12 / bf16_peak[0], "traffic": None},
-        "plain_ms_to_0.01": plain_ms, "denoised_ms_to_0.01": den_total_ms if in_spp else None,
         "train_ms": train_ms, "train_ms_per_step": train_ms / args.dn_steps,
         "train_tflops": train_step_flops * args.dn_steps / (train_ms * 1e-3) / 1e12,
         "weight_grad_impl": net.wgrad_impl, "weight_grad_48x48_ms": wgrad_ms,
-        "dataset_s": data_s, "losses": losses,
-        "params": net.parameters_count(),
+        "dataset_s": data_s, "losses": losses[::10],
+        "params": net.parameters_count(), "clocks": clk, "clocks_training": train_clk,
     }
     print(json.dumps(line), flush=True)
     return 0

@@ -271,6 +271,16 @@ int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile,
  * in one device pass).  The frame stays on the device (gbsp_frame_device_pointer)
  * and is also copied to imagePlane->pixels when that is not NULL. */
 int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics);
+/* Many tiles of one frame in one device pass (hash-per-sample seeding only):
+ * the caller's per-tile loop of src/main.cpp:819-844 for an arbitrary subset
+ * of tiles, e.g. the tiles a denoised frame must serve from plain samples.
+ * Each tile is clipped to the image and rendered exactly as
+ * gbsp_path_trace_tile renders it (bit-identical pixels); tiles should not
+ * overlap.  Results land in the runtime's frame buffer
+ * (gbsp_frame_device_pointer) and, when imagePlane->pixels is not NULL, in
+ * those host pixels.  metrics NULL and no host pixels: asynchronous. */
+int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, uint32_t count,
+    gbsp_metrics *metrics);
 /* Tile render that allocates no memory.  No counterpart in the reference: it
  * is for callers that must not allocate device memory per call - e.g. a
  * render loop that runs under a fixed device-memory budget, or that cannot
@@ -504,6 +514,24 @@ int gbsp_dn_status(uint32_t *status);
 int gbsp_dn_tile_fallback(void *stream, const float *denoised, const float *plainA,
     const float *plainC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile, float bound,
     float *out, float *tileErr, uint32_t *flags);
+/* The served-output check: per tile x tile block (tile <= 16) of B denoised
+ * frames D (H x W RGBA32F), judged by the plain path tracer from A, the
+ * plain render D was denoised from (sppA samples per pixel), and C, an
+ * independent plain render (sppC).  tileErr receives the tile's estimated
+ * relMSE (unbiased: (D - C)^2 less C's variance, over D^2 + 0.01), flags 1
+ * where the estimate exceeds `bound` by more than two standard errors, and
+ * needSpp the plain samples per pixel that bring the tile to `bound` (twice
+ * the per-sample relMSE estimated from A - C, over bound; 1..maxSpp).  No
+ * reference counterpart. */
+int gbsp_dn_tile_check(void *stream, const float *denoised, const float *plainA, uint32_t sppA,
+    const float *plainC, uint32_t sppC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile,
+    float bound, uint32_t maxSpp, float *tileErr, uint32_t *flags, uint32_t *needSpp);
+/* The served frame: D where flags[t] is 0; elsewhere the mean of all plain
+ * samples of the pixel, (sppA A + sppC C + sppF[t] F) / (sppA + sppC +
+ * sppF[t]), F the fallback render of the flagged tiles (NULL: none). */
+int gbsp_dn_tile_merge(void *stream, const float *denoised, const float *plainA, uint32_t sppA,
+    const float *plainC, uint32_t sppC, const float *fallback, const uint32_t *sppF, uint32_t B,
+    uint32_t H, uint32_t W, uint32_t tile, const uint32_t *flags, float *out);
 /* wt[8-tap][ci][co] = w[tap][co][ci]: weights of the data-gradient conv. */
 int gbsp_dn_flip_transpose(void *stream, const uint16_t *w, uint32_t cout, uint32_t cin,
     uint16_t *wt);

@@ -390,3 +390,72 @@ def test_tile_fallback_ignores_noise_alone(gpu_lib):
     fell = float(flags.float().mean())
     print(f"tiles with estimate above the bound {above:.2f}, fell back {fell:.2f}")
     assert above >= 0.25 and fell <= 0.1
+
+
+def test_tile_check_flags_bad_tiles_and_sizes_the_fallback(gpu_lib):
+    """gbsp_dn_tile_check on synthetic frames with known noise: a tile where D
+    is wrong is flagged, correct tiles are not, and the plain spp it asks for
+    matches the per-sample variance (sigma^2 = 0.36 per value at mean 1, so
+    relMSE 0.01 needs 0.36 / 1.01 / 0.01 = 36 samples; the estimate is doubled)."""
+    import torch
+
+    from vk_cinematic_gb300.denoiser import KPCNN
+
+    g = torch.Generator(device="cuda").manual_seed(21)
+    B, H, W, tile = 1, 48, 64, 16
+    sigma, spp_a, spp_c = 0.6, 4, 4
+    mu = torch.full((B, H, W, 4), 1.0, device="cuda")
+    A = mu + sigma / spp_a ** 0.5 * torch.randn((B, H, W, 4), device="cuda", generator=g)
+    C = mu + sigma / spp_c ** 0.5 * torch.randn((B, H, W, 4), device="cuda", generator=g)
+    D = mu.clone()
+    D[0, 16:32, 32:48, :3] += 0.5
+    net = KPCNN(seed=0)
+    err, flags, need = net.check_tiles(D, A, spp_a, C, spp_c, bound=0.01, tile=tile, max_spp=4096)
+    torch.cuda.synchronize()
+    f = flags.cpu().numpy().reshape(3, 4)
+    bad = np.zeros((3, 4), bool)
+    bad[1, 2] = True
+    print("estimates", err.cpu().numpy().round(4).reshape(3, 4))
+    print("need spp", need.cpu().numpy().reshape(3, 4))
+    assert np.array_equal(f.astype(bool), bad)
+    nd = need.cpu().numpy().astype(np.float64)
+    expect = 2 * sigma ** 2 / 1.01 / 0.01
+    assert np.all(np.abs(nd - expect) < 0.3 * expect), (nd, expect)
+    # merge: flagged tile = weighted mean of the plain samples (and a fallback render)
+    Fb = mu + 0.1 * torch.randn((B, H, W, 4), device="cuda", generator=g)
+    spp_f = torch.zeros(12, dtype=torch.int32, device="cuda")
+    spp_f[1 * 4 + 2] = 32
+    out = net.merge_tiles(D, A, spp_a, C, spp_c, Fb, spp_f, flags, tile)
+    torch.cuda.synchronize()
+    exp = (spp_a * A + spp_c * C + 32 * Fb) / (spp_a + spp_c + 32)
+    o = out.cpu()
+    assert torch.allclose(o[0, 16:32, 32:48, :3], exp.cpu()[0, 16:32, 32:48, :3], rtol=1e-6,
+                          atol=1e-6)
+    keep = torch.ones((H, W), dtype=torch.bool)
+    keep[16:32, 32:48] = False
+    assert torch.equal(o[0][keep][:, :3], D.cpu()[0][keep][:, :3])
+
+
+def test_served_output_runs_end_to_end(gpu_lib):
+    """KPCNN.serve on a small scene: input render + G-buffers, denoise, check
+    render, tile check, fallback tile-list renders, merge; the served image is
+    finite and, on flagged tiles, equals the mean of all their plain samples."""
+    import torch
+
+    from vk_cinematic_gb300 import denoiser
+
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rt = gbsp.Runtime(0, stream=stream.cuda_stream)
+    s = scenes.config3_scene(width=160, height=96, spp=2, n_spheres=32, level=2, seed=8)
+    sr = denoiser.SceneRenderer(rt, s)
+    net = denoiser.KPCNN(seed=0)
+    out, st = net.serve(sr, 0, 0, s.width, s.height, 2, seed=3, bound=0.01)
+    torch.cuda.synchronize()
+    print("served stats", {k: v for k, v in st.items() if k != "denoised"})
+    assert out.shape == (s.height, s.width, 4)
+    assert torch.isfinite(out).all()
+    assert st["tiles"] == 6 * 10
+    # an untrained network is far from the bound: most tiles fall back
+    assert st["flagged"] > 0 and st["fallback_samples"] > 0
+    torch.cuda.set_stream(torch.cuda.default_stream())

@@ -418,6 +418,39 @@ def test_node_width_changes_nothing(rt, kind):
         assert np.array_equal(res[8][1], res[4][1])
 
 
+def test_tile_list_matches_tile_renders(rt):
+    """gbsp_path_trace_tile_list renders the listed tiles in one pass exactly
+    as gbsp_path_trace_tile renders each one (bit-identical pixels, the same
+    path count); pixels outside the tiles keep the frame's previous values."""
+    import torch
+
+    s = scenes.config3_scene(width=200, height=120, spp=3, n_spheres=32, level=2, seed=31)
+    scene, ms, rend = gbsp.upload_scene(rt, s)
+    tiles = [(0, 0, 16, 16), (48, 32, 64, 48), (184, 112, 200, 120), (120, 90, 140, 130),
+             (100, 7, 133, 19)]
+    ref = np.zeros((s.height, s.width, 4), np.float32)
+    for t in tiles:
+        img, _, _ = rend.tile(t)
+        x0, y0, x1, y1 = t[0], t[1], min(t[2], s.width), min(t[3], s.height)
+        ref[y0:y1, x0:x1] = img[y0:y1, x0:x1]
+    rend.frame_device(metrics=False)
+    rt.synchronize()
+    frame = torch.empty((s.height, s.width, 4), dtype=torch.float32, device="cuda")
+    rend.copy_region(0, 0, s.width, s.height, frame.data_ptr())
+    rt.synchronize()
+    before = frame.cpu().numpy()
+    m = rend.tile_list_device(tiles, metrics=True)
+    rend.copy_region(0, 0, s.width, s.height, frame.data_ptr())
+    rt.synchronize()
+    got = frame.cpu().numpy()
+    inside = np.zeros((s.height, s.width), bool)
+    for t in tiles:
+        inside[t[1]:min(t[3], s.height), t[0]:min(t[2], s.width)] = True
+    assert np.array_equal(got[inside].view(np.uint32), ref[inside].view(np.uint32))
+    assert np.array_equal(got[~inside].view(np.uint32), before[~inside].view(np.uint32))
+    assert m.as_dict()["paths_traced"] == int(inside.sum()) * s.spp
+
+
 def test_tonemap_matches_oracle(rt, port):
     """Display conversion (post_processing.frag.glsl:19-26 + ToColor) of a
     path-traced frame against the C restatement; powf differs in the last

@@ -910,6 +910,52 @@ int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile, gbsp_rng *rng,
     return check_stream_status(rt);
 }
 
+int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, uint32_t count,
+    gbsp_metrics *metrics)
+{
+    if (count && !tiles) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tiles is NULL");
+    gbsp_options opt;
+    MaterialView mv;
+    DeviceBuffer<int32_t> slots;
+    int rc = prepare_render(ctx, opt, mv, slots);
+    if (rc) return rc;
+    if (opt.rng_mode != GBSP_RNG_HASH_PER_SAMPLE)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile lists render hash-per-sample only");
+    if (opt.flags & GBSP_FLAG_AOV)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile lists write no G-buffers (GBSP_FLAG_AOV)");
+    gbsp_runtime *rt = ctx->runtime;
+    cudaStream_t s = rt->stream;
+    gbsp_image_plane *ip = ctx->camera->imagePlane;
+    std::vector<uint4> rects;
+    rects.reserve(count);
+    for (uint32_t i = 0; i < count; i++) {
+        uint32_t x0 = tiles[i].minX, y0 = tiles[i].minY;
+        uint32_t x1 = std::min(tiles[i].maxX, ip->width), y1 = std::min(tiles[i].maxY, ip->height);
+        if (x1 > x0 && y1 > y0) rects.push_back(make_uint4(x0, y0, x1 - x0, y1 - y0));
+    }
+    if ((rc = ensure_frame(rt, ip->width, ip->height))) return rc;
+    rt->begin_call(false);
+    if (metrics && (rc = counters_begin(rt, (opt.flags & GBSP_FLAG_STAGE_TIMING) != 0))) return rc;
+    if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
+    if ((rc = render_tile_list(rt, ctx->scene->view(), mv, camera_params(ctx->camera), opt, rects,
+             rt->frame.ptr, ip->width)))
+        return rc;
+    if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
+    if (ip->pixels) {
+        size_t pitch = (size_t)ip->width * sizeof(float4);
+        for (const uint4 &r : rects)
+            GBSP_CUDA_TRY(cudaMemcpy2DAsync(ip->pixels + 4 * ((size_t)r.y * ip->width + r.x), pitch,
+                rt->frame.ptr + (size_t)r.y * ip->width + r.x, pitch, (size_t)r.z * sizeof(float4),
+                r.w, cudaMemcpyDeviceToHost, s));
+    }
+    if (!metrics && !ip->pixels) return GBSP_OK;
+    GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    if (metrics) cudaEventElapsedTime(&ms, rt->ev[0], rt->ev[1]);
+    if ((rc = counters_end(rt, metrics, ms))) return rc;
+    return check_stream_status(rt);
+}
+
 int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics)
 {
     gbsp_options opt;

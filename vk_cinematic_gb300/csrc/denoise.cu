@@ -1082,6 +1082,106 @@ __global__ void __launch_bounds__(256) k_tile_fallback(const float4 *__restrict_
                           : d;
 }
 
+// Served-output check of a denoised frame D against the plain path tracer,
+// per tile x tile block.  A: the plain render D was denoised from (sppA
+// samples per pixel); C: an independent plain render (sppC).  Per value v
+// (pixel and RGB channel), with sigma^2 the per-sample variance of the
+// pixel's estimator:
+//   E[(D - C)^2] = (D - mu)^2 + sigma^2 / sppC,
+//   E[(A - C)^2] = sigma^2 (1 / sppA + 1 / sppC),
+// so (D - C)^2 - (A - C)^2 * sppA / (sppA + sppC) estimates D's squared error
+// without bias, and (A - C)^2 * sppA * sppC / (sppA + sppC) estimates
+// sigma^2.  tileErr = the tile mean of the first over (D^2 + 0.01); the tile
+// is flagged when that estimate exceeds `bound` by more than kFallbackZ
+// standard errors of the mean.  needSpp = the plain samples per pixel that
+// reach `bound` on the tile, twice mean(sigma^2 / (M^2 + 0.01)) / bound with M
+// the pooled plain mean (a factor two for the noise of the variance
+// estimate), at least 1 and at most maxSpp.
+__global__ void __launch_bounds__(256) k_tile_check(const float4 *__restrict__ D,
+    const float4 *__restrict__ A, float sppA, const float4 *__restrict__ C, float sppC, int B,
+    int H, int W, int tile, float bound, uint32_t maxSpp, float *__restrict__ tileErr,
+    uint32_t *__restrict__ flags, uint32_t *__restrict__ needSpp)
+{
+    const int tilesX = (W + tile - 1) / tile, tilesY = (H + tile - 1) / tile;
+    const int t = blockIdx.x;
+    const int b = t / (tilesX * tilesY), ty = (t / tilesX) % tilesY, tx = t % tilesX;
+    const int lx = threadIdx.x % tile, ly = threadIdx.x / tile;
+    const int x = tx * tile + lx, y = ty * tile + ly;
+    const bool in = threadIdx.x < tile * tile && x < W && y < H;
+    const float wVarC = sppA / (sppA + sppC), wVar = sppA * sppC / (sppA + sppC);
+    const float wA = sppA / (sppA + sppC), wC = sppC / (sppA + sppC);
+    float e = 0.0f, e2 = 0.0f, n = 0.0f, r1 = 0.0f;
+    if (in) {
+        const size_t p = ((size_t)b * H + y) * W + x;
+        const float4 d = D[p], a = A[p], c = C[p];
+        float dv[3] = {d.x, d.y, d.z}, av[3] = {a.x, a.y, a.z}, cv[3] = {c.x, c.y, c.z};
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float dc = dv[k] - cv[k], ac = av[k] - cv[k];
+            const float term = (dc * dc - wVarC * ac * ac) / (dv[k] * dv[k] + 0.01f);
+            e += term;
+            e2 += term * term;
+            const float m = wA * av[k] + wC * cv[k];
+            r1 += wVar * ac * ac / (m * m + 0.01f);
+        }
+        n = 3.0f;
+    }
+    __shared__ float sE[8], sE2[8], sN[8], sR[8];
+    for (int off = 16; off; off >>= 1) {
+        e += __shfl_xor_sync(0xFFFFFFFFu, e, off);
+        e2 += __shfl_xor_sync(0xFFFFFFFFu, e2, off);
+        n += __shfl_xor_sync(0xFFFFFFFFu, n, off);
+        r1 += __shfl_xor_sync(0xFFFFFFFFu, r1, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sE[threadIdx.x >> 5] = e;
+        sE2[threadIdx.x >> 5] = e2;
+        sN[threadIdx.x >> 5] = n;
+        sR[threadIdx.x >> 5] = r1;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    float te = 0.0f, te2 = 0.0f, tn = 0.0f, tr = 0.0f;
+    for (int k = 0; k < 8; k++) {
+        te += sE[k];
+        te2 += sE2[k];
+        tn += sN[k];
+        tr += sR[k];
+    }
+    const float est = tn > 0.0f ? te / tn : 0.0f;
+    const float var = tn > 1.0f ? fmaxf(te2 - te * est, 0.0f) / (tn - 1.0f) : 0.0f;
+    const float se = tn > 0.0f ? sqrtf(var / tn) : 0.0f;
+    tileErr[t] = est;
+    flags[t] = est - kFallbackZ * se > bound ? 1u : 0u;
+    const float need = tn > 0.0f ? 2.0f * (tr / tn) / bound : 1.0f;
+    needSpp[t] = need >= (float)maxSpp ? maxSpp : (uint32_t)fmaxf(1.0f, ceilf(need));
+}
+
+// Served frame: D on unflagged tiles; on flagged tiles the mean of every
+// plain sample of the pixel, (sppA A + sppC C + sppF[t] F) / (sppA + sppC +
+// sppF[t]) with F the fallback render of the tile (sppF[t] = 0: none).
+__global__ void __launch_bounds__(256) k_tile_merge(const float4 *__restrict__ D,
+    const float4 *__restrict__ A, float sppA, const float4 *__restrict__ C, float sppC,
+    const float4 *__restrict__ F, const uint32_t *__restrict__ sppF, int B, int H, int W,
+    int tile, const uint32_t *__restrict__ flags, float4 *__restrict__ out)
+{
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (size_t)B * H * W) return;
+    const int x = (int)(p % W), y = (int)((p / W) % H), b = (int)(p / ((size_t)W * H));
+    const int tilesX = (W + tile - 1) / tile, tilesY = (H + tile - 1) / tile;
+    const int t = (b * tilesY + y / tile) * tilesX + x / tile;
+    if (!flags[t]) {
+        out[p] = D[p];
+        return;
+    }
+    const float f = F ? (float)sppF[t] : 0.0f;
+    const float inv = 1.0f / (sppA + sppC + f);
+    const float4 a = A[p], c = C[p];
+    const float4 g = f > 0.0f ? F[p] : make_float4(0, 0, 0, 0);
+    out[p] = make_float4((sppA * a.x + sppC * c.x + f * g.x) * inv,
+        (sppA * a.y + sppC * c.y + f * g.y) * inv, (sppA * a.z + sppC * c.z + f * g.z) * inv, 1.0f);
+}
+
 // relMSE = mean over pixels and channels of (out - ref)^2 / (ref^2 + 0.01);
 // writes dLogits (BF16, 32 channels, zeros beyond 25) and adds the loss sum.
 __global__ void k_relmse_bwd(const float *__restrict__ logits, const float4 *__restrict__ noisy,
@@ -1370,6 +1470,42 @@ int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32
     uint64_t n = (uint64_t)B * H * W;
     k_filter<<<blocks(n, 128), 128, 0, (cudaStream_t)stream>>>(logits,
         reinterpret_cast<const float4 *>(noisy), B, H, W, reinterpret_cast<float4 *>(out));
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_tile_check(void *stream, const float *denoised, const float *plainA, uint32_t sppA,
+    const float *plainC, uint32_t sppC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile,
+    float bound, uint32_t maxSpp, float *tileErr, uint32_t *flags, uint32_t *needSpp)
+{
+    if (!denoised || !plainA || !plainC || !tileErr || !flags || !needSpp || !B || !H || !W ||
+        !sppA || !sppC || !maxSpp || !(bound > 0.0f))
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad tile check args");
+    if (tile < 1 || tile > 16) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile must be 1..16");
+    const uint64_t tiles = (uint64_t)B * ((H + tile - 1) / tile) * ((W + tile - 1) / tile);
+    if (tiles > 0x7FFFFFFFull) return set_error(GBSP_ERR_CAPACITY, "too many tiles");
+    k_tile_check<<<(unsigned)tiles, 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(denoised), reinterpret_cast<const float4 *>(plainA),
+        (float)sppA, reinterpret_cast<const float4 *>(plainC), (float)sppC, (int)B, (int)H, (int)W,
+        (int)tile, bound, maxSpp, tileErr, flags, needSpp);
+    GBSP_CUDA_TRY(cudaGetLastError());
+    return GBSP_OK;
+}
+
+int gbsp_dn_tile_merge(void *stream, const float *denoised, const float *plainA, uint32_t sppA,
+    const float *plainC, uint32_t sppC, const float *fallback, const uint32_t *sppF, uint32_t B,
+    uint32_t H, uint32_t W, uint32_t tile, const uint32_t *flags, float *out)
+{
+    if (!denoised || !plainA || !plainC || !flags || !out || !B || !H || !W || !sppA || !sppC ||
+        (fallback && !sppF))
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad tile merge args");
+    if (tile < 1 || tile > 16) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile must be 1..16");
+    const uint64_t n = (uint64_t)B * H * W;
+    k_tile_merge<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(denoised), reinterpret_cast<const float4 *>(plainA),
+        (float)sppA, reinterpret_cast<const float4 *>(plainC), (float)sppC,
+        reinterpret_cast<const float4 *>(fallback), sppF, (int)B, (int)H, (int)W, (int)tile, flags,
+        reinterpret_cast<float4 *>(out));
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }

@@ -258,6 +258,12 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState,
     float4 *dAov = nullptr);
 
+// Renders the listed rectangles (x0, y0, width, height), hash-per-sample
+// seeding, into dImage (imageWidth pixels per row) in one wave sequence.
+int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, const gbsp_options &opt, const std::vector<uint4> &tiles,
+    float4 *dImage, uint32_t imageWidth);
+
 // api.cu
 int material_view(gbsp_material_system *ms, MaterialView *out);
 int resolve_material(const gbsp_material_system *ms, uint32_t id);

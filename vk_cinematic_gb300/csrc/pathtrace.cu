@@ -116,6 +116,10 @@ static int ensure_wave_buffers(gbsp_runtime *rt, uint32_t cap, uint32_t maxBounc
     return GBSP_OK;
 }
 
+static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, const gbsp_options &opt, WaveParams wp, uint64_t regionPixels,
+    float4 *dImage, uint32_t imageWidth, float4 *dAov);
+
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
     uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState, float4 *dAov)
@@ -162,7 +166,55 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
         return GBSP_OK;
     }
 
-    uint64_t regionPixels = (uint64_t)(x1 - x0) * (y1 - y0);
+    WaveParams wp;
+    wp.x0 = x0;
+    wp.y0 = y0;
+    wp.regionW = x1 - x0;
+    wp.tiles = nullptr;
+    wp.tileStart = nullptr;
+    wp.tileCount = 0;
+    return render_waves(rt, sv, mv, cam, opt, wp, (uint64_t)(x1 - x0) * (y1 - y0), dImage,
+        imageWidth, dAov);
+}
+
+int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, const gbsp_options &opt, const std::vector<uint4> &tiles,
+    float4 *dImage, uint32_t imageWidth)
+{
+    if (tiles.empty()) return GBSP_OK;
+    std::vector<uint64_t> start(tiles.size());
+    uint64_t total = 0;
+    for (size_t i = 0; i < tiles.size(); i++) {
+        start[i] = total;
+        total += (uint64_t)tiles[i].z * tiles[i].w;
+    }
+    if (total == 0) return GBSP_OK;
+    cudaStream_t s = rt->stream;
+    DeviceBuffer<uint4> dTiles;
+    DeviceBuffer<uint64_t> dStart;
+    int rc;
+    if ((rc = dTiles.upload(tiles.data(), tiles.size(), s)) ||
+        (rc = dStart.upload(start.data(), start.size(), s)))
+        return rc;
+    WaveParams wp;
+    wp.x0 = wp.y0 = 0;
+    wp.regionW = 1;
+    wp.tiles = dTiles.ptr;
+    wp.tileStart = dStart.ptr;
+    wp.tileCount = (uint32_t)tiles.size();
+    // the lists are freed in stream order behind the kernels that read them
+    return render_waves(rt, sv, mv, cam, opt, wp, total, dImage, imageWidth, nullptr);
+}
+
+static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
+    const CameraParams &cam, const gbsp_options &opt, WaveParams wp, uint64_t regionPixels,
+    float4 *dImage, uint32_t imageWidth, float4 *dAov)
+{
+    cudaStream_t s = rt->stream;
+    unsigned long long *counters = rt->dCounters;
+    unsigned int *ctl = reinterpret_cast<unsigned int *>(rt->dCounters + GBSP_METRIC_COUNT);
+    const uint32_t spp = opt.spp ? opt.spp : 1;
+    const uint32_t maxBounces = opt.max_bounces;
     uint64_t waveTarget = opt.wave_paths ? opt.wave_paths : (1u << 22);
     uint64_t pixelsPerWave = std::max<uint64_t>(1, waveTarget / spp);
     pixelsPerWave = std::min<uint64_t>(pixelsPerWave, regionPixels);
@@ -189,11 +241,7 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
         wb.pathAov = rt->pathAov.ptr;
     }
     wb.cap = cap;
-    WaveParams wp;
     wp.cam = cam;
-    wp.x0 = x0;
-    wp.y0 = y0;
-    wp.regionW = x1 - x0;
     wp.spp = spp;
     wp.maxBounces = maxBounces;
     wp.seed = opt.seed;
@@ -429,6 +477,9 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     wp.x0 = x0;
     wp.y0 = y0;
     wp.regionW = x1 - x0;
+    wp.tiles = nullptr;
+    wp.tileStart = nullptr;
+    wp.tileCount = 0;
     wp.spp = spp;
     wp.maxBounces = opt.max_bounces;
     wp.seed = opt.seed;

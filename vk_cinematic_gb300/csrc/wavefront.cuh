@@ -36,6 +36,12 @@ struct WaveBuffers {
 struct WaveParams {
     CameraParams cam;
     uint32_t x0, y0, regionW;
+    // optional list of rectangles rendered instead of the region: tile i is
+    // (x0, y0, width, height) = tiles[i], its pixels numbered row-major from
+    // tileStart[i] (an exclusive prefix sum over the tiles' pixel counts)
+    const uint4 *tiles;
+    const uint64_t *tileStart;
+    uint32_t tileCount;
     uint64_t pixelBase;   // first pixel (row-major in the region) of this wave
     uint32_t pixels;      // pixels in this wave
     uint32_t spp;
@@ -197,6 +203,31 @@ static __global__ void __launch_bounds__(256) k_octant_scatter(const float4 *__r
     }
 }
 
+// Image position of pixel `pix` of a wave's pixel numbering: row-major in
+// the region, or in the tile list (binary search over the tiles' first
+// pixels).
+__device__ __forceinline__ void wave_pixel(const WaveParams &wp, uint64_t pix, uint32_t &x,
+    uint32_t &y)
+{
+    if (!wp.tiles) {
+        x = wp.x0 + (uint32_t)(pix % wp.regionW);
+        y = wp.y0 + (uint32_t)(pix / wp.regionW);
+        return;
+    }
+    uint32_t lo = 0, hi = wp.tileCount - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(wp.tileStart + mid) <= pix)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const uint4 t = __ldg(wp.tiles + lo);
+    const uint64_t local = pix - __ldg(wp.tileStart + lo);
+    x = t.x + (uint32_t)(local % t.z);
+    y = t.y + (uint32_t)(local / t.z);
+}
+
 static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuffers wb)
 {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -204,8 +235,8 @@ static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuff
     if (p >= paths) return;
     uint64_t pix = wp.pixelBase + p / wp.spp;
     uint32_t s = p % wp.spp;
-    uint32_t x = wp.x0 + (uint32_t)(pix % wp.regionW);
-    uint32_t y = wp.y0 + (uint32_t)(pix / wp.regionW);
+    uint32_t x, y;
+    wave_pixel(wp, pix, x, y);
     uint32_t rng = sample_seed(wp.seed, x, y, s);
     V3 o, d;
     camera_ray(wp.cam, x, y, rng, o, d);
@@ -520,8 +551,8 @@ static __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBu
     uint32_t nans = 0;
     if (k < wp.pixels) {
         uint64_t pix = wp.pixelBase + k;
-        uint32_t x = wp.x0 + (uint32_t)(pix % wp.regionW);
-        uint32_t y = wp.y0 + (uint32_t)(pix / wp.regionW);
+        uint32_t x, y;
+        wave_pixel(wp, pix, x, y);
         CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
         for (uint32_t s = 0; s < wp.spp; s++) {
             float4 r = wb.pathRad[(size_t)k * wp.spp + s];

@@ -197,6 +197,85 @@ class KPCNN:
                                             _ptr(flags)))
         return out, err, flags
 
+    def check_tiles(self, denoised, plain_a, spp_a, plain_c, spp_c, bound=0.01, tile=16,
+                    max_spp=4096):
+        """gbsp_dn_tile_check: per tile x tile block, the estimated relMSE of the
+        denoised frames, the flag (estimate above `bound` by two standard
+        errors) and the plain spp that brings the tile to `bound`."""
+        import torch
+
+        B, H, W, _ = denoised.shape
+        tiles = B * ((H + tile - 1) // tile) * ((W + tile - 1) // tile)
+        err = torch.empty(tiles, dtype=torch.float32, device="cuda")
+        flags = torch.empty(tiles, dtype=torch.int32, device="cuda")
+        need = torch.empty(tiles, dtype=torch.int32, device="cuda")
+        _check(self.L.gbsp_dn_tile_check(_stream(), _ptr(denoised), _ptr(plain_a), _u32(spp_a),
+                                         _ptr(plain_c), _u32(spp_c), _u32(B), _u32(H), _u32(W),
+                                         _u32(tile), _f32(bound), _u32(max_spp), _ptr(err),
+                                         _ptr(flags), _ptr(need)))
+        return err, flags, need
+
+    def merge_tiles(self, denoised, plain_a, spp_a, plain_c, spp_c, fallback, spp_f, flags,
+                    tile=16):
+        """gbsp_dn_tile_merge: the served frames."""
+        import torch
+
+        B, H, W, _ = denoised.shape
+        out = torch.empty_like(denoised)
+        _check(self.L.gbsp_dn_tile_merge(_stream(), _ptr(denoised), _ptr(plain_a), _u32(spp_a),
+                                         _ptr(plain_c), _u32(spp_c),
+                                         _ptr(fallback) if fallback is not None else None,
+                                         _ptr(spp_f) if spp_f is not None else None, _u32(B),
+                                         _u32(H), _u32(W), _u32(tile), _ptr(flags), _ptr(out)))
+        return out
+
+    def serve(self, sr, x0, y0, w, h, spp, seed, bound=0.01, tile=16, max_spp=4096):
+        """The served output of a w x h window of `sr`'s frame: `spp`-sample plain
+        render + G-buffers -> denoised; an independent `spp`-sample plain render
+        checks every tile x tile block (check_tiles); blocks that fail are served
+        from all their plain samples, topped up by a fallback render of the
+        block (one tile-list pass per power-of-two sample count) to the spp the
+        check estimated for `bound`.  Returns (image, stats): stats counts the
+        flagged blocks and the fallback samples rendered, and holds the unchecked
+        denoised image under "denoised"."""
+        import torch
+
+        rad, aov = sr.render(x0, y0, w, h, spp, seed, aov=True)
+        chk, _ = sr.render(x0, y0, w, h, spp, (seed + 0x1B873593) & 0xFFFFFFFF)
+        den = self.denoise(rad.unsqueeze(0).contiguous(), aov.unsqueeze(0).contiguous())
+        err, flags, need = self.check_tiles(den, rad.unsqueeze(0).contiguous(), spp,
+                                            chk.unsqueeze(0).contiguous(), spp, bound, tile,
+                                            max_spp)
+        f = flags.cpu().numpy()
+        nd = need.cpu().numpy()
+        tx = (w + tile - 1) // tile
+        groups = {}
+        spp_f = np.zeros(len(f), np.int32)
+        for t in np.nonzero(f)[0]:
+            extra = int(nd[t]) - 2 * spp
+            if extra <= 0:
+                continue
+            k = 1 << (extra - 1).bit_length()
+            spp_f[t] = k
+            bx, by = int(t % tx) * tile, int(t // tx) * tile
+            groups.setdefault(k, []).append((x0 + bx, y0 + by, x0 + min(bx + tile, w),
+                                             y0 + min(by + tile, h)))
+        fb = None
+        fb_samples = 0
+        if groups:
+            for k, tl in sorted(groups.items()):
+                sr.render_tiles(tl, k, seed + 7919 * k)
+                fb_samples += k * sum((t[2] - t[0]) * (t[3] - t[1]) for t in tl)
+            fb = torch.empty((1, h, w, 4), dtype=torch.float32, device="cuda")
+            sr.rend.copy_region(x0, y0, w, h, fb.data_ptr())
+        out = self.merge_tiles(den, rad.unsqueeze(0).contiguous(), spp,
+                               chk.unsqueeze(0).contiguous(), spp, fb,
+                               torch.from_numpy(spp_f).cuda() if fb is not None else None, flags,
+                               tile)
+        stats = {"tiles": int(len(f)), "flagged": int(f.sum()), "fallback_samples": fb_samples,
+                 "fallback_groups": sorted(groups), "denoised": den[0]}
+        return out[0], stats
+
     # ---- training ------------------------------------------------------------------
     def data_grad(self, li, d):
         """dIn of layer li from its output gradient d (BF16), FP32; both
@@ -285,6 +364,14 @@ class SceneRenderer:
         av = torch.empty((h, w, 8), dtype=torch.float32, device="cuda") if aov else None
         self.rend.copy_region(x0, y0, w, h, rad.data_ptr(), av.data_ptr() if aov else 0)
         return rad, av
+
+    def render_tiles(self, tiles, spp, seed):
+        """Plain render of the listed (minX, minY, maxX, maxY) frame tiles at
+        `spp` in one pass, into the runtime's frame buffer."""
+        o = self.rend.options
+        o.spp, o.seed = spp, seed
+        o.flags = 0
+        self.rend.tile_list_device(tiles)
 
     def reference(self, x0, y0, w, h, spp_total, per_pass=1024, seed=1 << 20):
         """FP64-accumulated high-spp image: the mean of FP32 passes, summed in FP64."""

@@ -57,7 +57,8 @@ EXPORTS = [
     "gbsp_create_cube_map", "gbsp_create_irradiance_cube_map", "gbsp_xorshift32_jump",
     "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status", "gbsp_scene_set_intersection",
     "gbsp_dn_tile_fallback", "gbsp_scene_set_node_width", "gbsp_scene_node_width",
-    "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths",
+    "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths", "gbsp_path_trace_tile_list",
+    "gbsp_dn_tile_check", "gbsp_dn_tile_merge",
 ]
 
 
@@ -378,6 +379,16 @@ class Renderer:
                                            ctypes.byref(m)))
         self.set_host_pixels(None)
         return out, rng.value, m
+
+    def tile_list_device(self, tiles, metrics: bool = False):
+        """Renders the listed (minX, minY, maxX, maxY) tiles in one pass into the
+        runtime's frame buffer (device); returns the metrics when asked."""
+        self.set_host_pixels(None)
+        arr = (Tile * max(1, len(tiles)))(*[Tile(*[int(v) for v in t]) for t in tiles])
+        m = Metrics() if metrics else None
+        _check(self.L.gbsp_path_trace_tile_list(ctypes.byref(self.ctx), arr, _u32(len(tiles)),
+                                                ctypes.byref(m) if m is not None else None))
+        return m
 
     def frame_device_pointer(self) -> int:
         return self.L.gbsp_frame_device_pointer(self.rt.h)
