@@ -512,8 +512,18 @@ int gbsp_create_mesh(gbsp_scene *scene, const gbsp_vertex *vertices, uint32_t ve
     for (int w = 0; w < kNodeWidths; w++) scene->tlasRoot[w] = kEmptyChild;
     const uint32_t nodeBase[kNodeWidths] = {scene->meshNodeCount[0], scene->meshNodeCount[1]};
     WideTree trees[kNodeWidths];
+    // triangle boxes on the host too (the same min/max as k_mesh_prepare), for
+    // the host SAH build
+    std::vector<float4> hlo(triCount), hhi(triCount);
+    for (uint32_t t = 0; t < triCount; t++) {
+        V3 a = ld3(vertices[indices[3 * t]].position), b = ld3(vertices[indices[3 * t + 1]].position),
+           c = ld3(vertices[indices[3 * t + 2]].position);
+        V3 mn = vmin(a, vmin(b, c)), mx = vmax(a, vmax(b, c));
+        hlo[t] = make_float4(mn.x, mn.y, mn.z, 0.0f);
+        hhi[t] = make_float4(mx.x, mx.y, mx.z, 0.0f);
+    }
     if ((rc = build_wide_bvh(s, lo.ptr, hi.ptr, triCount, kMaxLeafPrims, scene->nodes, nodeBase,
-             trees, &order, rt->dStatus)))
+             trees, &order, rt->dStatus, hlo.data(), hhi.data())))
         return rc;
     uint64_t triBase = scene->triCount;
     if ((rc = append_device(scene->tris, triBase, triCount, s)) ||
@@ -626,7 +636,7 @@ int gbsp_build_scene_broadphase(gbsp_scene *scene)
     if ((rc = dlo.upload(lo.data(), n, s)) || (rc = dhi.upload(hi.data(), n, s))) return rc;
     WideTree trees[kNodeWidths];
     if ((rc = build_wide_bvh(s, dlo.ptr, dhi.ptr, n, 1, scene->nodes, scene->meshNodeCount, trees,
-             &order, rt->dStatus)))
+             &order, rt->dStatus, lo.data(), hi.data())))
         return rc;
     for (int w = 0; w < kNodeWidths; w++)
         if ((rc = offset_nodes(s, scene->nodes[w], trees[w].nodeCount, scene->meshNodeCount[w], 0)))

@@ -19,6 +19,7 @@
 //      serves the trees of both widths.
 // Every loop is bounded by the primitive count or log2 of it.
 
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 
@@ -547,9 +548,152 @@ static int grow_pool(cudaStream_t s, NodePool &pool, size_t nodes)
     return GBSP_OK;
 }
 
+// Binary tree in the form the collapse reads: internal nodes 0 .. n-2 (root
+// 0), child references with kBinLeaf for a primitive (its sorted position),
+// each internal node's range [first, last] of sorted positions and its box,
+// and order[sorted position] = primitive.
+struct HostBinaryTree {
+    std::vector<uint32_t> left, right, first, last, order;
+    std::vector<float4> lo, hi;
+};
+
+// Top-down binned SAH build (Wald, "On fast construction of SAH-based
+// bounding volume hierarchies", 2007) of the binary tree over n >= 2
+// primitive boxes, split down to single primitives: at every node the
+// primitives' centroids are binned into kSahBins slabs along each axis, and
+// the split between bins that minimises area(left) x count(left) +
+// area(right) x count(right) partitions the node's range (a median split
+// when every centroid coincides).  Node boxes are exact unions.
+constexpr int kSahBins = 16;
+// Above this many primitives the device LBVH (Morton order, Karras tree)
+// is built instead: the host build's time grows as n log n on one core.
+constexpr uint32_t kSahMaxPrims = 1u << 20;
+
+static float half_area_host(const float4 &lo, const float4 &hi)
+{
+    float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+static void sah_binary_tree(const float4 *plo, const float4 *phi, uint32_t n, HostBinaryTree &t)
+{
+    t.left.assign(n - 1, 0);
+    t.right.assign(n - 1, 0);
+    t.first.assign(n - 1, 0);
+    t.last.assign(n - 1, 0);
+    t.lo.assign(n - 1, make_float4(0, 0, 0, 0));
+    t.hi.assign(n - 1, make_float4(0, 0, 0, 0));
+    t.order.resize(n);
+    std::vector<float> cen(3 * (size_t)n);
+    for (uint32_t i = 0; i < n; i++) {
+        t.order[i] = i;
+        cen[3 * (size_t)i + 0] = (plo[i].x + phi[i].x) * 0.5f;
+        cen[3 * (size_t)i + 1] = (plo[i].y + phi[i].y) * 0.5f;
+        cen[3 * (size_t)i + 2] = (plo[i].z + phi[i].z) * 0.5f;
+    }
+    struct Job {
+        uint32_t node, begin, end;
+    };
+    std::vector<Job> jobs;
+    jobs.push_back({0, 0, n});
+    uint32_t next = 1;
+    const float inf = 3.0e38f;
+    while (!jobs.empty()) {
+        const Job j = jobs.back();
+        jobs.pop_back();
+        float4 blo = make_float4(inf, inf, inf, 0), bhi = make_float4(-inf, -inf, -inf, 0);
+        float cmin[3] = {inf, inf, inf}, cmax[3] = {-inf, -inf, -inf};
+        for (uint32_t k = j.begin; k < j.end; k++) {
+            const uint32_t p = t.order[k];
+            blo = make_float4(rmin(blo.x, plo[p].x), rmin(blo.y, plo[p].y), rmin(blo.z, plo[p].z), 0);
+            bhi = make_float4(rmax(bhi.x, phi[p].x), rmax(bhi.y, phi[p].y), rmax(bhi.z, phi[p].z), 0);
+            for (int a = 0; a < 3; a++) {
+                cmin[a] = std::min(cmin[a], cen[3 * (size_t)p + a]);
+                cmax[a] = std::max(cmax[a], cen[3 * (size_t)p + a]);
+            }
+        }
+        t.lo[j.node] = blo;
+        t.hi[j.node] = bhi;
+        t.first[j.node] = j.begin;
+        t.last[j.node] = j.end - 1;
+        int bestAxis = -1, bestBin = 0;
+        float bestCost = inf;
+        for (int a = 0; a < 3; a++) {
+            const float ext = cmax[a] - cmin[a];
+            if (!(ext > 0.0f)) continue;
+            const float scale = (float)kSahBins / ext;
+            uint32_t cnt[kSahBins] = {};
+            float4 lo[kSahBins], hi[kSahBins];
+            for (int b = 0; b < kSahBins; b++) {
+                lo[b] = make_float4(inf, inf, inf, 0);
+                hi[b] = make_float4(-inf, -inf, -inf, 0);
+            }
+            for (uint32_t k = j.begin; k < j.end; k++) {
+                const uint32_t p = t.order[k];
+                const int b = std::min(kSahBins - 1, (int)((cen[3 * (size_t)p + a] - cmin[a]) * scale));
+                cnt[b]++;
+                lo[b] = make_float4(std::min(lo[b].x, plo[p].x), std::min(lo[b].y, plo[p].y),
+                    std::min(lo[b].z, plo[p].z), 0);
+                hi[b] = make_float4(std::max(hi[b].x, phi[p].x), std::max(hi[b].y, phi[p].y),
+                    std::max(hi[b].z, phi[p].z), 0);
+            }
+            // suffix areas and counts, then a prefix sweep
+            float rArea[kSahBins];
+            uint32_t rCnt[kSahBins];
+            float4 rl = make_float4(inf, inf, inf, 0), rh = make_float4(-inf, -inf, -inf, 0);
+            uint32_t rc = 0;
+            for (int b = kSahBins - 1; b > 0; b--) {
+                rc += cnt[b];
+                rl = make_float4(std::min(rl.x, lo[b].x), std::min(rl.y, lo[b].y), std::min(rl.z, lo[b].z), 0);
+                rh = make_float4(std::max(rh.x, hi[b].x), std::max(rh.y, hi[b].y), std::max(rh.z, hi[b].z), 0);
+                rCnt[b] = rc;
+                rArea[b] = rc ? half_area_host(rl, rh) : 0.0f;
+            }
+            float4 ll = make_float4(inf, inf, inf, 0), lh = make_float4(-inf, -inf, -inf, 0);
+            uint32_t lc = 0;
+            for (int b = 0; b < kSahBins - 1; b++) {
+                lc += cnt[b];
+                ll = make_float4(std::min(ll.x, lo[b].x), std::min(ll.y, lo[b].y), std::min(ll.z, lo[b].z), 0);
+                lh = make_float4(std::max(lh.x, hi[b].x), std::max(lh.y, hi[b].y), std::max(lh.z, hi[b].z), 0);
+                if (lc == 0 || rCnt[b + 1] == 0) continue;
+                const float cost = half_area_host(ll, lh) * (float)lc + rArea[b + 1] * (float)rCnt[b + 1];
+                if (cost < bestCost) {
+                    bestCost = cost;
+                    bestAxis = a;
+                    bestBin = b;
+                }
+            }
+        }
+        uint32_t mid = j.begin + (j.end - j.begin) / 2;
+        if (bestAxis >= 0) {
+            const float scale = (float)kSahBins / (cmax[bestAxis] - cmin[bestAxis]);
+            const float c0 = cmin[bestAxis];
+            uint32_t *it = std::partition(t.order.data() + j.begin, t.order.data() + j.end,
+                [&](uint32_t p) {
+                    return std::min(kSahBins - 1, (int)((cen[3 * (size_t)p + bestAxis] - c0) * scale)) <=
+                        bestBin;
+                });
+            const uint32_t m = (uint32_t)(it - t.order.data());
+            if (m > j.begin && m < j.end) mid = m;
+        }
+        const uint32_t ranges[2][2] = {{j.begin, mid}, {mid, j.end}};
+        for (int side = 0; side < 2; side++) {
+            const uint32_t b = ranges[side][0], e = ranges[side][1];
+            uint32_t ref;
+            if (e - b == 1) {
+                ref = kBinLeaf | b;
+            } else {
+                ref = next++;
+                jobs.push_back({ref, b, e});
+            }
+            (side ? t.right : t.left)[j.node] = ref;
+        }
+    }
+}
+
 int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_t n,
     uint32_t leafMax, NodePool *pools, const uint32_t *nodeBase, WideTree *trees,
-    DeviceBuffer<uint32_t> *orderOut, uint32_t *dStatus)
+    DeviceBuffer<uint32_t> *orderOut, uint32_t *dStatus, const float4 *hLo, const float4 *hHi)
 {
     if (n == 0) return set_error(GBSP_ERR_INVALID_ARGUMENT, "BVH over zero primitives");
     if (n >= (1u << 27)) return set_error(GBSP_ERR_CAPACITY, "BVH over %u primitives (max 2^27)", n);
@@ -588,29 +732,53 @@ int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_
         (rc = q[1].reserve(capacity, s)))
         return rc;
 
-    init_bounds<<<1, 32, 0, s>>>(bounds.ptr);
-    centroid_bounds<<<min(blocks_for(n, 256), 1024u), 256, 0, s>>>(dLo, dHi, n, bounds.ptr);
-    morton_codes<<<blocks_for(n, 256), 256, 0, s>>>(dLo, dHi, n, bounds.ptr, codes[0].ptr,
-        vals[0].ptr);
-    GBSP_CUDA_TRY(cudaGetLastError());
-    int cur = 0;
-    for (int shift = 0; shift < 32; shift += 8) {
-        radix_histogram<<<sortBlocks, kSortThreads, 0, s>>>(codes[cur].ptr, n, shift, hist.ptr,
-            sortBlocks);
-        radix_scan<<<1, 1024, 0, s>>>(hist.ptr, 256 * sortBlocks);
-        radix_scatter<<<sortBlocks, kSortThreads, 0, s>>>(codes[cur].ptr, vals[cur].ptr,
-            codes[cur ^ 1].ptr, vals[cur ^ 1].ptr, n, shift, hist.ptr, sortBlocks);
-        cur ^= 1;
+    const uint32_t *order = nullptr;
+    if (hLo && hHi && n <= kSahMaxPrims) {
+        // binned SAH tree on the host (the host boxes are the device ones)
+        HostBinaryTree ht;
+        sah_binary_tree(hLo, hHi, n, ht);
+        GBSP_CUDA_TRY(cudaMemcpyAsync(left.ptr, ht.left.data(), 4 * (size_t)(n - 1),
+            cudaMemcpyHostToDevice, s));
+        GBSP_CUDA_TRY(cudaMemcpyAsync(right.ptr, ht.right.data(), 4 * (size_t)(n - 1),
+            cudaMemcpyHostToDevice, s));
+        GBSP_CUDA_TRY(cudaMemcpyAsync(first.ptr, ht.first.data(), 4 * (size_t)(n - 1),
+            cudaMemcpyHostToDevice, s));
+        GBSP_CUDA_TRY(cudaMemcpyAsync(last.ptr, ht.last.data(), 4 * (size_t)(n - 1),
+            cudaMemcpyHostToDevice, s));
+        GBSP_CUDA_TRY(cudaMemcpyAsync(nodeLo.ptr, ht.lo.data(), sizeof(float4) * (n - 1),
+            cudaMemcpyHostToDevice, s));
+        GBSP_CUDA_TRY(cudaMemcpyAsync(nodeHi.ptr, ht.hi.data(), sizeof(float4) * (n - 1),
+            cudaMemcpyHostToDevice, s));
+        GBSP_CUDA_TRY(cudaMemcpyAsync(vals[0].ptr, ht.order.data(), 4 * (size_t)n,
+            cudaMemcpyHostToDevice, s));
+        // the host vectors must outlive the copies
+        GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+        order = vals[0].ptr;
+    } else {
+        init_bounds<<<1, 32, 0, s>>>(bounds.ptr);
+        centroid_bounds<<<min(blocks_for(n, 256), 1024u), 256, 0, s>>>(dLo, dHi, n, bounds.ptr);
+        morton_codes<<<blocks_for(n, 256), 256, 0, s>>>(dLo, dHi, n, bounds.ptr, codes[0].ptr,
+            vals[0].ptr);
+        GBSP_CUDA_TRY(cudaGetLastError());
+        int cur = 0;
+        for (int shift = 0; shift < 32; shift += 8) {
+            radix_histogram<<<sortBlocks, kSortThreads, 0, s>>>(codes[cur].ptr, n, shift, hist.ptr,
+                sortBlocks);
+            radix_scan<<<1, 1024, 0, s>>>(hist.ptr, 256 * sortBlocks);
+            radix_scatter<<<sortBlocks, kSortThreads, 0, s>>>(codes[cur].ptr, vals[cur].ptr,
+                codes[cur ^ 1].ptr, vals[cur ^ 1].ptr, n, shift, hist.ptr, sortBlocks);
+            cur ^= 1;
+        }
+        GBSP_CUDA_TRY(cudaGetLastError());
+        const uint32_t *sorted = codes[cur].ptr;
+        order = vals[cur].ptr;
+        karras_hierarchy<<<blocks_for(n - 1, 256), 256, 0, s>>>(sorted, (int)n, left.ptr,
+            right.ptr, parent.ptr, first.ptr, last.ptr);
+        GBSP_CUDA_TRY(cudaMemsetAsync(arrivals.ptr, 0, 4 * (size_t)n, s));
+        refit<<<blocks_for(n, 256), 256, 0, s>>>((int)n, left.ptr, right.ptr, parent.ptr, dLo,
+            dHi, order, nodeLo.ptr, nodeHi.ptr, arrivals.ptr, dStatus);
+        GBSP_CUDA_TRY(cudaGetLastError());
     }
-    GBSP_CUDA_TRY(cudaGetLastError());
-    const uint32_t *sorted = codes[cur].ptr;
-    const uint32_t *order = vals[cur].ptr;
-    karras_hierarchy<<<blocks_for(n - 1, 256), 256, 0, s>>>(sorted, (int)n, left.ptr, right.ptr,
-        parent.ptr, first.ptr, last.ptr);
-    GBSP_CUDA_TRY(cudaMemsetAsync(arrivals.ptr, 0, 4 * (size_t)n, s));
-    refit<<<blocks_for(n, 256), 256, 0, s>>>((int)n, left.ptr, right.ptr, parent.ptr, dLo, dHi,
-        order, nodeLo.ptr, nodeHi.ptr, arrivals.ptr, dStatus);
-    GBSP_CUDA_TRY(cudaGetLastError());
 
     // collapse the same binary tree once per width, level by level;
     // counters: [0] node counter, [1..2] queue counts

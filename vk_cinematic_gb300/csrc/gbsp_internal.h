@@ -222,14 +222,17 @@ namespace gbsp {
 
 // bvh_build.cu
 // Builds the wide BVHs (8- and 4-wide, from one binary tree) over n
-// primitive boxes on the device.  Tree w is appended to pools[w] at
-// nodeBase[w] (growing the pool, keeping its contents), with node indices
-// relative to nodeBase[w]; trees[w] receives its node count and depth.
-// Returns the primitive order (sorted position -> primitive) both trees'
-// leaves index.
+// primitive boxes (dLo/dHi on the device).  The binary tree is a binned-SAH
+// tree built on the host when the host copies of the boxes (hLo/hHi) are
+// given and n <= 2^20, else a linear BVH built on the device.  Tree w is
+// appended to pools[w] at nodeBase[w] (growing the pool, keeping its
+// contents), with node indices relative to nodeBase[w]; trees[w] receives
+// its node count and depth.  Returns the primitive order (sorted position
+// -> primitive) both trees' leaves index.
 int build_wide_bvh(cudaStream_t s, const float4 *dLo, const float4 *dHi, uint32_t n,
     uint32_t leafMax, NodePool *pools, const uint32_t *nodeBase, WideTree *trees,
-    DeviceBuffer<uint32_t> *orderOut, uint32_t *dStatus);
+    DeviceBuffer<uint32_t> *orderOut, uint32_t *dStatus, const float4 *hLo = nullptr,
+    const float4 *hHi = nullptr);
 // Triangle boxes + records for a mesh: positions from VertexPNT, indices.
 int mesh_prepare(cudaStream_t s, const gbsp_vertex *dVerts, const uint32_t *dIdx,
     uint32_t triCount, float4 *dLo, float4 *dHi);

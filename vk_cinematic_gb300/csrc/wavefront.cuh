@@ -247,7 +247,7 @@ static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuff
 }
 
 template <class Src, bool kWT>
-__global__ void __launch_bounds__(128) k_trace(Src src, const float4 *__restrict__ rayO,
+__global__ void __launch_bounds__(128, 6) k_trace(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
@@ -304,7 +304,7 @@ constexpr uint32_t kMaxLaneRaySteps = 1u << 22;
 constexpr uint32_t kMaxLaneIterations = 1u << 28;
 
 template <class Src, bool kWT>
-__global__ void __launch_bounds__(128) k_trace_lane(Src src, const float4 *__restrict__ rayO,
+__global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
