@@ -70,7 +70,7 @@ def parse_args():
     ap.add_argument("--dn-eval-crop", type=int, default=256)
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--dn-conv", choices=["tcgen05", "mma"], default="tcgen05")
-    ap.add_argument("--dn-wgrad", choices=["mma", "simt"], default="mma")
+    ap.add_argument("--dn-wgrad", choices=["tcgen05", "mma", "simt"], default="mma")
     ap.add_argument("--sort-dirs", action="store_true",
                     help="sort bounce-ray queues by direction octant")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -890,7 +890,7 @@ def run_config5(args):
 
 def time_weight_grad(net, stream, reps=20):
     """Device time of one 48 -> 48 weight gradient on a 16 x 128 x 128 batch,
-    per implementation (tensor-core mma.sync and the FP32 SIMT kernel), in ms."""
+    per implementation (tcgen05, mma.sync and the FP32 SIMT kernel), in ms."""
     import torch
     from vk_cinematic_gb300 import denoiser
 
@@ -900,7 +900,8 @@ def time_weight_grad(net, stream, reps=20):
     dw = torch.zeros((9, 48, 48), device="cuda")
     db = torch.zeros(48, device="cuda")
     out = {}
-    for impl, fn in (("mma", net.L.gbsp_dn_conv3x3_weight_grad_tc),
+    for impl, fn in (("tcgen05", net.L.gbsp_dn_conv3x3_weight_grad_tcgen05),
+                     ("mma", net.L.gbsp_dn_conv3x3_weight_grad_tc),
                      ("simt", net.L.gbsp_dn_conv3x3_weight_grad)):
         args = (denoiser._stream(), denoiser._ptr(x), denoiser._ptr(d), denoiser._u32(16),
                 denoiser._u32(128), denoiser._u32(128), denoiser._u32(48), denoiser._u32(48),

@@ -546,6 +546,14 @@ int gbsp_dn_conv3x3_weight_grad(void *stream, const uint16_t *in, const uint16_t
  * identical results.  Same shapes as gbsp_dn_conv3x3_weight_grad. */
 int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint16_t *dOut,
     uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
+/* The same weight and bias gradients on the 5th-generation tensor cores
+ * (tcgen05.mma, FP32 accumulators in tensor memory): all nine taps of a
+ * 64-pixel input-row chunk as one GEMM, M = (tap row, input channel), N =
+ * (tap column, output channel), K = pixels; per-CTA partial sums added in a
+ * fixed order (deterministic).  Tensors 16-byte aligned.  No reference
+ * counterpart. */
+int gbsp_dn_conv3x3_weight_grad_tcgen05(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
 /* out[p] = sum_k softmax(logits[p][0..24])_k * noisy[p + off5x5(k)] (edge-clamped);
  * logits have 32 channels per pixel. */
 int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32_t B, uint32_t H,

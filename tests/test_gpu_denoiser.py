@@ -163,7 +163,9 @@ def test_conv3x3_tcgen05_matches_torch_and_mma(gpu_lib, cin, cout, epi, B, H, W)
 
 
 @pytest.mark.parametrize("wgrad,shape", [("mma", (2, 12, 67)), ("simt", (2, 12, 67)),
-                                         ("mma", (1, 37, 250)), ("mma", (3, 1, 1))])
+                                         ("mma", (1, 37, 250)), ("mma", (3, 1, 1)),
+                                         ("tcgen05", (2, 12, 67)), ("tcgen05", (1, 37, 250)),
+                                         ("tcgen05", (3, 1, 1)), ("tcgen05", (4, 40, 200))])
 def test_conv_gradients_match_autograd(gpu_lib, wgrad, shape):
     import torch
 
@@ -322,15 +324,16 @@ def test_tile_fallback_serves_bad_tiles_from_plain_samples(gpu_lib):
     assert torch.equal(o[..., :3][keep], D.cpu()[..., :3][keep])
 
 
-def test_tensor_core_weight_grad_is_deterministic(gpu_lib):
-    """The tensor-core weight gradient adds its per-CTA partial sums in a fixed
+@pytest.mark.parametrize("wgrad", ["mma", "tcgen05"])
+def test_tensor_core_weight_grad_is_deterministic(gpu_lib, wgrad):
+    """The tensor-core weight gradients add their per-CTA partial sums in a fixed
     order: two calls on the same inputs give bit-identical dW and dBias."""
     import torch
 
     from vk_cinematic_gb300.denoiser import KPCNN, to_planar
 
     torch.manual_seed(5)
-    net = KPCNN(seed=2, wgrad="mma")
+    net = KPCNN(seed=2, wgrad=wgrad)
     B, H, W, cin, cout = 2, 64, 96, 48, 48
     x = to_planar(torch.randn((B, H, W, cin), device="cuda").to(torch.bfloat16))
     d = to_planar((torch.randn((B, H, W, cout), device="cuda") * 0.1).to(torch.bfloat16))

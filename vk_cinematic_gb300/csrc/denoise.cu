@@ -19,6 +19,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 
@@ -986,6 +987,255 @@ __global__ void k_wgrad_reduce(const float *__restrict__ partial, int slices, in
         dBias[i - wCount] += sum;
 }
 
+// ---------------------------------------------------------------------------
+// Weight gradient on the 5th-generation tensor cores (tcgen05).
+//
+// dW[ty 3 + tx][co][ci] = sum_p d[y][p][co] x[y + ty - 1][p + tx - 1][ci] over
+// every output pixel (b, y, p).  Substituting the input pixel q = p + tx - 1,
+// one GEMM per input-row chunk gives all nine taps at once:
+//   D[(ty, ci)][(tx, co)] = sum_q x[y + ty - 1][q][ci] d[y][q - tx + 1][co],
+// M = 3 CIN rows (two M = 128 MMAs when CIN = 48, one when CIN = 16), N = 3
+// COUT, K = 64 input pixels q of a chunk (4 MMAs of K = 16 per M block).  A
+// = the three input rows around output row y, staged once; B = output-row
+// gradient d, staged three times shifted by tx (zero outside the image).
+// Both operands are K-major in the canonical no-swizzle layout: core matrix
+// (8 channels x 8 pixels, one 16-byte row per channel) number rb 8 + kb for
+// channel block rb and pixel block kb, so the leading (K) byte offset is 128
+// and the stride (M / N) byte offset 1,024.  A warp stages four core matrices
+// per step: each lane loads one 32-bit channel pair of one pixel (a warp
+// load is four 128-byte runs of the channel-group-planar tensors) and one
+// stmatrix.trans writes the four 8 x 8 blocks transposed.
+//
+// One persistent CTA per SM walks its chunks (b, y, 64-pixel segment) with
+// two staging buffers: warps 1-8 fill buffer i % 2 (waiting on its `empty`
+// barrier, committed by the MMAs that read it), fence the writes to the
+// async proxy and arrive on `full`; lane 0 of warp 0 waits on `full` and
+// issues the MMAs into FP32 accumulators in tensor memory that persist over
+// all of the CTA's chunks.  At the end warps 0-7 read the accumulators and
+// write the CTA's partial sums (and its bias-gradient sums, accumulated from
+// the unshifted staging of d) to its slice of the scratch buffer;
+// k_wgrad_reduce adds the slices in a fixed order (deterministic).  Every
+// wait is bounded and raises g_dnStatus on timeout.
+// ---------------------------------------------------------------------------
+constexpr int kWg5Px = 64;         // input pixels per chunk (K per chunk)
+constexpr int kWg5Threads = 288;   // warp 0: MMA issue; warps 1-8: staging
+constexpr int kWg5Stagers = 256;
+constexpr uint32_t kWg5MinSmem = 120 * 1024;  // one CTA per SM: it holds 512 TMEM columns
+
+// Four 8 x 8 BF16 blocks from registers to shared memory, transposed: lane
+// 8 m + r gives the address of row r of block m; the lane's register m holds
+// (row lane / 4, columns 2 (lane % 4), + 1) of block m before the transpose.
+__device__ __forceinline__ void stmatrix_x4_trans(uint32_t addr, uint32_t r0, uint32_t r1,
+    uint32_t r2, uint32_t r3)
+{
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};"
+                 :: "r"(addr), "r"(r0), "r"(r1), "r"(r2), "r"(r3) : "memory");
+}
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
+    const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ d, int B, int H, int W,
+    float *__restrict__ partial)
+{
+    constexpr int KGI = CIN / 8, KGO = COUT / 8;
+    constexpr int MROWS = 3 * CIN, N = 3 * COUT;
+    constexpr int MB = (MROWS + 127) / 128;              // M = 128 blocks
+    constexpr int KB = kWg5Px / 8;                       // pixel blocks per chunk
+    constexpr uint32_t kABytes = (uint32_t)MB * 128 * kWg5Px * 2;
+    constexpr uint32_t kBBytes = (uint32_t)N * kWg5Px * 2;
+    constexpr int TMEM_COLS = MB * N <= 256 ? 256 : 512;
+    static_assert(CIN % 8 == 0 && COUT % 16 == 0 && N <= 256 && MB * N <= 512, "tile shape");
+    static_assert(kWg5Px % 16 == 0, "chunk is whole K = 16 steps");
+    extern __shared__ __align__(1024) unsigned char smemRaw[];
+    const uint32_t base = (smem_u32(smemRaw) + 1023u) & ~1023u;
+    // buffer s: A at base + s (kABytes + kBBytes), B right after it
+    __shared__ __align__(8) uint64_t full[2], empty[2], done;
+    __shared__ uint32_t tmemBase;
+    __shared__ volatile uint32_t abortFlag;
+    __shared__ float sBias[8][COUT];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmemBase)), "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < 2; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&full[i])),
+                         "r"(kWg5Stagers));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&empty[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&done)));
+        abortFlag = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmemBase;
+    const int segs = (W + kWg5Px - 1) / kWg5Px;
+    const int chunks = B * H * segs;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc_bf16<128, N>();
+            uint32_t i = 0;
+            bool ok = true;
+            for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
+                const uint32_t sb = i & 1u;
+                if (!(ok = tc_wait(smem_u32(&full[sb]), (i >> 1) & 1u, &abortFlag))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t aAddr = base + sb * (kABytes + kBBytes);
+                const uint32_t bAddr = aAddr + kABytes;
+#pragma unroll
+                for (int kk = 0; kk < kWg5Px / 16; kk++) {
+                    const uint64_t bDesc = smem_desc(bAddr + (uint32_t)kk * 256u, 128, KB * 128);
+#pragma unroll
+                    for (int mb = 0; mb < MB; mb++) {
+                        const uint64_t aDesc = smem_desc(aAddr + (uint32_t)(mb * 16 * KB * 128) +
+                            (uint32_t)kk * 256u, 128, KB * 128);
+                        tc_mma(tmem + (uint32_t)(mb * N), aDesc, bDesc, idesc,
+                            (i > 0 || kk > 0) ? 1u : 0u);
+                    }
+                }
+                tc_commit(smem_u32(&empty[sb]));
+            }
+            // every MMA issued has finished before the accumulators are read
+            // or freed (waited for even after an abort)
+            tc_commit(smem_u32(&done));
+            volatile uint32_t never = 0u;
+            if (!tc_wait(smem_u32(&done), 0u, &never)) abortFlag = 1u;
+            if (!ok) abortFlag = 1u;
+        }
+        __syncwarp();
+    } else {
+        // ---- staging: warp-steps of four core matrices (one channel block, four
+        // consecutive pixel blocks); lane = (pixel lane / 4, channel pair lane % 4)
+        const int sw = warp - 1;
+        const int px = lane >> 2, pair = lane & 3;
+        float bsum[KGO][2];
+#pragma unroll
+        for (int g = 0; g < KGO; g++) bsum[g][0] = bsum[g][1] = 0.0f;
+        constexpr int kAStepsPerRow = KB / 4;             // warp-steps per channel block
+        constexpr int kASteps = 3 * KGI * kAStepsPerRow;
+        constexpr int kBSteps = 3 * KGO * kAStepsPerRow;
+        uint32_t i = 0;
+        bool ok = true;
+        for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
+            const int seg = c % segs, row = c / segs;
+            const int b = row / H, y = row % H, x0 = seg * kWg5Px;
+            const uint32_t sb = i & 1u;
+            if (i >= 2 && !(ok = tc_wait(smem_u32(&empty[sb]), ((i >> 1) - 1u) & 1u, &abortFlag)))
+                break;
+            const uint32_t aAddr = base + sb * (kABytes + kBBytes);
+            const uint32_t bAddr = aAddr + kABytes;
+            for (int step = sw; step < kASteps + kBSteps; step += 8) {
+                uint32_t r[4];
+                int rb, kb0;
+                uint32_t dst;
+                if (step < kASteps) {
+                    // A: channel block rb = ty KGI + cg of input row y + ty - 1
+                    rb = step / kAStepsPerRow;
+                    kb0 = 4 * (step % kAStepsPerRow);
+                    const int ty = rb / KGI, cg = rb % KGI, gy = y + ty - 1;
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        const int q = x0 + 8 * (kb0 + m) + px;
+                        uint32_t v = 0u;
+                        if (gy >= 0 && gy < H && q < W)
+                            v = __ldg(reinterpret_cast<const uint32_t *>(
+                                    in + cg_index((size_t)(b * H + gy), q, 8 * cg, W, CIN)) + pair);
+                        r[m] = v;
+                    }
+                    dst = aAddr;
+                } else {
+                    // B: channel block rb = tx KGO + cg of d, shifted: column q holds pixel
+                    // q - tx + 1
+                    const int st = step - kASteps;
+                    rb = st / kAStepsPerRow;
+                    kb0 = 4 * (st % kAStepsPerRow);
+                    const int tx = rb / KGO, cg = rb % KGO;
+#pragma unroll
+                    for (int m = 0; m < 4; m++) {
+                        const int p = x0 + 8 * (kb0 + m) + px - tx + 1;
+                        uint32_t v = 0u;
+                        if (p >= 0 && p < W)
+                            v = __ldg(reinterpret_cast<const uint32_t *>(
+                                    d + cg_index((size_t)row, p, 8 * cg, W, COUT)) + pair);
+                        r[m] = v;
+                        if (tx == 1) {
+                            // the unshifted copy covers every output pixel once
+                            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&v);
+#pragma unroll
+                            for (int g = 0; g < KGO; g++)
+                                if (g == cg) {
+                                    bsum[g][0] += __low2float(h);
+                                    bsum[g][1] += __high2float(h);
+                                }
+                        }
+                    }
+                    dst = bAddr;
+                }
+                // lane 8 m + j: row j (channel 8 rb + j) of core matrix (rb, kb0 + m)
+                const int m = lane >> 3, j = lane & 7;
+                stmatrix_x4_trans(dst + (uint32_t)((rb * KB + kb0 + m) * 128 + j * 16), r[0], r[1],
+                    r[2], r[3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(smem_u32(&full[sb]));
+        }
+        if (!ok) abortFlag = 1u;
+        // bias gradient: lanes with the same channel pair hold different pixels
+#pragma unroll
+        for (int g = 0; g < KGO; g++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                float v = bsum[g][h];
+                for (int off = 4; off < 32; off <<= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
+                if (lane < 4) sBias[sw][8 * g + 2 * lane + h] = v;
+            }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // ---- epilogue: warp w < 4 MB reads TMEM lanes 32 (w % 4) .. + 31 of M block w / 4:
+    // accumulator row R = (ty, ci), column n = (tx, co)
+    float *out = partial + (size_t)blockIdx.x * (9 * COUT * CIN + COUT);
+    if (blockIdx.x >= chunks) {
+        // no chunk: nothing accumulated (the launch sizes the grid to avoid this)
+        for (int k = tid; k < 9 * COUT * CIN; k += kWg5Threads) out[k] = 0.0f;
+    } else if (!abortFlag && warp < 4 * MB) {
+        const int mb = warp >> 2, quarter = warp & 3;
+        const int R = mb * 128 + quarter * 32 + lane;
+        const int ty = R / CIN, ci = R % CIN;
+#pragma unroll 1
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mb * N + c0), v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (R < MROWS) {
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const int n = c0 + k, tx = n / COUT, co = n % COUT;
+                    out[((size_t)(3 * ty + tx) * COUT + co) * CIN + ci] = __uint_as_float(v[k]);
+                }
+            }
+        }
+    }
+    if (tid < COUT) {
+        float sum = 0.0f;
+        for (int w = 0; w < 8; w++) sum += sBias[w][tid];
+        out[9 * COUT * CIN + tid] = sum;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && abortFlag) atomicOr(&g_dnStatus, 1u);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     :: "r"(tmem), "r"(TMEM_COLS));
+}
+
 // Per-pixel 5x5 filter from softmax(logits[0..24]) applied to the noisy
 // radiance (clamped to the image edge).
 __global__ void k_filter(const float *__restrict__ logits, const float4 *__restrict__ noisy, int B,
@@ -1288,6 +1538,33 @@ static int launch_wgrad_tc(cudaStream_t s, const __nv_bfloat16 *in, const __nv_b
     return GBSP_OK;
 }
 
+template <int CIN, int COUT>
+static int launch_wgrad_tc5(cudaStream_t s, const __nv_bfloat16 *in, const __nv_bfloat16 *d, int B,
+    int H, int W, float *dW, float *dBias)
+{
+    const int chunks = ((W + kWg5Px - 1) / kWg5Px) * B * H;
+    int grid = sm_count();
+    if (grid > chunks) grid = chunks;
+    constexpr int MB = (3 * CIN + 127) / 128;
+    const size_t smem = std::max<size_t>(
+        1024 + 2 * ((size_t)MB * 128 * kWg5Px * 2 + (size_t)3 * COUT * kWg5Px * 2), kWg5MinSmem);
+    auto kern = k_conv3x3_wgrad_tc5<CIN, COUT>;
+    GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int perSlice = 9 * COUT * CIN + COUT;
+    float *partial = nullptr;
+    GBSP_CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(float) * (size_t)grid * perSlice, s));
+    kern<<<grid, kWg5Threads, smem, s>>>(in, d, B, H, W, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_wgrad_reduce<<<(perSlice + 255) / 256, 256, 0, s>>>(partial, grid, perSlice,
+            9 * COUT * CIN, dW, dBias);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(partial, s);
+    if (e != cudaSuccess) return cuda_error(e, "tcgen05 weight gradient");
+    return GBSP_OK;
+}
+
 extern "C" {
 
 int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
@@ -1440,6 +1717,22 @@ int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint1
     if (cin == 16 && cout == 48) return launch_wgrad_tc<16, 48>(s, i16, d16, B, H, W, dW, dBias);
     if (cin == 48 && cout == 48) return launch_wgrad_tc<48, 48>(s, i16, d16, B, H, W, dW, dBias);
     if (cin == 48 && cout == 32) return launch_wgrad_tc<48, 32>(s, i16, d16, B, H, W, dW, dBias);
+    return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
+}
+
+int gbsp_dn_conv3x3_weight_grad_tcgen05(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!in || !dOut || !dW || !dBias || !B || !H || !W)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad weight-gradient args");
+    if (((uintptr_t)in | (uintptr_t)dOut) & 15u)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight-gradient tensors must be 16-byte aligned");
+    const __nv_bfloat16 *i16 = reinterpret_cast<const __nv_bfloat16 *>(in);
+    const __nv_bfloat16 *d16 = reinterpret_cast<const __nv_bfloat16 *>(dOut);
+    if (cin == 16 && cout == 48) return launch_wgrad_tc5<16, 48>(s, i16, d16, B, H, W, dW, dBias);
+    if (cin == 48 && cout == 48) return launch_wgrad_tc5<48, 48>(s, i16, d16, B, H, W, dW, dBias);
+    if (cin == 48 && cout == 32) return launch_wgrad_tc5<48, 32>(s, i16, d16, B, H, W, dW, dBias);
     return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
 }
 

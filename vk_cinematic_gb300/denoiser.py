@@ -73,9 +73,10 @@ def relmse(x, ref):
 class KPCNN:
     """conv: "tcgen05" (5th-generation tensor cores, accumulator in tensor
     memory) or "mma" (mma.sync BF16 fragments) for the forward and
-    data-gradient convolutions.  wgrad: "mma" (tensor cores, deterministic
-    per-CTA partial sums) or "simt" (FP32 FMA with atomics) for the weight
-    gradient."""
+    data-gradient convolutions.  wgrad: "tcgen05" (5th-generation tensor
+    cores, accumulators in tensor memory), "mma" (mma.sync fragments) - both
+    with deterministic per-CTA partial sums - or "simt" (FP32 FMA with
+    atomics) for the weight gradient."""
 
     def __init__(self, seed: int = 0, conv: str = "tcgen05", wgrad: str = "mma"):
         import torch
@@ -83,7 +84,8 @@ class KPCNN:
         self.L = gbsp.load()
         self._conv = {"tcgen05": self.L.gbsp_dn_conv3x3_forward_tc,
                       "mma": self.L.gbsp_dn_conv3x3_forward}[conv]
-        self._wgrad = {"mma": self.L.gbsp_dn_conv3x3_weight_grad_tc,
+        self._wgrad = {"tcgen05": self.L.gbsp_dn_conv3x3_weight_grad_tcgen05,
+                       "mma": self.L.gbsp_dn_conv3x3_weight_grad_tc,
                        "simt": self.L.gbsp_dn_conv3x3_weight_grad}[wgrad]
         self.conv_impl = conv
         self.wgrad_impl = wgrad

@@ -58,7 +58,7 @@ EXPORTS = [
     "gbsp_dn_conv3x3_forward_tc", "gbsp_dn_status", "gbsp_scene_set_intersection",
     "gbsp_dn_tile_fallback", "gbsp_scene_set_node_width", "gbsp_scene_node_width",
     "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths", "gbsp_path_trace_tile_list",
-    "gbsp_dn_tile_check", "gbsp_dn_tile_merge",
+    "gbsp_dn_tile_check", "gbsp_dn_tile_merge", "gbsp_dn_conv3x3_weight_grad_tcgen05",
 ]
 
 
