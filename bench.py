@@ -829,7 +829,11 @@ def run_config5(args):
             stats.append(st)
         torch.cuda.synchronize()
         served_ms = (time.perf_counter() - t1) * 1e3 / reps
+        stages = {}
+        for r in range(reps):
+            net.serve(sr, 0, 0, W, H, k, seed=11 + r, timing=stages)
         timing[k] = {"served_ms": served_ms,
+                     "stage_ms": {n: v / reps for n, v in stages.items()},
                      "flagged_tile_fraction": float(np.mean([x["flagged"] / x["tiles"]
                                                              for x in stats])),
                      "fallback_spp_per_pixel": float(np.mean([x["fallback_samples"] / (W * H)

@@ -520,12 +520,12 @@ int gbsp_dn_tile_fallback(void *stream, const float *denoised, const float *plai
  * independent plain render (sppC).  tileErr receives the tile's estimated
  * relMSE (unbiased: (D - C)^2 less C's variance, over D^2 + 0.01), flags 1
  * where the estimate exceeds `bound` by more than two standard errors, and
- * needSpp the plain samples per pixel that bring the tile to `bound` (twice
- * the per-sample relMSE estimated from A - C, over bound; 1..maxSpp).  No
- * reference counterpart. */
+ * needSpp the plain samples per pixel that bring the tile to `bound`
+ * (`margin` times the per-sample relMSE estimated from A - C, over bound;
+ * 1..maxSpp).  No reference counterpart. */
 int gbsp_dn_tile_check(void *stream, const float *denoised, const float *plainA, uint32_t sppA,
     const float *plainC, uint32_t sppC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile,
-    float bound, uint32_t maxSpp, float *tileErr, uint32_t *flags, uint32_t *needSpp);
+    float bound, float margin, uint32_t maxSpp, float *tileErr, uint32_t *flags, uint32_t *needSpp);
 /* The served frame: D where flags[t] is 0; elsewhere the mean of all plain
  * samples of the pixel, (sppA A + sppC C + sppF[t] F) / (sppA + sppC +
  * sppF[t]), F the fallback render of the flagged tiles (NULL: none). */

@@ -398,8 +398,9 @@ def test_tile_fallback_ignores_noise_alone(gpu_lib):
 def test_tile_check_flags_bad_tiles_and_sizes_the_fallback(gpu_lib):
     """gbsp_dn_tile_check on synthetic frames with known noise: a tile where D
     is wrong is flagged, correct tiles are not, and the plain spp it asks for
-    matches the per-sample variance (sigma^2 = 0.36 per value at mean 1, so
-    relMSE 0.01 needs 0.36 / 1.01 / 0.01 = 36 samples; the estimate is doubled)."""
+    follows the per-sample variance (sigma^2 = 0.36 per value at mean 1, so
+    relMSE 0.01 needs 0.36 / 1.01 / 0.01 = 36 samples, times the margin; the
+    noisy pooled mean in the denominator makes the estimate lean high)."""
     import torch
 
     from vk_cinematic_gb300.denoiser import KPCNN
@@ -413,7 +414,8 @@ def test_tile_check_flags_bad_tiles_and_sizes_the_fallback(gpu_lib):
     D = mu.clone()
     D[0, 16:32, 32:48, :3] += 0.5
     net = KPCNN(seed=0)
-    err, flags, need = net.check_tiles(D, A, spp_a, C, spp_c, bound=0.01, tile=tile, max_spp=4096)
+    err, flags, need = net.check_tiles(D, A, spp_a, C, spp_c, bound=0.01, tile=tile, max_spp=4096,
+                                       margin=2.0)
     torch.cuda.synchronize()
     f = flags.cpu().numpy().reshape(3, 4)
     bad = np.zeros((3, 4), bool)
@@ -423,7 +425,8 @@ def test_tile_check_flags_bad_tiles_and_sizes_the_fallback(gpu_lib):
     assert np.array_equal(f.astype(bool), bad)
     nd = need.cpu().numpy().astype(np.float64)
     expect = 2 * sigma ** 2 / 1.01 / 0.01
-    assert np.all(np.abs(nd - expect) < 0.3 * expect), (nd, expect)
+    assert np.all((nd > 0.85 * expect) & (nd < 1.6 * expect)), (nd, expect)
+    assert expect <= nd.mean() <= 1.35 * expect, (nd.mean(), expect)
     # merge: flagged tile = weighted mean of the plain samples (and a fallback render)
     Fb = mu + 0.1 * torch.randn((B, H, W, 4), device="cuda", generator=g)
     spp_f = torch.zeros(12, dtype=torch.int32, device="cuda")

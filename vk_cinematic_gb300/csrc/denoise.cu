@@ -1344,12 +1344,12 @@ __global__ void __launch_bounds__(256) k_tile_fallback(const float4 *__restrict_
 // sigma^2.  tileErr = the tile mean of the first over (D^2 + 0.01); the tile
 // is flagged when that estimate exceeds `bound` by more than kFallbackZ
 // standard errors of the mean.  needSpp = the plain samples per pixel that
-// reach `bound` on the tile, twice mean(sigma^2 / (M^2 + 0.01)) / bound with M
-// the pooled plain mean (a factor two for the noise of the variance
+// reach `bound` on the tile, margin x mean(sigma^2 / (M^2 + 0.01)) / bound
+// with M the pooled plain mean (margin > 1 covers the noise of the variance
 // estimate), at least 1 and at most maxSpp.
 __global__ void __launch_bounds__(256) k_tile_check(const float4 *__restrict__ D,
     const float4 *__restrict__ A, float sppA, const float4 *__restrict__ C, float sppC, int B,
-    int H, int W, int tile, float bound, uint32_t maxSpp, float *__restrict__ tileErr,
+    int H, int W, int tile, float bound, float margin, uint32_t maxSpp, float *__restrict__ tileErr,
     uint32_t *__restrict__ flags, uint32_t *__restrict__ needSpp)
 {
     const int tilesX = (W + tile - 1) / tile, tilesY = (H + tile - 1) / tile;
@@ -1403,7 +1403,7 @@ __global__ void __launch_bounds__(256) k_tile_check(const float4 *__restrict__ D
     const float se = tn > 0.0f ? sqrtf(var / tn) : 0.0f;
     tileErr[t] = est;
     flags[t] = est - kFallbackZ * se > bound ? 1u : 0u;
-    const float need = tn > 0.0f ? 2.0f * (tr / tn) / bound : 1.0f;
+    const float need = tn > 0.0f ? margin * (tr / tn) / bound : 1.0f;
     needSpp[t] = need >= (float)maxSpp ? maxSpp : (uint32_t)fmaxf(1.0f, ceilf(need));
 }
 
@@ -1769,10 +1769,10 @@ int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32
 
 int gbsp_dn_tile_check(void *stream, const float *denoised, const float *plainA, uint32_t sppA,
     const float *plainC, uint32_t sppC, uint32_t B, uint32_t H, uint32_t W, uint32_t tile,
-    float bound, uint32_t maxSpp, float *tileErr, uint32_t *flags, uint32_t *needSpp)
+    float bound, float margin, uint32_t maxSpp, float *tileErr, uint32_t *flags, uint32_t *needSpp)
 {
     if (!denoised || !plainA || !plainC || !tileErr || !flags || !needSpp || !B || !H || !W ||
-        !sppA || !sppC || !maxSpp || !(bound > 0.0f))
+        !sppA || !sppC || !maxSpp || !(bound > 0.0f) || !(margin > 0.0f))
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad tile check args");
     if (tile < 1 || tile > 16) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile must be 1..16");
     const uint64_t tiles = (uint64_t)B * ((H + tile - 1) / tile) * ((W + tile - 1) / tile);
@@ -1780,7 +1780,7 @@ int gbsp_dn_tile_check(void *stream, const float *denoised, const float *plainA,
     k_tile_check<<<(unsigned)tiles, 256, 0, (cudaStream_t)stream>>>(
         reinterpret_cast<const float4 *>(denoised), reinterpret_cast<const float4 *>(plainA),
         (float)sppA, reinterpret_cast<const float4 *>(plainC), (float)sppC, (int)B, (int)H, (int)W,
-        (int)tile, bound, maxSpp, tileErr, flags, needSpp);
+        (int)tile, bound, margin, maxSpp, tileErr, flags, needSpp);
     GBSP_CUDA_TRY(cudaGetLastError());
     return GBSP_OK;
 }

@@ -200,7 +200,7 @@ class KPCNN:
         return out, err, flags
 
     def check_tiles(self, denoised, plain_a, spp_a, plain_c, spp_c, bound=0.01, tile=16,
-                    max_spp=4096):
+                    max_spp=4096, margin=1.25):
         """gbsp_dn_tile_check: per tile x tile block, the estimated relMSE of the
         denoised frames, the flag (estimate above `bound` by two standard
         errors) and the plain spp that brings the tile to `bound`."""
@@ -213,8 +213,8 @@ class KPCNN:
         need = torch.empty(tiles, dtype=torch.int32, device="cuda")
         _check(self.L.gbsp_dn_tile_check(_stream(), _ptr(denoised), _ptr(plain_a), _u32(spp_a),
                                          _ptr(plain_c), _u32(spp_c), _u32(B), _u32(H), _u32(W),
-                                         _u32(tile), _f32(bound), _u32(max_spp), _ptr(err),
-                                         _ptr(flags), _ptr(need)))
+                                         _u32(tile), _f32(bound), _f32(margin), _u32(max_spp),
+                                         _ptr(err), _ptr(flags), _ptr(need)))
         return err, flags, need
 
     def merge_tiles(self, denoised, plain_a, spp_a, plain_c, spp_c, fallback, spp_f, flags,
@@ -231,7 +231,8 @@ class KPCNN:
                                          _u32(H), _u32(W), _u32(tile), _ptr(flags), _ptr(out)))
         return out
 
-    def serve(self, sr, x0, y0, w, h, spp, seed, bound=0.01, tile=16, max_spp=4096):
+    def serve(self, sr, x0, y0, w, h, spp, seed, bound=0.01, tile=16, max_spp=1024, margin=1.25,
+              timing=None):
         """The served output of a w x h window of `sr`'s frame: `spp`-sample plain
         render + G-buffers -> denoised; an independent `spp`-sample plain render
         checks every tile x tile block (check_tiles); blocks that fail are served
@@ -242,12 +243,24 @@ class KPCNN:
         denoised image under "denoised"."""
         import torch
 
+        ev = [] if timing is not None else None
+
+        def mark():
+            if ev is not None:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record()
+                ev.append(e)
+
+        mark()
         rad, aov = sr.render(x0, y0, w, h, spp, seed, aov=True)
+        mark()
         chk, _ = sr.render(x0, y0, w, h, spp, (seed + 0x1B873593) & 0xFFFFFFFF)
+        mark()
         den = self.denoise(rad.unsqueeze(0).contiguous(), aov.unsqueeze(0).contiguous())
+        mark()
         err, flags, need = self.check_tiles(den, rad.unsqueeze(0).contiguous(), spp,
                                             chk.unsqueeze(0).contiguous(), spp, bound, tile,
-                                            max_spp)
+                                            max_spp, margin)
         f = flags.cpu().numpy()
         nd = need.cpu().numpy()
         tx = (w + tile - 1) // tile
@@ -262,6 +275,7 @@ class KPCNN:
             bx, by = int(t % tx) * tile, int(t // tx) * tile
             groups.setdefault(k, []).append((x0 + bx, y0 + by, x0 + min(bx + tile, w),
                                              y0 + min(by + tile, h)))
+        mark()
         fb = None
         fb_samples = 0
         if groups:
@@ -270,10 +284,18 @@ class KPCNN:
                 fb_samples += k * sum((t[2] - t[0]) * (t[3] - t[1]) for t in tl)
             fb = torch.empty((1, h, w, 4), dtype=torch.float32, device="cuda")
             sr.rend.copy_region(x0, y0, w, h, fb.data_ptr())
+        mark()
         out = self.merge_tiles(den, rad.unsqueeze(0).contiguous(), spp,
                                chk.unsqueeze(0).contiguous(), spp, fb,
                                torch.from_numpy(spp_f).cuda() if fb is not None else None, flags,
                                tile)
+        mark()
+        if ev is not None:
+            torch.cuda.synchronize()
+            names = ["input_render", "check_render", "denoise", "check_and_readback",
+                     "fallback_renders", "merge"]
+            for k, n in enumerate(names):
+                timing[n] = timing.get(n, 0.0) + ev[k].elapsed_time(ev[k + 1])
         stats = {"tiles": int(len(f)), "flagged": int(f.sum()), "fallback_samples": fb_samples,
                  "fallback_groups": sorted(groups), "denoised": den[0]}
         return out[0], stats
