@@ -134,7 +134,12 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
         if constexpr (kWT) {
             h = ray_triangle_watertight(lo, ld, a, b, c, v3(A.w, B.w, C.w));
         } else {
-            // the reference only reaches triangles whose own box passes
+            // the three conditions of a hit, cheapest first (each is a pure
+            // predicate, so the order changes no result): the face culling of
+            // RayIntersectTriangleMT (src/ray_intersection.cpp:181-182), the
+            // triangle's own box (the reference only reaches triangles whose
+            // box passes), then the test itself
+            if (!(dot(ld, v3(A.w, B.w, C.w)) < 0.0f)) continue;
             V3 bl = vmin(a, vmin(b, c)), bh = vmax(a, vmax(b, c));
             if (slab_entry(bl, bh, lo, linvd) < 0.0f) continue;
             h = ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
