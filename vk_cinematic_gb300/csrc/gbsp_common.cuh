@@ -201,6 +201,23 @@ GBSP_HD float slab_entry(V3 lo, V3 hi, V3 o, V3 invd)
     return tn <= tf ? tn : -1.0f;
 }
 
+// The slab test of interior nodes for rays whose inverse direction is finite:
+// the same arithmetic with min / max instructions (fminf / fmaxf) in place of
+// the reference's `a < b ? a : b` form.  The two differ only when an operand
+// is NaN or the operands are zeros of opposite sign; with finite boxes, a
+// finite origin and a finite inverse direction no NaN can arise, and signed
+// zeros compare equal, so every decision and entry distance is the same.
+// Leaves (the triangle box gate) keep slab_entry.
+GBSP_HD float slab_entry_node(V3 lo, V3 hi, V3 o, V3 invd)
+{
+    float t0x = (lo.x - o.x) * invd.x, t1x = (hi.x - o.x) * invd.x;
+    float t0y = (lo.y - o.y) * invd.y, t1y = (hi.y - o.y) * invd.y;
+    float t0z = (lo.z - o.z) * invd.z, t1z = (hi.z - o.z) * invd.z;
+    float tn = fmaxf(fmaxf(0.0f, fminf(t0x, t1x)), fmaxf(fminf(t0y, t1y), fminf(t0z, t1z)));
+    float tf = fminf(fmaxf(t0x, t1x), fminf(fmaxf(t0y, t1y), fmaxf(t0z, t1z)));
+    return tn <= tf ? tn : -1.0f;
+}
+
 // The same test with the exit distance scaled by 1 + 2 gamma(3) (Ize, "Robust
 // BVH Ray Traversal", JCGT 2(2), 2013): a rounded slab test can no longer
 // reject a ray that touches the box, which the watertight mode relies on.

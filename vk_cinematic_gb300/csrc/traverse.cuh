@@ -54,10 +54,12 @@ __device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765
 // test.  With kKeepNearest the nearest hit child is not pushed but returned
 // in *next (ref kEmptyChild when no child is hit), for the caller to visit
 // straight away: one stack store and load fewer per node visit.
-template <bool kCount, bool kWT = false, bool kKeepNearest = false>
-__device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint32_t quads,
+// kFastSlab: slab_entry_node instead of the reference's slab_entry (see
+// visit_node for when that is allowed).
+template <bool kCount, bool kWT, bool kKeepNearest, bool kFastSlab>
+__device__ __forceinline__ void visit_node_impl(const float4 *__restrict__ pool, uint32_t quads,
     uint32_t ref, V3 o, V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
-    TraceCounters &cnt, StackEntry *next = nullptr)
+    TraceCounters &cnt, StackEntry *next)
 {
     const float4 *p = pool + node_offset(ref, quads);
     uint32_t nearRef = kEmptyChild;
@@ -79,7 +81,9 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint
             if (c == kEmptyChild) continue;
             if (kCount) cnt.boxTests++;
             V3 bl = v3(lxs[k], lys[k], lzs[k]), bh = v3(hxs[k], hys[k], hzs[k]);
-            float te = kWT ? slab_entry_robust(bl, bh, o, invd) : slab_entry(bl, bh, o, invd);
+            float te = kWT ? slab_entry_robust(bl, bh, o, invd)
+                           : (kFastSlab ? slab_entry_node(bl, bh, o, invd)
+                                        : slab_entry(bl, bh, o, invd));
             if (te < 0.0f || te > bound) continue;
             if (te < nearT) {
                 if (nearRef != kEmptyChild) {
@@ -112,6 +116,25 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint
             atomicOr(status, kStatusStackOverflow);
         }
     }
+}
+
+// Interior nodes take the min/max-instruction slab test when every component
+// of the inverse direction is finite: then no NaN can arise and it decides
+// exactly as the reference's form.  A ray with a zero direction component (an
+// infinite inverse, where (lo - o) * invd can be NaN and the reference's form
+// has its own NaN rules) keeps the reference's form, whose decisions below a
+// node are a superset of its leaves'.
+template <bool kCount, bool kWT = false, bool kKeepNearest = false>
+__device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint32_t quads,
+    uint32_t ref, V3 o, V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
+    TraceCounters &cnt, StackEntry *next = nullptr)
+{
+    if (kWT || !(isfinite(invd.x) && isfinite(invd.y) && isfinite(invd.z)))
+        visit_node_impl<kCount, kWT, kKeepNearest, false>(pool, quads, ref, o, invd, bound, stack,
+            sp, status, cnt, next);
+    else
+        visit_node_impl<kCount, kWT, kKeepNearest, true>(pool, quads, ref, o, invd, bound, stack,
+            sp, status, cnt, next);
 }
 
 // Triangle candidates of one mesh leaf, in object space.  kWT: the
