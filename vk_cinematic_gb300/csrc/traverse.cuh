@@ -62,6 +62,13 @@ __device__ __forceinline__ void visit_node_impl(const float4 *__restrict__ pool,
     TraceCounters &cnt, StackEntry *next)
 {
     const float4 *p = pool + node_offset(ref, quads);
+    // a node pushes at most 4 * quads entries: one room check per visit instead
+    // of one per push (a walk out of room reports the overflow and skips the node)
+    if (sp > kStackSize - 4 * (int)kMaxNodeQuads) {
+        atomicOr(status, kStatusStackOverflow);
+        if constexpr (kKeepNearest) next->ref = kEmptyChild;
+        return;
+    }
     uint32_t nearRef = kEmptyChild;
     float nearT = kInf;
 #pragma unroll
@@ -87,34 +94,22 @@ __device__ __forceinline__ void visit_node_impl(const float4 *__restrict__ pool,
             if (te < 0.0f || te > bound) continue;
             if (te < nearT) {
                 if (nearRef != kEmptyChild) {
-                    if (sp < kStackSize) {
-                        stack[sp] = StackEntry{nearRef, nearT};
-                        sp++;
-                    } else {
-                        atomicOr(status, kStatusStackOverflow);
-                    }
+                    stack[sp] = StackEntry{nearRef, nearT};
+                    sp++;
                 }
                 nearRef = c;
                 nearT = te;
             } else {
-                if (sp < kStackSize) {
-                    stack[sp] = StackEntry{c, te};
-                    sp++;
-                } else {
-                    atomicOr(status, kStatusStackOverflow);
-                }
+                stack[sp] = StackEntry{c, te};
+                sp++;
             }
         }
     }
     if constexpr (kKeepNearest) {
         *next = StackEntry{nearRef, nearT};
     } else if (nearRef != kEmptyChild) {
-        if (sp < kStackSize) {
-            stack[sp] = StackEntry{nearRef, nearT};
-            sp++;
-        } else {
-            atomicOr(status, kStatusStackOverflow);
-        }
+        stack[sp] = StackEntry{nearRef, nearT};
+        sp++;
     }
 }
 
