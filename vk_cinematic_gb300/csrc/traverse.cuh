@@ -134,10 +134,8 @@ __device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint
 
 // Triangle candidates of one mesh leaf, in object space.  kWT: the
 // watertight test on every candidate (no box gate: a rounded box test could
-// reject an edge ray); otherwise the reference's gate and MT test.  kUV: also
-// keep the winner's barycentrics (a walk that recomputes them once per ray
-// passes false and ignores bestU / bestV).
-template <bool kCount, bool kWT = false, bool kUV = true>
+// reject an edge ray); otherwise the reference's gate and MT test.
+template <bool kCount, bool kWT = false>
 __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
     V3 linvd, float &bestT, float &bestU, float &bestV, int32_t &bestPrim, TraceCounters &cnt)
 {
@@ -168,41 +166,14 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
             take = __ldg(sv.triIds + j) < __ldg(sv.triIds + bestPrim);
         if (take) {
             bestT = h.t;
-            if constexpr (kUV) {
-                bestU = h.u;
-                bestV = h.v;
-            }
+            bestU = h.u;
+            bestV = h.v;
             bestPrim = (int32_t)j;
         }
     }
 }
 
-// Barycentrics of a known closest hit (triangle prim of instance inst): the
-// same object-space ray and triangle test as the walk that found it, hence
-// the same bits.  Lets a walk carry only t and the triangle.
-template <bool kWT>
-__device__ __forceinline__ void hit_barycentrics(const SceneView &sv, V3 o, V3 d, int32_t prim,
-    int32_t inst, float &u, float &v)
-{
-    const Instance &in = sv.instances[inst];
-    Affine inv;
-#pragma unroll
-    for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
-    float len;
-    const V3 lo = transform_point(inv, o);
-    const V3 ld = normalize(transform_vector(inv, d), &len);
-    const float4 *tp = reinterpret_cast<const float4 *>(sv.tris + prim);
-    const float4 A = __ldg(tp + 0), B = __ldg(tp + 1), C = __ldg(tp + 2);
-    const V3 a = v3(A.x, A.y, A.z), b = v3(B.x, B.y, B.z), c = v3(C.x, C.y, C.z);
-    const TriHit h = kWT ? ray_triangle_watertight(lo, ld, a, b, c, v3(A.w, B.w, C.w))
-                         : ray_triangle_mt(lo, ld, a, b, c, v3(A.w, B.w, C.w));
-    u = h.u;
-    v = h.v;
-}
-
-// kUV false: the walk keeps only t and the triangle and the barycentrics are
-// recomputed once at the end (fewer live registers during the walk).
-template <bool kCount, bool kWT = false, bool kUV = true>
+template <bool kCount, bool kWT = false>
 __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *status,
     TraceCounters &cnt)
 {
@@ -278,7 +249,7 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
                 visit_node<kCount, kWT, true>(nodes, quads, r2, lo, linvd, bound, stack, sp, status,
                     cnt, &lnext);
             } else {
-                visit_leaf<kCount, kWT, kUV>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+                visit_leaf<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
             }
         }
         sp = base;
@@ -290,16 +261,11 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
         float tw = dot(sub(worldHit, o), d);
         if (tw < best.t || (tw == best.t && (int32_t)inst < best.inst)) {
             best.t = tw;
-            if constexpr (kUV) {
-                best.u = lU;
-                best.v = lV;
-            }
+            best.u = lU;
+            best.v = lV;
             best.prim = lPrim;
             best.inst = (int32_t)inst;
         }
-    }
-    if constexpr (!kUV) {
-        if (best.prim >= 0) hit_barycentrics<kWT>(sv, o, d, best.prim, best.inst, best.u, best.v);
     }
     return best;
 }

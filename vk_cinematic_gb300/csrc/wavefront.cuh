@@ -264,8 +264,8 @@ __global__ void __launch_bounds__(128, 6) k_trace(Src src, const float4 *__restr
         if (i < count) {
             float4 o4 = rayO[i], d4 = rayD[i];
             const SceneView &sv = src.scene((uint32_t)__float_as_int(o4.w));
-            RayHit h = trace_closest<true, kWT, false>(sv, v3(o4.x, o4.y, o4.z),
-                v3(d4.x, d4.y, d4.z), status, cnt);
+            RayHit h = trace_closest<true, kWT>(sv, v3(o4.x, o4.y, o4.z), v3(d4.x, d4.y, d4.z),
+                status, cnt);
             hitA[i] = make_int4(__float_as_int(h.t), __float_as_int(h.u), __float_as_int(h.v),
                 h.prim);
             hitInst[i] = h.inst;
@@ -322,13 +322,10 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
     int mode = 0;  // 0 needs a ray, 1 object level, 2 mesh level
     uint32_t slot = 0, steps = 0, inst = 0;
     V3 o = v3(0, 0, 0), d = v3(0, 0, 0), invd = v3(0, 0, 0);
-    // the walk keeps only t and the triangle of the best hit (fewer live
-    // registers); its barycentrics are recomputed once per ray when the hit
-    // record is written
-    float bestT = kInf;
+    float bestT = kInf, bestU = 0.0f, bestV = 0.0f;
     int32_t bestPrim = -1, bestInst = -1;
     V3 lo = v3(0, 0, 0), ld = v3(0, 0, 0), linvd = v3(0, 0, 0);
-    float len = 0.0f, lBestT = kInf;
+    float len = 0.0f, lBestT = kInf, lU = 0.0f, lV = 0.0f;
     int32_t lPrim = -1;
     uint32_t pathId = 0;
     bool drained = false;
@@ -352,6 +349,7 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
             pathId = (uint32_t)__float_as_int(o4.w);
             invd = inverse(d);
             bestT = kInf;
+            bestU = bestV = 0.0f;
             bestPrim = bestInst = -1;
             sp = 0;
             next = StackEntry{src.scene(pathId).tlasRoot, 0.0f};
@@ -375,17 +373,14 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
                 float tw = dot(sub(worldHit, o), d);
                 if (tw < bestT || (tw == bestT && (int32_t)inst < bestInst)) {
                     bestT = tw;
+                    bestU = lU;
+                    bestV = lV;
                     bestPrim = lPrim;
                     bestInst = (int32_t)inst;
                 }
             }
             mode = 1;
         } else if (mode == 1 && levelDone) {
-            // barycentrics of the winning triangle: the same object-space ray and
-            // triangle test as during the walk, hence the same bits
-            float bestU = 0.0f, bestV = 0.0f;
-            if (bestPrim >= 0)
-                hit_barycentrics<kWT>(src.scene(pathId), o, d, bestPrim, bestInst, bestU, bestV);
             hitA[slot] = make_int4(__float_as_int(bestT), __float_as_int(bestU),
                 __float_as_int(bestV), bestPrim);
             hitInst[slot] = bestInst;
@@ -426,14 +421,14 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
                 linvd = inverse(ld);
                 cnt.meshTests++;
                 lBestT = kInf;
+                lU = lV = 0.0f;
                 lPrim = -1;
                 base = sp;
                 next = StackEntry{__ldg(&in.blasRoot), 0.0f};
                 mode = 2;
             } else {
-                float du, dv;
-                visit_leaf<true, kWT, false>(src.scene(pathId), ref, lo, ld, linvd, lBestT, du, dv,
-                    lPrim, cnt);
+                visit_leaf<true, kWT>(src.scene(pathId), ref, lo, ld, linvd, lBestT, lU, lV, lPrim,
+                    cnt);
             }
         }
     }
