@@ -70,7 +70,10 @@ def parse_args():
     ap.add_argument("--dn-eval-crop", type=int, default=256)
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--dn-conv", choices=["tcgen05", "mma"], default="tcgen05")
-    ap.add_argument("--dn-wgrad", choices=["tcgen05", "mma", "simt"], default="mma")
+    ap.add_argument("--dn-wgrad", choices=["tcgen05", "mma", "simt"], default="tcgen05")
+    ap.add_argument("--dn-check-spp", default="same,1",
+                    help="config5: sample counts of the served output's check render, "
+                         "comma-separated; 'same' = the input render's spp")
     ap.add_argument("--sort-dirs", action="store_true",
                     help="sort bounce-ray queues by direction octant")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -768,9 +771,12 @@ def run_config5(args):
     in_spps = sorted(set([1, 2, 4, 8] + train_spp))
     plain = {k: [] for k in spps}
     den = {k: [] for k in in_spps}
-    served = {k: [] for k in in_spps}
-    flagged = {k: [] for k in in_spps}
-    fb_spp = {k: [] for k in in_spps}
+    check_opts = [None if v == "same" else int(v) for v in str(args.dn_check_spp).split(",") if v]
+    protos = [(k, c) for k in in_spps for c in check_opts]
+    pname = lambda kc: f"{kc[0]}/{kc[1] or kc[0]}"  # noqa: E731  input spp / check spp
+    served = {p: [] for p in protos}
+    flagged = {p: [] for p in protos}
+    fb_spp = {p: [] for p in protos}
     rng = np.random.default_rng(99)
     for e in range(args.dn_eval_seeds):
         se = denoiser.denoise_scene(20_000 + e)
@@ -781,12 +787,14 @@ def run_config5(args):
         for k in spps:
             img, _ = sre.render(x0, y0, crop, crop, k, seed=7 + k)
             plain[k].append(denoiser.relmse(img, ref))
-        for k in in_spps:
-            out, st = net.serve(sre, x0, y0, crop, crop, k, seed=5 + 31 * k, bound=0.01)
-            den[k].append(denoiser.relmse(st["denoised"], ref))
-            served[k].append(denoiser.relmse(out, ref))
-            flagged[k].append(st["flagged"] / st["tiles"])
-            fb_spp[k].append(st["fallback_samples"] / float(crop * crop))
+        for k, c in protos:
+            out, st = net.serve(sre, x0, y0, crop, crop, k, seed=5 + 31 * k, bound=0.01,
+                                check_spp=c)
+            if c == check_opts[0]:
+                den[k].append(denoiser.relmse(st["denoised"], ref))
+            served[(k, c)].append(denoiser.relmse(out, ref))
+            flagged[(k, c)].append(st["flagged"] / st["tiles"])
+            fb_spp[(k, c)].append(st["fallback_samples"] / float(crop * crop))
     plain_mean = {k: float(np.mean(v)) for k, v in plain.items()}
     den_mean = {k: float(np.mean(v)) for k, v in den.items()}
     served_mean = {k: float(np.mean(v)) for k, v in served.items()}
@@ -801,10 +809,11 @@ def run_config5(args):
     if need is None and plain_mean[spps[-1]] > 0.01:
         # extrapolate with the Monte Carlo rate relMSE ~ 1/spp from the last point
         need = spps[-1] * plain_mean[spps[-1]] / 0.01
-    # the quoted protocol's input spp, and the cheapest input whose served output
-    # meets the bound on the held-out crops
+    # the quoted protocol (the training input spp, check render of the same spp)
+    # and every protocol whose served output meets the bound on the held-out crops
     quoted_spp = train_spp[-1]
-    cheapest = next((k for k in in_spps if served_mean[k] <= 0.01), None)
+    quoted = (quoted_spp, check_opts[0])
+    valid = [p for p in protos if served_mean[p] <= 0.01]
 
     # ---- timing at 1920x1080: plain path tracing vs the served output
     s = denoiser.denoise_scene(10_000)
@@ -818,21 +827,21 @@ def run_config5(args):
     torch.cuda.synchronize()
     ms_per_spp = ev0.elapsed_time(ev1) / 64.0
     timing = {}
-    for k in sorted(set([quoted_spp] + ([cheapest] if cheapest else []))):
-        net.serve(sr, 0, 0, W, H, k, seed=1)  # warm-up
+    for k, c in sorted(set([quoted] + valid), key=lambda kc: (kc[0], kc[1] or kc[0])):
+        net.serve(sr, 0, 0, W, H, k, seed=1, check_spp=c)  # warm-up
         torch.cuda.synchronize()
         reps = 5
         t1 = time.perf_counter()
         stats = []
         for r in range(reps):
-            _, st = net.serve(sr, 0, 0, W, H, k, seed=11 + r)
+            _, st = net.serve(sr, 0, 0, W, H, k, seed=11 + r, check_spp=c)
             stats.append(st)
         torch.cuda.synchronize()
         served_ms = (time.perf_counter() - t1) * 1e3 / reps
         stages = {}
         for r in range(reps):
-            net.serve(sr, 0, 0, W, H, k, seed=11 + r, timing=stages)
-        timing[k] = {"served_ms": served_ms,
+            net.serve(sr, 0, 0, W, H, k, seed=11 + r, timing=stages, check_spp=c)
+        timing[(k, c)] = {"served_ms": served_ms,
                      "stage_ms": {n: v / reps for n, v in stages.items()},
                      "flagged_tile_fraction": float(np.mean([x["flagged"] / x["tiles"]
                                                              for x in stats])),
@@ -849,8 +858,10 @@ def run_config5(args):
     flops = 2.0 * W * H * sum(9 * ci * co for ci, co, _ in [(10, 48, 0)] + [(48, 48, 0)] * 6 +
                               [(48, 25, 1)])
     plain_ms = need * ms_per_spp if need else None
-    headline_spp = quoted_spp if served_mean[quoted_spp] <= 0.01 else cheapest
-    served_ms = timing[headline_spp]["served_ms"] if headline_spp in timing else None
+    # headline: the fastest protocol that meets the bound on the held-out crops
+    # (chosen on those crops, timed on a different scene)
+    headline = min(valid, key=lambda p: timing[p]["served_ms"]) if valid else None
+    served_ms = timing[headline]["served_ms"] if headline else None
     bf16_peak = measured_bf16_peak()
     value = (plain_ms / served_ms) if (plain_ms and served_ms) else None
     line = {
@@ -865,17 +876,21 @@ def run_config5(args):
                    "eval_seeds": args.dn_eval_seeds, "eval_crop": crop,
                    "oracle_spp": args.dn_oracle_spp, "conv": net.conv_impl,
                    "served": "denoised; 16x16 tiles checked against an independent plain render "
-                             "of the same spp; failing tiles served from all their plain "
-                             "samples topped up to the spp the check estimates for the bound"},
-        "served_input_spp": headline_spp, "quoted_input_spp": quoted_spp,
-        "served_relmse_by_input_spp": served_mean,
+                             "(protocols input spp / check spp); failing tiles served from all "
+                             "their plain samples topped up to the spp the check estimates for "
+                             "the bound"},
+        "served_protocol": pname(headline) if headline else None,
+        "quoted_protocol": pname(quoted),
+        "served_relmse_by_protocol": {pname(p): v for p, v in served_mean.items()},
         "denoised_unchecked_relmse_by_input_spp": den_mean,
-        "flagged_tile_fraction_by_input_spp": {k: float(np.mean(v)) for k, v in flagged.items()},
-        "fallback_spp_per_pixel_by_input_spp": {k: float(np.mean(v)) for k, v in fb_spp.items()},
-        "served_relmse_max_over_crops": {k: float(np.max(v)) for k, v in served.items()},
+        "flagged_tile_fraction_by_protocol": {pname(p): float(np.mean(v))
+                                              for p, v in flagged.items()},
+        "fallback_spp_per_pixel_by_protocol": {pname(p): float(np.mean(v))
+                                               for p, v in fb_spp.items()},
+        "served_relmse_max_over_crops": {pname(p): float(np.max(v)) for p, v in served.items()},
         "plain_relmse_by_spp": plain_mean, "plain_spp_for_0.01": need,
         "ms_plain_per_spp_1080p": ms_per_spp, "plain_ms_to_0.01": plain_ms,
-        "served_ms_1080p": {str(k): v for k, v in timing.items()},
+        "served_ms_1080p": {pname(p): v for p, v in timing.items()},
         "served_ms_to_0.01": served_ms,
         "ms_denoise_1080p": dn_ms, "denoiser_tflops": flops / (dn_ms * 1e-3) / 1e12,
         "roofline": {"bound": "tensor", "kernel": "denoiser inference (8 x k_conv3x3_tc + filter)",

@@ -442,10 +442,12 @@ def test_tile_check_flags_bad_tiles_and_sizes_the_fallback(gpu_lib):
     assert torch.equal(o[0][keep][:, :3], D.cpu()[0][keep][:, :3])
 
 
-def test_served_output_runs_end_to_end(gpu_lib):
+@pytest.mark.parametrize("check_spp", [None, 1])
+def test_served_output_runs_end_to_end(gpu_lib, check_spp):
     """KPCNN.serve on a small scene: input render + G-buffers, denoise, check
-    render, tile check, fallback tile-list renders, merge; the served image is
-    finite and, on flagged tiles, equals the mean of all their plain samples."""
+    render (the input's spp, or 1), tile check, fallback tile-list renders,
+    merge; the served image is finite and most tiles of an untrained network
+    fall back."""
     import torch
 
     from vk_cinematic_gb300 import denoiser
@@ -456,7 +458,7 @@ def test_served_output_runs_end_to_end(gpu_lib):
     s = scenes.config3_scene(width=160, height=96, spp=2, n_spheres=32, level=2, seed=8)
     sr = denoiser.SceneRenderer(rt, s)
     net = denoiser.KPCNN(seed=0)
-    out, st = net.serve(sr, 0, 0, s.width, s.height, 2, seed=3, bound=0.01)
+    out, st = net.serve(sr, 0, 0, s.width, s.height, 2, seed=3, bound=0.01, check_spp=check_spp)
     torch.cuda.synchronize()
     print("served stats", {k: v for k, v in st.items() if k != "denoised"})
     assert out.shape == (s.height, s.width, 4)

@@ -1110,7 +1110,10 @@ __global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
         __syncwarp();
     } else {
         // ---- staging: warp-steps of four core matrices (one channel block, four
-        // consecutive pixel blocks); lane = (pixel lane / 4, channel pair lane % 4)
+        // consecutive pixel blocks); lane = (pixel lane / 4, channel pair lane % 4).
+        // A warp loads all its steps of a chunk into registers at once (many loads
+        // in flight), and loads the next chunk right after storing this one, so
+        // the loads overlap the tensor core's work and the wait for a free buffer.
         const int sw = warp - 1;
         const int px = lane >> 2, pair = lane & 3;
         float bsum[KGO][2];
@@ -1119,24 +1122,20 @@ __global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
         constexpr int kAStepsPerRow = KB / 4;             // warp-steps per channel block
         constexpr int kASteps = 3 * KGI * kAStepsPerRow;
         constexpr int kBSteps = 3 * KGO * kAStepsPerRow;
-        uint32_t i = 0;
-        bool ok = true;
-        for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
+        constexpr int kSteps = kASteps + kBSteps;
+        constexpr int kMaxSteps = (kSteps + 7) / 8;       // per stager warp
+        uint32_t r[kMaxSteps][4];
+        // the staged values of chunk c (step k of this warp is sw + 8 k)
+        auto load_chunk = [&](int c) {
             const int seg = c % segs, row = c / segs;
             const int b = row / H, y = row % H, x0 = seg * kWg5Px;
-            const uint32_t sb = i & 1u;
-            if (i >= 2 && !(ok = tc_wait(smem_u32(&empty[sb]), ((i >> 1) - 1u) & 1u, &abortFlag)))
-                break;
-            const uint32_t aAddr = base + sb * (kABytes + kBBytes);
-            const uint32_t bAddr = aAddr + kABytes;
-            for (int step = sw; step < kASteps + kBSteps; step += 8) {
-                uint32_t r[4];
-                int rb, kb0;
-                uint32_t dst;
+#pragma unroll
+            for (int k = 0; k < kMaxSteps; k++) {
+                const int step = sw + 8 * k;
+                if (step >= kSteps) break;
                 if (step < kASteps) {
                     // A: channel block rb = ty KGI + cg of input row y + ty - 1
-                    rb = step / kAStepsPerRow;
-                    kb0 = 4 * (step % kAStepsPerRow);
+                    const int rb = step / kAStepsPerRow, kb0 = 4 * (step % kAStepsPerRow);
                     const int ty = rb / KGI, cg = rb % KGI, gy = y + ty - 1;
 #pragma unroll
                     for (int m = 0; m < 4; m++) {
@@ -1145,15 +1144,13 @@ __global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
                         if (gy >= 0 && gy < H && q < W)
                             v = __ldg(reinterpret_cast<const uint32_t *>(
                                     in + cg_index((size_t)(b * H + gy), q, 8 * cg, W, CIN)) + pair);
-                        r[m] = v;
+                        r[k][m] = v;
                     }
-                    dst = aAddr;
                 } else {
-                    // B: channel block rb = tx KGO + cg of d, shifted: column q holds pixel
-                    // q - tx + 1
+                    // B: channel block rb = tx KGO + cg of d, shifted: column q holds
+                    // pixel q - tx + 1
                     const int st = step - kASteps;
-                    rb = st / kAStepsPerRow;
-                    kb0 = 4 * (st % kAStepsPerRow);
+                    const int rb = st / kAStepsPerRow, kb0 = 4 * (st % kAStepsPerRow);
                     const int tx = rb / KGO, cg = rb % KGO;
 #pragma unroll
                     for (int m = 0; m < 4; m++) {
@@ -1162,10 +1159,34 @@ __global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
                         if (p >= 0 && p < W)
                             v = __ldg(reinterpret_cast<const uint32_t *>(
                                     d + cg_index((size_t)row, p, 8 * cg, W, COUT)) + pair);
-                        r[m] = v;
-                        if (tx == 1) {
-                            // the unshifted copy covers every output pixel once
-                            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&v);
+                        r[k][m] = v;
+                    }
+                }
+            }
+        };
+        // stores the staged values into buffer addresses aAddr / bAddr; bias sums
+        // from the unshifted copy of d, which covers every output pixel once
+        auto store_chunk = [&](uint32_t aAddr, uint32_t bAddr) {
+#pragma unroll
+            for (int k = 0; k < kMaxSteps; k++) {
+                const int step = sw + 8 * k;
+                if (step >= kSteps) break;
+                int rb, kb0;
+                uint32_t dst;
+                if (step < kASteps) {
+                    rb = step / kAStepsPerRow;
+                    kb0 = 4 * (step % kAStepsPerRow);
+                    dst = aAddr;
+                } else {
+                    const int st = step - kASteps;
+                    rb = st / kAStepsPerRow;
+                    kb0 = 4 * (st % kAStepsPerRow);
+                    dst = bAddr;
+                    if (rb / KGO == 1) {
+                        const int cg = rb % KGO;
+#pragma unroll
+                        for (int m = 0; m < 4; m++) {
+                            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&r[k][m]);
 #pragma unroll
                             for (int g = 0; g < KGO; g++)
                                 if (g == cg) {
@@ -1174,15 +1195,25 @@ __global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
                                 }
                         }
                     }
-                    dst = bAddr;
                 }
                 // lane 8 m + j: row j (channel 8 rb + j) of core matrix (rb, kb0 + m)
                 const int m = lane >> 3, j = lane & 7;
-                stmatrix_x4_trans(dst + (uint32_t)((rb * KB + kb0 + m) * 128 + j * 16), r[0], r[1],
-                    r[2], r[3]);
+                stmatrix_x4_trans(dst + (uint32_t)((rb * KB + kb0 + m) * 128 + j * 16), r[k][0],
+                    r[k][1], r[k][2], r[k][3]);
             }
+        };
+        uint32_t i = 0;
+        bool ok = true;
+        if ((int)blockIdx.x < chunks) load_chunk(blockIdx.x);
+        for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
+            const uint32_t sb = i & 1u;
+            if (i >= 2 && !(ok = tc_wait(smem_u32(&empty[sb]), ((i >> 1) - 1u) & 1u, &abortFlag)))
+                break;
+            const uint32_t aAddr = base + sb * (kABytes + kBBytes);
+            store_chunk(aAddr, aAddr + kABytes);
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_arrive(smem_u32(&full[sb]));
+            if (c + (int)gridDim.x < chunks) load_chunk(c + gridDim.x);
         }
         if (!ok) abortFlag = 1u;
         // bias gradient: lanes with the same channel pair hold different pixels

@@ -52,22 +52,22 @@ __device__ __forceinline__ float prune_bound(float t) { return t + t * 0.0009765
 // Tests the children of a node (4 per quad, `quads` = 1 or 2) against the
 // ray, pushing hits nearest-last.  kWT: the watertight mode's robust slab
 // test.  With kKeepNearest the nearest hit child is not pushed but returned
-// in *next (ref kEmptyChild when no child is hit), for the caller to visit
-// straight away: one stack store and load fewer per node visit.
+// (ref kEmptyChild when no child is hit), for the caller to visit straight
+// away: one stack store and load fewer per node visit.  Without it the
+// return value is an empty entry.
 // kFastSlab: slab_entry_node instead of the reference's slab_entry (see
 // visit_node for when that is allowed).
 template <bool kCount, bool kWT, bool kKeepNearest, bool kFastSlab>
-__device__ __forceinline__ void visit_node_impl(const float4 *__restrict__ pool, uint32_t quads,
-    uint32_t ref, V3 o, V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
-    TraceCounters &cnt, StackEntry *next)
+__device__ __forceinline__ StackEntry visit_node_impl(const float4 *__restrict__ pool,
+    uint32_t quads, uint32_t ref, V3 o, V3 invd, float bound, StackEntry *stack, int &sp,
+    uint32_t *status, TraceCounters &cnt)
 {
     const float4 *p = pool + node_offset(ref, quads);
     // a node pushes at most 4 * quads entries: one room check per visit instead
     // of one per push (a walk out of room reports the overflow and skips the node)
     if (sp > kStackSize - 4 * (int)kMaxNodeQuads) {
         atomicOr(status, kStatusStackOverflow);
-        if constexpr (kKeepNearest) next->ref = kEmptyChild;
-        return;
+        return StackEntry{kEmptyChild, 0.0f};
     }
     uint32_t nearRef = kEmptyChild;
     float nearT = kInf;
@@ -106,10 +106,13 @@ __device__ __forceinline__ void visit_node_impl(const float4 *__restrict__ pool,
         }
     }
     if constexpr (kKeepNearest) {
-        *next = StackEntry{nearRef, nearT};
-    } else if (nearRef != kEmptyChild) {
-        stack[sp] = StackEntry{nearRef, nearT};
-        sp++;
+        return StackEntry{nearRef, nearT};
+    } else {
+        if (nearRef != kEmptyChild) {
+            stack[sp] = StackEntry{nearRef, nearT};
+            sp++;
+        }
+        return StackEntry{kEmptyChild, 0.0f};
     }
 }
 
@@ -120,16 +123,15 @@ __device__ __forceinline__ void visit_node_impl(const float4 *__restrict__ pool,
 // has its own NaN rules) keeps the reference's form, whose decisions below a
 // node are a superset of its leaves'.
 template <bool kCount, bool kWT = false, bool kKeepNearest = false>
-__device__ __forceinline__ void visit_node(const float4 *__restrict__ pool, uint32_t quads,
+__device__ __forceinline__ StackEntry visit_node(const float4 *__restrict__ pool, uint32_t quads,
     uint32_t ref, V3 o, V3 invd, float bound, StackEntry *stack, int &sp, uint32_t *status,
-    TraceCounters &cnt, StackEntry *next = nullptr)
+    TraceCounters &cnt)
 {
     if (kWT || !(isfinite(invd.x) && isfinite(invd.y) && isfinite(invd.z)))
-        visit_node_impl<kCount, kWT, kKeepNearest, false>(pool, quads, ref, o, invd, bound, stack,
-            sp, status, cnt, next);
-    else
-        visit_node_impl<kCount, kWT, kKeepNearest, true>(pool, quads, ref, o, invd, bound, stack,
-            sp, status, cnt, next);
+        return visit_node_impl<kCount, kWT, kKeepNearest, false>(pool, quads, ref, o, invd, bound,
+            stack, sp, status, cnt);
+    return visit_node_impl<kCount, kWT, kKeepNearest, true>(pool, quads, ref, o, invd, bound,
+        stack, sp, status, cnt);
 }
 
 // Triangle candidates of one mesh leaf, in object space.  kWT: the
@@ -211,8 +213,8 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
         if (te > prune_bound(best.t)) continue;
         if (!child_is_leaf(ref)) {
             if (kCount) cnt.topNodes++;
-            visit_node<kCount, kWT, true>(nodes, quads, ref, o, invd, prune_bound(best.t), stack,
-                sp, status, cnt, &next);
+            next = visit_node<kCount, kWT, true>(nodes, quads, ref, o, invd, prune_bound(best.t),
+                stack, sp, status, cnt);
             continue;
         }
         // an object whose world box passed: descend into its mesh
@@ -246,8 +248,8 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
             if (t2 > bound) continue;
             if (!child_is_leaf(r2)) {
                 if (kCount) cnt.meshNodes++;
-                visit_node<kCount, kWT, true>(nodes, quads, r2, lo, linvd, bound, stack, sp, status,
-                    cnt, &lnext);
+                lnext = visit_node<kCount, kWT, true>(nodes, quads, r2, lo, linvd, bound, stack, sp,
+                    status, cnt);
             } else {
                 visit_leaf<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
             }

@@ -406,9 +406,9 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
                     cnt.topNodes++;
                 else
                     cnt.meshNodes++;
-                visit_node<true, kWT, true>(src.scene(pathId).nodes, src.scene(pathId).nodeQuads,
-                    ref, mode == 1 ? o : lo, mode == 1 ? invd : linvd, bound, stack, sp, status,
-                    cnt, &next);
+                next = visit_node<true, kWT, true>(src.scene(pathId).nodes,
+                    src.scene(pathId).nodeQuads, ref, mode == 1 ? o : lo,
+                    mode == 1 ? invd : linvd, bound, stack, sp, status, cnt);
             } else if (mode == 1) {
                 // an object whose world box passed: enter its mesh
                 inst = leaf_first(ref);

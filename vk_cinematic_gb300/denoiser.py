@@ -78,7 +78,7 @@ class KPCNN:
     with deterministic per-CTA partial sums - or "simt" (FP32 FMA with
     atomics) for the weight gradient."""
 
-    def __init__(self, seed: int = 0, conv: str = "tcgen05", wgrad: str = "mma"):
+    def __init__(self, seed: int = 0, conv: str = "tcgen05", wgrad: str = "tcgen05"):
         import torch
 
         self.L = gbsp.load()
@@ -232,10 +232,11 @@ class KPCNN:
         return out
 
     def serve(self, sr, x0, y0, w, h, spp, seed, bound=0.01, tile=16, max_spp=1024, margin=1.25,
-              timing=None):
+              timing=None, check_spp=None):
         """The served output of a w x h window of `sr`'s frame: `spp`-sample plain
-        render + G-buffers -> denoised; an independent `spp`-sample plain render
-        checks every tile x tile block (check_tiles); blocks that fail are served
+        render + G-buffers -> denoised; an independent `check_spp`-sample plain
+        render (default `spp`) checks every tile x tile block (check_tiles); blocks
+        that fail are served
         from all their plain samples, topped up by a fallback render of the
         block (one tile-list pass per power-of-two sample count) to the spp the
         check estimated for `bound`.  Returns (image, stats): stats counts the
@@ -243,6 +244,7 @@ class KPCNN:
         denoised image under "denoised"."""
         import torch
 
+        cspp = spp if check_spp is None else int(check_spp)
         ev = [] if timing is not None else None
 
         def mark():
@@ -254,12 +256,12 @@ class KPCNN:
         mark()
         rad, aov = sr.render(x0, y0, w, h, spp, seed, aov=True)
         mark()
-        chk, _ = sr.render(x0, y0, w, h, spp, (seed + 0x1B873593) & 0xFFFFFFFF)
+        chk, _ = sr.render(x0, y0, w, h, cspp, (seed + 0x1B873593) & 0xFFFFFFFF)
         mark()
         den = self.denoise(rad.unsqueeze(0).contiguous(), aov.unsqueeze(0).contiguous())
         mark()
         err, flags, need = self.check_tiles(den, rad.unsqueeze(0).contiguous(), spp,
-                                            chk.unsqueeze(0).contiguous(), spp, bound, tile,
+                                            chk.unsqueeze(0).contiguous(), cspp, bound, tile,
                                             max_spp, margin)
         f = flags.cpu().numpy()
         nd = need.cpu().numpy()
@@ -267,7 +269,7 @@ class KPCNN:
         groups = {}
         spp_f = np.zeros(len(f), np.int32)
         for t in np.nonzero(f)[0]:
-            extra = int(nd[t]) - 2 * spp
+            extra = int(nd[t]) - spp - cspp
             if extra <= 0:
                 continue
             k = 1 << (extra - 1).bit_length()
@@ -286,7 +288,7 @@ class KPCNN:
             sr.rend.copy_region(x0, y0, w, h, fb.data_ptr())
         mark()
         out = self.merge_tiles(den, rad.unsqueeze(0).contiguous(), spp,
-                               chk.unsqueeze(0).contiguous(), spp, fb,
+                               chk.unsqueeze(0).contiguous(), cspp, fb,
                                torch.from_numpy(spp_f).cuda() if fb is not None else None, flags,
                                tile)
         mark()
