@@ -281,6 +281,13 @@ int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics);
  * those host pixels.  metrics NULL and no host pixels: asynchronous. */
 int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, uint32_t count,
     gbsp_metrics *metrics);
+/* The same with a sample count per tile (extension): tile i is rendered
+ * exactly as gbsp_path_trace_tile renders it with options->spp = spp[i]
+ * (bit-identical pixels; spp[i] = 0 skips the tile), all tiles in one device
+ * pass - e.g. a denoised frame's fallback tiles, each topped up to the
+ * sample count its check estimated. */
+int gbsp_path_trace_tile_list_spp(const gbsp_context *ctx, const gbsp_tile *tiles,
+    const uint32_t *spp, uint32_t count, gbsp_metrics *metrics);
 /* Tile render that allocates no memory.  No counterpart in the reference: it
  * is for callers that must not allocate device memory per call - e.g. a
  * render loop that runs under a fixed device-memory budget, or that cannot

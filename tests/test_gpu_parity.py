@@ -452,6 +452,50 @@ def test_tile_list_matches_tile_renders(rt):
     assert m.as_dict()["paths_traced"] == int(inside.sum()) * s.spp
 
 
+@pytest.mark.parametrize("wave_paths", [0, 700])
+def test_tile_list_spp_matches_tile_renders(rt, wave_paths):
+    """gbsp_path_trace_tile_list_spp renders tile i at spp[i] in one pass
+    exactly as gbsp_path_trace_tile renders that tile at that spp
+    (bit-identical pixels, the summed path count); a tile with spp 0 is
+    skipped.  wave_paths 700 cuts the pass into many waves whose boundaries
+    fall inside tiles (never inside a pixel's samples)."""
+    import torch
+
+    s = scenes.config3_scene(width=200, height=120, spp=3, n_spheres=32, level=2, seed=33)
+    scene, ms, rend = gbsp.upload_scene(rt, s)
+    tiles = [(0, 0, 16, 16), (48, 32, 64, 48), (184, 112, 200, 120), (120, 90, 140, 130),
+             (100, 7, 133, 19), (16, 0, 32, 16)]
+    spps = [1, 7, 64, 3, 33, 0]
+    ref = np.zeros((s.height, s.width, 4), np.float32)
+    inside = np.zeros((s.height, s.width), bool)
+    paths = 0
+    for t, k in zip(tiles, spps):
+        if k == 0:
+            continue
+        rend.options.spp = k
+        img, _, _ = rend.tile(t)
+        x0, y0, x1, y1 = t[0], t[1], min(t[2], s.width), min(t[3], s.height)
+        ref[y0:y1, x0:x1] = img[y0:y1, x0:x1]
+        inside[y0:y1, x0:x1] = True
+        paths += (x1 - x0) * (y1 - y0) * k
+    rend.options.spp = s.spp
+    rend.frame_device(metrics=False)
+    rt.synchronize()
+    frame = torch.empty((s.height, s.width, 4), dtype=torch.float32, device="cuda")
+    rend.copy_region(0, 0, s.width, s.height, frame.data_ptr())
+    rt.synchronize()
+    before = frame.cpu().numpy()
+    rend.options.wave_paths = wave_paths
+    m = rend.tile_list_spp_device(tiles, spps, metrics=True)
+    rend.options.wave_paths = 0
+    rend.copy_region(0, 0, s.width, s.height, frame.data_ptr())
+    rt.synchronize()
+    got = frame.cpu().numpy()
+    assert np.array_equal(got[inside].view(np.uint32), ref[inside].view(np.uint32))
+    assert np.array_equal(got[~inside].view(np.uint32), before[~inside].view(np.uint32))
+    assert m.as_dict()["paths_traced"] == paths
+
+
 def test_tonemap_matches_oracle(rt, port):
     """Display conversion (post_processing.frag.glsl:19-26 + ToColor) of a
     path-traced frame against the C restatement; powf differs in the last

@@ -920,8 +920,8 @@ int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile, gbsp_rng *rng,
     return check_stream_status(rt);
 }
 
-int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, uint32_t count,
-    gbsp_metrics *metrics)
+static int tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, const uint32_t *spp,
+    uint32_t count, gbsp_metrics *metrics)
 {
     if (count && !tiles) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tiles is NULL");
     gbsp_options opt;
@@ -937,18 +937,21 @@ int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, u
     cudaStream_t s = rt->stream;
     gbsp_image_plane *ip = ctx->camera->imagePlane;
     std::vector<uint4> rects;
+    std::vector<uint32_t> rectSpp;
     rects.reserve(count);
     for (uint32_t i = 0; i < count; i++) {
         uint32_t x0 = tiles[i].minX, y0 = tiles[i].minY;
         uint32_t x1 = std::min(tiles[i].maxX, ip->width), y1 = std::min(tiles[i].maxY, ip->height);
-        if (x1 > x0 && y1 > y0) rects.push_back(make_uint4(x0, y0, x1 - x0, y1 - y0));
+        if (x1 <= x0 || y1 <= y0 || (spp && spp[i] == 0)) continue;
+        rects.push_back(make_uint4(x0, y0, x1 - x0, y1 - y0));
+        if (spp) rectSpp.push_back(spp[i]);
     }
     if ((rc = ensure_frame(rt, ip->width, ip->height))) return rc;
     rt->begin_call(false);
     if (metrics && (rc = counters_begin(rt, (opt.flags & GBSP_FLAG_STAGE_TIMING) != 0))) return rc;
     if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
     if ((rc = render_tile_list(rt, ctx->scene->view(), mv, camera_params(ctx->camera), opt, rects,
-             rt->frame.ptr, ip->width)))
+             rt->frame.ptr, ip->width, spp ? &rectSpp : nullptr)))
         return rc;
     if (metrics) GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
     if (ip->pixels) {
@@ -964,6 +967,19 @@ int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, u
     if (metrics) cudaEventElapsedTime(&ms, rt->ev[0], rt->ev[1]);
     if ((rc = counters_end(rt, metrics, ms))) return rc;
     return check_stream_status(rt);
+}
+
+int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, uint32_t count,
+    gbsp_metrics *metrics)
+{
+    return tile_list(ctx, tiles, nullptr, count, metrics);
+}
+
+int gbsp_path_trace_tile_list_spp(const gbsp_context *ctx, const gbsp_tile *tiles,
+    const uint32_t *spp, uint32_t count, gbsp_metrics *metrics)
+{
+    if (count && !spp) return set_error(GBSP_ERR_INVALID_ARGUMENT, "spp is NULL");
+    return tile_list(ctx, tiles, spp, count, metrics);
 }
 
 int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics)

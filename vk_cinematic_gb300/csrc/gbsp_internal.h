@@ -262,10 +262,11 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     float4 *dAov = nullptr);
 
 // Renders the listed rectangles (x0, y0, width, height), hash-per-sample
-// seeding, into dImage (imageWidth pixels per row) in one wave sequence.
+// seeding, into dImage (imageWidth pixels per row) in one wave sequence:
+// opt.spp samples per pixel, or (*tileSpp)[i] for tile i when tileSpp is given.
 int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, const std::vector<uint4> &tiles,
-    float4 *dImage, uint32_t imageWidth);
+    float4 *dImage, uint32_t imageWidth, const std::vector<uint32_t> *tileSpp = nullptr);
 
 // api.cu
 int material_view(gbsp_material_system *ms, MaterialView *out);

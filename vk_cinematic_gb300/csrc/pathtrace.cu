@@ -116,9 +116,20 @@ static int ensure_wave_buffers(gbsp_runtime *rt, uint32_t cap, uint32_t maxBounc
     return GBSP_OK;
 }
 
+// One wave of a render: a run of whole pixels (numbered row-major through the
+// region or tile list) and the paths of their samples.
+struct WavePlan {
+    uint64_t pixelBase, pathBase;
+    uint32_t pixels, paths;
+};
+
+static int uniform_waves(uint64_t pixels, uint32_t spp, uint64_t waveTarget,
+    std::vector<WavePlan> &waves);
+static int variable_waves(const std::vector<uint4> &tiles, const std::vector<uint32_t> &spp,
+    uint64_t waveTarget, std::vector<WavePlan> &waves);
 static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
-    const CameraParams &cam, const gbsp_options &opt, WaveParams wp, uint64_t regionPixels,
-    float4 *dImage, uint32_t imageWidth, float4 *dAov);
+    const CameraParams &cam, const gbsp_options &opt, WaveParams wp,
+    const std::vector<WavePlan> &waves, float4 *dImage, uint32_t imageWidth, float4 *dAov);
 
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
@@ -126,7 +137,6 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
 {
     cudaStream_t s = rt->stream;
     unsigned long long *counters = rt->dCounters;
-    unsigned int *ctl = reinterpret_cast<unsigned int *>(rt->dCounters + GBSP_METRIC_COUNT);
     if (x1 <= x0 || y1 <= y0) return GBSP_OK;
     uint32_t spp = opt.spp ? opt.spp : 1;
     uint32_t maxBounces = opt.max_bounces;
@@ -173,28 +183,52 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     wp.tiles = nullptr;
     wp.tileStart = nullptr;
     wp.tileCount = 0;
-    return render_waves(rt, sv, mv, cam, opt, wp, (uint64_t)(x1 - x0) * (y1 - y0), dImage,
-        imageWidth, dAov);
+    wp.tileSpp = nullptr;
+    wp.tilePath = nullptr;
+    std::vector<WavePlan> waves;
+    int rc = uniform_waves((uint64_t)(x1 - x0) * (y1 - y0), spp, opt.wave_paths, waves);
+    if (rc) return rc;
+    return render_waves(rt, sv, mv, cam, opt, wp, waves, dImage, imageWidth, dAov);
 }
 
 int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, const std::vector<uint4> &tiles,
-    float4 *dImage, uint32_t imageWidth)
+    float4 *dImage, uint32_t imageWidth, const std::vector<uint32_t> *tileSpp)
 {
     if (tiles.empty()) return GBSP_OK;
-    std::vector<uint64_t> start(tiles.size());
+    if (tileSpp && tileSpp->size() != tiles.size())
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "one spp per tile");
+    std::vector<uint64_t> start(tiles.size()), pathStart;
     uint64_t total = 0;
     for (size_t i = 0; i < tiles.size(); i++) {
         start[i] = total;
         total += (uint64_t)tiles[i].z * tiles[i].w;
     }
     if (total == 0) return GBSP_OK;
+    std::vector<WavePlan> waves;
+    int rc;
+    if (tileSpp) {
+        pathStart.resize(tiles.size());
+        uint64_t paths = 0;
+        for (size_t i = 0; i < tiles.size(); i++) {
+            if ((*tileSpp)[i] == 0) return set_error(GBSP_ERR_INVALID_ARGUMENT, "tile spp 0");
+            pathStart[i] = paths;
+            paths += (uint64_t)tiles[i].z * tiles[i].w * (*tileSpp)[i];
+        }
+        rc = variable_waves(tiles, *tileSpp, opt.wave_paths, waves);
+    } else {
+        rc = uniform_waves(total, opt.spp ? opt.spp : 1, opt.wave_paths, waves);
+    }
+    if (rc) return rc;
     cudaStream_t s = rt->stream;
     DeviceBuffer<uint4> dTiles;
-    DeviceBuffer<uint64_t> dStart;
-    int rc;
+    DeviceBuffer<uint64_t> dStart, dPath;
+    DeviceBuffer<uint32_t> dSpp;
     if ((rc = dTiles.upload(tiles.data(), tiles.size(), s)) ||
         (rc = dStart.upload(start.data(), start.size(), s)))
+        return rc;
+    if (tileSpp && ((rc = dSpp.upload(tileSpp->data(), tileSpp->size(), s)) ||
+                       (rc = dPath.upload(pathStart.data(), pathStart.size(), s))))
         return rc;
     WaveParams wp;
     wp.x0 = wp.y0 = 0;
@@ -202,27 +236,78 @@ int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &
     wp.tiles = dTiles.ptr;
     wp.tileStart = dStart.ptr;
     wp.tileCount = (uint32_t)tiles.size();
+    wp.tileSpp = tileSpp ? dSpp.ptr : nullptr;
+    wp.tilePath = tileSpp ? dPath.ptr : nullptr;
     // the lists are freed in stream order behind the kernels that read them
-    return render_waves(rt, sv, mv, cam, opt, wp, total, dImage, imageWidth, nullptr);
+    return render_waves(rt, sv, mv, cam, opt, wp, waves, dImage, imageWidth, nullptr);
+}
+
+// Waves of `spp` samples per pixel over `pixels` pixels: as many whole pixels
+// per wave as fit in waveTarget paths (default 2^22), at least one.
+static int uniform_waves(uint64_t pixels, uint32_t spp, uint64_t waveTarget,
+    std::vector<WavePlan> &waves)
+{
+    if (!waveTarget) waveTarget = 1u << 22;
+    const uint64_t perWave = std::min<uint64_t>(std::max<uint64_t>(1, waveTarget / spp), pixels);
+    if (perWave * spp > 0x7FFFFFFFull)
+        return set_error(GBSP_ERR_CAPACITY, "wave of %llu paths is too large",
+            (unsigned long long)(perWave * spp));
+    waves.clear();
+    for (uint64_t pb = 0; pb < pixels; pb += perWave) {
+        const uint32_t n = (uint32_t)std::min<uint64_t>(perWave, pixels - pb);
+        waves.push_back(WavePlan{pb, pb * spp, n, n * spp});
+    }
+    return GBSP_OK;
+}
+
+// Waves over a tile list whose tile i renders spp[i] samples per pixel: tiles
+// in order, each wave as many whole pixels as fit in waveTarget paths (at
+// least one pixel), so that a pixel's samples never straddle two waves.
+static int variable_waves(const std::vector<uint4> &tiles, const std::vector<uint32_t> &spp,
+    uint64_t waveTarget, std::vector<WavePlan> &waves)
+{
+    if (!waveTarget) waveTarget = 1u << 22;
+    uint32_t maxSpp = 0;
+    for (uint32_t v : spp) maxSpp = std::max(maxSpp, v);
+    const uint64_t cap = std::max<uint64_t>(waveTarget, maxSpp);
+    if (cap > 0x7FFFFFFFull)
+        return set_error(GBSP_ERR_CAPACITY, "wave of %llu paths is too large",
+            (unsigned long long)cap);
+    waves.clear();
+    WavePlan cur{0, 0, 0, 0};
+    uint64_t pixel = 0, path = 0;
+    for (size_t i = 0; i < tiles.size(); i++) {
+        uint64_t left = (uint64_t)tiles[i].z * tiles[i].w;
+        while (left > 0) {
+            uint64_t fit = (cap - cur.paths) / spp[i];
+            if (fit == 0) {
+                waves.push_back(cur);
+                cur = WavePlan{pixel, path, 0, 0};
+                continue;
+            }
+            const uint64_t k = std::min(fit, left);
+            cur.pixels += (uint32_t)k;
+            cur.paths += (uint32_t)(k * spp[i]);
+            pixel += k;
+            path += k * spp[i];
+            left -= k;
+        }
+    }
+    if (cur.pixels) waves.push_back(cur);
+    return GBSP_OK;
 }
 
 static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
-    const CameraParams &cam, const gbsp_options &opt, WaveParams wp, uint64_t regionPixels,
-    float4 *dImage, uint32_t imageWidth, float4 *dAov)
+    const CameraParams &cam, const gbsp_options &opt, WaveParams wp,
+    const std::vector<WavePlan> &waves, float4 *dImage, uint32_t imageWidth, float4 *dAov)
 {
     cudaStream_t s = rt->stream;
     unsigned long long *counters = rt->dCounters;
     unsigned int *ctl = reinterpret_cast<unsigned int *>(rt->dCounters + GBSP_METRIC_COUNT);
     const uint32_t spp = opt.spp ? opt.spp : 1;
     const uint32_t maxBounces = opt.max_bounces;
-    uint64_t waveTarget = opt.wave_paths ? opt.wave_paths : (1u << 22);
-    uint64_t pixelsPerWave = std::max<uint64_t>(1, waveTarget / spp);
-    pixelsPerWave = std::min<uint64_t>(pixelsPerWave, regionPixels);
-    uint64_t capWide = pixelsPerWave * spp;
-    if (capWide > 0x7FFFFFFFull)
-        return set_error(GBSP_ERR_CAPACITY, "wave of %llu paths is too large",
-            (unsigned long long)capWide);
-    uint32_t cap = (uint32_t)capWide;
+    uint32_t cap = 1;
+    for (const WavePlan &w : waves) cap = std::max(cap, w.paths);
     int rc = ensure_wave_buffers(rt, cap, std::max<uint32_t>(maxBounces, 1));
     if (rc) return rc;
     WaveBuffers wb;
@@ -254,10 +339,12 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
     const bool sortDirs = (opt.flags & GBSP_FLAG_SORT_DIRECTIONS) != 0 && maxBounces > 1;
     if (sortDirs && (rc = rt->sortHist.reserve(8 * (size_t)kSortBlocks, s))) return rc;
     bool timing = rt->stageTiming;
-    for (uint64_t pb = 0; pb < regionPixels; pb += pixelsPerWave) {
-        wp.pixelBase = pb;
-        wp.pixels = (uint32_t)std::min<uint64_t>(pixelsPerWave, regionPixels - pb);
-        uint32_t paths = wp.pixels * spp;
+    for (const WavePlan &w : waves) {
+        wp.pixelBase = w.pixelBase;
+        wp.pixels = w.pixels;
+        wp.pathBase = w.pathBase;
+        wp.paths = w.paths;
+        const uint32_t paths = w.paths;
         if (maxBounces == 0) {
             GBSP_CUDA_TRY(cudaMemsetAsync(wb.pathRad, 0, sizeof(float4) * (size_t)paths, s));
         } else {
@@ -480,6 +567,8 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     wp.tiles = nullptr;
     wp.tileStart = nullptr;
     wp.tileCount = 0;
+    wp.tileSpp = nullptr;
+    wp.tilePath = nullptr;
     wp.spp = spp;
     wp.maxBounces = opt.max_bounces;
     wp.seed = opt.seed;
@@ -497,6 +586,8 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
         uint64_t left = regionPixels - pb;
         wp.pixels = (uint32_t)(left < pixelsPerWave ? left : pixelsPerWave);
         uint32_t paths = wp.pixels * spp;
+        wp.pathBase = pb * spp;
+        wp.paths = paths;
         if (opt.max_bounces == 0) {
             GBSP_CUDA_TRY(cudaMemsetAsync(wb.pathRad, 0, sizeof(float4) * (size_t)paths, s));
         } else {

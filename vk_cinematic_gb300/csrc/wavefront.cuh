@@ -42,8 +42,16 @@ struct WaveParams {
     const uint4 *tiles;
     const uint64_t *tileStart;
     uint32_t tileCount;
+    // optional per-tile sample counts of a tile list: tile i renders
+    // tileSpp[i] samples per pixel, its paths numbered pixel-major from
+    // tilePath[i] (an exclusive prefix sum over pixels x spp); null: `spp`
+    // samples for every pixel
+    const uint32_t *tileSpp;
+    const uint64_t *tilePath;
     uint64_t pixelBase;   // first pixel (row-major in the region) of this wave
     uint32_t pixels;      // pixels in this wave
+    uint64_t pathBase;    // first path of this wave (with tileSpp)
+    uint32_t paths;       // paths in this wave
     uint32_t spp;
     uint32_t maxBounces;
     uint32_t seed;
@@ -206,6 +214,29 @@ static __global__ void __launch_bounds__(256) k_octant_scatter(const float4 *__r
 // Image position of pixel `pix` of a wave's pixel numbering: row-major in
 // the region, or in the tile list (binary search over the tiles' first
 // pixels).
+// The tile holding item `key` of a list numbered by the exclusive prefix sum
+// `start` (binary search: the last tile whose start is <= key).
+__device__ __forceinline__ uint32_t tile_of(const uint64_t *start, uint32_t count, uint64_t key)
+{
+    uint32_t lo = 0, hi = count - 1;
+    while (lo < hi) {
+        uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(start + mid) <= key)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void tile_pixel(const WaveParams &wp, uint32_t t, uint64_t local,
+    uint32_t &x, uint32_t &y)
+{
+    const uint4 r = __ldg(wp.tiles + t);
+    x = r.x + (uint32_t)(local % r.z);
+    y = r.y + (uint32_t)(local / r.z);
+}
+
 __device__ __forceinline__ void wave_pixel(const WaveParams &wp, uint64_t pix, uint32_t &x,
     uint32_t &y)
 {
@@ -214,29 +245,26 @@ __device__ __forceinline__ void wave_pixel(const WaveParams &wp, uint64_t pix, u
         y = wp.y0 + (uint32_t)(pix / wp.regionW);
         return;
     }
-    uint32_t lo = 0, hi = wp.tileCount - 1;
-    while (lo < hi) {
-        uint32_t mid = (lo + hi + 1) >> 1;
-        if (__ldg(wp.tileStart + mid) <= pix)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    const uint4 t = __ldg(wp.tiles + lo);
-    const uint64_t local = pix - __ldg(wp.tileStart + lo);
-    x = t.x + (uint32_t)(local % t.z);
-    y = t.y + (uint32_t)(local / t.z);
+    const uint32_t t = tile_of(wp.tileStart, wp.tileCount, pix);
+    tile_pixel(wp, t, pix - __ldg(wp.tileStart + t), x, y);
 }
 
 static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuffers wb)
 {
     uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t paths = wp.pixels * wp.spp;
-    if (p >= paths) return;
-    uint64_t pix = wp.pixelBase + p / wp.spp;
-    uint32_t s = p % wp.spp;
-    uint32_t x, y;
-    wave_pixel(wp, pix, x, y);
+    if (p >= wp.paths) return;
+    uint32_t x, y, s;
+    if (wp.tileSpp) {
+        const uint64_t gp = wp.pathBase + p;
+        const uint32_t t = tile_of(wp.tilePath, wp.tileCount, gp);
+        const uint32_t n = __ldg(wp.tileSpp + t);
+        const uint64_t local = gp - __ldg(wp.tilePath + t), lp = local / n;
+        s = (uint32_t)(local - lp * n);
+        tile_pixel(wp, t, lp, x, y);
+    } else {
+        s = p % wp.spp;
+        wave_pixel(wp, wp.pixelBase + p / wp.spp, x, y);
+    }
     uint32_t rng = sample_seed(wp.seed, x, y, s);
     V3 o, d;
     camera_ray(wp.cam, x, y, rng, o, d);
@@ -551,30 +579,41 @@ static __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBu
     uint32_t nans = 0;
     if (k < wp.pixels) {
         uint64_t pix = wp.pixelBase + k;
-        uint32_t x, y;
-        wave_pixel(wp, pix, x, y);
+        uint32_t x, y, n = wp.spp;
+        size_t first = (size_t)k * wp.spp;  // this pixel's first path in the wave
+        float inv = wp.invSpp;
+        if (wp.tileSpp) {
+            const uint32_t t = tile_of(wp.tileStart, wp.tileCount, pix);
+            const uint64_t lp = pix - __ldg(wp.tileStart + t);
+            n = __ldg(wp.tileSpp + t);
+            first = (size_t)(__ldg(wp.tilePath + t) + lp * n - wp.pathBase);
+            inv = 1.0f / (float)n;
+            tile_pixel(wp, t, lp, x, y);
+        } else {
+            wave_pixel(wp, pix, x, y);
+        }
         CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
-        for (uint32_t s = 0; s < wp.spp; s++) {
-            float4 r = wb.pathRad[(size_t)k * wp.spp + s];
+        for (uint32_t s = 0; s < n; s++) {
+            float4 r = wb.pathRad[first + s];
             if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
                 nans++;
                 if (wp.nanPolicy == GBSP_NAN_ZERO) continue;
             }
-            csum_add(acc[0], r.x * wp.invSpp);
-            csum_add(acc[1], r.y * wp.invSpp);
-            csum_add(acc[2], r.z * wp.invSpp);
+            csum_add(acc[0], r.x * inv);
+            csum_add(acc[1], r.y * inv);
+            csum_add(acc[2], r.z * inv);
         }
         image[(size_t)y * imageWidth + x] =
             make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
         if (wp.aovImage) {
             float4 a = make_float4(0, 0, 0, 0), b = make_float4(0, 0, 0, 0);
-            for (uint32_t s = 0; s < wp.spp; s++) {
-                float4 u = wb.pathAov[2 * ((size_t)k * wp.spp + s)];
-                float4 v = wb.pathAov[2 * ((size_t)k * wp.spp + s) + 1];
+            for (uint32_t s = 0; s < n; s++) {
+                float4 u = wb.pathAov[2 * (first + s)];
+                float4 v = wb.pathAov[2 * (first + s) + 1];
                 a = make_float4(a.x + u.x, a.y + u.y, a.z + u.z, a.w + u.w);
                 b = make_float4(b.x + v.x, b.y + v.y, b.z + v.z, b.w + v.w);
             }
-            float is = wp.invSpp;
+            float is = inv;
             size_t o = 2 * ((size_t)y * imageWidth + x);
             wp.aovImage[o] = make_float4(a.x * is, a.y * is, a.z * is, a.w * is);
             wp.aovImage[o + 1] = make_float4(b.x * is, b.y * is, b.z * is, b.w * is);

@@ -236,12 +236,12 @@ class KPCNN:
         """The served output of a w x h window of `sr`'s frame: `spp`-sample plain
         render + G-buffers -> denoised; an independent `check_spp`-sample plain
         render (default `spp`) checks every tile x tile block (check_tiles); blocks
-        that fail are served
-        from all their plain samples, topped up by a fallback render of the
-        block (one tile-list pass per power-of-two sample count) to the spp the
-        check estimated for `bound`.  Returns (image, stats): stats counts the
-        flagged blocks and the fallback samples rendered, and holds the unchecked
-        denoised image under "denoised"."""
+        that fail are served from all their plain samples, topped up by a
+        fallback render to the spp the check estimated for `bound` (every
+        flagged block in one tile-list pass, each at its own sample count).
+        Returns (image, stats): stats counts the flagged blocks and the fallback
+        samples rendered, and holds the unchecked denoised image under
+        "denoised"."""
         import torch
 
         cspp = spp if check_spp is None else int(check_spp)
@@ -266,24 +266,22 @@ class KPCNN:
         f = flags.cpu().numpy()
         nd = need.cpu().numpy()
         tx = (w + tile - 1) // tile
-        groups = {}
         spp_f = np.zeros(len(f), np.int32)
+        fb_tiles, fb_spp = [], []
         for t in np.nonzero(f)[0]:
             extra = int(nd[t]) - spp - cspp
             if extra <= 0:
                 continue
-            k = 1 << (extra - 1).bit_length()
-            spp_f[t] = k
+            spp_f[t] = extra
             bx, by = int(t % tx) * tile, int(t // tx) * tile
-            groups.setdefault(k, []).append((x0 + bx, y0 + by, x0 + min(bx + tile, w),
-                                             y0 + min(by + tile, h)))
+            fb_tiles.append((x0 + bx, y0 + by, x0 + min(bx + tile, w), y0 + min(by + tile, h)))
+            fb_spp.append(extra)
         mark()
         fb = None
         fb_samples = 0
-        if groups:
-            for k, tl in sorted(groups.items()):
-                sr.render_tiles(tl, k, seed + 7919 * k)
-                fb_samples += k * sum((t[2] - t[0]) * (t[3] - t[1]) for t in tl)
+        if fb_tiles:
+            sr.render_tiles_spp(fb_tiles, fb_spp, (seed + 7919) & 0xFFFFFFFF)
+            fb_samples = sum(k * (t[2] - t[0]) * (t[3] - t[1]) for t, k in zip(fb_tiles, fb_spp))
             fb = torch.empty((1, h, w, 4), dtype=torch.float32, device="cuda")
             sr.rend.copy_region(x0, y0, w, h, fb.data_ptr())
         mark()
@@ -299,7 +297,7 @@ class KPCNN:
             for k, n in enumerate(names):
                 timing[n] = timing.get(n, 0.0) + ev[k].elapsed_time(ev[k + 1])
         stats = {"tiles": int(len(f)), "flagged": int(f.sum()), "fallback_samples": fb_samples,
-                 "fallback_groups": sorted(groups), "denoised": den[0]}
+                 "fallback_tiles": len(fb_tiles), "denoised": den[0]}
         return out[0], stats
 
     # ---- training ------------------------------------------------------------------
@@ -398,6 +396,14 @@ class SceneRenderer:
         o.spp, o.seed = spp, seed
         o.flags = 0
         self.rend.tile_list_device(tiles)
+
+    def render_tiles_spp(self, tiles, spp, seed):
+        """Plain render of the listed (minX, minY, maxX, maxY) frame tiles, tile
+        i at spp[i], in one pass into the runtime's frame buffer."""
+        o = self.rend.options
+        o.seed = seed
+        o.flags = 0
+        self.rend.tile_list_spp_device(tiles, spp)
 
     def reference(self, x0, y0, w, h, spp_total, per_pass=1024, seed=1 << 20):
         """FP64-accumulated high-spp image: the mean of FP32 passes, summed in FP64."""

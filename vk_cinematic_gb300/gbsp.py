@@ -59,6 +59,7 @@ EXPORTS = [
     "gbsp_dn_tile_fallback", "gbsp_scene_set_node_width", "gbsp_scene_node_width",
     "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths", "gbsp_path_trace_tile_list",
     "gbsp_dn_tile_check", "gbsp_dn_tile_merge", "gbsp_dn_conv3x3_weight_grad_tcgen05",
+    "gbsp_path_trace_tile_list_spp",
 ]
 
 
@@ -388,6 +389,21 @@ class Renderer:
         m = Metrics() if metrics else None
         _check(self.L.gbsp_path_trace_tile_list(ctypes.byref(self.ctx), arr, _u32(len(tiles)),
                                                 ctypes.byref(m) if m is not None else None))
+        return m
+
+    def tile_list_spp_device(self, tiles, spp, metrics: bool = False):
+        """gbsp_path_trace_tile_list_spp: the listed (minX, minY, maxX, maxY)
+        tiles, tile i at spp[i] samples per pixel, in one pass into the
+        runtime's frame buffer (device); returns the metrics when asked."""
+        self.set_host_pixels(None)
+        arr = (Tile * max(1, len(tiles)))(*[Tile(*[int(v) for v in t]) for t in tiles])
+        sp = np.ascontiguousarray(spp, dtype=np.uint32).reshape(-1)
+        if len(sp) != len(tiles):
+            raise ValueError("one spp per tile")
+        m = Metrics() if metrics else None
+        _check(self.L.gbsp_path_trace_tile_list_spp(ctypes.byref(self.ctx), arr, _p(sp),
+                                                    _u32(len(tiles)),
+                                                    ctypes.byref(m) if m is not None else None))
         return m
 
     def frame_device_pointer(self) -> int:
