@@ -70,7 +70,7 @@ def parse_args():
     ap.add_argument("--dn-eval-crop", type=int, default=256)
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--dn-conv", choices=["tcgen05", "mma"], default="tcgen05")
-    ap.add_argument("--dn-wgrad", choices=["tcgen05", "mma", "simt"], default="tcgen05")
+    ap.add_argument("--dn-wgrad", choices=["tcgen05", "tma", "mma", "simt"], default="tcgen05")
     ap.add_argument("--dn-check-spp", default="same,1",
                     help="config5: sample counts of the served output's check render, "
                          "comma-separated; 'same' = the input render's spp")
@@ -81,6 +81,8 @@ def parse_args():
     ap.add_argument("--trace", choices=["hybrid", "warp", "lane"], default="hybrid",
                     help="closest-hit scheduling: per-warp for primary and per-lane for bounce "
                          "rays (library default), or one of the two for every bounce")
+    ap.add_argument("--wave-paths", type=int, default=0,
+                    help="paths per wave of the frame render (0: the library default)")
     ap.add_argument("--node-width", type=int, choices=[4, 8], default=8,
                     help="BVH node width of the rendered scene (8: library default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -400,6 +402,7 @@ def run_gpu(args):
     if args.sort_dirs:
         flags |= gbsp.FLAG_SORT_DIRECTIONS
     opt = gbsp.default_options(spp=s.spp, max_bounces=s.max_bounces, seed=s.seed, flags=flags)
+    opt.wave_paths = args.wave_paths
     scene, ms, rend = gbsp.upload_scene(rt, s, opt)
     scene.set_node_width(args.node_width)
     flush = torch.empty(FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -527,6 +530,7 @@ def run_gpu(args):
             "mrays_per_s": rays_all / (elapsed_ms / 1e3) / 1e6,
             "parallelism": f"replicas x{world}", "trace_scheduling": args.trace,
             "node_width": args.node_width,
+            "wave_paths": args.wave_paths or "library default",
             "sort_directions": bool(args.sort_dirs),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(M["kernel_launches"]), "clocks": clk,
@@ -909,7 +913,8 @@ def run_config5(args):
 
 def time_weight_grad(net, stream, reps=20):
     """Device time of one 48 -> 48 weight gradient on a 16 x 128 x 128 batch,
-    per implementation (tcgen05, mma.sync and the FP32 SIMT kernel), in ms."""
+    per implementation (tcgen05 with staging warps, tcgen05 fed by TMA,
+    mma.sync and the FP32 SIMT kernel), in ms."""
     import torch
     from vk_cinematic_gb300 import denoiser
 
@@ -920,6 +925,7 @@ def time_weight_grad(net, stream, reps=20):
     db = torch.zeros(48, device="cuda")
     out = {}
     for impl, fn in (("tcgen05", net.L.gbsp_dn_conv3x3_weight_grad_tcgen05),
+                     ("tma", net.L.gbsp_dn_conv3x3_weight_grad_tma),
                      ("mma", net.L.gbsp_dn_conv3x3_weight_grad_tc),
                      ("simt", net.L.gbsp_dn_conv3x3_weight_grad)):
         args = (denoiser._stream(), denoiser._ptr(x), denoiser._ptr(d), denoiser._u32(16),

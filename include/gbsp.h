@@ -561,6 +561,13 @@ int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint1
  * counterpart. */
 int gbsp_dn_conv3x3_weight_grad_tcgen05(void *stream, const uint16_t *in, const uint16_t *dOut,
     uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
+/* The same GEMM with both operands read by the tensor core straight from
+ * TMA-loaded boxes of the channel-group-planar tensors (MN-major operands:
+ * eight channels of one pixel per 16-byte row), the bias gradient from an
+ * extra row of ones.  Same results up to FP32 summation order; deterministic.
+ * Tensors 16-byte aligned.  No reference counterpart. */
+int gbsp_dn_conv3x3_weight_grad_tma(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
 /* out[p] = sum_k softmax(logits[p][0..24])_k * noisy[p + off5x5(k)] (edge-clamped);
  * logits have 32 channels per pixel. */
 int gbsp_dn_filter(void *stream, const float *logits, const float *noisy, uint32_t B, uint32_t H,

@@ -712,17 +712,19 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 
 // TMA map of a channel-group-planar BF16 activation tensor [B][H][cin/8][W][8]
 // (dimension order: 8 channels, pixel, channel group, row, image): one box =
-// 8 channels x kTcSpx pixels x every channel group of one row, i.e. cin/8
-// contiguous 2,080-byte runs, written to shared memory as [group][pixel][8
-// channels], zero outside the tensor.
-static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin)
+// 8 channels x boxPixels pixels x every channel group of one row, i.e. cin/8
+// contiguous runs of 16 boxPixels bytes, written to shared memory as
+// [group][pixel][8 channels], zero outside the tensor.  input_tensor_map: the
+// forward convolution's boxes of kTcSpx pixels.
+static int planar_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin,
+    int boxPixels)
 {
     PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
     if (!encode) return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)cin / 8, (cuuint64_t)H, (cuuint64_t)B};
     const cuuint64_t strides[4] = {16, (cuuint64_t)W * 16, (cuuint64_t)W * cin * 2,
         (cuuint64_t)H * W * cin * 2};
-    const cuuint32_t box[5] = {8, (cuuint32_t)kTcSpx, (cuuint32_t)cin / 8, 1, 1};
+    const cuuint32_t box[5] = {8, (cuuint32_t)boxPixels, (cuuint32_t)cin / 8, 1, 1};
     const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
     CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(in), dims,
         strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -730,6 +732,11 @@ static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int 
     if (r != CUDA_SUCCESS)
         return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     return GBSP_OK;
+}
+
+static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin)
+{
+    return planar_tensor_map(map, in, B, H, W, cin, kTcSpx);
 }
 
 template <int CIN, int COUT, int EPI>
@@ -1267,6 +1274,197 @@ __global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
                      :: "r"(tmem), "r"(TMEM_COLS));
 }
 
+// Weight gradient fed by TMA: the same GEMM as k_conv3x3_wgrad_tc5, D[(ty,
+// ci)][(tx, co)] = sum over a 64-pixel chunk q of x[y + ty - 1][q][ci] *
+// d[y][q - tx + 1][co], with both operands MN-major, which is the
+// channel-group-planar layout itself: a core matrix (8 pixels along K x 8
+// channels along M or N, 16-byte rows) is 128 contiguous bytes of one
+// channel group.  A chunk's operands are six TMA boxes of [group][64
+// pixels][8 channels]: the three input rows (A, one 8-row block per (ty,
+// group), 1 KB apart) and three copies of the output-gradient row shifted by
+// one pixel each (B, one block per (tx, group)), zero outside the tensor.
+// A block of ones after the input rows makes accumulator row 3 CIN the sum of
+// d over the chunk: the bias gradient (column block tx = 1).  Warp 0 lane 0
+// issues the loads into a ring of kWtStages stages, warp 1 lane 0 the MMAs;
+// every warp reads the accumulators at the end.
+constexpr int kWtPx = 64;
+constexpr int kWtStages = 4;
+constexpr int kWtThreads = 256;
+
+template <int CIN, int COUT>
+struct WtShape {
+    static constexpr int KGI = CIN / 8, KGO = COUT / 8;
+    static constexpr int MROWS = 3 * CIN, N = 3 * COUT;
+    static constexpr int MB = (MROWS + 8 + 127) / 128;          // M = 128 blocks, with the ones
+    static constexpr uint32_t kBlock = kWtPx * 16;              // 8 rows x 64 pixels: 1 KB
+    static constexpr uint32_t kBOff = (3 * KGI + 1) * kBlock;   // input rows, then the ones
+    static constexpr uint32_t kBBytes = 3 * KGO * kBlock;
+    static constexpr uint32_t kAExtent = MB * 16 * kBlock;      // what the M = 128 MMAs read
+    static constexpr uint32_t kStage =
+        ((kBOff + kBBytes > kAExtent ? kBOff + kBBytes : kAExtent) + 1023u) / 1024u * 1024u;
+    static constexpr uint32_t kTxBytes = (uint32_t)(3 * KGI + 3 * KGO) * kBlock;
+    static constexpr int TMEM_COLS = MB * N <= 256 ? 256 : 512;
+    static_assert(CIN % 8 == 0 && COUT % 16 == 0 && N <= 256 && MB * N <= 512, "tile shape");
+};
+
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(kWtThreads, 1) k_conv3x3_wgrad_tma(
+    const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmD, int B, int H,
+    int W, float *__restrict__ partial)
+{
+    using S = WtShape<CIN, COUT>;
+    constexpr int N = S::N, MB = S::MB, MROWS = S::MROWS;
+    extern __shared__ __align__(1024) unsigned char smemRaw[];
+    const uint32_t base = (smem_u32(smemRaw) + 1023u) & ~1023u;
+    __shared__ __align__(8) uint64_t full[kWtStages], empty[kWtStages], done;
+    __shared__ uint32_t tmemBase;
+    __shared__ volatile uint32_t abortFlag;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // the ones block of every stage (BF16 1.0 pairs), written once
+    for (int k = tid; k < kWtStages * (int)(S::kBlock / 4); k += kWtThreads) {
+        const uint32_t st = (uint32_t)k / (S::kBlock / 4), w = (uint32_t)k % (S::kBlock / 4);
+        asm volatile("st.shared.u32 [%0], %1;" :: "r"(base + st * S::kStage + (uint32_t)(3 * S::KGI) *
+            S::kBlock + 4u * w), "r"(0x3F803F80u) : "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(&tmemBase)), "r"(S::TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        for (int i = 0; i < kWtStages; i++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&empty[i])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&done)));
+        abortFlag = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmemBase;
+    const int segs = (W + kWtPx - 1) / kWtPx;
+    const int chunks = B * H * segs;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t i = 0;
+            bool ok = true;
+            for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
+                const uint32_t st = i % kWtStages, use = i / kWtStages;
+                if (use > 0 && !(ok = tc_wait(smem_u32(&empty[st]), (use - 1u) & 1u, &abortFlag)))
+                    break;
+                const int seg = c % segs, row = c / segs;
+                const int b = row / H, y = row % H, x0 = seg * kWtPx;
+                const uint32_t bar = smem_u32(&full[st]), sb = base + st * S::kStage;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                             :: "r"(bar), "r"(S::kTxBytes) : "memory");
+#pragma unroll
+                for (int t = 0; t < 3; t++) {
+                    asm volatile(
+                        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                        :: "r"(sb + (uint32_t)(t * S::KGI) * S::kBlock),
+                           "l"(reinterpret_cast<uint64_t>(&tmX)), "r"(0), "r"(x0), "r"(0),
+                           "r"(y + t - 1), "r"(b), "r"(bar)
+                        : "memory");
+                    asm volatile(
+                        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                        :: "r"(sb + S::kBOff + (uint32_t)(t * S::KGO) * S::kBlock),
+                           "l"(reinterpret_cast<uint64_t>(&tmD)), "r"(0), "r"(x0 + 1 - t), "r"(0),
+                           "r"(y), "r"(b), "r"(bar)
+                        : "memory");
+                }
+            }
+            // every box issued has landed before the CTA's shared memory is released
+            volatile uint32_t never = 0u;
+            for (uint32_t s0 = 0; s0 < (uint32_t)kWtStages && s0 < i; s0++) {
+                const uint32_t lastUse = (i - 1u - ((i - 1u - s0) % kWtStages)) / kWtStages;
+                if (!tc_wait(smem_u32(&full[s0]), lastUse & 1u, &never)) abortFlag = 1u;
+            }
+            if (!ok) abortFlag = 1u;
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            // A and B MN-major (instruction descriptor bits 15 and 16)
+            const uint32_t idesc = instr_desc_bf16<128, N>() | (1u << 15) | (1u << 16);
+            uint32_t i = 0;
+            bool ok = true;
+            for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
+                const uint32_t st = i % kWtStages, use = i / kWtStages;
+                if (!(ok = tc_wait(smem_u32(&full[st]), use & 1u, &abortFlag))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t aAddr = base + st * S::kStage, bAddr = aAddr + S::kBOff;
+#pragma unroll
+                for (int kk = 0; kk < kWtPx / 16; kk++) {
+                    // K-adjacent core matrices (8 pixels) 128 B apart, M- or N-adjacent
+                    // ones (8 channels) one block apart
+                    const uint64_t bDesc = smem_desc(bAddr + (uint32_t)kk * 256u, 128, S::kBlock);
+#pragma unroll
+                    for (int mb = 0; mb < MB; mb++) {
+                        const uint64_t aDesc = smem_desc(aAddr + (uint32_t)(mb * 16) * S::kBlock +
+                            (uint32_t)kk * 256u, 128, S::kBlock);
+                        tc_mma(tmem + (uint32_t)(mb * N), aDesc, bDesc, idesc,
+                            (i > 0 || kk > 0) ? 1u : 0u);
+                    }
+                }
+                tc_commit(smem_u32(&empty[st]));
+            }
+            // every MMA issued has finished before the accumulators are read
+            // or freed (waited for even after an abort)
+            tc_commit(smem_u32(&done));
+            volatile uint32_t never = 0u;
+            if (!tc_wait(smem_u32(&done), 0u, &never)) abortFlag = 1u;
+            if (!ok) abortFlag = 1u;
+        }
+        __syncwarp();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    // ---- epilogue: warp w < 4 MB reads TMEM lanes 32 (w % 4) .. + 31 of M block w / 4:
+    // accumulator row R = (ty, ci), or MROWS for the bias; column n = (tx, co)
+    float *out = partial + (size_t)blockIdx.x * (9 * COUT * CIN + COUT);
+    if (blockIdx.x >= chunks) {
+        // no chunk: nothing accumulated (the launch sizes the grid to avoid this)
+        for (int k = tid; k < 9 * COUT * CIN + COUT; k += kWtThreads) out[k] = 0.0f;
+    } else if (!abortFlag && warp < 4 * MB) {
+        const int mb = warp >> 2, quarter = warp & 3;
+        const int R = mb * 128 + quarter * 32 + lane;
+        const int ty = R / CIN, ci = R % CIN;
+#pragma unroll 1
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mb * N + c0), v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (R < MROWS) {
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const int n = c0 + k, tx = n / COUT, co = n % COUT;
+                    out[((size_t)(3 * ty + tx) * COUT + co) * CIN + ci] = __uint_as_float(v[k]);
+                }
+            } else if (R == MROWS) {
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const int n = c0 + k;
+                    if (n / COUT == 1) out[9 * COUT * CIN + n % COUT] = __uint_as_float(v[k]);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && abortFlag) atomicOr(&g_dnStatus, 1u);
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                     :: "r"(tmem), "r"(S::TMEM_COLS));
+}
+
 // Per-pixel 5x5 filter from softmax(logits[0..24]) applied to the noisy
 // radiance (clamped to the image edge).
 __global__ void k_filter(const float *__restrict__ logits, const float4 *__restrict__ noisy, int B,
@@ -1596,6 +1794,37 @@ static int launch_wgrad_tc5(cudaStream_t s, const __nv_bfloat16 *in, const __nv_
     return GBSP_OK;
 }
 
+template <int CIN, int COUT>
+static int launch_wgrad_tma(cudaStream_t s, const __nv_bfloat16 *in, const __nv_bfloat16 *d, int B,
+    int H, int W, float *dW, float *dBias)
+{
+    using S = WtShape<CIN, COUT>;
+    const int chunks = ((W + kWtPx - 1) / kWtPx) * B * H;
+    int grid = sm_count();
+    if (grid > chunks) grid = chunks;
+    const size_t smem = 1024 + (size_t)kWtStages * S::kStage;
+    auto kern = k_conv3x3_wgrad_tma<CIN, COUT>;
+    GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUtensorMap mapX, mapD;
+    int rc;
+    if ((rc = planar_tensor_map(&mapX, in, B, H, W, CIN, kWtPx)) ||
+        (rc = planar_tensor_map(&mapD, d, B, H, W, COUT, kWtPx)))
+        return rc;
+    const int perSlice = 9 * COUT * CIN + COUT;
+    float *partial = nullptr;
+    GBSP_CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(float) * (size_t)grid * perSlice, s));
+    kern<<<grid, kWtThreads, smem, s>>>(mapX, mapD, B, H, W, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_wgrad_reduce<<<(perSlice + 255) / 256, 256, 0, s>>>(partial, grid, perSlice,
+            9 * COUT * CIN, dW, dBias);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(partial, s);
+    if (e != cudaSuccess) return cuda_error(e, "TMA-fed weight gradient");
+    return GBSP_OK;
+}
+
 extern "C" {
 
 int gbsp_dn_features(void *stream, const float *radiance, const float *aov, uint64_t pixels,
@@ -1764,6 +1993,22 @@ int gbsp_dn_conv3x3_weight_grad_tcgen05(void *stream, const uint16_t *in, const 
     if (cin == 16 && cout == 48) return launch_wgrad_tc5<16, 48>(s, i16, d16, B, H, W, dW, dBias);
     if (cin == 48 && cout == 48) return launch_wgrad_tc5<48, 48>(s, i16, d16, B, H, W, dW, dBias);
     if (cin == 48 && cout == 32) return launch_wgrad_tc5<48, 32>(s, i16, d16, B, H, W, dW, dBias);
+    return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
+}
+
+int gbsp_dn_conv3x3_weight_grad_tma(void *stream, const uint16_t *in, const uint16_t *dOut,
+    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias)
+{
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!in || !dOut || !dW || !dBias || !B || !H || !W)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad weight-gradient args");
+    if (((uintptr_t)in | (uintptr_t)dOut) & 15u)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight-gradient tensors must be 16-byte aligned");
+    const __nv_bfloat16 *i16 = reinterpret_cast<const __nv_bfloat16 *>(in);
+    const __nv_bfloat16 *d16 = reinterpret_cast<const __nv_bfloat16 *>(dOut);
+    if (cin == 16 && cout == 48) return launch_wgrad_tma<16, 48>(s, i16, d16, B, H, W, dW, dBias);
+    if (cin == 48 && cout == 48) return launch_wgrad_tma<48, 48>(s, i16, d16, B, H, W, dW, dBias);
+    if (cin == 48 && cout == 32) return launch_wgrad_tma<48, 32>(s, i16, d16, B, H, W, dW, dBias);
     return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
 }
 

@@ -136,10 +136,11 @@ __device__ __forceinline__ StackEntry visit_node(const float4 *__restrict__ pool
 
 // Triangle candidates of one mesh leaf, in object space.  kWT: the
 // watertight test on every candidate (no box gate: a rounded box test could
-// reject an edge ray); otherwise the reference's gate and MT test.
-template <bool kCount, bool kWT = false>
-__device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
-    V3 linvd, float &bestT, float &bestU, float &bestV, int32_t &bestPrim, TraceCounters &cnt)
+// reject an edge ray); otherwise the reference's gate and MT test.  A closer
+// hit updates bestT and bestPrim and hands its barycentrics to keepUV(u, v).
+template <bool kCount, bool kWT, class KeepUV>
+__device__ __forceinline__ void visit_leaf_uv(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
+    V3 linvd, float &bestT, int32_t &bestPrim, KeepUV keepUV, TraceCounters &cnt)
 {
     uint32_t first = leaf_first(ref), count = leaf_count(ref);
     for (uint32_t k = 0; k < count; k++) {
@@ -168,11 +169,22 @@ __device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3
             take = __ldg(sv.triIds + j) < __ldg(sv.triIds + bestPrim);
         if (take) {
             bestT = h.t;
-            bestU = h.u;
-            bestV = h.v;
+            keepUV(h.u, h.v);
             bestPrim = (int32_t)j;
         }
     }
+}
+
+template <bool kCount, bool kWT = false>
+__device__ __forceinline__ void visit_leaf(const SceneView &sv, uint32_t ref, V3 lo, V3 ld,
+    V3 linvd, float &bestT, float &bestU, float &bestV, int32_t &bestPrim, TraceCounters &cnt)
+{
+    visit_leaf_uv<kCount, kWT>(sv, ref, lo, ld, linvd, bestT, bestPrim,
+        [&](float u, float v) {
+            bestU = u;
+            bestV = v;
+        },
+        cnt);
 }
 
 template <bool kCount, bool kWT = false>
@@ -186,8 +198,30 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
     best.inst = -1;
     if (sv.tlasRoot == kEmptyChild) return best;
     StackEntry stack[kStackSize];
+    // State used only when entering or leaving an object, kept in memory
+    // (local, L1-resident) on purpose so that the walks hold just the current
+    // level's ray, bounds and stack in registers.  Words: world origin 0-2,
+    // direction 3-5, inverse direction 6-8; best hit over objects u 9, v 10,
+    // triangle 11, object 12; the object's best triangle's u 13, v 14.
+    volatile uint32_t cold[15];
+    const auto put3 = [&](int w, V3 v) {
+        cold[w] = __float_as_uint(v.x);
+        cold[w + 1] = __float_as_uint(v.y);
+        cold[w + 2] = __float_as_uint(v.z);
+    };
+    const auto get3 = [&](int w) {
+        return v3(__uint_as_float(cold[w]), __uint_as_float(cold[w + 1]),
+            __uint_as_float(cold[w + 2]));
+    };
     int sp = 0;
     V3 invd = inverse(d);
+    put3(0, o);
+    put3(3, d);
+    put3(6, invd);
+    cold[9] = 0u;
+    cold[10] = 0u;
+    cold[11] = 0xFFFFFFFFu;
+    cold[12] = 0xFFFFFFFFu;
     // the entry to visit next (the nearest child of the last node visit),
     // kept out of the stack
     StackEntry next = StackEntry{sv.tlasRoot, 0.0f};
@@ -223,12 +257,12 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
         Affine inv, model;
 #pragma unroll
         for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
-        V3 lo = transform_point(inv, o);
+        const V3 lo = transform_point(inv, o);
         float len;
-        V3 ld = normalize(transform_vector(inv, d), &len);
-        V3 linvd = inverse(ld);
+        const V3 ld = normalize(transform_vector(inv, get3(3)), &len);
+        const V3 linvd = inverse(ld);
         if (kCount) cnt.meshTests++;
-        float lBestT = kInf, lU = 0.0f, lV = 0.0f;
+        float lBestT = kInf;
         int32_t lPrim = -1;
         float localBound = best.t * len;
         const int base = sp;
@@ -251,24 +285,36 @@ __device__ RayHit trace_closest(const SceneView &sv, V3 o, V3 d, uint32_t *statu
                 lnext = visit_node<kCount, kWT, true>(nodes, quads, r2, lo, linvd, bound, stack, sp,
                     status, cnt);
             } else {
-                visit_leaf<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lU, lV, lPrim, cnt);
+                visit_leaf_uv<kCount, kWT>(sv, r2, lo, ld, linvd, lBestT, lPrim,
+                    [&](float u, float v) {
+                        cold[13] = __float_as_uint(u);
+                        cold[14] = __float_as_uint(v);
+                    },
+                    cnt);
             }
         }
         sp = base;
+        // the world ray comes back from memory: it was not held through the mesh walk
+        o = get3(0);
+        invd = get3(6);
         if (lPrim < 0) continue;
 #pragma unroll
         for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
         V3 localHit = add(lo, mul(ld, lBestT));
         V3 worldHit = transform_point(model, localHit);
-        float tw = dot(sub(worldHit, o), d);
-        if (tw < best.t || (tw == best.t && (int32_t)inst < best.inst)) {
+        float tw = dot(sub(worldHit, o), get3(3));
+        if (tw < best.t || (tw == best.t && (int32_t)inst < (int32_t)cold[12])) {
             best.t = tw;
-            best.u = lU;
-            best.v = lV;
-            best.prim = lPrim;
-            best.inst = (int32_t)inst;
+            cold[9] = cold[13];
+            cold[10] = cold[14];
+            cold[11] = (uint32_t)lPrim;
+            cold[12] = inst;
         }
     }
+    best.u = __uint_as_float(cold[9]);
+    best.v = __uint_as_float(cold[10]);
+    best.prim = (int32_t)cold[11];
+    best.inst = (int32_t)cold[12];
     return best;
 }
 

@@ -343,20 +343,36 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
     TraceCounters cnt = {0, 0, 0, 0, 0};
     uint32_t done = 0, hits = 0;
     StackEntry stack[kStackSize];
+    // State a lane touches only when it fetches a ray, enters or leaves an
+    // object, or stores a hit, kept in memory (local, L1-resident) on purpose:
+    // the walk itself then holds just the current level's ray, bounds and
+    // stack in registers, which fit the 80 registers of 6 blocks per SM.
+    // Words: world origin 0-2, direction 3-5, inverse direction 6-8; best hit
+    // over objects u 9, v 10, triangle 11, object 12; queue slot 13; object
+    // being walked 14; its best triangle's u 15, v 16.
+    volatile uint32_t cold[17];
     // next: the entry to visit next (the nearest child of the last node
     // visit, or a root), kept out of the stack; ref kEmptyChild when none
     StackEntry next = StackEntry{kEmptyChild, 0.0f};
     int sp = 0, base = 0;
     int mode = 0;  // 0 needs a ray, 1 object level, 2 mesh level
-    uint32_t slot = 0, steps = 0, inst = 0;
-    V3 o = v3(0, 0, 0), d = v3(0, 0, 0), invd = v3(0, 0, 0);
-    float bestT = kInf, bestU = 0.0f, bestV = 0.0f;
-    int32_t bestPrim = -1, bestInst = -1;
-    V3 lo = v3(0, 0, 0), ld = v3(0, 0, 0), linvd = v3(0, 0, 0);
-    float len = 0.0f, lBestT = kInf, lU = 0.0f, lV = 0.0f;
+    uint32_t steps = 0;
+    // the ray of the level being walked: world (mode 1) or object space (mode 2)
+    V3 ro = v3(0, 0, 0), rinvd = v3(0, 0, 0), ld = v3(0, 0, 0);
+    float bestT = kInf;
+    float len = 0.0f, lBestT = kInf;
     int32_t lPrim = -1;
     uint32_t pathId = 0;
     bool drained = false;
+    const auto put3 = [&](int w, V3 v) {
+        cold[w] = __float_as_uint(v.x);
+        cold[w + 1] = __float_as_uint(v.y);
+        cold[w + 2] = __float_as_uint(v.z);
+    };
+    const auto get3 = [&](int w) {
+        return v3(__uint_as_float(cold[w]), __uint_as_float(cold[w + 1]),
+            __uint_as_float(cold[w + 2]));
+    };
     for (uint32_t it = 0; it < kMaxLaneIterations; it++) {
         if (mode == 0) {
             unsigned int m = __activemask();
@@ -369,16 +385,21 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
                 drained = true;
                 break;
             }
-            slot = idx;
             steps = 0;
             float4 o4 = rayO[idx], d4 = rayD[idx];
-            o = v3(o4.x, o4.y, o4.z);
-            d = v3(d4.x, d4.y, d4.z);
+            ro = v3(o4.x, o4.y, o4.z);
+            const V3 d = v3(d4.x, d4.y, d4.z);
             pathId = (uint32_t)__float_as_int(o4.w);
-            invd = inverse(d);
+            rinvd = inverse(d);
+            put3(0, ro);
+            put3(3, d);
+            put3(6, rinvd);
+            cold[9] = 0u;
+            cold[10] = 0u;
+            cold[11] = 0xFFFFFFFFu;
+            cold[12] = 0xFFFFFFFFu;
+            cold[13] = idx;
             bestT = kInf;
-            bestU = bestV = 0.0f;
-            bestPrim = bestInst = -1;
             sp = 0;
             next = StackEntry{src.scene(pathId).tlasRoot, 0.0f};
             mode = 1;
@@ -392,26 +413,31 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
         const bool levelDone = sp == (mode == 2 ? base : 0) && next.ref == kEmptyChild;
         if (mode == 2 && levelDone) {
             // leaving an object: its closest triangle goes back to world space
+            const V3 o = get3(0);
             if (lPrim >= 0) {
+                const uint32_t inst = cold[14];
                 const Instance &in = src.scene(pathId).instances[inst];
                 Affine model;
 #pragma unroll
                 for (int k = 0; k < 12; k++) model.r[k] = __ldg(&in.model.r[k]);
-                V3 worldHit = transform_point(model, add(lo, mul(ld, lBestT)));
-                float tw = dot(sub(worldHit, o), d);
-                if (tw < bestT || (tw == bestT && (int32_t)inst < bestInst)) {
+                V3 worldHit = transform_point(model, add(ro, mul(ld, lBestT)));
+                float tw = dot(sub(worldHit, o), get3(3));
+                if (tw < bestT || (tw == bestT && (int32_t)inst < (int32_t)cold[12])) {
                     bestT = tw;
-                    bestU = lU;
-                    bestV = lV;
-                    bestPrim = lPrim;
-                    bestInst = (int32_t)inst;
+                    cold[9] = cold[15];
+                    cold[10] = cold[16];
+                    cold[11] = (uint32_t)lPrim;
+                    cold[12] = inst;
                 }
             }
+            ro = o;
+            rinvd = get3(6);
             mode = 1;
         } else if (mode == 1 && levelDone) {
-            hitA[slot] = make_int4(__float_as_int(bestT), __float_as_int(bestU),
-                __float_as_int(bestV), bestPrim);
-            hitInst[slot] = bestInst;
+            const int32_t bestPrim = (int32_t)cold[11];
+            const uint32_t slot = cold[13];
+            hitA[slot] = make_int4(__float_as_int(bestT), (int)cold[9], (int)cold[10], bestPrim);
+            hitInst[slot] = (int)cold[12];
             done++;
             hits += (bestPrim >= 0 && bestT > 0.0f) ? 1u : 0u;
             mode = 0;
@@ -435,27 +461,31 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
                 else
                     cnt.meshNodes++;
                 next = visit_node<true, kWT, true>(src.scene(pathId).nodes,
-                    src.scene(pathId).nodeQuads, ref, mode == 1 ? o : lo,
-                    mode == 1 ? invd : linvd, bound, stack, sp, status, cnt);
+                    src.scene(pathId).nodeQuads, ref, ro, rinvd, bound, stack, sp, status, cnt);
             } else if (mode == 1) {
                 // an object whose world box passed: enter its mesh
-                inst = leaf_first(ref);
+                const uint32_t inst = leaf_first(ref);
+                cold[14] = inst;
                 const Instance &in = src.scene(pathId).instances[inst];
                 Affine inv;
 #pragma unroll
                 for (int k = 0; k < 12; k++) inv.r[k] = __ldg(&in.inv.r[k]);
-                lo = transform_point(inv, o);
+                const V3 d = get3(3);
+                ro = transform_point(inv, ro);
                 ld = normalize(transform_vector(inv, d), &len);
-                linvd = inverse(ld);
+                rinvd = inverse(ld);
                 cnt.meshTests++;
                 lBestT = kInf;
-                lU = lV = 0.0f;
                 lPrim = -1;
                 base = sp;
                 next = StackEntry{__ldg(&in.blasRoot), 0.0f};
                 mode = 2;
             } else {
-                visit_leaf<true, kWT>(src.scene(pathId), ref, lo, ld, linvd, lBestT, lU, lV, lPrim,
+                visit_leaf_uv<true, kWT>(src.scene(pathId), ref, ro, ld, rinvd, lBestT, lPrim,
+                    [&](float u, float v) {
+                        cold[15] = __float_as_uint(u);
+                        cold[16] = __float_as_uint(v);
+                    },
                     cnt);
             }
         }
