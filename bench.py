@@ -70,7 +70,7 @@ def parse_args():
     ap.add_argument("--dn-eval-crop", type=int, default=256)
     ap.add_argument("--dn-oracle-spp", type=int, default=16384)
     ap.add_argument("--dn-conv", choices=["tcgen05", "mma"], default="tcgen05")
-    ap.add_argument("--dn-wgrad", choices=["tcgen05", "tma", "mma", "simt"], default="tcgen05")
+    ap.add_argument("--dn-wgrad", choices=["tcgen05", "mma", "simt"], default="tcgen05")
     ap.add_argument("--dn-check-spp", default="same,1",
                     help="config5: sample counts of the served output's check render, "
                          "comma-separated; 'same' = the input render's spp")
@@ -913,8 +913,8 @@ def run_config5(args):
 
 def time_weight_grad(net, stream, reps=20):
     """Device time of one 48 -> 48 weight gradient on a 16 x 128 x 128 batch,
-    per implementation (tcgen05 with staging warps, tcgen05 fed by TMA,
-    mma.sync and the FP32 SIMT kernel), in ms."""
+    per implementation (tcgen05 fed by TMA, mma.sync and the FP32 SIMT
+    kernel), in ms."""
     import torch
     from vk_cinematic_gb300 import denoiser
 
@@ -925,7 +925,6 @@ def time_weight_grad(net, stream, reps=20):
     db = torch.zeros(48, device="cuda")
     out = {}
     for impl, fn in (("tcgen05", net.L.gbsp_dn_conv3x3_weight_grad_tcgen05),
-                     ("tma", net.L.gbsp_dn_conv3x3_weight_grad_tma),
                      ("mma", net.L.gbsp_dn_conv3x3_weight_grad_tc),
                      ("simt", net.L.gbsp_dn_conv3x3_weight_grad)):
         args = (denoiser._stream(), denoiser._ptr(x), denoiser._ptr(d), denoiser._u32(16),

@@ -150,7 +150,9 @@ typedef struct {
     uint32_t rng_mode;       /* GBSP_RNG_* */
     uint32_t nan_policy;     /* GBSP_NAN_* */
     float radiance_clamp;    /* RADIANCE_CLAMP (src/config.h:37); 0 disables */
-    uint32_t wave_paths;     /* paths in flight per wave (0 = library default) */
+    uint32_t wave_paths;     /* paths in flight per wave (0 = library default, 2^25:
+                              * about 270 bytes of device memory per path at 5 bounces,
+                              * never more paths than the render has) */
     uint32_t flags;          /* GBSP_FLAG_* */
 } gbsp_options;
 
@@ -350,7 +352,7 @@ typedef struct {
     uint32_t useGraph;     /* 1 = replay a captured CUDA graph */
     uint32_t kernel;       /* GBSP_BATCH_WAVEFRONT, GBSP_BATCH_PATH_STATE or
                               GBSP_BATCH_THREAD_PER_PIXEL */
-    uint32_t wavePaths;    /* wavefront: paths per wave (0 = 2^22) */
+    uint32_t wavePaths;    /* wavefront: paths per wave (0 = 2^25) */
 } gbsp_batch_config;
 
 /* gbsp_batch_config.kernel: one thread traces a whole pixel (all samples,
@@ -374,7 +376,7 @@ int gbsp_batch_get_config(const gbsp_batch *batch, gbsp_batch_config *config);
  * timed alone at both widths (spp capped at 8) and the faster is kept; then
  * times every candidate configuration (36: thread-per-pixel block x chunk x
  * blocks per SM, path-state block x blocks per SM, wavefront blocks per SM x
- * wave size 2^22..2^24) over `trials` launches each and keeps the fastest;
+ * wave size 2^22..2^25) over `trials` launches each and keeps the fastest;
  * *best receives it.  Items start at their scene's gbsp_scene_set_node_width. */
 int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *best);
 /* Node width per item (`widths` has one entry per item: 4 or 8), as chosen by
@@ -556,17 +558,13 @@ int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint1
 /* The same weight and bias gradients on the 5th-generation tensor cores
  * (tcgen05.mma, FP32 accumulators in tensor memory): all nine taps of a
  * 64-pixel input-row chunk as one GEMM, M = (tap row, input channel), N =
- * (tap column, output channel), K = pixels; per-CTA partial sums added in a
+ * (tap column, output channel), K = pixels, with both operands read by the
+ * tensor core straight from TMA-loaded boxes of the channel-group-planar
+ * tensors (MN-major: eight channels of one pixel per 16-byte row) and the
+ * bias gradient from an extra row of ones; per-CTA partial sums added in a
  * fixed order (deterministic).  Tensors 16-byte aligned.  No reference
  * counterpart. */
 int gbsp_dn_conv3x3_weight_grad_tcgen05(void *stream, const uint16_t *in, const uint16_t *dOut,
-    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
-/* The same GEMM with both operands read by the tensor core straight from
- * TMA-loaded boxes of the channel-group-planar tensors (MN-major operands:
- * eight channels of one pixel per 16-byte row), the bias gradient from an
- * extra row of ones.  Same results up to FP32 summation order; deterministic.
- * Tensors 16-byte aligned.  No reference counterpart. */
-int gbsp_dn_conv3x3_weight_grad_tma(void *stream, const uint16_t *in, const uint16_t *dOut,
     uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias);
 /* out[p] = sum_k softmax(logits[p][0..24])_k * noisy[p + off5x5(k)] (edge-clamped);
  * logits have 32 channels per pixel. */

@@ -586,7 +586,7 @@ static int tune_node_widths(gbsp_batch *b, uint32_t trials)
 static int plan_waves(gbsp_batch *b)
 {
     const std::vector<BatchItemDev> &dev = b->hostItems;
-    uint64_t want = b->cfg.wavePaths ? b->cfg.wavePaths : (1ull << 22);
+    uint64_t want = b->cfg.wavePaths ? b->cfg.wavePaths : kDefaultWavePaths;
     uint64_t cap = std::min<uint64_t>(want, std::max<uint64_t>(b->totalPaths, 1));
     uint32_t maxSpp = 1, maxB = 1;
     for (const BatchItemDev &d : dev) {
@@ -934,7 +934,7 @@ int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *b
                 cands.push_back({bl, ch, ps, keep.useGraph, GBSP_BATCH_THREAD_PER_PIXEL, keep.wavePaths});
         for (uint32_t bl : {64u, 128u})
             cands.push_back({bl, 1, ps, keep.useGraph, GBSP_BATCH_PATH_STATE, keep.wavePaths});
-        for (uint32_t wave : {1u << 22, 1u << 23, 1u << 24})
+        for (uint32_t wave : {1u << 22, 1u << 23, 1u << 24, 1u << 25})
             cands.push_back({128, 1, ps, keep.useGraph, GBSP_BATCH_WAVEFRONT, wave});
     }
     gbsp_batch_config bestCfg = keep;

@@ -734,6 +734,32 @@ static int planar_tensor_map(CUtensorMap *map, const void *in, int B, int H, int
     return GBSP_OK;
 }
 
+// The same tensor seen as 32-bit words [B][H][cin/8][W * 4] (dimension order:
+// word, channel group, row, image): one box = boxPixels * 4 words (boxPixels
+// <= 64) of every channel group of one row, landing as the same
+// [group][pixel][8 channels] bytes in one 16 boxPixels-byte run per group.
+// x coordinates are pixel * 4 (16-byte aligned, negative allowed).
+static int planar_words_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin,
+    int boxPixels)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
+    if (!encode) return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    if (boxPixels < 1 || boxPixels > 64)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "box of %d pixels", boxPixels);
+    const cuuint64_t dims[4] = {(cuuint64_t)W * 4, (cuuint64_t)cin / 8, (cuuint64_t)H,
+        (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)W * 16, (cuuint64_t)W * cin * 2,
+        (cuuint64_t)H * W * cin * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)boxPixels * 4, (cuuint32_t)cin / 8, 1, 1};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, const_cast<void *>(in), dims,
+        strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(GBSP_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return GBSP_OK;
+}
+
 static int input_tensor_map(CUtensorMap *map, const void *in, int B, int H, int W, int cin)
 {
     return planar_tensor_map(map, in, B, H, W, cin, kTcSpx);
@@ -995,298 +1021,38 @@ __global__ void k_wgrad_reduce(const float *__restrict__ partial, int slices, in
 }
 
 // ---------------------------------------------------------------------------
-// Weight gradient on the 5th-generation tensor cores (tcgen05).
+// Weight gradient on the 5th-generation tensor cores (tcgen05), fed by TMA.
 //
 // dW[ty 3 + tx][co][ci] = sum_p d[y][p][co] x[y + ty - 1][p + tx - 1][ci] over
 // every output pixel (b, y, p).  Substituting the input pixel q = p + tx - 1,
 // one GEMM per input-row chunk gives all nine taps at once:
 //   D[(ty, ci)][(tx, co)] = sum_q x[y + ty - 1][q][ci] d[y][q - tx + 1][co],
 // M = 3 CIN rows (two M = 128 MMAs when CIN = 48, one when CIN = 16), N = 3
-// COUT, K = 64 input pixels q of a chunk (4 MMAs of K = 16 per M block).  A
-// = the three input rows around output row y, staged once; B = output-row
-// gradient d, staged three times shifted by tx (zero outside the image).
-// Both operands are K-major in the canonical no-swizzle layout: core matrix
-// (8 channels x 8 pixels, one 16-byte row per channel) number rb 8 + kb for
-// channel block rb and pixel block kb, so the leading (K) byte offset is 128
-// and the stride (M / N) byte offset 1,024.  A warp stages four core matrices
-// per step: each lane loads one 32-bit channel pair of one pixel (a warp
-// load is four 128-byte runs of the channel-group-planar tensors) and one
-// stmatrix.trans writes the four 8 x 8 blocks transposed.
+// COUT, K = 64 input pixels q of a chunk (4 MMAs of K = 16 per M block).
 //
-// One persistent CTA per SM walks its chunks (b, y, 64-pixel segment) with
-// two staging buffers: warps 1-8 fill buffer i % 2 (waiting on its `empty`
-// barrier, committed by the MMAs that read it), fence the writes to the
-// async proxy and arrive on `full`; lane 0 of warp 0 waits on `full` and
-// issues the MMAs into FP32 accumulators in tensor memory that persist over
-// all of the CTA's chunks.  At the end warps 0-7 read the accumulators and
-// write the CTA's partial sums (and its bias-gradient sums, accumulated from
-// the unshifted staging of d) to its slice of the scratch buffer;
-// k_wgrad_reduce adds the slices in a fixed order (deterministic).  Every
-// wait is bounded and raises g_dnStatus on timeout.
+// Both operands are MN-major, which is the channel-group-planar layout
+// itself: a core matrix (8 pixels along K x 8 channels along M or N, one
+// 16-byte row per pixel) is 128 contiguous bytes of one channel group, so the
+// leading (K) byte offset is 128 and the stride (M / N) byte offset is one
+// 8-channel block.  A chunk's operands are six TMA boxes of [group][64
+// pixels][8 channels] (the tensor seen as 32-bit words, so that a box is one
+// 1 KB run per channel group): the three input rows (A, one 1 KB block per
+// (ty, group)) and three copies of the output-gradient row shifted by one pixel
+// each (B, one block per (tx, group)), zero outside the tensor; nothing is
+// transposed in registers.  A block of ones after the input rows makes
+// accumulator row 3 CIN the sum of d over the chunk: with column block
+// tx = 1, the bias gradient.
+//
+// One persistent CTA per SM walks its chunks (b, y, 64-pixel segment) through
+// a ring of kWtStages stages: lane 0 of warp 0 waits for a free stage (its
+// `empty` barrier, committed by the MMAs that read it) and issues the six
+// loads against the stage's `full` transaction count; lane 0 of warp 1 waits
+// on `full` and issues the MMAs into FP32 accumulators in tensor memory that
+// persist over all of the CTA's chunks.  At the end the warps read the
+// accumulators and write the CTA's partial sums to its slice of a scratch
+// buffer; k_wgrad_reduce adds the slices in a fixed order (deterministic).
+// Every wait is bounded and raises g_dnStatus on timeout.
 // ---------------------------------------------------------------------------
-constexpr int kWg5Px = 64;         // input pixels per chunk (K per chunk)
-constexpr int kWg5Threads = 288;   // warp 0: MMA issue; warps 1-8: staging
-constexpr int kWg5Stagers = 256;
-constexpr uint32_t kWg5MinSmem = 120 * 1024;  // one CTA per SM: it holds 512 TMEM columns
-
-// Four 8 x 8 BF16 blocks from registers to shared memory, transposed: lane
-// 8 m + r gives the address of row r of block m; the lane's register m holds
-// (row lane / 4, columns 2 (lane % 4), + 1) of block m before the transpose.
-__device__ __forceinline__ void stmatrix_x4_trans(uint32_t addr, uint32_t r0, uint32_t r1,
-    uint32_t r2, uint32_t r3)
-{
-    asm volatile("stmatrix.sync.aligned.m8n8.x4.trans.shared.b16 [%0], {%1, %2, %3, %4};"
-                 :: "r"(addr), "r"(r0), "r"(r1), "r"(r2), "r"(r3) : "memory");
-}
-
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(kWg5Threads, 1) k_conv3x3_wgrad_tc5(
-    const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ d, int B, int H, int W,
-    float *__restrict__ partial)
-{
-    constexpr int KGI = CIN / 8, KGO = COUT / 8;
-    constexpr int MROWS = 3 * CIN, N = 3 * COUT;
-    constexpr int MB = (MROWS + 127) / 128;              // M = 128 blocks
-    constexpr int KB = kWg5Px / 8;                       // pixel blocks per chunk
-    constexpr uint32_t kABytes = (uint32_t)MB * 128 * kWg5Px * 2;
-    constexpr uint32_t kBBytes = (uint32_t)N * kWg5Px * 2;
-    constexpr int TMEM_COLS = MB * N <= 256 ? 256 : 512;
-    static_assert(CIN % 8 == 0 && COUT % 16 == 0 && N <= 256 && MB * N <= 512, "tile shape");
-    static_assert(kWg5Px % 16 == 0, "chunk is whole K = 16 steps");
-    extern __shared__ __align__(1024) unsigned char smemRaw[];
-    const uint32_t base = (smem_u32(smemRaw) + 1023u) & ~1023u;
-    // buffer s: A at base + s (kABytes + kBBytes), B right after it
-    __shared__ __align__(8) uint64_t full[2], empty[2], done;
-    __shared__ uint32_t tmemBase;
-    __shared__ volatile uint32_t abortFlag;
-    __shared__ float sBias[8][COUT];
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     :: "r"(smem_u32(&tmemBase)), "r"(TMEM_COLS));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-    }
-    if (tid == 0) {
-        for (int i = 0; i < 2; i++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(&full[i])),
-                         "r"(kWg5Stagers));
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&empty[i])));
-        }
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&done)));
-        abortFlag = 0u;
-        asm volatile("fence.mbarrier_init.release.cluster;");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    const uint32_t tmem = tmemBase;
-    const int segs = (W + kWg5Px - 1) / kWg5Px;
-    const int chunks = B * H * segs;
-
-    if (warp == 0) {
-        if (lane == 0) {
-            const uint32_t idesc = instr_desc_bf16<128, N>();
-            uint32_t i = 0;
-            bool ok = true;
-            for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
-                const uint32_t sb = i & 1u;
-                if (!(ok = tc_wait(smem_u32(&full[sb]), (i >> 1) & 1u, &abortFlag))) break;
-                asm volatile("tcgen05.fence::after_thread_sync;");
-                const uint32_t aAddr = base + sb * (kABytes + kBBytes);
-                const uint32_t bAddr = aAddr + kABytes;
-#pragma unroll
-                for (int kk = 0; kk < kWg5Px / 16; kk++) {
-                    const uint64_t bDesc = smem_desc(bAddr + (uint32_t)kk * 256u, 128, KB * 128);
-#pragma unroll
-                    for (int mb = 0; mb < MB; mb++) {
-                        const uint64_t aDesc = smem_desc(aAddr + (uint32_t)(mb * 16 * KB * 128) +
-                            (uint32_t)kk * 256u, 128, KB * 128);
-                        tc_mma(tmem + (uint32_t)(mb * N), aDesc, bDesc, idesc,
-                            (i > 0 || kk > 0) ? 1u : 0u);
-                    }
-                }
-                tc_commit(smem_u32(&empty[sb]));
-            }
-            // every MMA issued has finished before the accumulators are read
-            // or freed (waited for even after an abort)
-            tc_commit(smem_u32(&done));
-            volatile uint32_t never = 0u;
-            if (!tc_wait(smem_u32(&done), 0u, &never)) abortFlag = 1u;
-            if (!ok) abortFlag = 1u;
-        }
-        __syncwarp();
-    } else {
-        // ---- staging: warp-steps of four core matrices (one channel block, four
-        // consecutive pixel blocks); lane = (pixel lane / 4, channel pair lane % 4).
-        // A warp loads all its steps of a chunk into registers at once (many loads
-        // in flight), and loads the next chunk right after storing this one, so
-        // the loads overlap the tensor core's work and the wait for a free buffer.
-        const int sw = warp - 1;
-        const int px = lane >> 2, pair = lane & 3;
-        float bsum[KGO][2];
-#pragma unroll
-        for (int g = 0; g < KGO; g++) bsum[g][0] = bsum[g][1] = 0.0f;
-        constexpr int kAStepsPerRow = KB / 4;             // warp-steps per channel block
-        constexpr int kASteps = 3 * KGI * kAStepsPerRow;
-        constexpr int kBSteps = 3 * KGO * kAStepsPerRow;
-        constexpr int kSteps = kASteps + kBSteps;
-        constexpr int kMaxSteps = (kSteps + 7) / 8;       // per stager warp
-        uint32_t r[kMaxSteps][4];
-        // the staged values of chunk c (step k of this warp is sw + 8 k)
-        auto load_chunk = [&](int c) {
-            const int seg = c % segs, row = c / segs;
-            const int b = row / H, y = row % H, x0 = seg * kWg5Px;
-#pragma unroll
-            for (int k = 0; k < kMaxSteps; k++) {
-                const int step = sw + 8 * k;
-                if (step >= kSteps) break;
-                if (step < kASteps) {
-                    // A: channel block rb = ty KGI + cg of input row y + ty - 1
-                    const int rb = step / kAStepsPerRow, kb0 = 4 * (step % kAStepsPerRow);
-                    const int ty = rb / KGI, cg = rb % KGI, gy = y + ty - 1;
-#pragma unroll
-                    for (int m = 0; m < 4; m++) {
-                        const int q = x0 + 8 * (kb0 + m) + px;
-                        uint32_t v = 0u;
-                        if (gy >= 0 && gy < H && q < W)
-                            v = __ldg(reinterpret_cast<const uint32_t *>(
-                                    in + cg_index((size_t)(b * H + gy), q, 8 * cg, W, CIN)) + pair);
-                        r[k][m] = v;
-                    }
-                } else {
-                    // B: channel block rb = tx KGO + cg of d, shifted: column q holds
-                    // pixel q - tx + 1
-                    const int st = step - kASteps;
-                    const int rb = st / kAStepsPerRow, kb0 = 4 * (st % kAStepsPerRow);
-                    const int tx = rb / KGO, cg = rb % KGO;
-#pragma unroll
-                    for (int m = 0; m < 4; m++) {
-                        const int p = x0 + 8 * (kb0 + m) + px - tx + 1;
-                        uint32_t v = 0u;
-                        if (p >= 0 && p < W)
-                            v = __ldg(reinterpret_cast<const uint32_t *>(
-                                    d + cg_index((size_t)row, p, 8 * cg, W, COUT)) + pair);
-                        r[k][m] = v;
-                    }
-                }
-            }
-        };
-        // stores the staged values into buffer addresses aAddr / bAddr; bias sums
-        // from the unshifted copy of d, which covers every output pixel once
-        auto store_chunk = [&](uint32_t aAddr, uint32_t bAddr) {
-#pragma unroll
-            for (int k = 0; k < kMaxSteps; k++) {
-                const int step = sw + 8 * k;
-                if (step >= kSteps) break;
-                int rb, kb0;
-                uint32_t dst;
-                if (step < kASteps) {
-                    rb = step / kAStepsPerRow;
-                    kb0 = 4 * (step % kAStepsPerRow);
-                    dst = aAddr;
-                } else {
-                    const int st = step - kASteps;
-                    rb = st / kAStepsPerRow;
-                    kb0 = 4 * (st % kAStepsPerRow);
-                    dst = bAddr;
-                    if (rb / KGO == 1) {
-                        const int cg = rb % KGO;
-#pragma unroll
-                        for (int m = 0; m < 4; m++) {
-                            __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&r[k][m]);
-#pragma unroll
-                            for (int g = 0; g < KGO; g++)
-                                if (g == cg) {
-                                    bsum[g][0] += __low2float(h);
-                                    bsum[g][1] += __high2float(h);
-                                }
-                        }
-                    }
-                }
-                // lane 8 m + j: row j (channel 8 rb + j) of core matrix (rb, kb0 + m)
-                const int m = lane >> 3, j = lane & 7;
-                stmatrix_x4_trans(dst + (uint32_t)((rb * KB + kb0 + m) * 128 + j * 16), r[k][0],
-                    r[k][1], r[k][2], r[k][3]);
-            }
-        };
-        uint32_t i = 0;
-        bool ok = true;
-        if ((int)blockIdx.x < chunks) load_chunk(blockIdx.x);
-        for (int c = blockIdx.x; c < chunks && ok; c += gridDim.x, i++) {
-            const uint32_t sb = i & 1u;
-            if (i >= 2 && !(ok = tc_wait(smem_u32(&empty[sb]), ((i >> 1) - 1u) & 1u, &abortFlag)))
-                break;
-            const uint32_t aAddr = base + sb * (kABytes + kBBytes);
-            store_chunk(aAddr, aAddr + kABytes);
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(smem_u32(&full[sb]));
-            if (c + (int)gridDim.x < chunks) load_chunk(c + gridDim.x);
-        }
-        if (!ok) abortFlag = 1u;
-        // bias gradient: lanes with the same channel pair hold different pixels
-#pragma unroll
-        for (int g = 0; g < KGO; g++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                float v = bsum[g][h];
-                for (int off = 4; off < 32; off <<= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, off);
-                if (lane < 4) sBias[sw][8 * g + 2 * lane + h] = v;
-            }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    // ---- epilogue: warp w < 4 MB reads TMEM lanes 32 (w % 4) .. + 31 of M block w / 4:
-    // accumulator row R = (ty, ci), column n = (tx, co)
-    float *out = partial + (size_t)blockIdx.x * (9 * COUT * CIN + COUT);
-    if (blockIdx.x >= chunks) {
-        // no chunk: nothing accumulated (the launch sizes the grid to avoid this)
-        for (int k = tid; k < 9 * COUT * CIN; k += kWg5Threads) out[k] = 0.0f;
-    } else if (!abortFlag && warp < 4 * MB) {
-        const int mb = warp >> 2, quarter = warp & 3;
-        const int R = mb * 128 + quarter * 32 + lane;
-        const int ty = R / CIN, ci = R % CIN;
-#pragma unroll 1
-        for (int c0 = 0; c0 < N; c0 += 16) {
-            uint32_t v[16];
-            tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(mb * N + c0), v);
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (R < MROWS) {
-#pragma unroll
-                for (int k = 0; k < 16; k++) {
-                    const int n = c0 + k, tx = n / COUT, co = n % COUT;
-                    out[((size_t)(3 * ty + tx) * COUT + co) * CIN + ci] = __uint_as_float(v[k]);
-                }
-            }
-        }
-    }
-    if (tid < COUT) {
-        float sum = 0.0f;
-        for (int w = 0; w < 8; w++) sum += sBias[w][tid];
-        out[9 * COUT * CIN + tid] = sum;
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (tid == 0 && abortFlag) atomicOr(&g_dnStatus, 1u);
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                     :: "r"(tmem), "r"(TMEM_COLS));
-}
-
-// Weight gradient fed by TMA: the same GEMM as k_conv3x3_wgrad_tc5, D[(ty,
-// ci)][(tx, co)] = sum over a 64-pixel chunk q of x[y + ty - 1][q][ci] *
-// d[y][q - tx + 1][co], with both operands MN-major, which is the
-// channel-group-planar layout itself: a core matrix (8 pixels along K x 8
-// channels along M or N, 16-byte rows) is 128 contiguous bytes of one
-// channel group.  A chunk's operands are six TMA boxes of [group][64
-// pixels][8 channels]: the three input rows (A, one 8-row block per (ty,
-// group), 1 KB apart) and three copies of the output-gradient row shifted by
-// one pixel each (B, one block per (tx, group)), zero outside the tensor.
-// A block of ones after the input rows makes accumulator row 3 CIN the sum of
-// d over the chunk: the bias gradient (column block tx = 1).  Warp 0 lane 0
-// issues the loads into a ring of kWtStages stages, warp 1 lane 0 the MMAs;
-// every warp reads the accumulators at the end.
 constexpr int kWtPx = 64;
 constexpr int kWtStages = 4;
 constexpr int kWtThreads = 256;
@@ -1314,7 +1080,8 @@ __global__ void __launch_bounds__(kWtThreads, 1) k_conv3x3_wgrad_tma(
 {
     using S = WtShape<CIN, COUT>;
     constexpr int N = S::N, MB = S::MB, MROWS = S::MROWS;
-    extern __shared__ __align__(1024) unsigned char smemRaw[];
+    // the ring starts at the first 1 KB boundary (the launch adds 1 KB of slack)
+    extern __shared__ __align__(128) unsigned char smemRaw[];
     const uint32_t base = (smem_u32(smemRaw) + 1023u) & ~1023u;
     __shared__ __align__(8) uint64_t full[kWtStages], empty[kWtStages], done;
     __shared__ uint32_t tmemBase;
@@ -1362,19 +1129,20 @@ __global__ void __launch_bounds__(kWtThreads, 1) k_conv3x3_wgrad_tma(
                 asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                              :: "r"(bar), "r"(S::kTxBytes) : "memory");
 #pragma unroll
+                // word coordinates: pixel * 4 (a 16-byte multiple)
                 for (int t = 0; t < 3; t++) {
                     asm volatile(
-                        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
-                        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5}], [%6];"
                         :: "r"(sb + (uint32_t)(t * S::KGI) * S::kBlock),
-                           "l"(reinterpret_cast<uint64_t>(&tmX)), "r"(0), "r"(x0), "r"(0),
+                           "l"(reinterpret_cast<uint64_t>(&tmX)), "r"(4 * x0), "r"(0),
                            "r"(y + t - 1), "r"(b), "r"(bar)
                         : "memory");
                     asm volatile(
-                        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
-                        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+                        " [%0], [%1, {%2, %3, %4, %5}], [%6];"
                         :: "r"(sb + S::kBOff + (uint32_t)(t * S::KGO) * S::kBlock),
-                           "l"(reinterpret_cast<uint64_t>(&tmD)), "r"(0), "r"(x0 + 1 - t), "r"(0),
+                           "l"(reinterpret_cast<uint64_t>(&tmD)), "r"(4 * (x0 + 1 - t)), "r"(0),
                            "r"(y), "r"(b), "r"(bar)
                         : "memory");
                 }
@@ -1768,33 +1536,6 @@ static int launch_wgrad_tc(cudaStream_t s, const __nv_bfloat16 *in, const __nv_b
 }
 
 template <int CIN, int COUT>
-static int launch_wgrad_tc5(cudaStream_t s, const __nv_bfloat16 *in, const __nv_bfloat16 *d, int B,
-    int H, int W, float *dW, float *dBias)
-{
-    const int chunks = ((W + kWg5Px - 1) / kWg5Px) * B * H;
-    int grid = sm_count();
-    if (grid > chunks) grid = chunks;
-    constexpr int MB = (3 * CIN + 127) / 128;
-    const size_t smem = std::max<size_t>(
-        1024 + 2 * ((size_t)MB * 128 * kWg5Px * 2 + (size_t)3 * COUT * kWg5Px * 2), kWg5MinSmem);
-    auto kern = k_conv3x3_wgrad_tc5<CIN, COUT>;
-    GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int perSlice = 9 * COUT * CIN + COUT;
-    float *partial = nullptr;
-    GBSP_CUDA_TRY(cudaMallocAsync((void **)&partial, sizeof(float) * (size_t)grid * perSlice, s));
-    kern<<<grid, kWg5Threads, smem, s>>>(in, d, B, H, W, partial);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) {
-        k_wgrad_reduce<<<(perSlice + 255) / 256, 256, 0, s>>>(partial, grid, perSlice,
-            9 * COUT * CIN, dW, dBias);
-        e = cudaGetLastError();
-    }
-    cudaFreeAsync(partial, s);
-    if (e != cudaSuccess) return cuda_error(e, "tcgen05 weight gradient");
-    return GBSP_OK;
-}
-
-template <int CIN, int COUT>
 static int launch_wgrad_tma(cudaStream_t s, const __nv_bfloat16 *in, const __nv_bfloat16 *d, int B,
     int H, int W, float *dW, float *dBias)
 {
@@ -1807,8 +1548,8 @@ static int launch_wgrad_tma(cudaStream_t s, const __nv_bfloat16 *in, const __nv_
     GBSP_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CUtensorMap mapX, mapD;
     int rc;
-    if ((rc = planar_tensor_map(&mapX, in, B, H, W, CIN, kWtPx)) ||
-        (rc = planar_tensor_map(&mapD, d, B, H, W, COUT, kWtPx)))
+    if ((rc = planar_words_tensor_map(&mapX, in, B, H, W, CIN, kWtPx)) ||
+        (rc = planar_words_tensor_map(&mapD, d, B, H, W, COUT, kWtPx)))
         return rc;
     const int perSlice = 9 * COUT * CIN + COUT;
     float *partial = nullptr;
@@ -1981,22 +1722,6 @@ int gbsp_dn_conv3x3_weight_grad_tc(void *stream, const uint16_t *in, const uint1
 }
 
 int gbsp_dn_conv3x3_weight_grad_tcgen05(void *stream, const uint16_t *in, const uint16_t *dOut,
-    uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias)
-{
-    cudaStream_t s = (cudaStream_t)stream;
-    if (!in || !dOut || !dW || !dBias || !B || !H || !W)
-        return set_error(GBSP_ERR_INVALID_ARGUMENT, "bad weight-gradient args");
-    if (((uintptr_t)in | (uintptr_t)dOut) & 15u)
-        return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight-gradient tensors must be 16-byte aligned");
-    const __nv_bfloat16 *i16 = reinterpret_cast<const __nv_bfloat16 *>(in);
-    const __nv_bfloat16 *d16 = reinterpret_cast<const __nv_bfloat16 *>(dOut);
-    if (cin == 16 && cout == 48) return launch_wgrad_tc5<16, 48>(s, i16, d16, B, H, W, dW, dBias);
-    if (cin == 48 && cout == 48) return launch_wgrad_tc5<48, 48>(s, i16, d16, B, H, W, dW, dBias);
-    if (cin == 48 && cout == 32) return launch_wgrad_tc5<48, 32>(s, i16, d16, B, H, W, dW, dBias);
-    return set_error(GBSP_ERR_INVALID_ARGUMENT, "weight grad %u->%u not instantiated", cin, cout);
-}
-
-int gbsp_dn_conv3x3_weight_grad_tma(void *stream, const uint16_t *in, const uint16_t *dOut,
     uint32_t B, uint32_t H, uint32_t W, uint32_t cin, uint32_t cout, float *dW, float *dBias)
 {
     cudaStream_t s = (cudaStream_t)stream;

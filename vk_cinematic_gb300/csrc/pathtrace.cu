@@ -243,11 +243,11 @@ int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &
 }
 
 // Waves of `spp` samples per pixel over `pixels` pixels: as many whole pixels
-// per wave as fit in waveTarget paths (default 2^22), at least one.
+// per wave as fit in waveTarget paths (default kDefaultWavePaths), at least one.
 static int uniform_waves(uint64_t pixels, uint32_t spp, uint64_t waveTarget,
     std::vector<WavePlan> &waves)
 {
-    if (!waveTarget) waveTarget = 1u << 22;
+    if (!waveTarget) waveTarget = kDefaultWavePaths;
     const uint64_t perWave = std::min<uint64_t>(std::max<uint64_t>(1, waveTarget / spp), pixels);
     if (perWave * spp > 0x7FFFFFFFull)
         return set_error(GBSP_ERR_CAPACITY, "wave of %llu paths is too large",
@@ -266,7 +266,7 @@ static int uniform_waves(uint64_t pixels, uint32_t spp, uint64_t waveTarget,
 static int variable_waves(const std::vector<uint4> &tiles, const std::vector<uint32_t> &spp,
     uint64_t waveTarget, std::vector<WavePlan> &waves)
 {
-    if (!waveTarget) waveTarget = 1u << 22;
+    if (!waveTarget) waveTarget = kDefaultWavePaths;
     uint32_t maxSpp = 0;
     for (uint32_t v : spp) maxSpp = std::max(maxSpp, v);
     const uint64_t cap = std::max<uint64_t>(waveTarget, maxSpp);

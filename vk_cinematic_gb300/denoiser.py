@@ -74,9 +74,8 @@ class KPCNN:
     """conv: "tcgen05" (5th-generation tensor cores, accumulator in tensor
     memory) or "mma" (mma.sync BF16 fragments) for the forward and
     data-gradient convolutions.  wgrad: "tcgen05" (5th-generation tensor
-    cores, accumulators in tensor memory, operands staged by warps), "tma"
-    (the same with operands loaded by TMA and read MN-major), "mma"
-    (mma.sync fragments) - all with deterministic per-CTA partial sums - or
+    cores, operands loaded by TMA, accumulators in tensor memory), "mma"
+    (mma.sync fragments) - both with deterministic per-CTA partial sums - or
     "simt" (FP32 FMA with atomics) for the weight gradient."""
 
     def __init__(self, seed: int = 0, conv: str = "tcgen05", wgrad: str = "tcgen05"):
@@ -86,7 +85,6 @@ class KPCNN:
         self._conv = {"tcgen05": self.L.gbsp_dn_conv3x3_forward_tc,
                       "mma": self.L.gbsp_dn_conv3x3_forward}[conv]
         self._wgrad = {"tcgen05": self.L.gbsp_dn_conv3x3_weight_grad_tcgen05,
-                       "tma": self.L.gbsp_dn_conv3x3_weight_grad_tma,
                        "mma": self.L.gbsp_dn_conv3x3_weight_grad_tc,
                        "simt": self.L.gbsp_dn_conv3x3_weight_grad}[wgrad]
         self.conv_impl = conv

@@ -59,7 +59,7 @@ EXPORTS = [
     "gbsp_dn_tile_fallback", "gbsp_scene_set_node_width", "gbsp_scene_node_width",
     "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths", "gbsp_path_trace_tile_list",
     "gbsp_dn_tile_check", "gbsp_dn_tile_merge", "gbsp_dn_conv3x3_weight_grad_tcgen05",
-    "gbsp_path_trace_tile_list_spp", "gbsp_dn_conv3x3_weight_grad_tma",
+    "gbsp_path_trace_tile_list_spp",
 ]
 
 
