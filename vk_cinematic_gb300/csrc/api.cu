@@ -289,8 +289,6 @@ static void runtime_teardown(gbsp_runtime *rt)
     rt->rayD.release();
     rt->hitA.release();
     rt->hitInst.release();
-    rt->pathRng.release();
-    rt->pathLen.release();
     rt->vertE.release();
     rt->vertA.release();
     rt->pathRad.release();

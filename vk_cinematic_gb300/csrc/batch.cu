@@ -111,9 +111,7 @@ __global__ void __launch_bounds__(256) k_bgenerate(const BatchItemDev *__restric
     V3 o, d;
     camera_ray(it.cam, x, y, rng, o, d);
     wb.rayO[p] = make_float4(o.x, o.y, o.z, __int_as_float((int)p));
-    wb.rayD[p] = make_float4(d.x, d.y, d.z, 0.0f);
-    wb.pathRng[p] = rng;
-    wb.pathLen[p] = 0;
+    wb.rayD[p] = make_float4(d.x, d.y, d.z, __uint_as_float(rng));
     pathItem[p] = k;
 }
 
@@ -525,7 +523,7 @@ struct gbsp_batch {
     DeviceBuffer<float4> rayO, rayD, vertE, vertA, pathRad;
     DeviceBuffer<int4> hitA;
     DeviceBuffer<int> hitInst;
-    DeviceBuffer<uint32_t> pathRng, pathLen, pathItem;
+    DeviceBuffer<uint32_t> pathItem;
     std::vector<uint32_t> nodeWidth;  // per item: BVH node width its scene view walks
 };
 
@@ -619,7 +617,6 @@ static int plan_waves(gbsp_batch *b)
     int rc;
     if ((rc = b->rayO.reserve(2 * c, s)) || (rc = b->rayD.reserve(2 * c, s)) ||
         (rc = b->hitA.reserve(c, s)) || (rc = b->hitInst.reserve(c, s)) ||
-        (rc = b->pathRng.reserve(c, s)) || (rc = b->pathLen.reserve(c, s)) ||
         (rc = b->pathItem.reserve(c, s)) || (rc = b->vertE.reserve((size_t)maxB * c, s)) ||
         (rc = b->vertA.reserve((size_t)maxB * c, s)) || (rc = b->pathRad.reserve(c, s)))
         return rc;
@@ -637,8 +634,6 @@ static void enqueue_wavefront(gbsp_batch *b)
     wb.rayD = b->rayD.ptr;
     wb.hitA = b->hitA.ptr;
     wb.hitInst = b->hitInst.ptr;
-    wb.pathRng = b->pathRng.ptr;
-    wb.pathLen = b->pathLen.ptr;
     wb.vertE = b->vertE.ptr;
     wb.vertA = b->vertA.ptr;
     wb.pathRad = b->pathRad.ptr;

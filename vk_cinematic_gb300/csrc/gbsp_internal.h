@@ -110,8 +110,6 @@ struct gbsp_runtime {
     gbsp::DeviceBuffer<int4> hitA;                 // t, u, v, prim
     gbsp::DeviceBuffer<int> hitInst;
     gbsp::DeviceBuffer<uint32_t> sortHist;       // octant histograms of the ray sort
-    gbsp::DeviceBuffer<uint32_t> pathRng;
-    gbsp::DeviceBuffer<uint32_t> pathLen;
     gbsp::DeviceBuffer<float4> vertE;              // emission xyz, cosine
     gbsp::DeviceBuffer<float4> vertA;              // response xyz
     gbsp::DeviceBuffer<float4> pathRad;            // radiance per path

@@ -108,7 +108,6 @@ static int ensure_wave_buffers(gbsp_runtime *rt, uint32_t cap, uint32_t maxBounc
     int rc;
     if ((rc = rt->rayO.reserve(2 * (size_t)cap, s)) || (rc = rt->rayD.reserve(2 * (size_t)cap, s)) ||
         (rc = rt->hitA.reserve(cap, s)) || (rc = rt->hitInst.reserve(cap, s)) ||
-        (rc = rt->pathRng.reserve(cap, s)) || (rc = rt->pathLen.reserve(cap, s)) ||
         (rc = rt->vertE.reserve((size_t)maxBounces * cap, s)) ||
         (rc = rt->vertA.reserve((size_t)maxBounces * cap, s)) ||
         (rc = rt->pathRad.reserve(cap, s)))
@@ -315,8 +314,6 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
     wb.rayD = rt->rayD.ptr;
     wb.hitA = rt->hitA.ptr;
     wb.hitInst = rt->hitInst.ptr;
-    wb.pathRng = rt->pathRng.ptr;
-    wb.pathLen = rt->pathLen.ptr;
     wb.vertE = rt->vertE.ptr;
     wb.vertA = rt->vertA.ptr;
     wb.pathRad = rt->pathRad.ptr;
@@ -336,6 +333,7 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
     wp.aovImage = dAov;
     OneScene one = {sv, mv, maxBounces, opt.radiance_clamp};
     int persistentGrid = rt->smCount * 8;
+    const int shadeGrid = shade_grid<OneScene>(rt->smCount);
     const bool sortDirs = (opt.flags & GBSP_FLAG_SORT_DIRECTIONS) != 0 && maxBounces > 1;
     if (sortDirs && (rc = rt->sortHist.reserve(8 * (size_t)kSortBlocks, s))) return rc;
     bool timing = rt->stageTiming;
@@ -365,7 +363,7 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
                 launch_trace_stage(perLane, sv.watertight != 0, persistentGrid, s, one, qO, qD,
                     ctl + inQ, wb.hitA, wb.hitInst, ctl, counters, rt->dStatus);
                 int e1 = timing ? rt->stage_event(s) : -1;
-                k_shade<<<persistentGrid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
+                k_shade<<<shadeGrid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
                 if (sortDirs && b + 1 < maxBounces) {
                     k_octant_count<<<kSortBlocks, 256, 0, s>>>(wb.rayD + cap, ctl, kCtlQueue1,
                         rt->sortHist.ptr);
@@ -410,9 +408,7 @@ constexpr size_t kNaRayO = na_align(kNaSlots + 4 * (size_t)kNoAllocMaxObjects);
 constexpr size_t kNaRayD = na_align(kNaRayO + 2 * 16 * (size_t)kNoAllocMaxPaths);
 constexpr size_t kNaHitA = na_align(kNaRayD + 2 * 16 * (size_t)kNoAllocMaxPaths);
 constexpr size_t kNaHitInst = na_align(kNaHitA + 16 * (size_t)kNoAllocMaxPaths);
-constexpr size_t kNaRng = na_align(kNaHitInst + 4 * (size_t)kNoAllocMaxPaths);
-constexpr size_t kNaLen = na_align(kNaRng + 4 * (size_t)kNoAllocMaxPaths);
-constexpr size_t kNaVertE = na_align(kNaLen + 4 * (size_t)kNoAllocMaxPaths);
+constexpr size_t kNaVertE = na_align(kNaHitInst + 4 * (size_t)kNoAllocMaxPaths);
 constexpr size_t kNaVertA = na_align(kNaVertE + 16 * (size_t)kNoAllocMaxBounces * kNoAllocMaxPaths);
 constexpr size_t kNaRad = na_align(kNaVertA + 16 * (size_t)kNoAllocMaxBounces * kNoAllocMaxPaths);
 constexpr size_t kNoAllocBytes = na_align(kNaRad + 16 * (size_t)kNoAllocMaxPaths);
@@ -550,8 +546,6 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     wb.rayD = reinterpret_cast<float4 *>(base + kNaRayD);
     wb.hitA = reinterpret_cast<int4 *>(base + kNaHitA);
     wb.hitInst = reinterpret_cast<int *>(base + kNaHitInst);
-    wb.pathRng = reinterpret_cast<uint32_t *>(base + kNaRng);
-    wb.pathLen = reinterpret_cast<uint32_t *>(base + kNaLen);
     wb.vertE = reinterpret_cast<float4 *>(base + kNaVertE);
     wb.vertA = reinterpret_cast<float4 *>(base + kNaVertA);
     wb.pathRad = reinterpret_cast<float4 *>(base + kNaRad);
@@ -605,7 +599,8 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
                 launch_trace_stage(perLane, one.sv.watertight != 0, grid, s, one,
                     wb.rayO + ((b & 1) ? wb.cap : 0), wb.rayD + ((b & 1) ? wb.cap : 0), ctl + inQ,
                     wb.hitA, wb.hitInst, ctl, counters, status);
-                k_shade<<<grid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);
+                k_shade<<<shade_grid<OneScene>(rt->smCount), 128, 0, s>>>(one, wb, b, inQ, ctl,
+                    counters);
                 launches += 3;
                 traceLaunches += 1;
             }

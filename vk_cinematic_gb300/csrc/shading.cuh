@@ -109,20 +109,36 @@ __device__ __forceinline__ void vertex_terms(const MaterialView &mv, int slot, V
     aa = make_float4(A.x, A.y, A.z, 0.0f);
 }
 
+// One step of the reverse pass: radiance = E + (A * clamp(radiance)) * cosine.
+__device__ __forceinline__ V3 radiance_step(V3 radiance, float4 ec, float4 aa, float clampValue)
+{
+    V3 Li = radiance;
+    if (clampValue != 0.0f)
+        Li = v3(rclamp(Li.x, 0.0f, clampValue), rclamp(Li.y, 0.0f, clampValue),
+            rclamp(Li.z, 0.0f, clampValue));
+    return add(v3(ec.x, ec.y, ec.z), mul(hadamard(v3(aa.x, aa.y, aa.z), Li), ec.w));
+}
+
 // Reverse pass over stored vertex terms.
 __device__ __forceinline__ V3 path_radiance(const float4 *vertE, const float4 *vertA,
     size_t stride, uint32_t p, uint32_t len, float clampValue)
 {
     V3 radiance = v3(0.0f, 0.0f, 0.0f);
-    for (int i = (int)len - 1; i >= 0; i--) {
-        float4 ec = vertE[(size_t)i * stride + p];
-        float4 aa = vertA[(size_t)i * stride + p];
-        V3 Li = radiance;
-        if (clampValue != 0.0f)
-            Li = v3(rclamp(Li.x, 0.0f, clampValue), rclamp(Li.y, 0.0f, clampValue),
-                rclamp(Li.z, 0.0f, clampValue));
-        radiance = add(v3(ec.x, ec.y, ec.z), mul(hadamard(v3(aa.x, aa.y, aa.z), Li), ec.w));
-    }
+    for (int i = (int)len - 1; i >= 0; i--)
+        radiance = radiance_step(radiance, vertE[(size_t)i * stride + p],
+            vertA[(size_t)i * stride + p], clampValue);
+    return radiance;
+}
+
+// The same with the last vertex's terms given (not stored) and the len - 1
+// before it read from memory.
+__device__ __forceinline__ V3 path_radiance_last(const float4 *vertE, const float4 *vertA,
+    size_t stride, uint32_t p, uint32_t len, float4 lastE, float4 lastA, float clampValue)
+{
+    V3 radiance = radiance_step(v3(0.0f, 0.0f, 0.0f), lastE, lastA, clampValue);
+    for (int i = (int)len - 2; i >= 0; i--)
+        radiance = radiance_step(radiance, vertE[(size_t)i * stride + p],
+            vertA[(size_t)i * stride + p], clampValue);
     return radiance;
 }
 

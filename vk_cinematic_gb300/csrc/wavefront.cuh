@@ -20,13 +20,13 @@ enum Ctl : int {
 };
 
 struct WaveBuffers {
+    // a queued ray carries its path's state: the path id and the RNG state ride
+    // in the w lanes, and its path length is the bounce number of the queue
     float4 *rayO;      // 2 * cap: (origin, path id bits)
-    float4 *rayD;      // 2 * cap: (direction, 0)
+    float4 *rayD;      // 2 * cap: (direction, RNG state bits)
     int4 *hitA;        // cap: (t, u, v, prim) bits
     int *hitInst;      // cap
-    uint32_t *pathRng; // cap
-    uint32_t *pathLen; // cap
-    float4 *vertE;     // maxBounces * cap: (emission xyz, cosine)
+    float4 *vertE;     // maxBounces * cap: (emission xyz, cosine), vertices of paths that go on
     float4 *vertA;     // maxBounces * cap: (A xyz, 0)
     float4 *pathRad;   // cap
     float4 *pathAov;   // 2 * cap first-hit G-buffer per path, or null
@@ -269,9 +269,7 @@ static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuff
     V3 o, d;
     camera_ray(wp.cam, x, y, rng, o, d);
     wb.rayO[p] = make_float4(o.x, o.y, o.z, __int_as_float((int)p));
-    wb.rayD[p] = make_float4(d.x, d.y, d.z, 0.0f);
-    wb.pathRng[p] = rng;
-    wb.pathLen[p] = 0;
+    wb.rayD[p] = make_float4(d.x, d.y, d.z, __uint_as_float(rng));
 }
 
 template <class Src, bool kWT>
@@ -545,7 +543,8 @@ __global__ void __launch_bounds__(128) k_shade(Src src, WaveBuffers wb, uint32_t
             h.prim = hA.w;
             h.inst = wb.hitInst[i];
             V3 o = v3(o4.x, o4.y, o4.z), d = v3(d4.x, d4.y, d4.z);
-            uint32_t len = wb.pathLen[p];
+            // every path in this queue has `bounce` vertices so far
+            const uint32_t len = bounce;
             float4 ec, aa;
             if (h.prim >= 0 && h.t > 0.0f) {
                 // hit vertex (src/simd_path_tracer.cpp:268-288)
@@ -553,14 +552,13 @@ __global__ void __launch_bounds__(128) k_shade(Src src, WaveBuffers wb, uint32_t
                 float ux, uy;
                 hit_surface(sv, h, n, ux, uy);
                 V3 pos = add(o, mul(d, h.t));
-                uint32_t rng = wb.pathRng[p];
+                uint32_t rng = __float_as_uint(d4.w);
                 V3 dir = random_hemisphere(n, rng);
-                wb.pathRng[p] = rng;
                 int slot = mv.instanceSlot[h.inst];
                 vertex_terms(mv, slot, n, dir, neg(d), ux, uy, ec, aa);
                 V3 no = add(pos, mul(n, 0.0001f));
                 newO = make_float4(no.x, no.y, no.z, __int_as_float((int)p));
-                newD = make_float4(dir.x, dir.y, dir.z, 0.0f);
+                newD = make_float4(dir.x, dir.y, dir.z, __uint_as_float(rng));
                 cont = !lastBounce;
                 if (wb.pathAov && bounce == 0) {
                     V3 al = material_albedo(mv, slot, ux, uy);
@@ -576,12 +574,13 @@ __global__ void __launch_bounds__(128) k_shade(Src src, WaveBuffers wb, uint32_t
                     wb.pathAov[2 * (size_t)p + 1] = make_float4(0, 0, 0, 0);
                 }
             }
-            wb.vertE[(size_t)len * wb.cap + p] = ec;
-            wb.vertA[(size_t)len * wb.cap + p] = aa;
-            len++;
-            wb.pathLen[p] = len;
-            if (!cont) {
-                V3 r = path_radiance(wb.vertE, wb.vertA, wb.cap, p, len, src.clamp(p));
+            if (cont) {
+                wb.vertE[(size_t)len * wb.cap + p] = ec;
+                wb.vertA[(size_t)len * wb.cap + p] = aa;
+            } else {
+                // the path ends at this vertex: the reverse pass starts from it
+                V3 r = path_radiance_last(wb.vertE, wb.vertA, wb.cap, p, len + 1, ec, aa,
+                    src.clamp(p));
                 wb.pathRad[p] = make_float4(r.x, r.y, r.z, 0.0f);
                 finished++;
             }
@@ -652,6 +651,22 @@ static __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBu
     for (int off = 16; off; off >>= 1) nans += __shfl_xor_sync(0xFFFFFFFFu, nans, off);
     if ((threadIdx.x & 31) == 0 && nans)
         atomicAdd(&counters[GBSP_METRIC_NAN_SAMPLES], (unsigned long long)nans);
+}
+
+// Persistent grid of k_shade: every block an SM can hold (the kernel waits on
+// scattered loads, so more resident warps hide more of that latency).
+template <class Src>
+int shade_grid(int smCount)
+{
+    static int perSm = 0;
+    if (perSm == 0) {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shade<Src>, 128, 0) !=
+                cudaSuccess || n < 1)
+            n = 8;
+        perSm = n;
+    }
+    return smCount * perSm;
 }
 
 // Launches the closest-hit kernel of one bounce: per-warp or per-lane
