@@ -74,6 +74,9 @@ def parse_args():
     ap.add_argument("--dn-check-spp", default="same,1",
                     help="config5: sample counts of the served output's check render, "
                          "comma-separated; 'same' = the input render's spp")
+    ap.add_argument("--dn-margins", default="1.25,1.0",
+                    help="config5: margins of the fallback spp over the check's estimate, "
+                         "comma-separated; the first is the quoted protocol's")
     ap.add_argument("--sort-dirs", action="store_true",
                     help="sort bounce-ray queues by direction octant")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
@@ -776,8 +779,10 @@ def run_config5(args):
     plain = {k: [] for k in spps}
     den = {k: [] for k in in_spps}
     check_opts = [None if v == "same" else int(v) for v in str(args.dn_check_spp).split(",") if v]
-    protos = [(k, c) for k in in_spps for c in check_opts]
-    pname = lambda kc: f"{kc[0]}/{kc[1] or kc[0]}"  # noqa: E731  input spp / check spp
+    margins = [float(v) for v in str(args.dn_margins).split(",") if v]
+    protos = [(k, c, m) for k in in_spps for c in check_opts for m in margins]
+    # input spp / check spp, with the fallback margin when it is not the quoted one
+    pname = lambda p: f"{p[0]}/{p[1] or p[0]}" + (f"@{p[2]:g}" if p[2] != margins[0] else "")  # noqa: E731
     served = {p: [] for p in protos}
     flagged = {p: [] for p in protos}
     fb_spp = {p: [] for p in protos}
@@ -791,14 +796,14 @@ def run_config5(args):
         for k in spps:
             img, _ = sre.render(x0, y0, crop, crop, k, seed=7 + k)
             plain[k].append(denoiser.relmse(img, ref))
-        for k, c in protos:
+        for k, c, m in protos:
             out, st = net.serve(sre, x0, y0, crop, crop, k, seed=5 + 31 * k, bound=0.01,
-                                check_spp=c)
-            if c == check_opts[0]:
+                                check_spp=c, margin=m)
+            if c == check_opts[0] and m == margins[0]:
                 den[k].append(denoiser.relmse(st["denoised"], ref))
-            served[(k, c)].append(denoiser.relmse(out, ref))
-            flagged[(k, c)].append(st["flagged"] / st["tiles"])
-            fb_spp[(k, c)].append(st["fallback_samples"] / float(crop * crop))
+            served[(k, c, m)].append(denoiser.relmse(out, ref))
+            flagged[(k, c, m)].append(st["flagged"] / st["tiles"])
+            fb_spp[(k, c, m)].append(st["fallback_samples"] / float(crop * crop))
     plain_mean = {k: float(np.mean(v)) for k, v in plain.items()}
     den_mean = {k: float(np.mean(v)) for k, v in den.items()}
     served_mean = {k: float(np.mean(v)) for k, v in served.items()}
@@ -816,7 +821,7 @@ def run_config5(args):
     # the quoted protocol (the training input spp, check render of the same spp)
     # and every protocol whose served output meets the bound on the held-out crops
     quoted_spp = train_spp[-1]
-    quoted = (quoted_spp, check_opts[0])
+    quoted = (quoted_spp, check_opts[0], margins[0])
     valid = [p for p in protos if served_mean[p] <= 0.01]
 
     # ---- timing at 1920x1080: plain path tracing vs the served output
@@ -831,21 +836,21 @@ def run_config5(args):
     torch.cuda.synchronize()
     ms_per_spp = ev0.elapsed_time(ev1) / 64.0
     timing = {}
-    for k, c in sorted(set([quoted] + valid), key=lambda kc: (kc[0], kc[1] or kc[0])):
-        net.serve(sr, 0, 0, W, H, k, seed=1, check_spp=c)  # warm-up
+    for k, c, m in sorted(set([quoted] + valid), key=lambda p: (p[0], p[1] or p[0], -p[2])):
+        net.serve(sr, 0, 0, W, H, k, seed=1, check_spp=c, margin=m)  # warm-up
         torch.cuda.synchronize()
         reps = 5
         t1 = time.perf_counter()
         stats = []
         for r in range(reps):
-            _, st = net.serve(sr, 0, 0, W, H, k, seed=11 + r, check_spp=c)
+            _, st = net.serve(sr, 0, 0, W, H, k, seed=11 + r, check_spp=c, margin=m)
             stats.append(st)
         torch.cuda.synchronize()
         served_ms = (time.perf_counter() - t1) * 1e3 / reps
         stages = {}
         for r in range(reps):
-            net.serve(sr, 0, 0, W, H, k, seed=11 + r, timing=stages, check_spp=c)
-        timing[(k, c)] = {"served_ms": served_ms,
+            net.serve(sr, 0, 0, W, H, k, seed=11 + r, timing=stages, check_spp=c, margin=m)
+        timing[(k, c, m)] = {"served_ms": served_ms,
                      "stage_ms": {n: v / reps for n, v in stages.items()},
                      "flagged_tile_fraction": float(np.mean([x["flagged"] / x["tiles"]
                                                              for x in stats])),
@@ -880,9 +885,10 @@ def run_config5(args):
                    "eval_seeds": args.dn_eval_seeds, "eval_crop": crop,
                    "oracle_spp": args.dn_oracle_spp, "conv": net.conv_impl,
                    "served": "denoised; 16x16 tiles checked against an independent plain render "
-                             "(protocols input spp / check spp); failing tiles served from all "
-                             "their plain samples topped up to the spp the check estimates for "
-                             "the bound"},
+                             "(protocols input spp / check spp [@ fallback margin]); failing "
+                             "tiles served from all their plain samples topped up to margin x "
+                             "the spp the check estimates for the bound",
+                   "fallback_margins": margins},
         "served_protocol": pname(headline) if headline else None,
         "quoted_protocol": pname(quoted),
         "served_relmse_by_protocol": {pname(p): v for p, v in served_mean.items()},

@@ -283,6 +283,16 @@ int gbsp_path_trace_frame(const gbsp_context *ctx, gbsp_metrics *metrics);
  * those host pixels.  metrics NULL and no host pixels: asynchronous. */
 int gbsp_path_trace_tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, uint32_t count,
     gbsp_metrics *metrics);
+/* One pass of options->spp samples per pixel over the tile whose samples
+ * split in two images (extension, hash-per-sample seeding only): the mean of
+ * samples [0, firstSpp) goes to the runtime's frame buffer (and the
+ * G-buffers with GBSP_FLAG_AOV) - bit-identical to gbsp_path_trace_tile with
+ * options->spp = firstSpp - and the mean of samples [firstSpp, spp) to
+ * deviceImage2 (device memory, imagePlane->width x height RGBA32F; only the
+ * tile is written).  E.g. a denoiser's input and an independent check render
+ * in one launch sequence.  metrics NULL and no host pixels: asynchronous. */
+int gbsp_path_trace_tile_split(const gbsp_context *ctx, gbsp_tile tile, uint32_t firstSpp,
+    float *deviceImage2, gbsp_metrics *metrics);
 /* The same with a sample count per tile (extension): tile i is rendered
  * exactly as gbsp_path_trace_tile renders it with options->spp = spp[i]
  * (bit-identical pixels; spp[i] = 0 skips the tile), all tiles in one device

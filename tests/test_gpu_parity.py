@@ -496,6 +496,51 @@ def test_tile_list_spp_matches_tile_renders(rt, wave_paths):
     assert m.as_dict()["paths_traced"] == paths
 
 
+def test_split_render_matches_separate_renders(rt):
+    """gbsp_path_trace_tile_split renders a + c samples per pixel in one pass:
+    the first image (radiance and G-buffers) is bit-identical to an a-spp
+    render, (a A + c C) / (a + c) matches an (a + c)-spp render to FP32
+    rounding, and the second image is written only inside the tile."""
+    import torch
+
+    a, c = 2, 3
+    s = scenes.config3_scene(width=200, height=120, spp=a, n_spheres=32, level=2, seed=35)
+    scene, ms, rend = gbsp.upload_scene(rt, s)
+    tile = (8, 4, 180, 100)
+    x0, y0, x1, y1 = tile
+    w, h = x1 - x0, y1 - y0
+
+    def grab(aov):
+        rad = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+        av = torch.empty((h, w, 8), dtype=torch.float32, device="cuda") if aov else None
+        rend.copy_region(x0, y0, w, h, rad.data_ptr(), av.data_ptr() if aov else 0)
+        rt.synchronize()
+        return rad.cpu().numpy(), (av.cpu().numpy() if aov else None)
+
+    rend.options.spp, rend.options.flags = a, gbsp.FLAG_AOV
+    rend.tile_device(tile)
+    refA, refAov = grab(True)
+    rend.options.spp, rend.options.flags = a + c, 0
+    rend.tile_device(tile)
+    full, _ = grab(False)
+    rend.options.spp, rend.options.flags = a + c, gbsp.FLAG_AOV
+    image2 = torch.full((s.height, s.width, 4), -7.0, dtype=torch.float32, device="cuda")
+    m = rend.tile_split_device(tile, a, image2.data_ptr(), metrics=True)
+    gotA, gotAov = grab(True)
+    img2 = image2.cpu().numpy()
+    assert np.array_equal(gotA.view(np.uint32), refA.view(np.uint32))
+    assert np.array_equal(gotAov.view(np.uint32), refAov.view(np.uint32))
+    inside = np.zeros((s.height, s.width), bool)
+    inside[y0:y1, x0:x1] = True
+    assert np.all(img2[~inside] == -7.0)
+    comb = (a * gotA[..., :3].astype(np.float64) + c * img2[y0:y1, x0:x1, :3]) / (a + c)
+    err = np.abs(comb - full[..., :3]) / (np.abs(full[..., :3]) + 1e-3)
+    print("split render: max rel error of the recombined image", float(err.max()))
+    assert float(err.max()) < 1e-5
+    assert m.as_dict()["paths_traced"] == w * h * (a + c)
+    rend.options.flags = 0
+
+
 def test_tonemap_matches_oracle(rt, port):
     """Display conversion (post_processing.frag.glsl:19-26 + ToColor) of a
     path-traced frame against the C restatement; powf differs in the last

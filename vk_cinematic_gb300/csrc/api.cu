@@ -918,6 +918,47 @@ int gbsp_path_trace_tile(const gbsp_context *ctx, gbsp_tile tile, gbsp_rng *rng,
     return check_stream_status(rt);
 }
 
+int gbsp_path_trace_tile_split(const gbsp_context *ctx, gbsp_tile tile, uint32_t firstSpp,
+    float *deviceImage2, gbsp_metrics *metrics)
+{
+    if (!deviceImage2) return set_error(GBSP_ERR_INVALID_ARGUMENT, "deviceImage2 is NULL");
+    gbsp_options opt;
+    MaterialView mv;
+    DeviceBuffer<int32_t> slots;
+    int rc = prepare_render(ctx, opt, mv, slots);
+    if (rc) return rc;
+    if (opt.rng_mode != GBSP_RNG_HASH_PER_SAMPLE)
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "split renders seed hash-per-sample only");
+    if (firstSpp == 0 || firstSpp >= (opt.spp ? opt.spp : 1u))
+        return set_error(GBSP_ERR_INVALID_ARGUMENT, "first spp %u of %u", firstSpp, opt.spp);
+    gbsp_runtime *rt = ctx->runtime;
+    cudaStream_t s = rt->stream;
+    gbsp_image_plane *ip = ctx->camera->imagePlane;
+    uint32_t x0 = tile.minX, y0 = tile.minY;
+    uint32_t x1 = std::min(tile.maxX, ip->width), y1 = std::min(tile.maxY, ip->height);
+    if ((rc = ensure_frame(rt, ip->width, ip->height, (opt.flags & GBSP_FLAG_AOV) != 0))) return rc;
+    if ((rc = counters_begin(rt, (opt.flags & GBSP_FLAG_STAGE_TIMING) != 0))) return rc;
+    GBSP_CUDA_TRY(cudaEventRecord(rt->ev[0], s));
+    if (x1 > x0 && y1 > y0 &&
+        (rc = render_frame(rt, ctx->scene->view(), mv, camera_params(ctx->camera), opt, x0, y0, x1,
+             y1, rt->frame.ptr, ip->width, nullptr, aov_target(rt, opt), firstSpp,
+             reinterpret_cast<float4 *>(deviceImage2))))
+        return rc;
+    GBSP_CUDA_TRY(cudaEventRecord(rt->ev[1], s));
+    if (ip->pixels && x1 > x0 && y1 > y0) {
+        size_t pitch = (size_t)ip->width * sizeof(float4);
+        GBSP_CUDA_TRY(cudaMemcpy2DAsync(ip->pixels + 4 * ((size_t)y0 * ip->width + x0), pitch,
+            rt->frame.ptr + (size_t)y0 * ip->width + x0, pitch, (size_t)(x1 - x0) * sizeof(float4),
+            y1 - y0, cudaMemcpyDeviceToHost, s));
+    }
+    if (!metrics && !ip->pixels) return GBSP_OK;
+    GBSP_CUDA_TRY(cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, rt->ev[0], rt->ev[1]);
+    if ((rc = counters_end(rt, metrics, ms))) return rc;
+    return check_stream_status(rt);
+}
+
 static int tile_list(const gbsp_context *ctx, const gbsp_tile *tiles, const uint32_t *spp,
     uint32_t count, gbsp_metrics *metrics)
 {

@@ -263,7 +263,7 @@ int launch_intersect(cudaStream_t s, const SceneView &sv, uint32_t count, const 
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
     uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState,
-    float4 *dAov = nullptr);
+    float4 *dAov = nullptr, uint32_t splitSpp = 0, float4 *dImage2 = nullptr);
 
 // Renders the listed rectangles (x0, y0, width, height), hash-per-sample
 // seeding, into dImage (imageWidth pixels per row) in one wave sequence:

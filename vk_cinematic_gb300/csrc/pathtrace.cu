@@ -132,12 +132,16 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
 
 int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     const CameraParams &cam, const gbsp_options &opt, uint32_t x0, uint32_t y0, uint32_t x1,
-    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState, float4 *dAov)
+    uint32_t y1, float4 *dImage, uint32_t imageWidth, uint32_t *rngState, float4 *dAov,
+    uint32_t splitSpp, float4 *dImage2)
 {
     cudaStream_t s = rt->stream;
     unsigned long long *counters = rt->dCounters;
     if (x1 <= x0 || y1 <= y0) return GBSP_OK;
     uint32_t spp = opt.spp ? opt.spp : 1;
+    if (splitSpp && (splitSpp >= spp || !dImage2 || opt.rng_mode == GBSP_RNG_TILE_SEQUENTIAL))
+        return set_error(GBSP_ERR_INVALID_ARGUMENT,
+            "a split render needs 0 < first spp < spp, a second image and hash-per-sample seeding");
     uint32_t maxBounces = opt.max_bounces;
     if (maxBounces == 0) {
         // no bounce at all: every path has zero vertices and zero radiance
@@ -184,6 +188,8 @@ int render_frame(gbsp_runtime *rt, const SceneView &sv, const MaterialView &mv,
     wp.tileCount = 0;
     wp.tileSpp = nullptr;
     wp.tilePath = nullptr;
+    wp.splitSpp = splitSpp;
+    wp.image2 = splitSpp ? dImage2 : nullptr;
     std::vector<WavePlan> waves;
     int rc = uniform_waves((uint64_t)(x1 - x0) * (y1 - y0), spp, opt.wave_paths, waves);
     if (rc) return rc;
@@ -237,6 +243,8 @@ int render_tile_list(gbsp_runtime *rt, const SceneView &sv, const MaterialView &
     wp.tileCount = (uint32_t)tiles.size();
     wp.tileSpp = tileSpp ? dSpp.ptr : nullptr;
     wp.tilePath = tileSpp ? dPath.ptr : nullptr;
+    wp.splitSpp = 0;
+    wp.image2 = nullptr;
     // the lists are freed in stream order behind the kernels that read them
     return render_waves(rt, sv, mv, cam, opt, wp, waves, dImage, imageWidth, nullptr);
 }
@@ -563,6 +571,8 @@ extern "C" int gbsp_path_trace_tile_noalloc(const gbsp_context *ctx, gbsp_tile t
     wp.tileCount = 0;
     wp.tileSpp = nullptr;
     wp.tilePath = nullptr;
+    wp.splitSpp = 0;
+    wp.image2 = nullptr;
     wp.spp = spp;
     wp.maxBounces = opt.max_bounces;
     wp.seed = opt.seed;

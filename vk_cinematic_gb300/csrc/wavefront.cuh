@@ -59,6 +59,10 @@ struct WaveParams {
     uint32_t nanPolicy;
     float invSpp;
     float4 *aovImage;     // 2 float4 per image pixel, or null
+    // split accumulation (0: off): samples [0, splitSpp) of a pixel go to the
+    // image (and the G-buffers), samples [splitSpp, spp) to image2
+    uint32_t splitSpp;
+    float4 *image2;
 };
 
 // Scene source of the wave kernels: everything a path needs from its scene.
@@ -621,8 +625,11 @@ static __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBu
         } else {
             wave_pixel(wp, pix, x, y);
         }
+        // with a split, the image holds the first splitSpp samples, image2 the rest
+        const uint32_t nFirst = wp.splitSpp ? wp.splitSpp : n;
+        if (wp.splitSpp) inv = 1.0f / (float)nFirst;
         CSum acc[3] = {{0, 0}, {0, 0}, {0, 0}};
-        for (uint32_t s = 0; s < n; s++) {
+        for (uint32_t s = 0; s < nFirst; s++) {
             float4 r = wb.pathRad[first + s];
             if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
                 nans++;
@@ -634,9 +641,25 @@ static __global__ void __launch_bounds__(256) k_accumulate(WaveParams wp, WaveBu
         }
         image[(size_t)y * imageWidth + x] =
             make_float4(csum_value(acc[0]), csum_value(acc[1]), csum_value(acc[2]), 1.0f);
+        if (wp.splitSpp) {
+            const float inv2 = 1.0f / (float)(n - nFirst);
+            CSum acc2[3] = {{0, 0}, {0, 0}, {0, 0}};
+            for (uint32_t s = nFirst; s < n; s++) {
+                float4 r = wb.pathRad[first + s];
+                if (isnan(r.x) || isnan(r.y) || isnan(r.z)) {
+                    nans++;
+                    if (wp.nanPolicy == GBSP_NAN_ZERO) continue;
+                }
+                csum_add(acc2[0], r.x * inv2);
+                csum_add(acc2[1], r.y * inv2);
+                csum_add(acc2[2], r.z * inv2);
+            }
+            wp.image2[(size_t)y * imageWidth + x] =
+                make_float4(csum_value(acc2[0]), csum_value(acc2[1]), csum_value(acc2[2]), 1.0f);
+        }
         if (wp.aovImage) {
             float4 a = make_float4(0, 0, 0, 0), b = make_float4(0, 0, 0, 0);
-            for (uint32_t s = 0; s < n; s++) {
+            for (uint32_t s = 0; s < nFirst; s++) {
                 float4 u = wb.pathAov[2 * (first + s)];
                 float4 v = wb.pathAov[2 * (first + s) + 1];
                 a = make_float4(a.x + u.x, a.y + u.y, a.z + u.z, a.w + u.w);

@@ -235,8 +235,10 @@ class KPCNN:
               timing=None, check_spp=None):
         """The served output of a w x h window of `sr`'s frame: `spp`-sample plain
         render + G-buffers -> denoised; an independent `check_spp`-sample plain
-        render (default `spp`) checks every tile x tile block (check_tiles); blocks
-        that fail are served from all their plain samples, topped up by a
+        render (default `spp`; the next samples of the same per-pixel sequence,
+        rendered in the same pass as the input) checks every tile x tile block
+        (check_tiles); blocks that fail are served from all their plain samples,
+        topped up by a
         fallback render to the spp the check estimated for `bound` (every
         flagged block in one tile-list pass, each at its own sample count).
         Returns (image, stats): stats counts the flagged blocks and the fallback
@@ -254,9 +256,10 @@ class KPCNN:
                 ev.append(e)
 
         mark()
-        rad, aov = sr.render(x0, y0, w, h, spp, seed, aov=True)
-        mark()
-        chk, _ = sr.render(x0, y0, w, h, cspp, (seed + 0x1B873593) & 0xFFFFFFFF)
+        # input (samples 0 .. spp - 1, with G-buffers) and the independent check
+        # render (samples spp .. spp + cspp - 1 of the same per-pixel sequence) in
+        # one pass
+        rad, aov, chk = sr.render_split(x0, y0, w, h, spp, cspp, seed, aov=True)
         mark()
         den = self.denoise(rad.unsqueeze(0).contiguous(), aov.unsqueeze(0).contiguous())
         mark()
@@ -264,24 +267,24 @@ class KPCNN:
                                             chk.unsqueeze(0).contiguous(), cspp, bound, tile,
                                             max_spp, margin)
         f = flags.cpu().numpy()
-        nd = need.cpu().numpy()
+        nd = need.cpu().numpy().astype(np.int64)
         tx = (w + tile - 1) // tile
+        # flagged tiles that need samples beyond the two plain renders
+        extra = np.where(f != 0, nd - spp - cspp, 0)
+        sel = np.nonzero(extra > 0)[0]
         spp_f = np.zeros(len(f), np.int32)
-        fb_tiles, fb_spp = [], []
-        for t in np.nonzero(f)[0]:
-            extra = int(nd[t]) - spp - cspp
-            if extra <= 0:
-                continue
-            spp_f[t] = extra
-            bx, by = int(t % tx) * tile, int(t // tx) * tile
-            fb_tiles.append((x0 + bx, y0 + by, x0 + min(bx + tile, w), y0 + min(by + tile, h)))
-            fb_spp.append(extra)
+        spp_f[sel] = extra[sel]
+        bx, by = (sel % tx) * tile, (sel // tx) * tile
+        fb_tiles = np.stack([x0 + bx, y0 + by, x0 + np.minimum(bx + tile, w),
+                             y0 + np.minimum(by + tile, h)], axis=1).astype(np.uint32)
+        fb_spp = extra[sel].astype(np.uint32)
         mark()
         fb = None
         fb_samples = 0
-        if fb_tiles:
+        if len(sel):
             sr.render_tiles_spp(fb_tiles, fb_spp, (seed + 7919) & 0xFFFFFFFF)
-            fb_samples = sum(k * (t[2] - t[0]) * (t[3] - t[1]) for t, k in zip(fb_tiles, fb_spp))
+            area = (fb_tiles[:, 2].astype(np.int64) - fb_tiles[:, 0]) * (fb_tiles[:, 3].astype(np.int64) - fb_tiles[:, 1])
+            fb_samples = int((fb_spp.astype(np.int64) * area).sum())
             fb = torch.empty((1, h, w, 4), dtype=torch.float32, device="cuda")
             sr.rend.copy_region(x0, y0, w, h, fb.data_ptr())
         mark()
@@ -292,12 +295,12 @@ class KPCNN:
         mark()
         if ev is not None:
             torch.cuda.synchronize()
-            names = ["input_render", "check_render", "denoise", "check_and_readback",
+            names = ["input_and_check_render", "denoise", "check_and_readback",
                      "fallback_renders", "merge"]
             for k, n in enumerate(names):
                 timing[n] = timing.get(n, 0.0) + ev[k].elapsed_time(ev[k + 1])
         stats = {"tiles": int(len(f)), "flagged": int(f.sum()), "fallback_samples": fb_samples,
-                 "fallback_tiles": len(fb_tiles), "denoised": den[0]}
+                 "fallback_tiles": int(len(sel)), "denoised": den[0]}
         return out[0], stats
 
     # ---- training ------------------------------------------------------------------
@@ -376,6 +379,7 @@ class SceneRenderer:
     def __init__(self, rt, s):
         self.s = s
         self.scene, self.ms, self.rend = gbsp.upload_scene(rt, s)
+        self._image2 = None  # second image of split renders (full frame)
 
     def render(self, x0, y0, w, h, spp, seed, aov=False):
         import torch
@@ -388,6 +392,25 @@ class SceneRenderer:
         av = torch.empty((h, w, 8), dtype=torch.float32, device="cuda") if aov else None
         self.rend.copy_region(x0, y0, w, h, rad.data_ptr(), av.data_ptr() if aov else 0)
         return rad, av
+
+    def render_split(self, x0, y0, w, h, spp_a, spp_c, seed, aov=True):
+        """One pass of spp_a + spp_c samples per pixel over the window: returns
+        the mean of the first spp_a (the image a spp_a render gives, with its
+        G-buffers) and the mean of the other spp_c, an independent render."""
+        import torch
+
+        o = self.rend.options
+        o.spp, o.seed = spp_a + spp_c, seed
+        o.flags = gbsp.FLAG_AOV if aov else 0
+        if self._image2 is None:
+            self._image2 = torch.empty((self.s.height, self.s.width, 4), dtype=torch.float32,
+                                       device="cuda")
+        self.rend.tile_split_device((x0, y0, x0 + w, y0 + h), spp_a, self._image2.data_ptr())
+        rad = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+        av = torch.empty((h, w, 8), dtype=torch.float32, device="cuda") if aov else None
+        self.rend.copy_region(x0, y0, w, h, rad.data_ptr(), av.data_ptr() if aov else 0)
+        chk = self._image2[y0:y0 + h, x0:x0 + w].contiguous()
+        return rad, av, chk
 
     def render_tiles(self, tiles, spp, seed):
         """Plain render of the listed (minX, minY, maxX, maxY) frame tiles at

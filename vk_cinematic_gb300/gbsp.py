@@ -59,7 +59,7 @@ EXPORTS = [
     "gbsp_dn_tile_fallback", "gbsp_scene_set_node_width", "gbsp_scene_node_width",
     "gbsp_batch_set_node_widths", "gbsp_batch_get_node_widths", "gbsp_path_trace_tile_list",
     "gbsp_dn_tile_check", "gbsp_dn_tile_merge", "gbsp_dn_conv3x3_weight_grad_tcgen05",
-    "gbsp_path_trace_tile_list_spp",
+    "gbsp_path_trace_tile_list_spp", "gbsp_path_trace_tile_split",
 ]
 
 
@@ -370,6 +370,19 @@ class Renderer:
                                            ctypes.byref(m)))
         return m
 
+    def tile_split_device(self, tile, first_spp: int, image2_ptr: int, metrics: bool = False):
+        """gbsp_path_trace_tile_split: options.spp samples per pixel in one pass;
+        the mean of the first `first_spp` lands in the runtime's frame buffer
+        (and G-buffers), the mean of the rest in the device image at
+        image2_ptr (width x height RGBA32F).  Returns the metrics when asked."""
+        self.set_host_pixels(None)
+        m = Metrics() if metrics else None
+        t = Tile(*[int(v) for v in tile])
+        _check(self.L.gbsp_path_trace_tile_split(ctypes.byref(self.ctx), t, _u32(first_spp),
+                                                 _vp(image2_ptr),
+                                                 ctypes.byref(m) if m is not None else None))
+        return m
+
     def tile(self, tile, rng_state: int = 0, pixels: np.ndarray | None = None):
         out = pixels if pixels is not None else np.zeros((self.height, self.width, 4), np.float32)
         self.set_host_pixels(out)
@@ -385,9 +398,10 @@ class Renderer:
         """Renders the listed (minX, minY, maxX, maxY) tiles in one pass into the
         runtime's frame buffer (device); returns the metrics when asked."""
         self.set_host_pixels(None)
-        arr = (Tile * max(1, len(tiles)))(*[Tile(*[int(v) for v in t]) for t in tiles])
+        # gbsp_tile is four uint32 (minX, minY, maxX, maxY): an (n, 4) array is its layout
+        tl = np.ascontiguousarray(tiles, dtype=np.uint32).reshape(-1, 4)
         m = Metrics() if metrics else None
-        _check(self.L.gbsp_path_trace_tile_list(ctypes.byref(self.ctx), arr, _u32(len(tiles)),
+        _check(self.L.gbsp_path_trace_tile_list(ctypes.byref(self.ctx), _p(tl), _u32(len(tl)),
                                                 ctypes.byref(m) if m is not None else None))
         return m
 
@@ -396,13 +410,14 @@ class Renderer:
         tiles, tile i at spp[i] samples per pixel, in one pass into the
         runtime's frame buffer (device); returns the metrics when asked."""
         self.set_host_pixels(None)
-        arr = (Tile * max(1, len(tiles)))(*[Tile(*[int(v) for v in t]) for t in tiles])
+        # gbsp_tile is four uint32 (minX, minY, maxX, maxY): an (n, 4) array is its layout
+        tl = np.ascontiguousarray(tiles, dtype=np.uint32).reshape(-1, 4)
         sp = np.ascontiguousarray(spp, dtype=np.uint32).reshape(-1)
-        if len(sp) != len(tiles):
+        if len(sp) != len(tl):
             raise ValueError("one spp per tile")
         m = Metrics() if metrics else None
-        _check(self.L.gbsp_path_trace_tile_list_spp(ctypes.byref(self.ctx), arr, _p(sp),
-                                                    _u32(len(tiles)),
+        _check(self.L.gbsp_path_trace_tile_list_spp(ctypes.byref(self.ctx), _p(tl), _p(sp),
+                                                    _u32(len(tl)),
                                                     ctypes.byref(m) if m is not None else None))
         return m
 
