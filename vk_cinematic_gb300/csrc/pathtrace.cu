@@ -340,7 +340,6 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
     wp.invSpp = 1.0f / (float)spp;
     wp.aovImage = dAov;
     OneScene one = {sv, mv, maxBounces, opt.radiance_clamp};
-    int persistentGrid = rt->smCount * 8;
     const int shadeGrid = shade_grid<OneScene>(rt->smCount);
     const bool sortDirs = (opt.flags & GBSP_FLAG_SORT_DIRECTIONS) != 0 && maxBounces > 1;
     if (sortDirs && (rc = rt->sortHist.reserve(8 * (size_t)kSortBlocks, s))) return rc;
@@ -368,7 +367,8 @@ static int render_waves(gbsp_runtime *rt, const SceneView &sv, const MaterialVie
                 int e0 = timing ? rt->stage_event(s) : -1;
                 bool perLane = (opt.flags & GBSP_FLAG_TRACE_PER_LANE) ||
                     (!(opt.flags & GBSP_FLAG_TRACE_PER_WARP) && b > 0);
-                launch_trace_stage(perLane, sv.watertight != 0, persistentGrid, s, one, qO, qD,
+                launch_trace_stage(perLane, sv.watertight != 0,
+                    trace_grid<OneScene>(perLane, sv.watertight != 0, rt->smCount), s, one, qO, qD,
                     ctl + inQ, wb.hitA, wb.hitInst, ctl, counters, rt->dStatus);
                 int e1 = timing ? rt->stage_event(s) : -1;
                 k_shade<<<shadeGrid, 128, 0, s>>>(one, wb, b, inQ, ctl, counters);

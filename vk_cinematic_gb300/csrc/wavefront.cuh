@@ -692,6 +692,28 @@ int shade_grid(int smCount)
     return smCount * perSm;
 }
 
+// Persistent grid of the closest-hit kernel launch_trace_stage picks: every
+// block the SMs hold at once (blocks beyond that would only start once others
+// have drained the queue).
+template <class K>
+int resident_blocks_per_sm(K kernel)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, 128, 0) != cudaSuccess || n < 1)
+        n = 6;
+    return n;
+}
+
+template <class Src>
+int trace_grid(bool perLane, bool watertight, int smCount)
+{
+    static const int lane[2] = {resident_blocks_per_sm(k_trace_lane<Src, false>),
+        resident_blocks_per_sm(k_trace_lane<Src, true>)};
+    static const int warp[2] = {resident_blocks_per_sm(k_trace<Src, false>),
+        resident_blocks_per_sm(k_trace<Src, true>)};
+    return smCount * (perLane ? lane[watertight ? 1 : 0] : warp[watertight ? 1 : 0]);
+}
+
 // Launches the closest-hit kernel of one bounce: per-warp or per-lane
 // scheduling, reference MT or watertight triangle test (template arguments,
 // so neither choice costs the other anything).
