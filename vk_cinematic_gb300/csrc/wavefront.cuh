@@ -276,8 +276,11 @@ static __global__ void __launch_bounds__(256) k_generate(WaveParams wp, WaveBuff
     wb.rayD[p] = make_float4(d.x, d.y, d.z, __uint_as_float(rng));
 }
 
+// Closest hit, 32 queued rays per warp (primary rays by default).  7 blocks of
+// 128 per SM (72 registers): 1,521 Msamples/s on the 1080p benchmark frame
+// against 1,516 at 6 blocks and 1,521 at 8 (which spills more).
 template <class Src, bool kWT>
-__global__ void __launch_bounds__(128, 6) k_trace(Src src, const float4 *__restrict__ rayO,
+__global__ void __launch_bounds__(128, 7) k_trace(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
@@ -329,12 +332,14 @@ __global__ void __launch_bounds__(128, 6) k_trace(Src src, const float4 *__restr
 // moment (__activemask), and a lane leaves the loop as soon as the queue is
 // exhausted: there is no whole-warp vote or shuffle inside the loop.  Same
 // candidate sets, arithmetic and tie rules as trace_closest, hence the same
-// hit records.
+// hit records.  8 blocks of 128 per SM (64 registers): on the 1080p benchmark
+// frame 8 blocks gave 1,516 Msamples/s against 1,468 at 7 (72 registers) and
+// 1,461 at 9 (56 registers, which spill).
 constexpr uint32_t kMaxLaneRaySteps = 1u << 22;
 constexpr uint32_t kMaxLaneIterations = 1u << 28;
 
 template <class Src, bool kWT>
-__global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__restrict__ rayO,
+__global__ void __launch_bounds__(128, 8) k_trace_lane(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
@@ -348,7 +353,7 @@ __global__ void __launch_bounds__(128, 6) k_trace_lane(Src src, const float4 *__
     // State a lane touches only when it fetches a ray, enters or leaves an
     // object, or stores a hit, kept in memory (local, L1-resident) on purpose:
     // the walk itself then holds just the current level's ray, bounds and
-    // stack in registers, which fit the 80 registers of 6 blocks per SM.
+    // stack pointer in registers.
     // Words: world origin 0-2, direction 3-5, inverse direction 6-8; best hit
     // over objects u 9, v 10, triangle 11, object 12; queue slot 13; object
     // being walked 14; its best triangle's u 15, v 16.
