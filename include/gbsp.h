@@ -358,7 +358,8 @@ typedef struct {
 typedef struct {
     uint32_t block;        /* threads per block: 64, 128 or 256 */
     uint32_t chunk;        /* pixels a thread takes per queue pop: 1..8 */
-    uint32_t blocksPerSm;  /* persistent grid = SM count * blocksPerSm */
+    uint32_t blocksPerSm;  /* persistent grid = SM count * blocksPerSm; 0 (wavefront
+                              kernel only): each kernel at the blocks the SMs hold */
     uint32_t useGraph;     /* 1 = replay a captured CUDA graph */
     uint32_t kernel;       /* GBSP_BATCH_WAVEFRONT, GBSP_BATCH_PATH_STATE or
                               GBSP_BATCH_THREAD_PER_PIXEL */

@@ -42,13 +42,17 @@ def test_batch_matches_single_scene_renders(gpu_lib):
     batch = gbsp.Batch(rt, rends, [t.data_ptr() for t in imgs])
     total = sum(s.width * s.height * s.spp for s in ss)
     # wavefront: one wave, then waves of 1,000 paths (items split across waves)
-    for kernel, use_graph, wave in ((gbsp.BATCH_THREAD_PER_PIXEL, 0, 0),
-                                    (gbsp.BATCH_THREAD_PER_PIXEL, 1, 0),
-                                    (gbsp.BATCH_PATH_STATE, 0, 0), (gbsp.BATCH_PATH_STATE, 1, 0),
-                                    (gbsp.BATCH_WAVEFRONT, 0, 0), (gbsp.BATCH_WAVEFRONT, 1, 0),
-                                    (gbsp.BATCH_WAVEFRONT, 1, 1000)):
-        batch.set_config(block=128, chunk=1, blocks_per_sm=4, use_graph=use_graph, kernel=kernel,
-                         wave_paths=wave)
+    # (blocks per SM 0: the wavefront's kernels at the blocks the SMs hold)
+    for kernel, use_graph, wave, bps in ((gbsp.BATCH_THREAD_PER_PIXEL, 0, 0, 4),
+                                         (gbsp.BATCH_THREAD_PER_PIXEL, 1, 0, 4),
+                                         (gbsp.BATCH_PATH_STATE, 0, 0, 4),
+                                         (gbsp.BATCH_PATH_STATE, 1, 0, 4),
+                                         (gbsp.BATCH_WAVEFRONT, 0, 0, 4),
+                                         (gbsp.BATCH_WAVEFRONT, 1, 0, 4),
+                                         (gbsp.BATCH_WAVEFRONT, 1, 1000, 4),
+                                         (gbsp.BATCH_WAVEFRONT, 1, 0, 0)):
+        batch.set_config(block=128, chunk=1, blocks_per_sm=bps, use_graph=use_graph,
+                         kernel=kernel, wave_paths=wave)
         for _ in range(2):  # a replayed graph must reset its queue each time
             for t in imgs:
                 t.fill_(-1.0)
@@ -58,7 +62,7 @@ def test_batch_matches_single_scene_renders(gpu_lib):
             for k, (t, ref) in enumerate(zip(imgs, refs)):
                 got = t.cpu().numpy()
                 assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), \
-                    f"item {k} differs (kernel={kernel}, graph={use_graph}, wave={wave})"
+                    f"item {k} differs (kernel={kernel}, graph={use_graph}, wave={wave}, bps={bps})"
     # every item on 4-wide BVHs, then mixed widths: the same bits
     for widths in ([4] * len(ss), [4 if k % 2 else 8 for k in range(len(ss))]):
         batch.set_node_widths(widths)

@@ -641,7 +641,10 @@ static void enqueue_wavefront(gbsp_batch *b)
     wb.cap = b->waveCap;
     ManyScenes src = {b->dItems.ptr, b->pathItem.ptr};
     uint32_t n = (uint32_t)b->items.size();
-    int grid = rt->smCount * (int)b->cfg.blocksPerSm;
+    // blocksPerSm 0: every kernel at the blocks the SMs hold (occupancy)
+    const bool resident = b->cfg.blocksPerSm == 0;
+    const int grid = rt->smCount * (int)b->cfg.blocksPerSm;
+    const int shadeGrid = resident ? shade_grid<ManyScenes>(rt->smCount) : grid;
     for (const BatchWave &w : b->waves) {
         k_reset_ctl<<<1, 32, 0, s>>>(ctl, w.paths);
         if (w.maxBounces == 0) {
@@ -657,9 +660,10 @@ static void enqueue_wavefront(gbsp_batch *b)
             const float4 *qD = wb.rayD + ((bn & 1) ? wb.cap : 0);
             k_reset_stage<<<1, 1, 0, s>>>(ctl, outQ);
             // primary rays per warp, bounce rays per lane (the frame renderer's default)
-            launch_trace_stage(bn > 0, b->watertight, grid, s, src, qO, qD, ctl + inQ, wb.hitA,
-                wb.hitInst, ctl, counters, rt->dStatus);
-            k_shade<<<grid, 128, 0, s>>>(src, wb, bn, inQ, ctl, counters);
+            launch_trace_stage(bn > 0, b->watertight,
+                resident ? trace_grid<ManyScenes>(bn > 0, b->watertight, rt->smCount) : grid, s,
+                src, qO, qD, ctl + inQ, wb.hitA, wb.hitInst, ctl, counters, rt->dStatus);
+            k_shade<<<shadeGrid, 128, 0, s>>>(src, wb, bn, inQ, ctl, counters);
         }
         k_baccumulate<<<(w.pixels + 255) / 256, 256, 0, s>>>(b->dItems.ptr, n, w, wb, counters);
     }
@@ -726,8 +730,9 @@ static int check_config(const gbsp_batch_config *c)
     if (c->kernel == GBSP_BATCH_PATH_STATE && c->block > 128)
         return set_error(GBSP_ERR_INVALID_ARGUMENT, "the path-state kernel takes 64 or 128 threads");
     if (c->chunk < 1 || c->chunk > 8) return set_error(GBSP_ERR_INVALID_ARGUMENT, "chunk must be 1..8");
-    if (c->blocksPerSm < 1 || c->blocksPerSm > 32)
-        return set_error(GBSP_ERR_INVALID_ARGUMENT, "blocksPerSm must be 1..32");
+    if (c->blocksPerSm > 32 || (c->blocksPerSm == 0 && c->kernel != GBSP_BATCH_WAVEFRONT))
+        return set_error(GBSP_ERR_INVALID_ARGUMENT,
+            "blocksPerSm must be 1..32 (0: occupancy, wavefront kernel only)");
     return GBSP_OK;
 }
 
@@ -932,6 +937,8 @@ int gbsp_batch_autotune(gbsp_batch *batch, uint32_t trials, gbsp_batch_config *b
         for (uint32_t wave : {1u << 22, 1u << 23, 1u << 24, 1u << 25})
             cands.push_back({128, 1, ps, keep.useGraph, GBSP_BATCH_WAVEFRONT, wave});
     }
+    for (uint32_t wave : {1u << 24, 1u << 25})
+        cands.push_back({128, 1, 0, keep.useGraph, GBSP_BATCH_WAVEFRONT, wave});
     gbsp_batch_config bestCfg = keep;
     float bestMs = 3.0e38f;
     for (const gbsp_batch_config &c : cands) {
