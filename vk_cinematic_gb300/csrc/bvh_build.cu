@@ -564,7 +564,10 @@ struct HostBinaryTree {
 // the split between bins that minimises area(left) x count(left) +
 // area(right) x count(right) partitions the node's range (a median split
 // when every centroid coincides).  Node boxes are exact unions.
-constexpr int kSahBins = 16;
+// 64 bins: on the 1080p benchmark scene 16, 32, 64 and 128 bins gave 6.71,
+// 6.48, 6.45 and 6.44 node visits per ray (1,518, 1,542, 1,547 and 1,550
+// Msamples/s) for a host build time that grows with the bin count.
+constexpr int kSahBins = 64;
 // Above this many primitives the device LBVH (Morton order, Karras tree)
 // is built instead: the host build's time grows as n log n on one core.
 constexpr uint32_t kSahMaxPrims = 1u << 20;
