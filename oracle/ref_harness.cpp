@@ -626,6 +626,17 @@ void ref_world_radiance_for_path(void *p, const void *vertices,
     Put3(out, r);
 }
 
+// ToColor (src/math_lib.h:523-532) over n RGBA pixels; the reference's cast
+// to u8 is defined for channels whose floor(c * 255) lies in [0, 255].
+void ref_to_color(const float *rgba, uint64_t n, uint32_t *out)
+{
+    for (uint64_t i = 0; i < n; i++)
+    {
+        const float *c = rgba + 4 * i;
+        out[i] = ToColor(Vec4(c[0], c[1], c[2], c[3]));
+    }
+}
+
 int ref_sizeof(int which)
 {
     switch (which)

@@ -1452,24 +1452,44 @@ void oracle_ray_triangle_watertight(const float *o, const float *d, const float 
     out[2] = h.uv.y;
 }
 
+// One channel of ToColor (src/math_lib.h:525-528): floor(c * 255) cast to
+// u8.  The reference's cast is defined for results in [0, 255]; outside it
+// (and for NaN, which the device's fminf/fmaxf send to 0) the value is clamped.
+static uint32_t to_color_channel(float c)
+{
+    float f = floorf(c * 255.0f);
+    if (!(f >= 0.0f)) f = 0.0f;
+    if (f > 255.0f) f = 255.0f;
+    return (uint32_t)f;
+}
+
+// ToColor (src/math_lib.h:523-532) over n RGBA pixels, packed A8B8G8R8.
+void oracle_to_color(const float *rgba, uint64_t n, uint32_t *out)
+{
+    for (uint64_t i = 0; i < n; i++)
+    {
+        const float *c = rgba + 4 * i;
+        out[i] = (to_color_channel(c[3]) << 24) | (to_color_channel(c[2]) << 16) |
+                 (to_color_channel(c[1]) << 8) | to_color_channel(c[0]);
+    }
+}
+
 // PerformToneMapping (src/shaders/post_processing.frag.glsl:19-26) restated
-// in C, then ToColor (src/math_lib.h:523-532).
+// in C, then ToColor (src/math_lib.h:523-532) with the shader's alpha of 1.
 void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out)
 {
     for (uint64_t i = 0; i < pixels; i++)
     {
         const float *c = frame + 4 * i;
-        uint32_t v[3];
+        float m[4];
         for (int k = 0; k < 3; k++)
         {
             float x = c[k] * 1.0f;
             x = x / (1.0f + x);
-            x = powf(x, 1.0f / 2.2f);
-            float f = floorf(x * 255.0f);
-            f = f < 0.0f ? 0.0f : (f > 255.0f ? 255.0f : f);
-            v[k] = (uint32_t)f;
+            m[k] = powf(x, 1.0f / 2.2f);
         }
-        out[i] = (255u << 24) | (v[2] << 16) | (v[1] << 8) | v[0];
+        m[3] = 1.0f;
+        oracle_to_color(m, 1, out + i);
     }
 }
 

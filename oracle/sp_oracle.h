@@ -126,7 +126,9 @@ void oracle_world_set_watertight(void *w, int on);
 // out = t (-1 miss), u, v of the watertight test with the reference's culling.
 void oracle_ray_triangle_watertight(const float *o, const float *d, const float *a,
     const float *b, const float *c, float *out);
-// Display conversion: Reinhard + gamma 1/2.2, then 8-bit packing.
+// 8-bit packing of RGBA pixels (ToColor), and the display conversion:
+// Reinhard + gamma 1/2.2, then that packing.
+void oracle_to_color(const float *rgba, uint64_t n, uint32_t *out);
 void oracle_tonemap(const float *frame, uint64_t pixels, uint32_t *out);
 int oracle_world_closest_brute(void *w, uint32_t rayCount, const float *rays,
     uint32_t threads, float *tOut, int32_t *objectOut, int32_t *triangleOut, int32_t *tiedOut);

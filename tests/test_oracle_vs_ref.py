@@ -69,3 +69,29 @@ def test_random_scenes_match_reference(ref, seed):
     img_p = wp.path_trace_hashed(s.width, s.height, s.camera_position, s.camera_rotation,
                                  s.film_distance, s.seed)[0]
     assert np.array_equal(bits(img_r), bits(img_p))
+
+
+def test_to_color_matches_reference(ref):
+    """ToColor (src/math_lib.h:523-532), the last step of the display
+    conversion: every level boundary k/255 with its neighbouring floats, the
+    ends of [0, 1] and random values, bit for bit."""
+    levels = np.arange(256, dtype=np.float32) / np.float32(255.0)
+    vals = np.concatenate([
+        levels, np.nextafter(levels, np.float32(0)), np.nextafter(levels, np.float32(1)),
+        np.float32([0.0, -0.0, 1.0, 0.5, np.nextafter(np.float32(1), np.float32(0))]),
+        np.random.default_rng(5).random(4000, dtype=np.float32),
+    ]).astype(np.float32)
+    vals = np.clip(vals, 0, 1)
+    rgba = np.ascontiguousarray(np.stack(
+        [vals, vals[::-1], np.roll(vals, 7), np.roll(vals, 101)], 1), dtype=np.float32)
+    n = rgba.shape[0]
+    got = np.zeros(n, np.uint32)
+    want = np.zeros(n, np.uint32)
+    ctypes.CDLL(po.PORT_LIB).oracle_to_color(rgba.ctypes.data_as(ctypes.c_void_p),
+                                             ctypes.c_uint64(n),
+                                             got.ctypes.data_as(ctypes.c_void_p))
+    ctypes.CDLL(po.REF_LIB).ref_to_color(rgba.ctypes.data_as(ctypes.c_void_p),
+                                         ctypes.c_uint64(n),
+                                         want.ctypes.data_as(ctypes.c_void_p))
+    assert np.array_equal(got, want)
+    assert len(np.unique(want & 0xFF)) == 256
