@@ -353,6 +353,18 @@ __global__ void collapse_level(const CollapseItem *in, uint32_t inCount, Collaps
         child_box(ch[cnt], nodeLo, nodeHi, primLo, primHi, order, clo[cnt], chi[cnt]);
         cnt++;
     }
+    // the node's internal children get consecutive indices (and work-list
+    // slots) from one atomic each, so that siblings lie side by side in memory
+    uint32_t internal = 0;
+    for (int c = 0; c < cnt; c++) {
+        const uint32_t r = ch[c];
+        if (!(r & kBinLeaf) && last[r] - first[r] + 1u > leafMax) internal++;
+    }
+    const uint32_t w = internal ? atomicAdd(nodeCounter, internal) : 0u;
+    // children past the capacity are reported and left out, and get no slot
+    const uint32_t fit = w >= nodeCapacity ? 0u : min(internal, nodeCapacity - w);
+    const uint32_t slot = fit ? atomicAdd(outCount, fit) : 0u;
+    uint32_t taken = 0;
     float lo[3 * W], hi[3 * W];
     uint32_t child[W];
     for (int c = 0; c < W; c++) {
@@ -374,15 +386,14 @@ __global__ void collapse_level(const CollapseItem *in, uint32_t inCount, Collaps
         } else if (last[r] - first[r] + 1u <= leafMax) {
             child[c] = make_leaf(first[r], last[r] - first[r] + 1u);
         } else {
-            uint32_t w = atomicAdd(nodeCounter, 1u);
-            if (w >= nodeCapacity) {
+            if (taken >= fit) {
                 atomicOr(status, kStatusBuildLoop);
                 child[c] = kEmptyChild;
                 continue;
             }
-            child[c] = w;
-            uint32_t slot = atomicAdd(outCount, 1u);
-            out[slot] = CollapseItem{r, w};
+            child[c] = w + taken;
+            out[slot + taken] = CollapseItem{r, w + taken};
+            taken++;
         }
     }
     store_node(nodes + node_offset(item.wide, W / 4), W / 4, lo, hi, child);
