@@ -336,10 +336,11 @@ __global__ void __launch_bounds__(128, 7) k_trace(Src src, const float4 *__restr
 // frame 8 blocks gave 1,516 Msamples/s against 1,468 at 7 (72 registers) and
 // 1,461 at 9 (56 registers, which spill).
 constexpr uint32_t kMaxLaneRaySteps = 1u << 22;
+constexpr int kLaneThreads = 128;  // block size of k_trace_lane
 constexpr uint32_t kMaxLaneIterations = 1u << 28;
 
 template <class Src, bool kWT>
-__global__ void __launch_bounds__(128, 8) k_trace_lane(Src src, const float4 *__restrict__ rayO,
+__global__ void __launch_bounds__(kLaneThreads, 8) k_trace_lane(Src src, const float4 *__restrict__ rayO,
     const float4 *__restrict__ rayD, const unsigned int *queueCount, int4 *hitA, int *hitInst,
     unsigned int *ctl, unsigned long long *counters, uint32_t *status)
 {
@@ -351,13 +352,24 @@ __global__ void __launch_bounds__(128, 8) k_trace_lane(Src src, const float4 *__
     uint32_t done = 0, hits = 0;
     StackEntry stack[kStackSize];
     // State a lane touches only when it fetches a ray, enters or leaves an
-    // object, or stores a hit, kept in memory (local, L1-resident) on purpose:
-    // the walk itself then holds just the current level's ray, bounds and
-    // stack pointer in registers.
-    // Words: world origin 0-2, direction 3-5, inverse direction 6-8; best hit
-    // over objects u 9, v 10, triangle 11, object 12; queue slot 13; object
-    // being walked 14; its best triangle's u 15, v 16.
-    volatile uint32_t cold[17];
+    // object, or stores a hit, kept in shared memory on purpose: the walk
+    // itself then holds just the current level's ray, bounds and stack
+    // pointer in registers.  (In a local array its stores were written
+    // through to L2; shared memory keeps them on the SM: 1,556 against
+    // 1,552 Msamples/s on the 1080p benchmark frame.)  Word w of the lane
+    // is column threadIdx.x of row w, so a warp's accesses to one word are
+    // contiguous.  Words: world origin 0-2, direction 3-5, inverse direction
+    // 6-8; best hit over objects u 9, v 10, triangle 11, object 12; queue
+    // slot 13; object being walked 14; its best triangle's u 15, v 16.
+    __shared__ uint32_t coldWords[17 * kLaneThreads];
+    struct ColdWords {
+        volatile uint32_t *p;
+        __device__ __forceinline__ volatile uint32_t &operator[](int w) const
+        {
+            return p[w * kLaneThreads];
+        }
+    };
+    const ColdWords cold{coldWords + threadIdx.x};
     // next: the entry to visit next (the nearest child of the last node
     // visit, or a root), kept out of the stack; ref kEmptyChild when none
     StackEntry next = StackEntry{kEmptyChild, 0.0f};
@@ -729,10 +741,10 @@ void launch_trace_stage(bool perLane, bool watertight, int grid, cudaStream_t s,
 {
     if (perLane) {
         if (watertight)
-            k_trace_lane<Src, true><<<grid, 128, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst,
+            k_trace_lane<Src, true><<<grid, kLaneThreads, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst,
                 ctl, counters, status);
         else
-            k_trace_lane<Src, false><<<grid, 128, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst,
+            k_trace_lane<Src, false><<<grid, kLaneThreads, 0, s>>>(src, qO, qD, queueCount, hitA, hitInst,
                 ctl, counters, status);
     } else {
         if (watertight)
