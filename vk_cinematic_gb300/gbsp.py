@@ -243,6 +243,12 @@ class Scene:
         h = _vp()
         _check(self.L.gbsp_scene_create(rt.h, ctypes.byref(h)))
         self.h = h
+        # add_object's transform (position 3, rotation 4, scale 3 floats) goes
+        # through this buffer, whose three pointers are made once: converting
+        # three arrays per call cost more than the call itself
+        self._xf = np.empty(10, np.float32)
+        base = self._xf.ctypes.data
+        self._xf_ptrs = (_vp(base), _vp(base + 12), _vp(base + 28))
 
     def set_intersection(self, mode: int):
         """ISECT_REFERENCE_MT (default) or ISECT_WATERTIGHT."""
@@ -265,11 +271,14 @@ class Scene:
         return out.value
 
     def add_object(self, mesh, material, position, rotation, scale):
-        p = np.ascontiguousarray(position, dtype=np.float32)
-        r = np.ascontiguousarray(rotation, dtype=np.float32)
-        s = np.ascontiguousarray(scale, dtype=np.float32)
-        _check(self.L.gbsp_add_object_to_scene(self.h, _u32(mesh), _u32(material), _p(p), _p(r),
-                                               _p(s)))
+        """sp_AddObjectToScene.  The library copies the transform during the
+        call; like the scene itself, one Scene takes one call at a time."""
+        xf = self._xf
+        xf[0:3] = position
+        xf[3:7] = rotation
+        xf[7:10] = scale
+        _check(self.L.gbsp_add_object_to_scene(self.h, _u32(mesh), _u32(material),
+                                               *self._xf_ptrs))
 
     def clear_objects(self):
         _check(self.L.gbsp_clear_objects(self.h))
