@@ -107,3 +107,48 @@ def test_denoiser_planar_layout_round_trip():
     for b, y, x, c in ((0, 0, 0, 0), (1, 2, 4, 23), (0, 1, 3, 9), (1, 0, 2, 16)):
         idx = (((b * H + y) * (C // 8) + c // 8) * W + x) * 8 + c % 8
         assert flat[idx].item() == t[b, y, x, c].item()
+
+
+def test_add_object_passes_the_transform_it_was_given():
+    """Scene.add_object hands gbsp_add_object_to_scene (sp_AddObjectToScene,
+    src/sp_scene.cpp:77-117) pointers to the position, rotation and scale it
+    was called with, rounded to float32 as the reference's f32 fields are,
+    call after call; a vector of the wrong length is refused before the call."""
+    import ctypes
+
+    calls = []
+
+    def read(ptr, n):
+        return list(np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_float)),
+                                          shape=(n,)).copy())
+
+    class FakeLib:
+        def gbsp_scene_create(self, rt, out):
+            return 0
+
+        def gbsp_add_object_to_scene(self, h, mesh, material, p, r, s):
+            calls.append((mesh.value, material.value, read(p, 3), read(r, 4), read(s, 3)))
+            return 0
+
+    class FakeRuntime:
+        L = FakeLib()
+        h = None
+
+    scene = gbsp.Scene(FakeRuntime())
+    objs = scenes.config3_scene().objects[:20]
+    for o in objs:
+        scene.add_object(o.mesh, o.material, o.position, o.rotation, o.scale)
+    scene.add_object(3, 7, (0.1, 2, -3), (0, 0, 0, 1), [1.5, 1.5, 1.5])
+    assert len(calls) == len(objs) + 1
+    for (mesh, mat, p, r, s), o in zip(calls, objs):
+        assert (mesh, mat) == (o.mesh, o.material)
+        assert np.array_equal(bits(p), bits(o.position))
+        assert np.array_equal(bits(r), bits(o.rotation))
+        assert np.array_equal(bits(s), bits(o.scale))
+    mesh, mat, p, r, s = calls[-1]
+    assert (mesh, mat) == (3, 7)
+    assert np.array_equal(bits(p), bits(np.float32([0.1, 2, -3])))
+    assert r == [0, 0, 0, 1] and s == [1.5, 1.5, 1.5]
+    with pytest.raises(ValueError):
+        scene.add_object(0, 0, (1, 2), (0, 0, 0, 1), (1, 1, 1))
+    assert len(calls) == len(objs) + 1
