@@ -80,7 +80,8 @@ def parse_args():
     ap.add_argument("--sort-dirs", action="store_true",
                     help="sort bounce-ray queues by direction octant")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
-                    help="target CPU work of the cpu_baseline sample")
+                    help="target CPU work of the cpu_baseline sample and of each step of "
+                         "--impl reference")
     ap.add_argument("--trace", choices=["hybrid", "warp", "lane"], default="hybrid",
                     help="closest-hit scheduling: per-warp for primary and per-lane for bounce "
                          "rays (library default), or one of the two for every bounce")
@@ -351,8 +352,10 @@ def run_reference(args):
     w = _cpu_world(s)
     pixels = np.zeros((s.height, s.width, 4), np.float32)
     per_tile, total = _cpu_calibrate(w, s, threads, pixels)
-    # each step renders the same spread tile sample, about 4 s of work
-    n = cpu_tile_count(per_tile, 4.0, threads, total)
+    # each step renders the same spread tile sample as the cpu_baseline leg
+    # (the same work target, --cpu-seconds), so that the two legs time the
+    # same mix of tiles with the same number of tiles per thread
+    n = cpu_tile_count(per_tile, args.cpu_seconds, threads, total)
     ids = spread_tiles(total, n)
     for _ in range(args.warmup):
         w.render_tile_list(s.width, s.height, s.camera_position, s.camera_rotation,
