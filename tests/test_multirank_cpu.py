@@ -70,3 +70,26 @@ def test_reference_arm_other_ranks_exit_without_work():
                        timeout=120)
     assert r.returncode == 0, r.stderr
     assert r.stdout.strip() == ""
+
+
+def test_cpu_tile_samples_are_whole_waves_spread_over_the_frame():
+    """The CPU legs (cpu_baseline and --impl reference) time the same sample:
+    distinct tile ids spread over the whole frame in row-major order, as many
+    tiles as the work target asks for, rounded up to whole waves of threads."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    total = 30 * 17  # 64x64 tiles of a 1920x1080 frame
+    for n in (1, 16, 48, 112, 509, 510, 600):
+        ids = bench.spread_tiles(total, n)
+        assert len(ids) == min(n, total) == len(set(ids))
+        assert ids == sorted(ids) and 0 <= ids[0] and ids[-1] < total
+        if len(ids) > 1:
+            gaps = [b - a for a, b in zip(ids, ids[1:])]
+            assert max(gaps) - min(gaps) <= 1
+    for per_tile, target, threads in ((0.7, 12.0, 16), (0.7, 4.0, 16), (0.05, 12.0, 16),
+                                      (3.0, 1.0, 8), (1e-9, 12.0, 16)):
+        n = bench.cpu_tile_count(per_tile, target, threads, total)
+        assert 1 <= n <= total
+        assert n == total or n % threads == 0
+        assert n == total or n * per_tile / threads >= target * 0.999 or n == threads
