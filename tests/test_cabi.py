@@ -152,3 +152,38 @@ def test_add_object_passes_the_transform_it_was_given():
     with pytest.raises(ValueError):
         scene.add_object(0, 0, (1, 2), (0, 0, 0, 1), (1, 1, 1))
     assert len(calls) == len(objs) + 1
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/gbsp.h is a C header: a C99 program (-pedantic, warnings as
+    errors) that takes the address of every function it declares compiles,
+    links against libgbsp.so and runs (no device call), which is what a cgo,
+    JNI or other FFI binding of the library does."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    gbsp.load()
+    header = open(os.path.join(ROOT, "include", "gbsp.h")).read()
+    names = sorted(set(re.findall(r"\b(gbsp_[a-z0-9_]+)\s*\(", header)))
+    src = tmp_path / "abi.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "gbsp.h"\n'
+        "typedef void (*fn)(void);\n"
+        "int main(void)\n{\n    fn table[] = {\n"
+        + "".join(f"        (fn){n},\n" for n in names)
+        + "    };\n    size_t n = 0, i;\n"
+        "    for (i = 0; i < sizeof(table) / sizeof(table[0]); i++) n += table[i] != 0;\n"
+        '    printf("%lu\\n", (unsigned long)n);\n    return 0;\n}\n')
+    exe = tmp_path / "abi"
+    build = os.path.dirname(gbsp._build.LIB)
+    r = subprocess.run([cc, "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe), "-L", build, "-lgbsp", "-Wl,-rpath," + build],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert int(r.stdout.strip()) == len(names)
