@@ -189,3 +189,23 @@ def test_closest_flags_exact_ties(port):
             assert np.allclose(t[:2], 5.0) and t[2] == -1.0
             assert tied.tolist() == [expect_tie, expect_tie, False], (copies, obj_count, fn)
         w.close()
+
+
+def test_to_color_clamps_where_the_reference_cast_is_undefined(port):
+    """ToColor (src/math_lib.h:523-532) casts floor(c * 255) to u8, which C++
+    leaves undefined outside [0, 255] and for NaN.  The restatement (like the
+    device's display conversion, fminf/fmaxf) sends NaN and values below 0 to
+    0 and values above 1 to 255; inside [0, 1] it is the reference's value."""
+    import ctypes
+
+    import pyoracle as po
+
+    v = np.float32([np.nan, -np.inf, -1.0, -0.0, 0.0, 0.5, 1.0, 1.5, np.inf])
+    want = [0, 0, 0, 0, 0, 127, 255, 255, 255]
+    rgba = np.ascontiguousarray(np.stack([v, v, v, v], 1), dtype=np.float32)
+    out = np.zeros(len(v), np.uint32)
+    lib = ctypes.CDLL(po.PORT_LIB)
+    lib.oracle_to_color(rgba.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint64(len(v)),
+                        out.ctypes.data_as(ctypes.c_void_p))
+    for k, w in enumerate(want):
+        assert out[k] == w * 0x01010101, (v[k], hex(out[k]))
